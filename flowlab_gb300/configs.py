@@ -1,0 +1,51 @@
+"""The benchmark configurations' scenes and engine parameters.
+
+  karman(...)  vortex street: inflow u = 1 at the left wall, Air outlet
+               column, cylinder of radius 0.1*ny cells at (0.25 nx, 0.5 ny),
+               seeded 1e-3 noise, seeded horizontal dye stripes; MacCormack,
+               CFL 0.5, red-black SOR omega 1.9 x 60 per step.
+  plume(...)   thermal plume in a closed box: heat + smoke sources whose
+               coverage is a Gaussian of sigma 8 cells at (0.35, 0.1) and
+               (0.65, 0.1) of the box, the draught seed of src/scenes/plume.ts;
+               buoyancy beta 1 (heat) and alpha 0.05 (smoke), confinement 0.3,
+               MacCormack, multigrid V(3,3) to an 8x8 coarsest level, solved
+               to a relative residual of 1e-6.
+Scenes come from flowlab_gb300.scenes (float64 host arrays, the reference's
+helpers); parameters are fl_params for the engine.
+"""
+from . import native, scenes as sc
+
+# The plume fades its heat and keeps its smoke (src/scenes/catalog.ts:304).
+PLUME_DECAY = (1.5, 0.1, 0.0)
+
+
+def plume(n=1024, sigma_cells=8.0):
+    g = sc.Grid(n, n, 1.0 / n)
+    w = n * g.h
+    spec = sc.SceneSpec(seed=sc.draught(), dye_source=sc.gaussian_sources(
+        [(0.35 * w, 0.1), (0.65 * w, 0.1)], sigma_cells=sigma_cells))
+    f, patch = sc.reset_fields(g, g, spec)
+    return g, f, patch
+
+
+def plume_params(tol=1e-6, max_cycles=20, mixed=0, coarse_sweeps=32):
+    return native.default_params(
+        cfl_target=2.0, dt_max=1 / 30, scheme=native.FL_MACCORMACK, solver=native.FL_SOLVER_MG, tol=tol,
+        mg_max_cycles=max_cycles, mg_pre=3, mg_post=3, mg_coarse_sweeps=coarse_sweeps, mg_coarsest=8,
+        dye_decay=PLUME_DECAY, beta=1.0, alpha=0.05, confinement=0.3, mixed=mixed)
+
+
+def karman(nx=128, ny=128, noise=1e-3):
+    g = sc.Grid(nx, ny, 1.0 / ny)
+    r = 0.1 * ny * g.h
+    spec = sc.SceneSpec(
+        labels=sc.all_labels(sc.open_right(), sc.solid_disk(0.25 * nx * g.h, 0.5 * ny * g.h, r)),
+        seed=sc.chain_seeds(sc.uniform_flow(1.0), sc.lcg_noise(noise)),
+        dye=lambda dg, dye: sc.add_dye_stripes(dg, dye))
+    f, patch = sc.reset_fields(g, g, spec)
+    return g, f, patch
+
+
+def karman_params(iters=60, omega=1.9):
+    return native.default_params(cfl_target=0.5, dt_max=1 / 30, scheme=native.FL_MACCORMACK,
+                                 solver=native.FL_SOLVER_RBSOR, pressure_iters=iters, omega=omega, tol=0.0)

@@ -1,0 +1,214 @@
+// Shared device-side definitions of the flowlab_gb300 engine.
+//
+// Numerics note: the library is compiled with -fmad=false and IEEE division /
+// square root, and every formula below keeps the reference's operation order
+// (src/core/*.ts), so each kernel performs the same float32 operations as the
+// reference's arithmetic evaluated in float32.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fl {
+
+// src/core/grid.ts:41-45
+constexpr uint8_t FLUID = 0, AIR = 1, SOLID = 2;
+constexpr int DYE_CHANNELS = 3;
+
+// Per-cell stencil code, built once per label change: the label in bits 0-1
+// and, for each neighbour in the pressure stencil's order, whether it is
+// non-solid AND in the domain (the negation of grid.ts:159-161
+// isSolidOrOutside). Cells outside the domain are coded SOLID with no links.
+constexpr uint8_t LINK_XP = 1u << 2;  // (i+1, j)
+constexpr uint8_t LINK_XM = 1u << 3;  // (i-1, j)
+constexpr uint8_t LINK_YP = 1u << 4;  // (i, j+1)
+constexpr uint8_t LINK_YM = 1u << 5;  // (i, j-1)
+constexpr uint8_t CODE_OUTSIDE = SOLID;
+
+__host__ __device__ inline uint8_t code_label(uint8_t c) { return c & 3u; }
+__host__ __device__ inline int code_count(uint8_t c) {
+  return ((c >> 2) & 1) + ((c >> 3) & 1) + ((c >> 4) & 1) + ((c >> 5) & 1);
+}
+
+// Scalars of one step, written on the device (from the CFL reduction) or by
+// the host, and read by every kernel of the step through a pointer so that a
+// captured graph needs no re-recording when dt changes.
+struct StepScalars {
+  float dt;          // simulation.ts:477
+  float scale;       // rho*h^2/dt (simulation.ts:478)
+  float grad_scale;  // dt/(rho*h) (simulation.ts:479)
+  float keep[3];     // exp(-decay*dt) per channel (simulation.ts:243-247)
+  float gain_beta;   // beta*dt (buoyancy.ts:80)
+  float gain_alpha;  // -alpha*dt (soot term)
+  float half_dt;     // 0.5*dt (confinement face average)
+  float neg_scale;   // -scale: b = (-scale)*div (pressureMultigrid.ts:311)
+  int pad[6];
+};
+
+// Double-precision accumulators of one step. The first four fields are
+// cleared before every solve; the last four are managed by the kernels that
+// use them (the CFL reduction clears its own running max and block counter).
+struct StepAccum {
+  double b_sq;                  // sum b^2 over fluid cells (fluidDivRms, pressure.ts:177-186)
+  double res_sq;                // sum r^2 over fluid cells with links (pressure.ts:127-167)
+  unsigned long long n_fluid;
+  unsigned long long n_res;
+  unsigned int max_speed_bits;  // running max |u|,|v| as float bits (non-negative floats order as ints)
+  unsigned int blocks_done;     // last-block detection of the CFL reduction
+  unsigned int last_max_bits;   // the finished max face speed, for the report
+  unsigned int nonfinite;
+};
+
+// ------------------------------------------------------------ sampling
+
+struct AxisF {
+  int i0;
+  float f;
+};
+
+// min/max with the C++ standard library's semantics ((b < a) ? b : a), so
+// that signed zeros and NaNs resolve exactly as in a host evaluation of the
+// same formula.
+__device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
+
+// grid.ts:173-177 clampedAxis: position clamped to [0, count-1], index to
+// count-2.
+__device__ __forceinline__ AxisF clamped_axis(float pos, int count) {
+  float c = smin(smax(pos, 0.0f), (float)(count - 1));
+  int i0 = min((int)floorf(c), count - 2);
+  AxisF a;
+  a.i0 = i0;
+  a.f = c - (float)i0;
+  return a;
+}
+
+// grid.ts:180-191
+__device__ __forceinline__ float bilerp(float v00, float v10, float v01, float v11, float fx, float fy) {
+  float lo = v00 + fx * (v10 - v00);
+  float hi = v01 + fx * (v11 - v01);
+  return lo + fy * (hi - lo);
+}
+
+__device__ __forceinline__ float ldg(const float* p) { return __ldg(p); }
+
+// grid.ts:197-208 sampleU: u[i,j] at (i*h, (j+0.5)*h), (nx+1) x ny values.
+__device__ __forceinline__ float sample_u(const float* __restrict__ u, int nx, int ny, float h, float x, float y) {
+  AxisF a = clamped_axis(x / h, nx + 1);
+  AxisF b = clamped_axis(y / h - 0.5f, ny);
+  long s = nx + 1;
+  long k = a.i0 + (long)b.i0 * s;
+  return bilerp(ldg(u + k), ldg(u + k + 1), ldg(u + k + s), ldg(u + k + s + 1), a.f, b.f);
+}
+
+// grid.ts:214-225 sampleV: v[i,j] at ((i+0.5)*h, j*h), nx x (ny+1) values.
+__device__ __forceinline__ float sample_v(const float* __restrict__ v, int nx, int ny, float h, float x, float y) {
+  AxisF a = clamped_axis(x / h - 0.5f, nx);
+  AxisF b = clamped_axis(y / h, ny + 1);
+  long s = nx;
+  long k = a.i0 + (long)b.i0 * s;
+  return bilerp(ldg(v + k), ldg(v + k + 1), ldg(v + k + s), ldg(v + k + s + 1), a.f, b.f);
+}
+
+// grid.ts:239-250 sampleP on a cell-centred field of nx x ny.
+__device__ __forceinline__ float sample_p(const float* __restrict__ q, int nx, int ny, float h, float x, float y) {
+  AxisF a = clamped_axis(x / h - 0.5f, nx);
+  AxisF b = clamped_axis(y / h - 0.5f, ny);
+  long s = nx;
+  long k = a.i0 + (long)b.i0 * s;
+  return bilerp(ldg(q + k), ldg(q + k + 1), ldg(q + k + s), ldg(q + k + s + 1), a.f, b.f);
+}
+
+// grid.ts:268-270
+__device__ __forceinline__ float clamp_to_range(float q, float a, float b, float c, float d) {
+  float lo = smin(smin(a, b), smin(c, d));
+  float hi = smax(smax(a, b), smax(c, d));
+  return smin(smax(q, lo), hi);
+}
+
+// grid.ts:273-315 clampToStencil{U,V,P}
+__device__ __forceinline__ float clamp_stencil_u(const float* __restrict__ u, int nx, int ny, float h, float x, float y,
+                                                 float q) {
+  int i0 = clamped_axis(x / h, nx + 1).i0;
+  int j0 = clamped_axis(y / h - 0.5f, ny).i0;
+  long s = nx + 1;
+  long k = i0 + (long)j0 * s;
+  return clamp_to_range(q, ldg(u + k), ldg(u + k + 1), ldg(u + k + s), ldg(u + k + s + 1));
+}
+__device__ __forceinline__ float clamp_stencil_v(const float* __restrict__ v, int nx, int ny, float h, float x, float y,
+                                                 float q) {
+  int i0 = clamped_axis(x / h - 0.5f, nx).i0;
+  int j0 = clamped_axis(y / h, ny + 1).i0;
+  long s = nx;
+  long k = i0 + (long)j0 * s;
+  return clamp_to_range(q, ldg(v + k), ldg(v + k + 1), ldg(v + k + s), ldg(v + k + s + 1));
+}
+__device__ __forceinline__ float clamp_stencil_p(const float* __restrict__ q, int nx, int ny, float h, float x, float y,
+                                                 float val) {
+  int i0 = clamped_axis(x / h - 0.5f, nx).i0;
+  int j0 = clamped_axis(y / h - 0.5f, ny).i0;
+  long s = nx;
+  long k = i0 + (long)j0 * s;
+  return clamp_to_range(val, ldg(q + k), ldg(q + k + 1), ldg(q + k + s), ldg(q + k + s + 1));
+}
+
+// grid.ts:159-161 isSolidOrOutside on the velocity grid's labels.
+__device__ __forceinline__ bool solid_or_outside(const uint8_t* __restrict__ label, int nx, int ny, int i, int j) {
+  return i < 0 || j < 0 || i >= nx || j >= ny || __ldg(label + i + (long)j * nx) == SOLID;
+}
+// boundaries.ts:23-25 isSolidCell
+__device__ __forceinline__ bool solid_cell(const uint8_t* __restrict__ label, int nx, int ny, int i, int j) {
+  return i >= 0 && j >= 0 && i < nx && j < ny && __ldg(label + i + (long)j * nx) == SOLID;
+}
+
+// Block-wide reductions (thread count a multiple of 32, <= 1024); the result
+// is valid in the block's first thread.
+__device__ inline double block_sum(double v, double* shm32) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  int lane = tid & 31, w = tid >> 5;
+  __syncthreads();
+  if (lane == 0) shm32[w] = v;
+  __syncthreads();
+  double t = 0;
+  if (w == 0) {
+    int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    t = lane < nw ? shm32[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  return t;  // valid in thread 0
+}
+
+__device__ inline unsigned long long block_sum_u64(unsigned long long v, unsigned long long* shm32) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  int lane = tid & 31, w = tid >> 5;
+  __syncthreads();
+  if (lane == 0) shm32[w] = v;
+  __syncthreads();
+  unsigned long long t = 0;
+  if (w == 0) {
+    int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    t = lane < nw ? shm32[lane] : 0ull;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  return t;
+}
+
+__device__ inline float block_max(float v, float* shm32) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+  int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  int lane = tid & 31, w = tid >> 5;
+  __syncthreads();
+  if (lane == 0) shm32[w] = v;
+  __syncthreads();
+  float t = 0.0f;
+  if (w == 0) {
+    int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    t = lane < nw ? shm32[lane] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) t = fmaxf(t, __shfl_down_sync(0xffffffffu, t, o));
+  }
+  return t;
+}
+
+}  // namespace fl

@@ -1,0 +1,846 @@
+// The C ABI (include/flowlab_gb300.h): the engine object, field residency,
+// the fused step and the per-pass entry points.
+//
+// The step (stepGpu.ts:393-559 re-designed for one GB300):
+//   advect u,v -> [stir] -> [confinement force] -> body forces -> divergence
+//   -> pressure solve -> subtract gradient + outflow -> advect dye (+decay,
+//   +inlet) -> CFL reduction that writes the NEXT step's dt on the device.
+// u, v, p and the dye stay resident; nothing crosses the bus per step except
+// the residual scalars the tolerance test needs (32 bytes per V-cycle).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "fl_internal.h"
+
+using namespace fl;
+
+struct fl_engine {
+  Engine e;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int fail(Engine* e, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (e)
+    e->err = buf;
+  else
+    g_create_error = buf;
+  return code;
+}
+
+int cuda_status(Engine* e, cudaError_t err, const char* where) {
+  if (err == cudaSuccess) return FL_OK;
+  if (err == cudaErrorMemoryAllocation) return fail(e, FL_ENOMEM, "%s: %s", where, cudaGetErrorString(err));
+  return fail(e, FL_EDEVICE, "%s: %s", where, cudaGetErrorString(err));
+}
+
+int check_launch(Engine* e, const char* where) { return cuda_status(e, cudaGetLastError(), where); }
+
+int sync(Engine* e, const char* where) {
+  cudaError_t err = cudaStreamSynchronize(e->stream);
+  if (err == cudaSuccess) err = cudaGetLastError();
+  return cuda_status(e, err, where);
+}
+
+// One call at a time per engine (the reference's busy flags,
+// stepGpu.ts:160, 402-405).
+struct Call {
+  Engine* e;
+  bool ok;
+  explicit Call(fl_engine* h) : e(h ? &h->e : nullptr), ok(false) {
+    if (!e) return;
+    int expected = 0;
+    ok = e->busy.compare_exchange_strong(expected, 1);
+    if (ok) cudaSetDevice(e->device);
+  }
+  ~Call() {
+    if (ok) e->busy.store(0);
+  }
+};
+
+#define ENTER(h)                                                                    \
+  if (!(h)) return fail(nullptr, FL_EINVAL, "null engine");                        \
+  Call call_(h);                                                                    \
+  Engine* e = call_.e;                                                              \
+  if (!call_.ok) return fail(e, FL_EBUSY, "engine call is not re-entrant");
+
+#define TRY(x)            \
+  do {                    \
+    int st_ = (x);        \
+    if (st_) return st_;  \
+  } while (0)
+
+int dalloc(Engine* e, void** p, size_t bytes, const char* what) {
+  cudaError_t err = cudaMalloc(p, bytes);
+  if (err != cudaSuccess) return cuda_status(e, err, what);
+  return cudaMemsetAsync(*p, 0, bytes, e->stream) == cudaSuccess ? FL_OK : cuda_status(e, cudaGetLastError(), what);
+}
+
+void free_all(Engine* e) {
+  cudaFree(e->u[0]);
+  cudaFree(e->u[1]);
+  cudaFree(e->v[0]);
+  cudaFree(e->v[1]);
+  cudaFree(e->u_hat);
+  cudaFree(e->v_hat);
+  cudaFree(e->dye[0]);
+  cudaFree(e->dye[1]);
+  cudaFree(e->dye_hat);
+  cudaFree(e->w);
+  cudaFree(e->fx);
+  cudaFree(e->fy);
+  cudaFree(e->patch);
+  cudaFree(e->sc);
+  cudaFree(e->acc);
+  cudaFree(e->time_dev);
+  cudaFree(e->staging);
+  if (!e->levels.empty()) cudaFree(e->levels[0].label);
+  mg_free(*e);
+  if (e->acc_host) cudaFreeHost(e->acc_host);
+  if (e->stream) cudaStreamDestroy(e->stream);
+}
+
+int validate_params(Engine* e, const fl_params* p) {
+  if (p->scheme != FL_SEMI_LAGRANGIAN && p->scheme != FL_MACCORMACK) return fail(e, FL_EINVAL, "scheme %d", p->scheme);
+  if (p->solver != FL_SOLVER_RBSOR && p->solver != FL_SOLVER_MG) return fail(e, FL_EINVAL, "solver %d", p->solver);
+  if (p->mg_pre < 0 || p->mg_pre > 4 || p->mg_post < 0 || p->mg_post > 4)
+    return fail(e, FL_EINVAL, "mg_pre/mg_post must be in [0, 4] (got %d, %d)", p->mg_pre, p->mg_post);
+  if (p->mg_coarse_sweeps < 0 || p->mg_max_cycles < 0 || p->pressure_iters < 0)
+    return fail(e, FL_EINVAL, "negative sweep or cycle count");
+  if (p->mg_coarsest < 1) return fail(e, FL_EINVAL, "mg_coarsest must be >= 1");
+  if (!(p->cfl_target > 0) || !(p->dt_max > 0) || !(p->rho > 0))
+    return fail(e, FL_EINVAL, "cfl_target, dt_max and rho must be positive");
+  return FL_OK;
+}
+
+// Host-side float32 evaluation of the step scalars (simulation.ts:477-479,
+// buoyancy.ts:80) for calls that are handed dt.
+StepScalars host_scalars(const Engine* e, float dt, float scale, float grad_scale, const double keep[3]) {
+  StepScalars s{};
+  s.dt = dt;
+  s.scale = scale;
+  s.grad_scale = grad_scale;
+  for (int c = 0; c < 3; c++) s.keep[c] = keep ? (float)keep[c] : 1.0f;
+  s.gain_beta = (float)e->prm.beta * dt;
+  s.gain_alpha = -(float)e->prm.alpha * dt;
+  s.half_dt = 0.5f * dt;
+  s.neg_scale = -scale;
+  return s;
+}
+
+int put_scalars(Engine* e, const StepScalars& s) {
+  return cuda_status(e, cudaMemcpy(e->sc, &s, sizeof s, cudaMemcpyHostToDevice), "scalars");
+}
+
+int upload(Engine* e, void* dst, const void* src, long n, int dtype, const char* what) {
+  if (!src) return fail(e, FL_EINVAL, "%s: null pointer", what);
+  if (dtype == FL_F32) return cuda_status(e, cudaMemcpyAsync(dst, src, n * sizeof(float), cudaMemcpyHostToDevice, e->stream), what);
+  if (dtype != FL_F64) return fail(e, FL_EINVAL, "%s: dtype %d", what, dtype);
+  TRY(cuda_status(e, cudaMemcpyAsync(e->staging, src, n * sizeof(double), cudaMemcpyHostToDevice, e->stream), what));
+  launch_convert(e->stream, e->staging, FL_F64, dst, FL_F32, n);
+  TRY(check_launch(e, what));
+  // the staging buffer is reused by the next conversion
+  return sync(e, what);
+}
+
+int download(Engine* e, void* dst, const float* src, long n, int dtype, const char* what) {
+  if (!dst) return fail(e, FL_EINVAL, "%s: null pointer", what);
+  if (dtype == FL_F32) return cuda_status(e, cudaMemcpyAsync(dst, src, n * sizeof(float), cudaMemcpyDeviceToHost, e->stream), what);
+  if (dtype != FL_F64) return fail(e, FL_EINVAL, "%s: dtype %d", what, dtype);
+  launch_convert(e->stream, src, FL_F32, e->staging, FL_F64, n);
+  TRY(check_launch(e, what));
+  TRY(cuda_status(e, cudaMemcpyAsync(dst, e->staging, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream), what));
+  return sync(e, what);
+}
+
+int up32(Engine* e, void* dst, const void* src, size_t bytes, const char* what) {
+  if (!src) return fail(e, FL_EINVAL, "%s: null pointer", what);
+  return cuda_status(e, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, e->stream), what);
+}
+int down32(Engine* e, void* dst, const void* src, size_t bytes, const char* what) {
+  if (!dst) return fail(e, FL_EINVAL, "%s: null pointer", what);
+  return cuda_status(e, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, e->stream), what);
+}
+
+int zero_solve_accum(Engine* e) {
+  return cuda_status(e, cudaMemsetAsync(e->acc, 0, 4 * sizeof(double), e->stream), "accumulators");
+}
+int zero_residual_accum(Engine* e) {
+  StepAccum* a = e->acc;
+  cudaError_t err = cudaMemsetAsync(&a->res_sq, 0, sizeof(double), e->stream);
+  if (err == cudaSuccess) err = cudaMemsetAsync(&a->n_res, 0, sizeof(unsigned long long), e->stream);
+  return cuda_status(e, err, "residual accumulators");
+}
+int read_accum(Engine* e) {
+  TRY(cuda_status(e, cudaMemcpyAsync(e->acc_host, e->acc, sizeof(StepAccum), cudaMemcpyDeviceToHost, e->stream), "read accumulators"));
+  return sync(e, "read accumulators");
+}
+
+double rms(double sq, unsigned long long n) { return n > 0 ? std::sqrt(sq / (double)n) : 0.0; }
+
+// fluidDivRms of a host array (pressure.ts:177-186), used where the reference
+// evaluates it on the host before the device solve (pressureGpu.ts:228,
+// multigridGpu.ts:323).
+double host_fluid_div_rms(const float* div, const uint8_t* label, long n) {
+  double s = 0;
+  long c = 0;
+  for (long k = 0; k < n; k++) {
+    if (label[k] != FLUID) continue;
+    s += (double)div[k] * (double)div[k];
+    c++;
+  }
+  return c > 0 ? std::sqrt(s / (double)c) : 0.0;
+}
+
+// Multigrid to tolerance on levels[0].b (pressureMultigrid.ts:284-319): the
+// warm start is levels[0].x[0]; b's fluid sums must already be in acc.
+int mg_solve_device(Engine* e, int max_cycles, double tol, int* cycles, double* relres) {
+  TRY(read_accum(e));
+  const double b_rms = rms(e->acc_host->b_sq, e->acc_host->n_fluid);
+  e->last_div_rms = b_rms;
+  *relres = -1;
+  *cycles = 0;
+  if (b_rms == 0) {
+    // p = 0 is the exact answer; a warm-started leftover would re-inject
+    // divergence (pressureMultigrid.ts:294-300).
+    TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].x[0], 0, e->cells() * sizeof(float), e->stream), "zero p"));
+    *relres = 0;
+    return FL_OK;
+  }
+  if (!std::isfinite(b_rms)) return fail(e, FL_ENONFINITE, "non-finite divergence");
+  for (int c = 0; c < max_cycles; c++) {
+    if (tol > 0) TRY(zero_residual_accum(e));
+    mg_vcycle(*e, tol > 0 ? e->acc : nullptr);
+    TRY(check_launch(e, "v-cycle"));
+    *cycles = c + 1;
+    if (tol > 0) {
+      TRY(read_accum(e));
+      const double rel = rms(e->acc_host->res_sq, e->acc_host->n_res) / b_rms;
+      *relres = rel;
+      if (!std::isfinite(rel)) return fail(e, FL_ENONFINITE, "non-finite residual after %d V-cycles", c + 1);
+      if (rel <= tol) break;
+    }
+  }
+  return FL_OK;
+}
+
+// Red-black SOR to tolerance (pressureRedBlack.ts:88-113) on div in
+// levels[0].b with the warm start in levels[0].x[0]. Sweep pairs are grouped
+// up to four per launch (temporal blocking) and never across a 12-sweep check.
+int rb_solve_device(Engine* e, float scale, int iterations, float omega, double tol, double div_rms, int* used) {
+  Level& L = e->levels[0];
+  *used = iterations;
+  const double target = tol > 0 ? tol * div_rms : -1;
+  int k = 0;
+  int src = 0;
+  while (k < iterations) {
+    int chunk = std::min(4, iterations - k);
+    if (target >= 0) chunk = std::min(chunk, 12 - (k % 12));
+    launch_rb_sweeps(e->stream, L.nx, L.ny, L.x[src], L.x[1 - src], L.b, L.code, scale, omega, chunk);
+    TRY(check_launch(e, "red-black sweeps"));
+    src = 1 - src;
+    k += chunk;
+    if (target >= 0 && k % 12 == 0) {
+      TRY(zero_residual_accum(e));
+      launch_rms_remaining(e->stream, L.nx, L.ny, L.x[src], L.b, L.code, scale, e->acc);
+      TRY(check_launch(e, "residual"));
+      TRY(read_accum(e));
+      const double r = rms(e->acc_host->res_sq, e->acc_host->n_res);
+      e->last_relres = div_rms > 0 ? r / div_rms : 0;
+      if (r <= target) {
+        *used = k;
+        break;
+      }
+    }
+  }
+  if (src == 1)
+    TRY(cuda_status(e, cudaMemcpyAsync(L.x[0], L.x[1], e->cells() * sizeof(float), cudaMemcpyDeviceToDevice, e->stream),
+                    "p copy"));
+  return FL_OK;
+}
+
+// One fused step. host_dt: scalars already in e->sc from the caller.
+int step_once(Engine* e, bool device_dt) {
+  cudaStream_t s = e->stream;
+  Level& L0 = e->levels[0];
+  if (e->labels_dirty) {
+    launch_commit_labels(s, e->nx, e->ny, L0.label, L0.x[0], e->u[e->cur], e->v[e->cur], e->dye[e->dcur],
+                         e->dye_cells());
+    mg_build_codes(*e);
+    TRY(check_launch(e, "commit labels"));
+    e->labels_dirty = false;
+  }
+  const int mac = e->prm.scheme == FL_MACCORMACK;
+  const int in = e->cur, out = 1 - e->cur;
+  launch_advect_velocity(s, e->nx, e->ny, e->h, mac, e->u[in], e->v[in], e->u_hat, e->v_hat, e->u[out], e->v[out],
+                         L0.label, e->sc);
+  TRY(check_launch(e, "advect velocity"));
+  e->cur = out;
+  float* u = e->u[e->cur];
+  float* v = e->v[e->cur];
+  if (e->stir_pending) {
+    launch_stir(s, e->nx, e->ny, e->h, u, v, L0.label, e->stir);
+    e->stir_pending = false;
+  }
+  const bool conf = e->prm.confinement != 0;
+  if (conf) {
+    launch_vorticity(s, e->nx, e->ny, e->h, u, v, e->w);
+    launch_confinement_force(s, e->nx, e->ny, e->h, e->w, L0.label, (float)e->prm.confinement, e->fx, e->fy);
+  }
+  const bool beta_on = e->prm.beta != 0, alpha_on = e->prm.alpha != 0;
+  if (beta_on || alpha_on || conf)
+    launch_forces(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, u, v, e->dye[e->dcur], L0.label, beta_on, alpha_on,
+                  conf, e->fx, e->fy, e->sc);
+  TRY(zero_solve_accum(e));
+  const bool mg = e->prm.solver == FL_SOLVER_MG;
+  launch_divergence(s, e->nx, e->ny, e->h, u, v, L0.b, mg, L0.label, e->sc, e->acc);
+  TRY(check_launch(e, "body forces / divergence"));
+
+  int iters = 0;
+  if (mg) {
+    double rr;
+    TRY(mg_solve_device(e, e->prm.mg_max_cycles, e->prm.tol, &iters, &rr));
+    e->last_relres = rr;
+  } else {
+    TRY(read_accum(e));
+    const double div_rms = rms(e->acc_host->b_sq, e->acc_host->n_fluid);
+    e->last_div_rms = div_rms;
+    StepScalars hs;
+    TRY(cuda_status(e, cudaMemcpy(&hs, e->sc, sizeof hs, cudaMemcpyDeviceToHost), "read scalars"));
+    if (div_rms == 0) {
+      TRY(cuda_status(e, cudaMemsetAsync(L0.x[0], 0, e->cells() * sizeof(float), s), "zero p"));
+    } else {
+      TRY(rb_solve_device(e, hs.scale, e->prm.pressure_iters, (float)e->prm.omega, e->prm.tol, div_rms, &iters));
+    }
+  }
+  e->last_iters = iters;
+  launch_subtract_outflow(s, e->nx, e->ny, L0.x[0], u, v, L0.label, e->sc, true, true);
+  const int din = e->dcur, dout = 1 - e->dcur;
+  launch_advect_dye(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, mac, u, v, e->dye[din], e->dye_hat, e->dye[dout],
+                    L0.label, e->sc, true, e->patch, e->pi0, e->pj0, e->pnx, e->pny);
+  e->dcur = dout;
+  launch_max_speed(s, e->nx, e->ny, u, v, e->acc, e->sc, e->time_dev, &e->prm, e->h, device_dt, device_dt);
+  TRY(check_launch(e, "project / dye / CFL"));
+  e->steps++;
+  return FL_OK;
+}
+
+}  // namespace
+
+// ====================================================================== ABI
+
+extern "C" {
+
+void fl_default_params(fl_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof *p);
+  p->cfl_target = 2.0;
+  p->dt_max = 1.0 / 30.0;
+  p->rho = 1.0;
+  p->scheme = FL_SEMI_LAGRANGIAN;
+  p->solver = FL_SOLVER_MG;
+  p->pressure_iters = 100;
+  p->mg_max_cycles = 3;
+  p->omega = 1.9;
+  p->tol = 5e-3;
+  p->mg_pre = 2;
+  p->mg_post = 2;
+  p->mg_coarse_sweeps = 8;
+  p->mg_coarsest = 4;
+  p->mg_omega = 1.0;
+}
+
+int fl_abi_version(void) { return FL_ABI_VERSION; }
+
+const char* fl_last_error(const fl_engine* h) { return h ? h->e.err.c_str() : g_create_error.c_str(); }
+
+int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, int device, fl_engine** out) {
+  if (!out) return fail(nullptr, FL_EINVAL, "null output pointer");
+  *out = nullptr;
+  if (nx < 2 || ny < 2 || nx > 32768 || ny > 32768) return fail(nullptr, FL_EINVAL, "grid %dx%d out of range", nx, ny);
+  if (!(h > 0)) return fail(nullptr, FL_EINVAL, "cell size must be positive");
+  if (dye_scale < 1 || dye_scale > 8) return fail(nullptr, FL_EINVAL, "dye_scale %d out of [1, 8]", dye_scale);
+  int ndev = 0;
+  cudaError_t err = cudaGetDeviceCount(&ndev);
+  if (err != cudaSuccess || ndev == 0)
+    return fail(nullptr, FL_EDEVICE, "no CUDA device (%s)", err != cudaSuccess ? cudaGetErrorString(err) : "count 0");
+  if (device < 0 || device >= ndev) return fail(nullptr, FL_EINVAL, "device %d of %d", device, ndev);
+  if (cudaSetDevice(device) != cudaSuccess) return fail(nullptr, FL_EDEVICE, "cudaSetDevice(%d) failed", device);
+
+  fl_engine* H = new (std::nothrow) fl_engine();
+  if (!H) return fail(nullptr, FL_ENOMEM, "host allocation");
+  Engine* e = &H->e;
+  e->device = device;
+  e->nx = nx;
+  e->ny = ny;
+  e->dye_scale = dye_scale;
+  e->dnx = nx * dye_scale;
+  e->dny = ny * dye_scale;
+  e->h = (float)h;
+  e->dh = (float)(h / dye_scale);
+  if (params) e->prm = *params; else fl_default_params(&e->prm);
+  int st = validate_params(e, &e->prm);
+  if (st) {
+    g_create_error = e->err;
+    delete H;
+    return st;
+  }
+  auto bail = [&](int code) {
+    g_create_error = e->err;
+    free_all(e);
+    delete H;
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    fail(e, FL_EDEVICE, "stream creation failed");
+    return bail(FL_EDEVICE);
+  }
+  const size_t uf = (size_t)e->ufaces() * 4, vf = (size_t)e->vfaces() * 4, cf = (size_t)e->cells() * 4;
+  const size_t df = (size_t)3 * e->dye_cells() * 4;
+  e->staging_bytes = 2 * std::max(std::max(uf, vf), df);
+  int s = FL_OK;
+  s = s ? s : dalloc(e, (void**)&e->u[0], uf, "u");
+  s = s ? s : dalloc(e, (void**)&e->u[1], uf, "u");
+  s = s ? s : dalloc(e, (void**)&e->v[0], vf, "v");
+  s = s ? s : dalloc(e, (void**)&e->v[1], vf, "v");
+  s = s ? s : dalloc(e, (void**)&e->u_hat, uf, "u_hat");
+  s = s ? s : dalloc(e, (void**)&e->v_hat, vf, "v_hat");
+  s = s ? s : dalloc(e, (void**)&e->dye[0], df, "dye");
+  s = s ? s : dalloc(e, (void**)&e->dye[1], df, "dye");
+  s = s ? s : dalloc(e, (void**)&e->dye_hat, df, "dye_hat");
+  s = s ? s : dalloc(e, (void**)&e->w, cf, "vorticity");
+  s = s ? s : dalloc(e, (void**)&e->fx, cf, "force");
+  s = s ? s : dalloc(e, (void**)&e->fy, cf, "force");
+  s = s ? s : dalloc(e, (void**)&e->sc, sizeof(StepScalars), "scalars");
+  s = s ? s : dalloc(e, (void**)&e->acc, sizeof(StepAccum), "accumulators");
+  s = s ? s : dalloc(e, (void**)&e->time_dev, sizeof(double), "clock");
+  s = s ? s : dalloc(e, &e->staging, e->staging_bytes, "staging");
+  if (s) return bail(s);
+  if (cudaMallocHost(&e->acc_host, sizeof(StepAccum)) != cudaSuccess) {
+    fail(e, FL_ENOMEM, "pinned accumulator");
+    return bail(FL_ENOMEM);
+  }
+  mg_setup(*e);
+  uint8_t* label0 = nullptr;
+  if (cuda_status(e, cudaGetLastError(), "multigrid levels")) return bail(FL_ENOMEM);
+  s = dalloc(e, (void**)&label0, (size_t)e->cells(), "label");
+  if (s) return bail(s);
+  e->levels[0].label = label0;
+  if (sync(e, "create")) return bail(FL_EDEVICE);
+  *out = H;
+  return FL_OK;
+}
+
+int fl_destroy(fl_engine* h) {
+  if (!h) return FL_OK;
+  cudaSetDevice(h->e.device);
+  cudaStreamSynchronize(h->e.stream);
+  free_all(&h->e);
+  delete h;
+  return FL_OK;
+}
+
+int fl_set_params(fl_engine* h, const fl_params* p) {
+  ENTER(h);
+  if (!p) return fail(e, FL_EINVAL, "null params");
+  TRY(validate_params(e, p));
+  const bool reshape = p->mg_coarsest != e->prm.mg_coarsest;
+  e->prm = *p;
+  if (reshape) {
+    uint8_t* label0 = e->levels[0].label;
+    float* p0 = nullptr;
+    TRY(dalloc(e, (void**)&p0, (size_t)e->cells() * 4, "p"));
+    cudaMemcpyAsync(p0, e->levels[0].x[0], (size_t)e->cells() * 4, cudaMemcpyDeviceToDevice, e->stream);
+    TRY(sync(e, "set params"));
+    e->levels[0].label = nullptr;
+    mg_setup(*e);
+    e->levels[0].label = label0;
+    cudaMemcpyAsync(e->levels[0].x[0], p0, (size_t)e->cells() * 4, cudaMemcpyDeviceToDevice, e->stream);
+    TRY(sync(e, "set params"));
+    cudaFree(p0);
+    mg_build_codes(*e);
+  }
+  // the CFL scalars depend on cfl_target / dt_max / decay / weights
+  if (e->uploaded) {
+    launch_max_speed(e->stream, e->nx, e->ny, e->u[e->cur], e->v[e->cur], e->acc, e->sc, e->time_dev, &e->prm, e->h,
+                     true, false);
+  }
+  return sync(e, "set params");
+}
+
+void* fl_stream(fl_engine* h) { return h ? (void*)h->e.stream : nullptr; }
+
+int fl_synchronize(fl_engine* h) {
+  ENTER(h);
+  return sync(e, "synchronize");
+}
+
+int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
+                     const void* dye) {
+  ENTER(h);
+  e->cur = 0;
+  e->dcur = 0;
+  TRY(upload(e, e->u[0], u, e->ufaces(), dtype, "upload u"));
+  TRY(upload(e, e->v[0], v, e->vfaces(), dtype, "upload v"));
+  if (p)
+    TRY(upload(e, e->levels[0].x[0], p, e->cells(), dtype, "upload p"));
+  else
+    TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].x[0], 0, e->cells() * 4, e->stream), "zero p"));
+  TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "upload label"));
+  TRY(upload(e, e->dye[0], dye, 3 * e->dye_cells(), dtype, "upload dye"));
+  mg_build_codes(*e);
+  TRY(cuda_status(e, cudaMemsetAsync(e->time_dev, 0, sizeof(double), e->stream), "clock"));
+  launch_max_speed(e->stream, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);
+  TRY(sync(e, "upload"));
+  e->uploaded = true;
+  e->labels_dirty = false;
+  e->steps = 0;
+  e->time = 0;
+  return FL_OK;
+}
+
+int fl_set_labels(fl_engine* h, const uint8_t* label) {
+  ENTER(h);
+  TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "upload label"));
+  e->labels_dirty = true;
+  return sync(e, "set labels");
+}
+
+int fl_set_dye_patch(fl_engine* h, int i0, int j0, int pnx, int pny, const float* data) {
+  ENTER(h);
+  cudaFree(e->patch);
+  e->patch = nullptr;
+  e->pnx = e->pny = 0;
+  if (!data) return FL_OK;
+  if (pnx <= 0 || pny <= 0) return fail(e, FL_EINVAL, "patch %dx%d", pnx, pny);
+  const size_t bytes = (size_t)4 * pnx * pny * sizeof(float);
+  TRY(dalloc(e, (void**)&e->patch, bytes, "patch"));
+  TRY(up32(e, e->patch, data, bytes, "upload patch"));
+  e->pi0 = i0;
+  e->pj0 = j0;
+  e->pnx = pnx;
+  e->pny = pny;
+  return sync(e, "set patch");
+}
+
+int fl_set_buoyancy(fl_engine* h, double beta, double alpha) {
+  ENTER(h);
+  e->prm.beta = beta;
+  e->prm.alpha = alpha;
+  if (e->uploaded)
+    launch_max_speed(e->stream, e->nx, e->ny, e->u[e->cur], e->v[e->cur], e->acc, e->sc, e->time_dev, &e->prm, e->h,
+                     true, false);
+  return sync(e, "set buoyancy");
+}
+
+int fl_set_confinement(fl_engine* h, double eps) {
+  ENTER(h);
+  e->prm.confinement = eps;
+  return FL_OK;
+}
+
+int fl_set_stir(fl_engine* h, const double* st) {
+  ENTER(h);
+  e->stir_pending = st != nullptr;
+  if (st)
+    for (int k = 0; k < 5; k++) e->stir[k] = (float)st[k];
+  return FL_OK;
+}
+
+int fl_step(fl_engine* h, double dt, double scale, double grad_scale, const double keep[3], int* iters) {
+  ENTER(h);
+  if (!e->uploaded) return fail(e, FL_ESTATE, "step before fl_upload_fields");
+  if (!(dt > 0)) return fail(e, FL_EINVAL, "dt must be positive");
+  TRY(put_scalars(e, host_scalars(e, (float)dt, (float)scale, (float)grad_scale, keep)));
+  TRY(step_once(e, false));
+  e->time += dt;
+  if (iters) *iters = e->last_iters;
+  return sync(e, "step");
+}
+
+int fl_step_auto(fl_engine* h, int nsteps, int* iters_last) {
+  ENTER(h);
+  if (!e->uploaded) return fail(e, FL_ESTATE, "step before fl_upload_fields");
+  if (nsteps < 0) return fail(e, FL_EINVAL, "nsteps < 0");
+  for (int n = 0; n < nsteps; n++) TRY(step_once(e, true));
+  if (iters_last) *iters_last = e->last_iters;
+  return check_launch(e, "step");
+}
+
+int fl_get_stats(fl_engine* h, fl_stats* out) {
+  ENTER(h);
+  if (!out) return fail(e, FL_EINVAL, "null stats");
+  StepScalars s;
+  double t = 0;
+  TRY(sync(e, "stats"));
+  TRY(cuda_status(e, cudaMemcpy(&s, e->sc, sizeof s, cudaMemcpyDeviceToHost), "stats"));
+  TRY(cuda_status(e, cudaMemcpy(&t, e->time_dev, sizeof t, cudaMemcpyDeviceToHost), "stats"));
+  TRY(read_accum(e));
+  std::memset(out, 0, sizeof *out);
+  out->dt = s.dt;
+  out->scale = s.scale;
+  out->grad_scale = s.grad_scale;
+  out->time = e->time > 0 ? e->time : t;
+  out->cycles = e->last_iters;
+  out->steps = e->steps;
+  out->rel_residual = e->last_relres;
+  out->div_rms = e->last_div_rms;
+  unsigned int bits = e->acc_host->last_max_bits;
+  float m;
+  std::memcpy(&m, &bits, 4);
+  out->max_face_speed = m;
+  return FL_OK;
+}
+
+int fl_read_velocity(fl_engine* h, int dtype, void* u, void* v) {
+  ENTER(h);
+  TRY(download(e, u, e->u[e->cur], e->ufaces(), dtype, "read u"));
+  TRY(download(e, v, e->v[e->cur], e->vfaces(), dtype, "read v"));
+  return sync(e, "read velocity");
+}
+
+int fl_read_dye(fl_engine* h, int dtype, void* dye) {
+  ENTER(h);
+  TRY(download(e, dye, e->dye[e->dcur], 3 * e->dye_cells(), dtype, "read dye"));
+  return sync(e, "read dye");
+}
+
+int fl_read_pressure(fl_engine* h, int dtype, void* p) {
+  ENTER(h);
+  TRY(download(e, p, e->levels[0].x[0], e->cells(), dtype, "read p"));
+  return sync(e, "read pressure");
+}
+
+// ----------------------------------------------------------- Advector seam
+
+int fl_advect_velocity(fl_engine* h, int scheme, const float* u_in, const float* v_in, float* u_out, float* v_out,
+                       const uint8_t* label, float dt) {
+  ENTER(h);
+  e->uploaded = false;
+  TRY(up32(e, e->u[0], u_in, e->ufaces() * 4, "u"));
+  TRY(up32(e, e->v[0], v_in, e->vfaces() * 4, "v"));
+  TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "label"));
+  TRY(put_scalars(e, host_scalars(e, dt, 0, 0, nullptr)));
+  launch_advect_velocity(e->stream, e->nx, e->ny, e->h, scheme == FL_MACCORMACK, e->u[0], e->v[0], e->u_hat,
+                         e->v_hat, e->u[1], e->v[1], e->levels[0].label, e->sc);
+  TRY(check_launch(e, "advect velocity"));
+  TRY(down32(e, u_out, e->u[1], e->ufaces() * 4, "u"));
+  TRY(down32(e, v_out, e->v[1], e->vfaces() * 4, "v"));
+  return sync(e, "advect velocity");
+}
+
+int fl_advect_dye(fl_engine* h, int scheme, const float* u, const float* v, const float* q_in, float* q_out,
+                  const uint8_t* label, float dt) {
+  ENTER(h);
+  e->uploaded = false;
+  TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
+  TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
+  TRY(up32(e, e->dye[0], q_in, 3 * e->dye_cells() * 4, "dye"));
+  TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "label"));
+  TRY(put_scalars(e, host_scalars(e, dt, 0, 0, nullptr)));
+  launch_advect_dye(e->stream, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, scheme == FL_MACCORMACK, e->u[0], e->v[0],
+                    e->dye[0], e->dye_hat, e->dye[1], e->levels[0].label, e->sc, false, nullptr, 0, 0, 0, 0);
+  TRY(check_launch(e, "advect dye"));
+  TRY(down32(e, q_out, e->dye[1], 3 * e->dye_cells() * 4, "dye"));
+  return sync(e, "advect dye");
+}
+
+// ------------------------------------------------------ PressureSolver seam
+
+int fl_rb_solve(fl_engine* h, float* p, const float* div, const uint8_t* label, float scale, int iterations,
+                float omega, double tol, int* used) {
+  ENTER(h);
+  e->uploaded = false;
+  if (!p || !div || !label) return fail(e, FL_EINVAL, "null pointer");
+  const long n = e->cells();
+  // pressureRedBlack.ts:335-339 — zero divergence: p = 0, no sweeps.
+  const double div_rms = host_fluid_div_rms(div, label, n);
+  if (used) *used = 0;
+  if (div_rms == 0) {
+    std::memset(p, 0, n * sizeof(float));
+    return FL_OK;
+  }
+  if (iterations <= 0) return FL_OK;
+  Level& L = e->levels[0];
+  TRY(up32(e, L.x[0], p, n * 4, "p"));
+  TRY(up32(e, L.b, div, n * 4, "div"));
+  TRY(up32(e, L.label, label, (size_t)n, "label"));
+  launch_build_codes(e->stream, L.nx, L.ny, L.label, L.code);
+  e->codes_valid = false;
+  int u = 0;
+  TRY(rb_solve_device(e, scale, iterations, omega, tol, div_rms, &u));
+  if (used) *used = u;
+  TRY(down32(e, p, L.x[0], n * 4, "p"));
+  return sync(e, "rb solve");
+}
+
+int fl_mg_solve(fl_engine* h, float* p, const float* div, const uint8_t* label, float scale, int max_cycles,
+                double tol, int* cycles_used, double* rel_residual) {
+  ENTER(h);
+  e->uploaded = false;
+  if (!p || !div || !label) return fail(e, FL_EINVAL, "null pointer");
+  const long n = e->cells();
+  Level& L = e->levels[0];
+  TRY(up32(e, L.x[0], p, n * 4, "p"));
+  TRY(up32(e, e->u_hat, div, n * 4, "div"));  // u_hat is free scratch of >= n floats here
+  TRY(up32(e, L.label, label, (size_t)n, "label"));
+  mg_build_codes(*e);
+  TRY(zero_solve_accum(e));
+  launch_scale_rhs(e->stream, n, e->u_hat, L.b, -scale, L.label, e->acc);
+  TRY(check_launch(e, "rhs"));
+  int cycles = 0;
+  double rr = -1;
+  TRY(mg_solve_device(e, max_cycles, tol, &cycles, &rr));
+  if (cycles_used) *cycles_used = cycles;
+  if (rel_residual) *rel_residual = rr;
+  TRY(down32(e, p, L.x[0], n * 4, "p"));
+  return sync(e, "mg solve");
+}
+
+// ------------------------------------------------------------ single passes
+
+int fl_divergence(fl_engine* h, const float* u, const float* v, float* div) {
+  ENTER(h);
+  e->uploaded = false;
+  TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
+  TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
+  launch_divergence(e->stream, e->nx, e->ny, e->h, e->u[0], e->v[0], e->levels[0].b, false, nullptr, e->sc, nullptr);
+  TRY(check_launch(e, "divergence"));
+  TRY(down32(e, div, e->levels[0].b, e->cells() * 4, "div"));
+  return sync(e, "divergence");
+}
+
+int fl_rb_sweep(fl_engine* h, float* p, const float* div, const uint8_t* label, float scale, float omega, int color) {
+  ENTER(h);
+  e->uploaded = false;
+  if (color != 0 && color != 1) return fail(e, FL_EINVAL, "color %d", color);
+  Level& L = e->levels[0];
+  const long n = e->cells();
+  TRY(up32(e, L.x[0], p, n * 4, "p"));
+  TRY(up32(e, L.b, div, n * 4, "div"));
+  TRY(up32(e, L.label, label, (size_t)n, "label"));
+  launch_build_codes(e->stream, L.nx, L.ny, L.label, L.code);
+  e->codes_valid = false;
+  launch_rb_halfsweep(e->stream, L.nx, L.ny, L.x[0], L.b, L.code, scale, omega, color);
+  TRY(check_launch(e, "rb sweep"));
+  TRY(down32(e, p, L.x[0], n * 4, "p"));
+  return sync(e, "rb sweep");
+}
+
+int fl_subtract_gradient(fl_engine* h, const float* p, float* u, float* v, const uint8_t* label, float grad_scale) {
+  ENTER(h);
+  e->uploaded = false;
+  Level& L = e->levels[0];
+  TRY(up32(e, L.x[0], p, e->cells() * 4, "p"));
+  TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
+  TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
+  TRY(up32(e, L.label, label, (size_t)e->cells(), "label"));
+  TRY(put_scalars(e, host_scalars(e, 1.0f, 1.0f, grad_scale, nullptr)));
+  launch_subtract_outflow(e->stream, e->nx, e->ny, L.x[0], e->u[0], e->v[0], L.label, e->sc, true, false);
+  TRY(check_launch(e, "subtract gradient"));
+  TRY(down32(e, u, e->u[0], e->ufaces() * 4, "u"));
+  TRY(down32(e, v, e->v[0], e->vfaces() * 4, "v"));
+  return sync(e, "subtract gradient");
+}
+
+int fl_outflow(fl_engine* h, float* u, float* v, const uint8_t* label) {
+  ENTER(h);
+  e->uploaded = false;
+  Level& L = e->levels[0];
+  TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
+  TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
+  TRY(up32(e, L.label, label, (size_t)e->cells(), "label"));
+  launch_subtract_outflow(e->stream, e->nx, e->ny, L.x[0], e->u[0], e->v[0], L.label, e->sc, false, true);
+  TRY(check_launch(e, "outflow"));
+  TRY(down32(e, u, e->u[0], e->ufaces() * 4, "u"));
+  TRY(down32(e, v, e->v[0], e->vfaces() * 4, "v"));
+  return sync(e, "outflow");
+}
+
+int fl_commit_labels(fl_engine* h, float* p, float* u, float* v, float* dye, const uint8_t* label) {
+  ENTER(h);
+  e->uploaded = false;
+  Level& L = e->levels[0];
+  TRY(up32(e, L.x[0], p, e->cells() * 4, "p"));
+  TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
+  TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
+  TRY(up32(e, e->dye[0], dye, 3 * e->dye_cells() * 4, "dye"));
+  TRY(up32(e, L.label, label, (size_t)e->cells(), "label"));
+  launch_commit_labels(e->stream, e->nx, e->ny, L.label, L.x[0], e->u[0], e->v[0], e->dye[0], e->dye_cells());
+  TRY(check_launch(e, "commit labels"));
+  TRY(down32(e, p, L.x[0], e->cells() * 4, "p"));
+  TRY(down32(e, u, e->u[0], e->ufaces() * 4, "u"));
+  TRY(down32(e, v, e->v[0], e->vfaces() * 4, "v"));
+  TRY(down32(e, dye, e->dye[0], 3 * e->dye_cells() * 4, "dye"));
+  return sync(e, "commit labels");
+}
+
+int fl_body_forces(fl_engine* h, float* u, float* v, const float* dye, const uint8_t* label, float beta, float alpha,
+                   float eps, float dt) {
+  ENTER(h);
+  e->uploaded = false;
+  Level& L = e->levels[0];
+  TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
+  TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
+  TRY(up32(e, e->dye[0], dye, 3 * e->dye_cells() * 4, "dye"));
+  TRY(up32(e, L.label, label, (size_t)e->cells(), "label"));
+  StepScalars s{};
+  s.dt = dt;
+  s.gain_beta = beta * dt;
+  s.gain_alpha = -alpha * dt;
+  s.half_dt = 0.5f * dt;
+  TRY(put_scalars(e, s));
+  const bool conf = eps != 0.0f;
+  if (conf) {
+    launch_vorticity(e->stream, e->nx, e->ny, e->h, e->u[0], e->v[0], e->w);
+    launch_confinement_force(e->stream, e->nx, e->ny, e->h, e->w, L.label, eps, e->fx, e->fy);
+  }
+  if (beta != 0.0f || alpha != 0.0f || conf)
+    launch_forces(e->stream, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, e->u[0], e->v[0], e->dye[0], L.label,
+                  beta != 0.0f, alpha != 0.0f, conf, e->fx, e->fy, e->sc);
+  TRY(check_launch(e, "body forces"));
+  TRY(down32(e, u, e->u[0], e->ufaces() * 4, "u"));
+  TRY(down32(e, v, e->v[0], e->vfaces() * 4, "v"));
+  return sync(e, "body forces");
+}
+
+int fl_stir(fl_engine* h, float* u, float* v, const uint8_t* label, float x, float y, float r, float dx, float dy) {
+  ENTER(h);
+  e->uploaded = false;
+  Level& L = e->levels[0];
+  TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
+  TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
+  TRY(up32(e, L.label, label, (size_t)e->cells(), "label"));
+  const float st[5] = {x, y, r, dx, dy};
+  launch_stir(e->stream, e->nx, e->ny, e->h, e->u[0], e->v[0], L.label, st);
+  TRY(check_launch(e, "stir"));
+  TRY(down32(e, u, e->u[0], e->ufaces() * 4, "u"));
+  TRY(down32(e, v, e->v[0], e->vfaces() * 4, "v"));
+  return sync(e, "stir");
+}
+
+int fl_dye_patch(fl_engine* h, float* dye, int i0, int j0, int pnx, int pny, const float* data) {
+  ENTER(h);
+  e->uploaded = false;
+  if (!data || pnx <= 0 || pny <= 0) return fail(e, FL_EINVAL, "patch");
+  const size_t pbytes = (size_t)4 * pnx * pny * sizeof(float);
+  if (pbytes > e->staging_bytes) return fail(e, FL_EINVAL, "patch larger than the staging buffer");
+  TRY(up32(e, e->dye[0], dye, 3 * e->dye_cells() * 4, "dye"));
+  TRY(up32(e, e->staging, data, pbytes, "patch"));
+  launch_dye_patch(e->stream, e->dnx, e->dny, e->dye[0], (const float*)e->staging, i0, j0, pnx, pny);
+  TRY(check_launch(e, "dye patch"));
+  TRY(down32(e, dye, e->dye[0], 3 * e->dye_cells() * 4, "dye"));
+  return sync(e, "dye patch");
+}
+
+}  // extern "C"

@@ -1,0 +1,136 @@
+// Host-side internals shared by the engine's translation units: the engine
+// object behind fl_engine* and the kernel launchers each .cu file provides.
+#pragma once
+
+#include <atomic>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/flowlab_gb300.h"
+#include "fl_common.cuh"
+
+namespace fl {
+
+// One multigrid level (pressureMultigrid.ts:211-217). x is double-buffered so
+// the temporally blocked smoother can read the pre-sweep values of its halo
+// while neighbouring tiles write their results.
+struct Level {
+  int nx = 0, ny = 0;
+  float* x[2] = {nullptr, nullptr};
+  float* b = nullptr;
+  uint8_t* label = nullptr;
+  uint8_t* code = nullptr;
+};
+
+struct Engine {
+  int device = 0;
+  int nx = 0, ny = 0, dnx = 0, dny = 0, dye_scale = 1;
+  float h = 0, dh = 0;
+  fl_params prm{};
+  cudaStream_t stream = nullptr;
+  std::atomic<int> busy{0};
+  std::string err;
+
+  // velocity: u[cur]/v[cur] is the field; the other is the advection target
+  float* u[2] = {nullptr, nullptr};
+  float* v[2] = {nullptr, nullptr};
+  float* u_hat = nullptr;
+  float* v_hat = nullptr;
+  int cur = 0;
+  // dye: 3 planes of dnx*dny each
+  float* dye[2] = {nullptr, nullptr};
+  float* dye_hat = nullptr;
+  int dcur = 0;
+
+  std::vector<Level> levels;  // levels[0].x[0] is the resident pressure
+  int coarse_level = 0;       // first level solved inside the single-CTA kernel
+  size_t coarse_smem = 0;
+
+  float* w = nullptr;   // vorticity scratch
+  float* fx = nullptr;  // confinement force scratch
+  float* fy = nullptr;
+
+  float* patch = nullptr;
+  int pi0 = 0, pj0 = 0, pnx = 0, pny = 0;
+  bool stir_pending = false;
+  float stir[5] = {0, 0, 0, 0, 0};
+
+  StepScalars* sc = nullptr;   // device
+  StepAccum* acc = nullptr;    // device
+  StepAccum* acc_host = nullptr;  // pinned mirror
+  double* time_dev = nullptr;  // device-accumulated sim time
+
+  // staging for dtype conversion and the per-pass entry points
+  void* staging = nullptr;
+  size_t staging_bytes = 0;
+
+  bool uploaded = false;
+  bool labels_dirty = false;
+  bool codes_valid = false;
+
+  // report
+  double time = 0;
+  int steps = 0;
+  int last_iters = 0;
+  double last_relres = -1;
+  double last_div_rms = 0;
+  double last_dt = 0, last_scale = 0, last_grad_scale = 0;
+
+  long cells() const { return (long)nx * ny; }
+  long ufaces() const { return (long)(nx + 1) * ny; }
+  long vfaces() const { return (long)nx * (ny + 1); }
+  long dye_cells() const { return (long)dnx * dny; }
+};
+
+// ------------------------------------------------------------- launchers
+
+// fl_advect.cu
+void launch_advect_velocity(cudaStream_t s, int nx, int ny, float h, int mac, const float* u_in, const float* v_in,
+                            float* u_hat, float* v_hat, float* u_out, float* v_out, const uint8_t* label,
+                            const StepScalars* sc);
+void launch_advect_dye(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, int mac, const float* u,
+                       const float* v, const float* q_in, float* q_hat, float* q_out, const uint8_t* label,
+                       const StepScalars* sc, bool tail, const float* patch, int pi0, int pj0, int pnx, int pny);
+
+// fl_project.cu
+void launch_vorticity(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* w);
+void launch_confinement_force(cudaStream_t s, int nx, int ny, float h, const float* w, const uint8_t* label,
+                              float eps, float* fx, float* fy);
+void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, float* u, float* v,
+                   const float* dye, const uint8_t* label, bool beta_on, bool alpha_on, bool conf_on,
+                   const float* fx, const float* fy, const StepScalars* sc);
+void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
+                       bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc);
+void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
+                             const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow);
+void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const float* v, StepAccum* acc,
+                      StepScalars* sc_next, double* time_dev, const fl_params* prm, float h, bool write_scalars,
+                      bool add_time);
+// b = (-scale)*div (b may be null: only accumulate div^2) with fluid sums.
+void launch_scale_rhs(cudaStream_t s, long n, const float* div, float* b, float neg_scale, const uint8_t* label,
+                      StepAccum* acc);
+void launch_commit_labels(cudaStream_t s, int nx, int ny, const uint8_t* label, float* p, float* u, float* v,
+                          float* dye, long dye_cells);
+void launch_stir(cudaStream_t s, int nx, int ny, float h, float* u, float* v, const uint8_t* label,
+                 const float* stir5);
+void launch_dye_patch(cudaStream_t s, int dnx, int dny, float* dye, const float* patch, int pi0, int pj0, int pnx,
+                      int pny);
+void launch_convert(cudaStream_t s, const void* src, int src_dtype, void* dst, int dst_dtype, long n);
+
+// fl_multigrid.cu
+void mg_setup(Engine& e);  // allocates levels for e.nx, e.ny and the coarsest size
+void mg_free(Engine& e);
+void mg_build_codes(Engine& e);  // label chain + stencil codes from levels[0].label
+void mg_vcycle(Engine& e, StepAccum* acc_for_residual);
+void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* x_out, const float* b,
+                      const uint8_t* code, float scale, float omega, int pairs);
+void launch_rms_remaining(cudaStream_t s, int nx, int ny, const float* p, const float* div, const uint8_t* code,
+                          float scale, StepAccum* acc);
+void launch_build_codes(cudaStream_t s, int nx, int ny, const uint8_t* label, uint8_t* code);
+void launch_rb_halfsweep(cudaStream_t s, int nx, int ny, float* p, const float* b, const uint8_t* code,
+                         float scale, float omega, int color);
+
+}  // namespace fl

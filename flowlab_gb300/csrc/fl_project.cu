@@ -1,0 +1,430 @@
+// The projection's glue passes (src/core/divergence.ts, subtractGradient.ts,
+// boundaries.ts, buoyancy.ts, stir.ts, dye.ts, vorticity.ts; WGSL twin
+// src/gpu/project.wgsl) plus the NEW vorticity confinement and the device-
+// side CFL reduction that sets the next step's dt.
+#include <cmath>
+
+#include "fl_internal.h"
+
+namespace fl {
+
+// vorticity.ts:9-14
+__device__ __forceinline__ float curl_at_corner(const float* __restrict__ u, const float* __restrict__ v, int nx,
+                                                float h, int i, int j) {
+  return (v[i + (long)j * nx] - v[(i - 1) + (long)j * nx]) / h -
+         (u[i + (long)j * (nx + 1)] - u[i + (long)(j - 1) * (nx + 1)]) / h;
+}
+
+// vorticity.ts:24-42 — corner curls averaged to the centre, clamped at walls.
+__global__ void k_vorticity(int nx, int ny, float h, const float* __restrict__ u, const float* __restrict__ v,
+                            float* __restrict__ w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const int hiI = nx - 1, hiJ = ny - 1;
+  const int j0 = min(max(j, 1), hiJ), j1 = min(max(j + 1, 1), hiJ);
+  const int i0 = min(max(i, 1), hiI), i1 = min(max(i + 1, 1), hiI);
+  w[i + (long)j * nx] = 0.25f * (curl_at_corner(u, v, nx, h, i0, j0) + curl_at_corner(u, v, nx, h, i1, j0) +
+                                 curl_at_corner(u, v, nx, h, i0, j1) + curl_at_corner(u, v, nx, h, i1, j1));
+}
+
+// NEW — vorticity confinement force at cell centres (Fedkiw, Stam & Jensen
+// 2001): N = grad|w| / (|grad|w|| + 1e-20), f = eps*h * (N_y w, -N_x w),
+// zero in solid cells. Centred differences, one-sided at the walls.
+__global__ void k_confinement_force(int nx, int ny, float h, const float* __restrict__ w,
+                                    const uint8_t* __restrict__ label, float epsh, float* __restrict__ fx,
+                                    float* __restrict__ fy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const long k = i + (long)j * nx;
+  if (label[k] == SOLID) {
+    fx[k] = 0.0f;
+    fy[k] = 0.0f;
+    return;
+  }
+  const int ie = min(i + 1, nx - 1), iw = max(i - 1, 0);
+  const int jn = min(j + 1, ny - 1), js = max(j - 1, 0);
+  const float gx = (fabsf(w[ie + (long)j * nx]) - fabsf(w[iw + (long)j * nx])) / ((float)(ie - iw) * h);
+  const float gy = (fabsf(w[i + (long)jn * nx]) - fabsf(w[i + (long)js * nx])) / ((float)(jn - js) * h);
+  const float mag = sqrtf(gx * gx + gy * gy) + 1e-20f;
+  const float Nx = gx / mag, Ny = gy / mag;
+  const float wk = w[k];
+  fx[k] = epsh * (Ny * wk);
+  fy[k] = epsh * (-(Nx * wk));
+}
+
+// Body forces on the faces they may write (buoyancy.ts:70-88 bounds for v,
+// stir.ts:49-83 bounds for u): v += (beta*dt)*T + (-alpha*dt)*s, then the
+// confinement face average. One thread per (u face, v face) pair, in place:
+// every write depends only on the thread's own face.
+__global__ void __launch_bounds__(256) k_forces(int nx, int ny, float h, int dnx, int dny, float dh,
+                                                float* __restrict__ u, float* __restrict__ v,
+                                                const float* __restrict__ dye, const uint8_t* __restrict__ label,
+                                                int beta_on, int alpha_on, int conf_on,
+                                                const float* __restrict__ fx, const float* __restrict__ fy,
+                                                const StepScalars* __restrict__ sc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (conf_on && i >= 1 && i < nx && j < ny) {
+    if (!(solid_cell(label, nx, ny, i - 1, j) || solid_cell(label, nx, ny, i, j))) {
+      const long k = i + (long)j * (nx + 1);
+      u[k] += sc->half_dt * (fx[(i - 1) + (long)j * nx] + fx[i + (long)j * nx]);
+    }
+  }
+  if (i < nx && j >= 1 && j < ny) {
+    if (!(solid_cell(label, nx, ny, i, j - 1) || solid_cell(label, nx, ny, i, j))) {
+      const long k = i + (long)j * nx;
+      const float x = ((float)i + 0.5f) * h;
+      const float y = (float)j * h;
+      const long dcells = (long)dnx * dny;
+      float vk = v[k];
+      if (beta_on) vk += sc->gain_beta * sample_p(dye, dnx, dny, dh, x, y);
+      if (alpha_on) vk += sc->gain_alpha * sample_p(dye + dcells, dnx, dny, dh, x, y);
+      if (conf_on) vk += sc->half_dt * (fy[i + (long)(j - 1) * nx] + fy[i + (long)j * nx]);
+      v[k] = vk;
+    }
+  }
+}
+
+// divergence.ts:17-25. as_rhs: write b = (-scale)*div (pressureMultigrid.ts:
+// 311) instead of div. Also accumulates the sum of squares of what it writes
+// and the count over FLUID cells (pressure.ts:177-186's fluidDivRms).
+__global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, const float* __restrict__ u,
+                                                    const float* __restrict__ v, float* __restrict__ out, int as_rhs,
+                                                    const uint8_t* __restrict__ label,
+                                                    const StepScalars* __restrict__ sc, StepAccum* acc) {
+  __shared__ double red[32];
+  __shared__ unsigned long long redn[32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  double sq = 0.0;
+  unsigned long long n = 0;
+  if (i < nx && j < ny) {
+    const float coef = 1.0f / h;
+    const long k = i + (long)j * nx;
+    const float d = coef * (u[(i + 1) + (long)j * (nx + 1)] - u[i + (long)j * (nx + 1)] + v[i + (long)(j + 1) * nx] -
+                            v[i + (long)j * nx]);
+    const float o = as_rhs ? sc->neg_scale * d : d;
+    out[k] = o;
+    if (label != nullptr && label[k] == FLUID) {
+      sq = (double)o * (double)o;
+      n = 1;
+    }
+  }
+  if (acc == nullptr) return;
+  double bs = block_sum(sq, red);
+  unsigned long long bn = block_sum_u64(n, redn);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    atomicAdd(&acc->b_sq, bs);
+    atomicAdd(&acc->n_fluid, bn);
+  }
+}
+
+// subtractGradient.ts:40-61 then applyOutflow (boundaries.ts:115-143). Thread
+// (i,j) owns u face (i,j) and v face (i,j). Outflow's writes land on the
+// faces of the edge rows/columns; each is owned by the thread that computes
+// the value it copies, so every face has exactly one writer:
+//   u(1,j) and u(0,j): thread (1,j); u(nx-1,j) and u(nx,j): thread (nx-1,j).
+// With nx == 2 both edges meet at face 1, handled left then right as the
+// reference's loop order does.
+__device__ __forceinline__ float projected_u(const float* __restrict__ p, const float* __restrict__ u,
+                                             const uint8_t* __restrict__ label, int nx, int ny, int i, int j,
+                                             float gs, bool subtract) {
+  float val = u[i + (long)j * (nx + 1)];
+  if (subtract && i >= 1 && i < nx) {
+    if (!(solid_or_outside(label, nx, ny, i - 1, j) || solid_or_outside(label, nx, ny, i, j)))
+      val -= gs * (p[i + (long)j * nx] - p[(i - 1) + (long)j * nx]);
+  }
+  return val;
+}
+__device__ __forceinline__ float projected_v(const float* __restrict__ p, const float* __restrict__ v,
+                                             const uint8_t* __restrict__ label, int nx, int ny, int i, int j,
+                                             float gs, bool subtract) {
+  float val = v[i + (long)j * nx];
+  if (subtract && j >= 1 && j < ny) {
+    if (!(solid_or_outside(label, nx, ny, i, j - 1) || solid_or_outside(label, nx, ny, i, j)))
+      val -= gs * (p[i + (long)j * nx] - p[i + (long)(j - 1) * nx]);
+  }
+  return val;
+}
+
+__global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const float* __restrict__ p,
+                                                          float* __restrict__ u, float* __restrict__ v,
+                                                          const uint8_t* __restrict__ label,
+                                                          const StepScalars* __restrict__ sc, int subtract,
+                                                          int outflow) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const float gs = subtract ? sc->grad_scale : 0.0f;
+  // u faces: threads 1..nx-1 write; faces 0 and nx are written only by outflow.
+  if (j < ny && i >= 1 && i < nx) {
+    float val = projected_u(p, u, label, nx, ny, i, j, gs, subtract);
+    if (outflow) {
+      if (i == 1 && label[0 + (long)j * nx] == AIR) {
+        val = smin(val, 0.0f);
+        u[0 + (long)j * (nx + 1)] = val;
+      }
+      if (i == nx - 1 && label[(nx - 1) + (long)j * nx] == AIR) {
+        val = smax(val, 0.0f);
+        u[nx + (long)j * (nx + 1)] = val;
+      }
+    }
+    u[i + (long)j * (nx + 1)] = val;
+  }
+  if (i < nx && j >= 1 && j < ny) {
+    float val = projected_v(p, v, label, nx, ny, i, j, gs, subtract);
+    if (outflow) {
+      if (j == 1 && label[i] == AIR) {
+        val = smin(val, 0.0f);
+        v[i] = val;
+      }
+      if (j == ny - 1 && label[i + (long)(ny - 1) * nx] == AIR) {
+        val = smax(val, 0.0f);
+        v[i + (long)ny * nx] = val;
+      }
+    }
+    v[i + (long)j * nx] = val;
+  }
+}
+
+// max |u|, |v| over every face (simulation.ts:451-459). The last block to
+// finish turns it into the next step's scalars (simulation.ts:474-479,
+// 243-247) and adds this step's dt to the device clock — no host round trip.
+__global__ void __launch_bounds__(256) k_max_speed(long nu, long nv, const float* __restrict__ u,
+                                                   const float* __restrict__ v, StepAccum* acc,
+                                                   StepScalars* sc_next, double* time_dev, float h, float cfl,
+                                                   float dt_max, float rho, double d0, double d1, double d2,
+                                                   float beta, float alpha, int write_scalars, int add_time) {
+  __shared__ float red[32];
+  float m = 0.0f;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < nu; k += stride) m = smax(m, fabsf(u[k]));
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < nv; k += stride) m = smax(m, fabsf(v[k]));
+  float bm = block_max(m, red);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    atomicMax(&acc->max_speed_bits, __float_as_uint(bm));
+    __threadfence();
+    unsigned int done = atomicAdd(&acc->blocks_done, 1u);
+    last = (done == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  const float umax = __uint_as_float(atomicExch(&acc->max_speed_bits, 0u));
+  acc->blocks_done = 0u;
+  acc->last_max_bits = __float_as_uint(umax);
+  // The step that just finished ran with the current scalars: its dt joins
+  // the clock before the scalars are replaced (simulation.ts:585).
+  if (add_time && time_dev) *time_dev += (double)sc_next->dt;
+  if (!write_scalars) return;
+  // simulation.ts:477-479, evaluated in float32 in the reference's order.
+  const float dt = umax > 1e-9f ? smin(dt_max, (cfl * h) / umax) : dt_max;
+  StepScalars s;
+  s.dt = dt;
+  s.scale = (rho * h * h) / dt;
+  s.grad_scale = dt / (rho * h);
+  const double dd = (double)dt;
+  s.keep[0] = d0 > 0 ? (float)exp(-d0 * dd) : 1.0f;
+  s.keep[1] = d1 > 0 ? (float)exp(-d1 * dd) : 1.0f;
+  s.keep[2] = d2 > 0 ? (float)exp(-d2 * dd) : 1.0f;
+  s.gain_beta = beta * dt;
+  s.gain_alpha = -alpha * dt;
+  s.half_dt = 0.5f * dt;
+  s.neg_scale = -s.scale;
+  for (int q = 0; q < 6; q++) s.pad[q] = 0;
+  *sc_next = s;
+}
+
+// b = (-scale) * div with the fluid sum of squares (pressureMultigrid.ts:311,
+// pressure.ts:177-186), for solves handed a divergence field.
+__global__ void __launch_bounds__(256) k_scale_rhs(long n, const float* __restrict__ div, float* __restrict__ b,
+                                                   float neg_scale, const uint8_t* __restrict__ label,
+                                                   StepAccum* acc) {
+  __shared__ double red[32];
+  __shared__ unsigned long long redn[32];
+  double sq = 0.0;
+  unsigned long long cnt = 0;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    const float o = b ? neg_scale * div[k] : div[k];
+    if (b) b[k] = o;
+    if (label[k] == FLUID) {
+      sq += (double)o * (double)o;
+      cnt += 1;
+    }
+  }
+  const double bs = block_sum(sq, red);
+  const unsigned long long bn = block_sum_u64(cnt, redn);
+  if (threadIdx.x == 0) {
+    atomicAdd(&acc->b_sq, bs);
+    atomicAdd(&acc->n_fluid, bn);
+  }
+}
+
+// boundaries.ts:45-64 on the device (project.wgsl:155-165 for the faces),
+// extended to p and dye as the host version does.
+__global__ void k_commit_labels(int nx, int ny, const uint8_t* __restrict__ label, float* __restrict__ p,
+                                float* __restrict__ u, float* __restrict__ v, float* __restrict__ dye,
+                                long dye_cells) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i < nx && j < ny) {
+    const long k = i + (long)j * nx;
+    const uint8_t l = label[k];
+    if (l != FLUID) {
+      if (p) p[k] = 0.0f;
+      if (l == SOLID && dye && k < dye_cells)
+        for (int c = 0; c < DYE_CHANNELS; c++) dye[k + c * dye_cells] = 0.0f;
+    }
+  }
+  if (i <= nx && j < ny) {
+    if (solid_cell(label, nx, ny, i - 1, j) || solid_cell(label, nx, ny, i, j)) u[i + (long)j * (nx + 1)] = 0.0f;
+  }
+  if (i < nx && j <= ny) {
+    if (solid_cell(label, nx, ny, i, j - 1) || solid_cell(label, nx, ny, i, j)) v[i + (long)j * nx] = 0.0f;
+  }
+}
+
+// stir.ts:49-83 — every interior face (the WGSL version's whole-grid sweep,
+// project.wgsl:180-207); faces beyond three radii get exp() of a large
+// negative number, which the host version skips by its bounding box. The
+// host's box is replicated here so both write exactly the same faces.
+__global__ void k_stir(int nx, int ny, float h, float* __restrict__ u, float* __restrict__ v,
+                       const uint8_t* __restrict__ label, float sx, float sy, float sr, float sdx, float sdy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const float invR2 = 1.0f / (sr * sr);
+  const float reach = 3.0f * sr;
+  const int c0 = (int)floorf((sx - reach) / h), c1 = (int)ceilf((sx + reach) / h);
+  const int r0 = (int)floorf((sy - reach) / h), r1 = (int)ceilf((sy + reach) / h);
+  if (j >= min(max(r0, 0), ny - 1) && j <= min(max(r1, 0), ny - 1) && i >= min(max(c0, 1), nx - 1) &&
+      i <= min(max(c1, 1), nx - 1) && i <= nx && j < ny) {
+    if (!(solid_cell(label, nx, ny, i - 1, j) || solid_cell(label, nx, ny, i, j))) {
+      const float dy = ((float)j + 0.5f) * h - sy;
+      const float dx = (float)i * h - sx;
+      u[i + (long)j * (nx + 1)] += sdx * expf(-(dx * dx + dy * dy) * invR2);
+    }
+  }
+  if (j >= min(max(r0, 1), ny - 1) && j <= min(max(r1, 1), ny - 1) && i >= min(max(c0, 0), nx - 1) &&
+      i <= min(max(c1, 0), nx - 1) && i < nx && j <= ny) {
+    if (!(solid_cell(label, nx, ny, i, j - 1) || solid_cell(label, nx, ny, i, j))) {
+      const float dy = (float)j * h - sy;
+      const float dx = ((float)i + 0.5f) * h - sx;
+      v[i + (long)j * nx] += sdy * expf(-(dx * dx + dy * dy) * invR2);
+    }
+  }
+}
+
+// dye.ts:158-175 (project.wgsl:363-379)
+__global__ void k_dye_patch(int dnx, int dny, float* __restrict__ dye, const float* __restrict__ patch, int pi0,
+                            int pj0, int pnx, int pny) {
+  const int pi = blockIdx.x * blockDim.x + threadIdx.x;
+  const int pj = blockIdx.y * blockDim.y + threadIdx.y;
+  if (pi >= pnx || pj >= pny) return;
+  const int di = pi0 + pi, dj = pj0 + pj;
+  if (di < 0 || dj < 0 || di >= dnx || dj >= dny) return;
+  const long pc = (long)pnx * pny;
+  const long s = pi + (long)pj * pnx;
+  const float cov = patch[DYE_CHANNELS * pc + s];
+  if (cov == 0.0f) return;
+  const long cells = (long)dnx * dny;
+  const long k = di + (long)dj * dnx;
+  for (int c = 0; c < DYE_CHANNELS; c++) dye[k + c * cells] += cov * (patch[c * pc + s] - dye[k + c * cells]);
+}
+
+__global__ void k_convert_f64_f32(const double* __restrict__ a, float* __restrict__ b, long n) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+    b[k] = (float)a[k];
+}
+__global__ void k_convert_f32_f64(const float* __restrict__ a, double* __restrict__ b, long n) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+    b[k] = (double)a[k];
+}
+
+// ------------------------------------------------------------- launchers
+
+static dim3 grid2(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
+
+void launch_vorticity(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* w) {
+  dim3 b(32, 8);
+  k_vorticity<<<grid2(nx, ny, b), b, 0, s>>>(nx, ny, h, u, v, w);
+}
+
+void launch_confinement_force(cudaStream_t s, int nx, int ny, float h, const float* w, const uint8_t* label,
+                              float eps, float* fx, float* fy) {
+  dim3 b(32, 8);
+  k_confinement_force<<<grid2(nx, ny, b), b, 0, s>>>(nx, ny, h, w, label, eps * h, fx, fy);
+}
+
+void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, float* u, float* v,
+                   const float* dye, const uint8_t* label, bool beta_on, bool alpha_on, bool conf_on,
+                   const float* fx, const float* fy, const StepScalars* sc) {
+  dim3 b(32, 8);
+  k_forces<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, h, dnx, dny, dh, u, v, dye, label, beta_on, alpha_on,
+                                                  conf_on, fx, fy, sc);
+}
+
+void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
+                       bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc) {
+  dim3 b(32, 8);
+  k_divergence<<<grid2(nx, ny, b), b, 0, s>>>(nx, ny, h, u, v, out, as_rhs, label, sc, acc);
+}
+
+void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
+                             const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow) {
+  dim3 b(32, 8);
+  k_subtract_outflow<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, p, u, v, label, sc, subtract, outflow);
+}
+
+void launch_scale_rhs(cudaStream_t s, long n, const float* div, float* b, float neg_scale, const uint8_t* label,
+                      StepAccum* acc) {
+  long blocks = (n + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  k_scale_rhs<<<(unsigned)blocks, 256, 0, s>>>(n, div, b, neg_scale, label, acc);
+}
+
+void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const float* v, StepAccum* acc,
+                      StepScalars* sc_next, double* time_dev, const fl_params* prm, float h, bool write_scalars,
+                      bool add_time) {
+  long nu = (long)(nx + 1) * ny, nv = (long)nx * (ny + 1);
+  long blocks = (nu + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  k_max_speed<<<(unsigned)blocks, 256, 0, s>>>(nu, nv, u, v, acc, sc_next, time_dev, h, (float)prm->cfl_target,
+                                              (float)prm->dt_max, (float)prm->rho, prm->dye_decay[0],
+                                              prm->dye_decay[1], prm->dye_decay[2], (float)prm->beta,
+                                              (float)prm->alpha, write_scalars, add_time);
+}
+
+void launch_commit_labels(cudaStream_t s, int nx, int ny, const uint8_t* label, float* p, float* u, float* v,
+                          float* dye, long dye_cells) {
+  dim3 b(32, 8);
+  k_commit_labels<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, label, p, u, v, dye, dye_cells);
+}
+
+void launch_stir(cudaStream_t s, int nx, int ny, float h, float* u, float* v, const uint8_t* label,
+                 const float* st) {
+  dim3 b(32, 8);
+  k_stir<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, h, u, v, label, st[0], st[1], st[2], st[3], st[4]);
+}
+
+void launch_dye_patch(cudaStream_t s, int dnx, int dny, float* dye, const float* patch, int pi0, int pj0, int pnx,
+                      int pny) {
+  if (!patch || pnx <= 0 || pny <= 0) return;
+  dim3 b(32, 8);
+  k_dye_patch<<<grid2(pnx, pny, b), b, 0, s>>>(dnx, dny, dye, patch, pi0, pj0, pnx, pny);
+}
+
+void launch_convert(cudaStream_t s, const void* src, int src_dtype, void* dst, int dst_dtype, long n) {
+  long blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  if (blocks < 1) blocks = 1;
+  if (src_dtype == FL_F64 && dst_dtype == FL_F32)
+    k_convert_f64_f32<<<(unsigned)blocks, 256, 0, s>>>((const double*)src, (float*)dst, n);
+  else if (src_dtype == FL_F32 && dst_dtype == FL_F64)
+    k_convert_f32_f64<<<(unsigned)blocks, 256, 0, s>>>((const float*)src, (double*)dst, n);
+}
+
+}  // namespace fl

@@ -1,0 +1,217 @@
+"""ctypes binding of the engine's C ABI (include/flowlab_gb300.h).
+
+The shared library is built in-tree by flowlab_gb300.build into
+flowlab_gb300/_lib/libflowlab_gb300.so. There is no fallback: if the library
+is missing, or no CUDA device is usable, the calls below raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libflowlab_gb300.so")
+
+FL_OK, FL_EINVAL, FL_EBUSY, FL_EDEVICE, FL_ETIMEOUT, FL_ENONFINITE, FL_ENOMEM, FL_ESTATE = range(8)
+FL_F32, FL_F64 = 0, 1
+FL_SEMI_LAGRANGIAN, FL_MACCORMACK = 0, 1
+FL_SOLVER_RBSOR, FL_SOLVER_MG = 0, 1
+
+STATUS_NAMES = {
+    FL_OK: "ok", FL_EINVAL: "invalid argument", FL_EBUSY: "not re-entrant", FL_EDEVICE: "device error",
+    FL_ETIMEOUT: "device wait timed out", FL_ENONFINITE: "non-finite result", FL_ENOMEM: "out of device memory",
+    FL_ESTATE: "call out of order",
+}
+
+
+class FlowlabError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s (%d): %s" % (STATUS_NAMES.get(status, "error"), status, message))
+        self.status = status
+
+
+class Params(ctypes.Structure):
+    """fl_params (field order is the ABI)."""
+
+    _fields_ = [
+        ("cfl_target", ctypes.c_double),
+        ("dt_max", ctypes.c_double),
+        ("rho", ctypes.c_double),
+        ("scheme", ctypes.c_int),
+        ("solver", ctypes.c_int),
+        ("pressure_iters", ctypes.c_int),
+        ("mg_max_cycles", ctypes.c_int),
+        ("omega", ctypes.c_double),
+        ("tol", ctypes.c_double),
+        ("dye_decay", ctypes.c_double * 3),
+        ("beta", ctypes.c_double),
+        ("alpha", ctypes.c_double),
+        ("confinement", ctypes.c_double),
+        ("mg_pre", ctypes.c_int),
+        ("mg_post", ctypes.c_int),
+        ("mg_coarse_sweeps", ctypes.c_int),
+        ("mg_coarsest", ctypes.c_int),
+        ("mg_omega", ctypes.c_double),
+        ("mixed", ctypes.c_int),
+        ("reserved", ctypes.c_int * 7),
+    ]
+
+
+class Stats(ctypes.Structure):
+    """fl_stats."""
+
+    _fields_ = [
+        ("dt", ctypes.c_double),
+        ("scale", ctypes.c_double),
+        ("grad_scale", ctypes.c_double),
+        ("time", ctypes.c_double),
+        ("cycles", ctypes.c_int),
+        ("steps", ctypes.c_int),
+        ("rel_residual", ctypes.c_double),
+        ("div_rms", ctypes.c_double),
+        ("max_face_speed", ctypes.c_double),
+    ]
+
+
+# (name, restype, argtypes) for every entry point of include/flowlab_gb300.h
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_F = ctypes.c_float
+_D = ctypes.c_double
+SIGNATURES = [
+    ("fl_default_params", None, [_P]),
+    ("fl_abi_version", _I, []),
+    ("fl_last_error", ctypes.c_char_p, [_P]),
+    ("fl_create", _I, [_I, _I, _D, _I, _P, _I, ctypes.POINTER(_P)]),
+    ("fl_destroy", _I, [_P]),
+    ("fl_set_params", _I, [_P, _P]),
+    ("fl_stream", _P, [_P]),
+    ("fl_synchronize", _I, [_P]),
+    ("fl_upload_fields", _I, [_P, _I, _P, _P, _P, _P, _P]),
+    ("fl_set_labels", _I, [_P, _P]),
+    ("fl_set_dye_patch", _I, [_P, _I, _I, _I, _I, _P]),
+    ("fl_set_buoyancy", _I, [_P, _D, _D]),
+    ("fl_set_confinement", _I, [_P, _D]),
+    ("fl_set_stir", _I, [_P, _P]),
+    ("fl_step", _I, [_P, _D, _D, _D, _P, _P]),
+    ("fl_step_auto", _I, [_P, _I, _P]),
+    ("fl_get_stats", _I, [_P, _P]),
+    ("fl_read_velocity", _I, [_P, _I, _P, _P]),
+    ("fl_read_dye", _I, [_P, _I, _P]),
+    ("fl_read_pressure", _I, [_P, _I, _P]),
+    ("fl_advect_velocity", _I, [_P, _I, _P, _P, _P, _P, _P, _F]),
+    ("fl_advect_dye", _I, [_P, _I, _P, _P, _P, _P, _P, _F]),
+    ("fl_rb_solve", _I, [_P, _P, _P, _P, _F, _I, _F, _D, _P]),
+    ("fl_mg_solve", _I, [_P, _P, _P, _P, _F, _I, _D, _P, _P]),
+    ("fl_divergence", _I, [_P, _P, _P, _P]),
+    ("fl_rb_sweep", _I, [_P, _P, _P, _P, _F, _F, _I]),
+    ("fl_subtract_gradient", _I, [_P, _P, _P, _P, _P, _F]),
+    ("fl_outflow", _I, [_P, _P, _P, _P]),
+    ("fl_commit_labels", _I, [_P, _P, _P, _P, _P, _P]),
+    ("fl_body_forces", _I, [_P, _P, _P, _P, _P, _F, _F, _F, _F]),
+    ("fl_stir", _I, [_P, _P, _P, _P, _F, _F, _F, _F, _F]),
+    ("fl_dye_patch", _I, [_P, _P, _I, _I, _I, _I, _P]),
+]
+
+_lib = None
+
+
+def load():
+    """Load the engine library (built in-tree). Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            "flowlab_gb300 CUDA library not built: %s is missing (run flowlab_gb300.build.build())" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.fl_abi_version() != 1:
+        raise RuntimeError("flowlab_gb300 ABI version mismatch")
+    _lib = lib
+    return lib
+
+
+def default_params(**overrides):
+    p = Params()
+    load().fl_default_params(ctypes.byref(p))
+    for k, v in overrides.items():
+        if k == "dye_decay":
+            p.dye_decay[:] = list(v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Engine:
+    """Owns one fl_engine*: the device side for an nx*ny grid."""
+
+    def __init__(self, nx, ny, h=None, dye_scale=1, params=None, device=0):
+        self.lib = load()
+        self.nx, self.ny, self.dye_scale = nx, ny, dye_scale
+        self.dnx, self.dny = nx * dye_scale, ny * dye_scale
+        self.h = 1.0 / ny if h is None else h
+        self.params = params if params is not None else default_params()
+        handle = ctypes.c_void_p()
+        st = self.lib.fl_create(nx, ny, self.h, dye_scale, ctypes.byref(self.params), device, ctypes.byref(handle))
+        if st != FL_OK:
+            raise FlowlabError(st, self.lib.fl_last_error(None).decode())
+        self.handle = handle
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.fl_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st):
+        if st != FL_OK:
+            raise FlowlabError(st, self.lib.fl_last_error(self.handle).decode())
+
+    def call(self, name, *args):
+        self.check(getattr(self.lib, name)(self.handle, *args))
+
+    # sizes
+    @property
+    def cells(self):
+        return self.nx * self.ny
+
+    @property
+    def ufaces(self):
+        return (self.nx + 1) * self.ny
+
+    @property
+    def vfaces(self):
+        return self.nx * (self.ny + 1)
+
+    @property
+    def dye_len(self):
+        return 3 * self.dnx * self.dny
+
+    def stream(self):
+        return self.lib.fl_stream(self.handle)
+
+    def set_params(self, params):
+        self.params = params
+        self.call("fl_set_params", ctypes.byref(params))
+
+    def stats(self):
+        s = Stats()
+        self.call("fl_get_stats", ctypes.byref(s))
+        return {k: getattr(s, k) for k, _ in Stats._fields_}

@@ -1,0 +1,200 @@
+/*
+ * flowlab_gb300 — C ABI of the GB300 (sm_103a) engine for flowlab's 2D
+ * incompressible MAC-grid projection step.
+ *
+ * This is the drop-in boundary for the reference's three GPU seams:
+ *   GpuStep        src/core/simulation.ts:35-84   (implemented by src/gpu/stepGpu.ts:89)
+ *   PressureSolver src/core/pressureSolver.ts:21-41 (src/gpu/multigridGpu.ts:59,
+ *                                                   src/gpu/pressureGpu.ts:68)
+ *   Advector       src/core/advector.ts:28-63      (src/gpu/advectGpu.ts:54)
+ * plus the per-kernel passes of src/core (one entry point each) so every pass
+ * can be diffed against its CPU twin, as the reference's *.gputest.ts files do.
+ *
+ * Conventions
+ *   - Plain C types only. Host arrays are caller-owned; the engine copies on
+ *     upload and readback and never keeps a host pointer (the reference's
+ *     writeBuffer/mapAsync discipline). Device buffers belong to the engine
+ *     and are freed by fl_destroy.
+ *   - MAC layout of src/core/grid.ts:1-36: p and label nx*ny (stride nx),
+ *     u (nx+1)*ny (stride nx+1), v nx*(ny+1) (stride nx). Dye is the three
+ *     channels' dnx*dny planes laid end to end (dnx = nx*dye_scale).
+ *   - Labels are uint8: 0 Fluid, 1 Air, 2 Solid (grid.ts:41-45).
+ *   - Every function returns an int status (FL_OK = 0). On failure
+ *     fl_last_error(engine) describes it; fl_last_error(NULL) describes a
+ *     failed fl_create. There is no CPU fallback: without a usable CUDA
+ *     device every compute entry point fails with FL_EDEVICE.
+ *   - An engine is not re-entrant: a call made while another call on the
+ *     same engine is running returns FL_EBUSY (the reference throws
+ *     "... is not re-entrant", stepGpu.ts:402, multigridGpu.ts:318).
+ *   - Compute is float32 (the reference's WGSL precision), optionally with a
+ *     float64 fine-level pressure for iterative refinement (fl_params.mixed).
+ */
+#ifndef FLOWLAB_GB300_H
+#define FLOWLAB_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FL_ABI_VERSION 1
+
+typedef struct fl_engine fl_engine;
+
+enum fl_status {
+  FL_OK = 0,
+  FL_EINVAL = 1,     /* bad argument or size */
+  FL_EBUSY = 2,      /* engine already inside a call (not re-entrant) */
+  FL_EDEVICE = 3,    /* CUDA error or no device ("GPU device lost", stepGpu.ts:403) */
+  FL_ETIMEOUT = 4,   /* a bounded device wait gave up */
+  FL_ENONFINITE = 5, /* the solve produced NaN/Inf */
+  FL_ENOMEM = 6,     /* device allocation failed */
+  FL_ESTATE = 7      /* call out of order (e.g. step before any upload) */
+};
+
+enum fl_dtype { FL_F32 = 0, FL_F64 = 1 };
+
+/* src/core/advect.ts:21 AdvectionScheme */
+enum fl_scheme { FL_SEMI_LAGRANGIAN = 0, FL_MACCORMACK = 1 };
+
+/* Which pressure solver the fused step runs. */
+enum fl_solver { FL_SOLVER_RBSOR = 0, FL_SOLVER_MG = 1 };
+
+/*
+ * Step parameters: src/core/simulation.ts:134-234 (SimulationParams) reduced
+ * to what the projection step reads, the multigrid constants of
+ * src/core/pressureMultigrid.ts:47-67 made runtime values, and the knobs the
+ * reference does not have (alpha, confinement, mixed precision).
+ */
+typedef struct fl_params {
+  double cfl_target;     /* simulation.ts:141 */
+  double dt_max;         /* simulation.ts:150 */
+  double rho;            /* simulation.ts:165 */
+  int scheme;            /* enum fl_scheme */
+  int solver;            /* enum fl_solver */
+  int pressure_iters;    /* red-black sweep budget (simulation.ts:152) */
+  int mg_max_cycles;     /* V-cycle cap (pressureMultigrid.ts:63 MG_CYCLES) */
+  double omega;          /* SOR relaxation for the red-black solver */
+  double tol;            /* relative residual target; <= 0 runs the full budget */
+  double dye_decay[3];   /* per channel, per second of sim time (simulation.ts:184) */
+  double beta;           /* buoyancy weight on dye channel 0 (simulation.ts:191) */
+  double alpha;          /* soot weight on dye channel 1 (force -alpha*s) */
+  double confinement;    /* vorticity confinement epsilon; 0 = off */
+  int mg_pre, mg_post;   /* smoothing sweep pairs per level (reference 2, 2) */
+  int mg_coarse_sweeps;  /* sweep pairs on the coarsest level (reference 8) */
+  int mg_coarsest;       /* stop coarsening at <= this many cells a side (reference 4) */
+  double mg_omega;       /* smoother relaxation (reference 1.0) */
+  int mixed;             /* 1: float64 fine pressure + float64 residual (defect correction) */
+  int reserved[7];
+} fl_params;
+
+/* Per-step report (the reference's sim.iters / sim.dt plus the residual the
+ * GPU path never computed). */
+typedef struct fl_stats {
+  double dt, scale, grad_scale;
+  double time;           /* accumulated sim time */
+  int cycles;            /* V-cycles (multigrid) or sweep pairs (red-black) of the last solve */
+  int steps;             /* steps taken since the last upload */
+  double rel_residual;   /* RMS remaining divergence / RMS fluid divergence, last solve; -1 if unchecked */
+  double div_rms;        /* RMS of b = -scale*div over fluid cells, last solve */
+  double max_face_speed; /* max |u|,|v| after the last step (CFL input of the next one) */
+} fl_stats;
+
+/* Fills `p` with the reference defaults (simulation.ts:223-234,
+ * pressureMultigrid.ts:47-67). */
+void fl_default_params(fl_params* p);
+
+int fl_abi_version(void);
+const char* fl_last_error(const fl_engine* e);
+
+/* ------------------------------------------------------------ lifecycle */
+
+/* Builds the device side for an nx*ny grid with cell size h and a dye grid
+ * refined by dye_scale (simulation.ts:353-374, stepGpu.ts:176-289). */
+int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, int device, fl_engine** out);
+/* Frees every device buffer (advectGpu.ts:382-398, stepGpu.ts:674-689). */
+int fl_destroy(fl_engine* e);
+int fl_set_params(fl_engine* e, const fl_params* params);
+/* The engine's CUDA stream (a cudaStream_t), for callers that time or order
+ * work against it. */
+void* fl_stream(fl_engine* e);
+int fl_synchronize(fl_engine* e);
+
+/* ------------------------------------------------- GpuStep (simulation.ts:35-84) */
+
+/* invalidate() + the dirty upload of stepGpu.ts:419-433: the host holds truth
+ * for u, v, p, label and dye. dtype is FL_F32 or FL_F64 for the float fields;
+ * p may be NULL (zero warm start). */
+int fl_upload_fields(fl_engine* e, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
+                     const void* dye);
+/* setLabels: labels changed under resident fields (stepGpu.ts:323-330); the
+ * next step first zeroes faces touching new solids (commit_labels) and
+ * re-coarsens. */
+int fl_set_labels(fl_engine* e, const uint8_t* label);
+/* setDyePatch (stepGpu.ts:337-362): data is 4 planes of pnx*pny floats (3 value
+ * planes + coverage, dye.ts:108-127); NULL clears it. */
+int fl_set_dye_patch(fl_engine* e, int i0, int j0, int pnx, int pny, const float* data);
+/* setBuoyancy (stepGpu.ts:366-368), extended with the soot weight alpha. */
+int fl_set_buoyancy(fl_engine* e, double beta, double alpha);
+int fl_set_confinement(fl_engine* e, double eps);
+/* setStir (stepGpu.ts:319-321): x, y, r, dx, dy in world units; consumed by
+ * the next step. NULL clears. */
+int fl_set_stir(fl_engine* e, const double* stir5);
+/* step (stepGpu.ts:393-559) with the caller's dt, scale, gradScale and
+ * per-channel keep factors. Returns the pressure iterations in *iters. */
+int fl_step(fl_engine* e, double dt, double scale, double grad_scale, const double keep[3], int* iters);
+/* `nsteps` steps with dt from the CURRENT velocity on the device
+ * (simulation.ts:474-479 without the host scan or the one-step-stale
+ * readback). No host synchronisation between steps unless tol > 0 requires
+ * a residual readback. */
+int fl_step_auto(fl_engine* e, int nsteps, int* iters_last);
+int fl_get_stats(fl_engine* e, fl_stats* out);
+/* Readbacks (drainReadback / readDye, stepGpu.ts:372-391, 578-604). */
+int fl_read_velocity(fl_engine* e, int dtype, void* u, void* v);
+int fl_read_dye(fl_engine* e, int dtype, void* dye);
+int fl_read_pressure(fl_engine* e, int dtype, void* p);
+
+/* ------------------------------------ Advector (advector.ts:28-63), float32 host arrays */
+
+/* advectVelocity / advectVelocityMacCormack (advect.ts:126-211). */
+int fl_advect_velocity(fl_engine* e, int scheme, const float* u_in, const float* v_in, float* u_out, float* v_out,
+                       const uint8_t* label, float dt);
+/* advectScalar / advectScalarMacCormack over all 3 channels (advect.ts:241-312). */
+int fl_advect_dye(fl_engine* e, int scheme, const float* u, const float* v, const float* q_in, float* q_out,
+                  const uint8_t* label, float dt);
+
+/* ---------------------------- PressureSolver (pressureSolver.ts:21-41), float32 host arrays */
+
+/* Red-black SOR (pressureRedBlack.ts:88-113): p is the in/out warm start. */
+int fl_rb_solve(fl_engine* e, float* p, const float* div, const uint8_t* label, float scale, int iterations,
+                float omega, double tol, int* sweeps_used);
+/* Geometric multigrid (pressureMultigrid.ts:284-319) with the engine's
+ * V(pre,post)/coarsest shape; runs until the relative residual <= tol or
+ * max_cycles. */
+int fl_mg_solve(fl_engine* e, float* p, const float* div, const uint8_t* label, float scale, int max_cycles,
+                double tol, int* cycles_used, double* rel_residual);
+
+/* ------------------------------------------- single passes, float32 host arrays */
+
+int fl_divergence(fl_engine* e, const float* u, const float* v, float* div);           /* divergence.ts:17-25 */
+int fl_rb_sweep(fl_engine* e, float* p, const float* div, const uint8_t* label, float scale, float omega,
+                int color);                                                           /* pressureRedBlack.ts:32-72 */
+int fl_subtract_gradient(fl_engine* e, const float* p, float* u, float* v, const uint8_t* label,
+                         float grad_scale);                                           /* subtractGradient.ts:40-61 */
+int fl_outflow(fl_engine* e, float* u, float* v, const uint8_t* label);                /* boundaries.ts:115-143 */
+int fl_commit_labels(fl_engine* e, float* p, float* u, float* v, float* dye,
+                     const uint8_t* label);                                           /* boundaries.ts:45-64 */
+/* buoyancy.ts:70-88 (+ alpha term) and vorticity confinement, in the step's
+ * order: confinement force from the incoming velocity, buoyancy added, then
+ * confinement added. */
+int fl_body_forces(fl_engine* e, float* u, float* v, const float* dye, const uint8_t* label, float beta,
+                   float alpha, float eps, float dt);
+int fl_stir(fl_engine* e, float* u, float* v, const uint8_t* label, float x, float y, float r, float dx,
+            float dy);                                                                /* stir.ts:49-83 */
+int fl_dye_patch(fl_engine* e, float* dye, int i0, int j0, int pnx, int pny, const float* data); /* dye.ts:158-175 */
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLOWLAB_GB300_H */

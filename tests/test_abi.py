@@ -1,0 +1,58 @@
+"""The C ABI library builds for sm_103a, loads, and exports every entry point
+include/flowlab_gb300.h declares. No GPU needed (nothing is computed)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from flowlab_gb300 import build, native
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "flowlab_gb300.h")
+
+
+def declared():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(fl_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return native.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_bindings_cover_the_header():
+    bound = {n for n, _, _ in native.SIGNATURES}
+    assert set(declared()) == bound
+
+
+def test_abi_version_and_defaults(lib):
+    assert lib.fl_abi_version() == 1
+    p = native.default_params()
+    # simulation.ts:223-234 and pressureMultigrid.ts:47-67
+    assert p.cfl_target == 2.0 and abs(p.dt_max - 1 / 30) < 1e-15 and p.tol == 5e-3
+    assert (p.mg_pre, p.mg_post, p.mg_coarse_sweeps, p.mg_coarsest, p.mg_max_cycles) == (2, 2, 8, 4, 3)
+    assert ctypes.sizeof(native.Params) == 160
+
+
+def test_create_fails_loudly_without_a_device(lib):
+    h = ctypes.c_void_p()
+    st = lib.fl_create(8, 8, 0.125, 1, None, 0, ctypes.byref(h))
+    if st == native.FL_OK:  # a GPU is present: nothing to check here
+        lib.fl_destroy(h)
+        pytest.skip("a CUDA device is present")
+    assert st == native.FL_EDEVICE
+    assert b"CUDA" in lib.fl_last_error(None)
+
+
+def test_null_engine_is_rejected(lib):
+    assert lib.fl_synchronize(None) == native.FL_EINVAL

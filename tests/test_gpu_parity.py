@@ -1,0 +1,270 @@
+"""CUDA engine vs the oracle, through the C ABI, on the reference's own
+fixtures (src/gpu/*.gputest.ts) plus larger and odd-sized grids that exercise
+the tiled kernels' edges.
+
+Two bars per pass, the reference's debugging ladder (pressureRedBlack.ts:
+1-27): against the float32 oracle the result must be IDENTICAL (same
+operations in the same order: ordering, indexing, solid mask and boundary
+handling exact); against the float64 oracle it must agree within the
+reference's own tolerances — 1e-5 x peak for p/u/v/dye
+(redBlack.gputest.ts:158, advect.gputest.ts:272) and 1e-6 absolute for the
+projection passes on O(1) data (project.gputest.ts:288).
+"""
+import numpy as np
+import pytest
+
+from flowlab_gb300 import native
+from flowlab_gb300.native import f32, ptr
+from tests import fixtures as fx
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_identical(exp32, got, what):
+    exp32 = np.asarray(exp32, np.float32)
+    got = np.asarray(got, np.float32)
+    assert exp32.shape == got.shape, what
+    bad = exp32 != got
+    if bad.any():
+        k = np.nonzero(bad)[0]
+        d = np.abs(exp32[k].astype(np.float64) - got[k].astype(np.float64)).max()
+        raise AssertionError("%s: %d of %d values differ from the float32 oracle (max %.3g), first at %d: %r vs %r"
+                             % (what, k.size, exp32.size, d, k[0], exp32[k[0]], got[k[0]]))
+
+
+def assert_close_rel(exp64, got, what, rel=1e-5):
+    diff, peak = fx.max_rel(exp64, got)
+    assert peak > 1e-3, "%s: vacuous, field ~0" % what
+    assert diff < rel * peak, "%s: differs from the float64 oracle by %.3g on peak %.3g" % (what, diff, peak)
+
+
+@pytest.fixture(scope="module")
+def eng40():
+    e = native.Engine(fx.NX, fx.NY)
+    yield e
+    e.close()
+
+
+# --------------------------------------------------------------- pressure
+
+def test_rb_halfsweep_identical(eng40, o32):
+    label, div = fx.pressure_fixture()
+    p0 = f32(np.linspace(-1, 1, fx.NX * fx.NY))
+    for color in (0, 1):
+        p = p0.copy()
+        eng40.call("fl_rb_sweep", ptr(p), ptr(f32(div)), ptr(label), 0.02, 1.85, color)
+        exp = o32.rb_sweep(fx.NX, fx.NY, p0, f32(div), label, 0.02, 1.85, color)
+        assert_identical(exp, p, "half-sweep colour %d" % color)
+
+
+def rb_solve(eng, p, div, label, scale, iters, omega, tol):
+    p = f32(p).copy()
+    used = native.ctypes.c_int()
+    eng.call("fl_rb_solve", ptr(p), ptr(f32(div)), ptr(label), scale, iters, omega, tol, native.ctypes.byref(used))
+    return p, used.value
+
+
+def test_rb_solver_200_sweeps(eng40, o32, o64):
+    # redBlack.gputest.ts:125-169 — 200 sweeps, omega 1.85, scale 0.02
+    label, div = fx.pressure_fixture()
+    p, used = rb_solve(eng40, np.zeros(fx.NX * fx.NY), div, label, 0.02, 200, 1.85, 0.0)
+    assert used == 200
+    e32, _ = o32.rb_solve(fx.NX, fx.NY, np.zeros(fx.NX * fx.NY), f32(div), label, 0.02, 200, 1.85, 0.0)
+    assert_identical(e32, p, "red-black 200 sweeps")
+    e64, _ = o64.rb_solve(fx.NX, fx.NY, np.zeros(fx.NX * fx.NY), div, label, 0.02, 200, 1.85, 0.0)
+    assert_close_rel(e64, p, "red-black vs float64")
+    r_cpu = o64.rms_remaining(fx.NX, fx.NY, e64, div, label, 0.02)
+    r_gpu = o64.rms_remaining(fx.NX, fx.NY, p.astype(np.float64), div, label, 0.02)
+    assert abs(r_gpu - r_cpu) < 0.01 * r_cpu
+
+
+def test_rb_solver_tolerance_stops_on_check(eng40, o32):
+    # pressureRedBlack.ts:341-349 — checks every 12 sweeps
+    label, div = fx.pressure_fixture()
+    p, used = rb_solve(eng40, np.zeros(fx.NX * fx.NY), div, label, 0.02, 600, 1.9, 1e-3)
+    e, used32 = o32.rb_solve(fx.NX, fx.NY, np.zeros(fx.NX * fx.NY), f32(div), label, 0.02, 600, 1.9, 1e-3)
+    assert used == used32 and used % 12 == 0 and used < 600
+    assert_identical(e, p, "red-black to tolerance")
+
+
+def test_rb_zero_divergence(eng40):
+    label, _ = fx.pressure_fixture()
+    p, used = rb_solve(eng40, np.ones(fx.NX * fx.NY), np.zeros(fx.NX * fx.NY), label, 0.02, 50, 1.9, 0.0)
+    assert used == 0 and not p.any()
+
+
+def mg_solve(eng, p, div, label, scale, cycles, tol):
+    p = f32(p).copy()
+    used = native.ctypes.c_int()
+    rr = native.ctypes.c_double()
+    eng.call("fl_mg_solve", ptr(p), ptr(f32(div)), ptr(label), scale, cycles, tol, native.ctypes.byref(used),
+             native.ctypes.byref(rr))
+    return p, used.value, rr.value
+
+
+def test_mg_fixture_4_cycles(eng40, o32, o64):
+    # multigrid.gputest.ts:194-243 — V(2,2), coarsest 4, 4 cycles, identical and 1e-5
+    label, div = fx.pressure_fixture()
+    p, used, _ = mg_solve(eng40, np.zeros(fx.NX * fx.NY), div, label, 0.02, 4, 0.0)
+    assert used == 4
+    e32, _, _ = o32.mg_solve(fx.NX, fx.NY, np.zeros(fx.NX * fx.NY), f32(div), label, 0.02, 4, 0.0)
+    assert_identical(e32, p, "multigrid 4 cycles")
+    e64, _, _ = o64.mg_solve(fx.NX, fx.NY, np.zeros(fx.NX * fx.NY), div, label, 0.02, 4, 0.0)
+    assert_close_rel(e64, p, "multigrid vs float64")
+    r_cpu = o64.rms_remaining(fx.NX, fx.NY, e64, div, label, 0.02)
+    r_gpu = o64.rms_remaining(fx.NX, fx.NY, p.astype(np.float64), div, label, 0.02)
+    assert abs(r_gpu - r_cpu) < 0.01 * max(r_cpu, 1e-12)
+
+
+@pytest.mark.parametrize("nx,ny,pre,post,coarse,coarsest", [
+    (256, 192, 3, 3, 32, 8),     # tiled levels + single-CTA tail
+    (301, 203, 2, 2, 8, 4),      # odd sizes: ragged tiles, odd coarsening
+    (1024, 1024, 3, 3, 32, 8),   # the 1024^2 tile shape
+    (130, 66, 1, 4, 16, 4),      # asymmetric smoothing
+])
+def test_mg_tiled_identical(o32, o64, nx, ny, pre, post, coarse, coarsest):
+    label = fx.scaled_block_labels(nx, ny)
+    div = fx.js_lcg_uniform(nx * ny, 4242)
+    prm = native.default_params(mg_pre=pre, mg_post=post, mg_coarse_sweeps=coarse, mg_coarsest=coarsest,
+                                solver=native.FL_SOLVER_MG)
+    eng = native.Engine(nx, ny, params=prm)
+    try:
+        warm = f32(fx.js_lcg_uniform(nx * ny, 7) * 0.01)
+        warm[label != 0] = 0
+        p, used, _ = mg_solve(eng, warm, div, label, 0.02, 3, 0.0)
+    finally:
+        eng.close()
+    e32, _, _ = o32.mg_solve(nx, ny, warm, f32(div), label, 0.02, 3, 0.0, pre, post, coarse, coarsest)
+    assert_identical(e32, p, "multigrid %dx%d" % (nx, ny))
+    e64, _, _ = o64.mg_solve(nx, ny, warm.astype(np.float64), div, label, 0.02, 3, 0.0, pre, post, coarse, coarsest)
+    assert_close_rel(e64, p, "multigrid %dx%d vs float64" % (nx, ny), rel=1e-4)
+
+
+def test_mg_tolerance_matches_oracle(o32):
+    nx, ny = 256, 256
+    label = np.zeros(nx * ny, np.uint8)
+    div = fx.js_lcg_uniform(nx * ny, 99)
+    div -= div.mean()
+    prm = native.default_params(mg_pre=3, mg_post=3, mg_coarse_sweeps=32, mg_coarsest=8)
+    eng = native.Engine(nx, ny, params=prm)
+    try:
+        p, used, rr = mg_solve(eng, np.zeros(nx * ny), div, label, 0.02, 30, 1e-4)
+    finally:
+        eng.close()
+    e32, used32, rr32 = o32.mg_solve(nx, ny, np.zeros(nx * ny), f32(div), label, 0.02, 30, 1e-4, 3, 3, 32, 8)
+    assert used == used32 and 1 <= used < 30
+    assert rr <= 1e-4 and abs(rr - rr32) <= 1e-6 * rr32
+    assert_identical(e32, p, "multigrid to tolerance")
+
+
+# -------------------------------------------------------------- advection
+
+@pytest.mark.parametrize("mac", [False, True])
+@pytest.mark.parametrize("dye_scale", [1, 2])
+def test_advection(o32, o64, mac, dye_scale):
+    # advect.gputest.ts:208-277 — 2 schemes x dye scale {1, 2}
+    h, dt, u, v, label, dye, dnx, dny, dh = fx.advect_fixture(dye_scale)
+    eng = native.Engine(fx.NX, fx.NY, h, dye_scale)
+    try:
+        uo = np.empty_like(f32(u))
+        vo = np.empty_like(f32(v))
+        scheme = native.FL_MACCORMACK if mac else native.FL_SEMI_LAGRANGIAN
+        eng.call("fl_advect_velocity", scheme, ptr(f32(u)), ptr(f32(v)), ptr(uo), ptr(vo), ptr(label), np.float32(dt))
+        qo = np.empty_like(f32(dye))
+        eng.call("fl_advect_dye", scheme, ptr(f32(u)), ptr(f32(v)), ptr(f32(dye)), ptr(qo), ptr(label), np.float32(dt))
+    finally:
+        eng.close()
+    hf, dtf, dhf = float(np.float32(h)), float(np.float32(dt)), float(np.float32(dh))
+    eu, ev = o32.advect_velocity(fx.NX, fx.NY, hf, mac, f32(u), f32(v), label, dtf)
+    assert_identical(eu, uo, "u")
+    assert_identical(ev, vo, "v")
+    eq = o32.advect_dye(fx.NX, fx.NY, hf, dnx, dny, dhf, mac, f32(u), f32(v), f32(dye), label, dtf)
+    assert_identical(eq, qo, "dye")
+    eu, ev = o64.advect_velocity(fx.NX, fx.NY, h, mac, u, v, label, dt)
+    eq = o64.advect_dye(fx.NX, fx.NY, h, dnx, dny, dh, mac, u, v, dye, label, dt)
+    assert_close_rel(eu, uo, "u vs float64")
+    assert_close_rel(ev, vo, "v vs float64")
+    assert_close_rel(eq, qo, "dye vs float64")
+
+
+# ------------------------------------------------------- projection passes
+
+def test_projection_passes(eng40, o32, o64):
+    # project.gputest.ts:111-295, pass by pass
+    label, u, v, p, dye = fx.project_fixture()
+    h = float(np.float32(1.0 / fx.NY))
+    # divergence
+    div = np.empty(fx.NX * fx.NY, np.float32)
+    eng40.call("fl_divergence", ptr(f32(u)), ptr(f32(v)), ptr(div))
+    assert_identical(o32.divergence(fx.NX, fx.NY, h, f32(u), f32(v)), div, "divergence")
+    d64 = o64.divergence(fx.NX, fx.NY, 1.0 / fx.NY, u, v)
+    assert np.abs(d64 - div).max() < 1e-6 * np.abs(d64).max()
+    # subtract gradient
+    uu, vv = f32(u).copy(), f32(v).copy()
+    eng40.call("fl_subtract_gradient", ptr(f32(p)), ptr(uu), ptr(vv), ptr(label), 0.5)
+    eu, ev = o32.subtract_gradient(fx.NX, fx.NY, f32(p), f32(u), f32(v), label, 0.5)
+    assert_identical(eu, uu, "subtract u")
+    assert_identical(ev, vv, "subtract v")
+    eu64, ev64 = o64.subtract_gradient(fx.NX, fx.NY, p, u, v, label, 0.5)
+    assert np.abs(eu64 - uu).max() < 1e-6 and np.abs(ev64 - vv).max() < 1e-6
+    # outflow on the projected field
+    eng40.call("fl_outflow", ptr(uu), ptr(vv), ptr(label))
+    eu, ev = o32.outflow(fx.NX, fx.NY, eu, ev, label)
+    assert_identical(eu, uu, "outflow u")
+    assert_identical(ev, vv, "outflow v")
+    # commit labels
+    pp, u2, v2, d2 = f32(p).copy(), f32(u).copy(), f32(v).copy(), f32(dye).copy()
+    eng40.call("fl_commit_labels", ptr(pp), ptr(u2), ptr(v2), ptr(d2), ptr(label))
+    ep, eu, ev, ed = o32.commit_labels(fx.NX, fx.NY, f32(p), f32(u), f32(v), label, f32(dye), fx.NX * fx.NY)
+    for name, a, b in (("p", ep, pp), ("u", eu, u2), ("v", ev, v2), ("dye", ed, d2)):
+        assert_identical(a, b, "commit labels " + name)
+    # dye patch (+ decay is covered by the step test)
+    data = fx.patch_fixture()
+    d3 = f32(dye).copy()
+    eng40.call("fl_dye_patch", ptr(d3), 0, 0, 3, fx.NY, ptr(data))
+    assert_identical(o32.dye_patch(fx.NX, fx.NY, f32(dye), 0, 0, 3, fx.NY, data), d3, "dye patch")
+
+
+@pytest.mark.parametrize("beta,alpha,eps", [(0.37, 0.0, 0.0), (0.37, 0.05, 0.0), (0.0, 0.0, 0.3), (1.0, 0.05, 0.3)])
+def test_body_forces(eng40, o32, o64, beta, alpha, eps):
+    # project.gputest.ts:46-47's weights; NEW alpha term and confinement
+    label, u, v, p, dye = fx.project_fixture()
+    h = 1.0 / fx.NY
+    dt = 0.023
+    uu, vv = f32(u).copy(), f32(v).copy()
+    eng40.call("fl_body_forces", ptr(uu), ptr(vv), ptr(f32(dye)), ptr(label), beta, alpha, eps, dt)
+    n = fx.NX * fx.NY
+    d32 = f32(dye)
+    eu, ev = o32.body_forces(fx.NX, fx.NY, float(np.float32(h)), fx.NX, fx.NY, float(np.float32(h)), f32(u), f32(v),
+                             d32[:n], d32[n:2 * n], label, beta, alpha, eps, dt)
+    assert_identical(eu, uu, "forces u")
+    assert_identical(ev, vv, "forces v")
+    eu64, ev64 = o64.body_forces(fx.NX, fx.NY, h, fx.NX, fx.NY, h, u, v, dye[:n], dye[n:2 * n], label, beta, alpha,
+                                 eps, dt)
+    assert np.abs(eu64 - uu).max() < 1e-5 and np.abs(ev64 - vv).max() < 1e-5
+
+
+def test_stir(eng40, o64):
+    # stir.ts:49-83 — exp() differs in the last bits between libraries, so
+    # float64 agreement is the bar here.
+    label, u, v, _, _ = fx.project_fixture()
+    uu, vv = f32(u).copy(), f32(v).copy()
+    eng40.call("fl_stir", ptr(uu), ptr(vv), ptr(label), 0.3, 0.4, 0.1, 0.7, -0.4)
+    eu, ev = o64.stir(fx.NX, fx.NY, 1.0 / fx.NY, u, v, label, 0.3, 0.4, 0.1, 0.7, -0.4)
+    assert np.abs(eu - uu).max() < 1e-6 and np.abs(ev - vv).max() < 1e-6
+    assert np.abs(uu - f32(u)).max() > 0.1  # the stir did something
+
+
+# ----------------------------------------------------------- error paths
+
+def test_errors_are_status_codes(eng40):
+    with pytest.raises(native.FlowlabError) as ei:
+        eng40.call("fl_step", 0.01, 1.0, 1.0, None, None)
+    assert ei.value.status == native.FL_ESTATE
+    bad = native.default_params(mg_pre=9)
+    with pytest.raises(native.FlowlabError) as ei:
+        eng40.set_params(bad)
+    assert ei.value.status == native.FL_EINVAL
+    with pytest.raises(native.FlowlabError) as ei:
+        native.Engine(1, 1)
+    assert ei.value.status == native.FL_EINVAL

@@ -1,0 +1,135 @@
+"""The fused step (GpuStep seam, C ABI fl_upload_fields / fl_step /
+fl_step_auto) against the oracle's Simulation (simulation.ts:467-587) on the
+benchmark configurations at test sizes, plus the reference's whole-step
+invariants (src/core/simulation.test.ts, src/scenes/emitters.test.ts)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from flowlab_gb300 import configs, native, scenes as sc
+from flowlab_gb300.native import f32, ptr
+from tests.scene_setups import oracle_params
+
+pytestmark = pytest.mark.gpu
+
+
+def run_engine(g, f, patch, prm, steps, auto=True):
+    eng = native.Engine(g.nx, g.ny, g.h, params=prm)
+    try:
+        if patch is not None:
+            eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+        eng.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
+                 ptr(f32(f.dye)))
+        iters = ctypes.c_int()
+        eng.call("fl_step_auto", steps, ctypes.byref(iters))
+        u = np.empty(eng.ufaces, np.float32)
+        v = np.empty(eng.vfaces, np.float32)
+        p = np.empty(eng.cells, np.float32)
+        d = np.empty(eng.dye_len, np.float32)
+        eng.call("fl_read_velocity", native.FL_F32, ptr(u), ptr(v))
+        eng.call("fl_read_pressure", native.FL_F32, ptr(p))
+        eng.call("fl_read_dye", native.FL_F32, ptr(d))
+        st = eng.stats()
+    finally:
+        eng.close()
+    return u, v, p, d, st
+
+
+def run_oracle(o, g, f, patch, prm, steps):
+    sim = o.simulation(g.nx, g.ny, 1, **oracle_params(prm))
+    sim.set_fields(f.u, f.v, f.p, f.label, f.dye)
+    if patch is not None:
+        sim.set_patch(patch.i0, patch.j0, patch.nx, patch.ny, patch.data)
+    for _ in range(steps):
+        sim.step()
+    u, v, p, d = sim.get_fields()
+    return u, v, p, d, sim.info()
+
+
+def mismatch(a, b):
+    a = np.asarray(a, np.float32)
+    b = np.asarray(b, np.float32)
+    return int((a != b).sum())
+
+
+def test_plume_steps_match_float32_oracle(o32, o64):
+    g, f, patch = configs.plume(64)
+    prm = configs.plume_params(tol=1e-4, max_cycles=12)
+    steps = 12
+    u, v, p, d, st = run_engine(g, f, patch, prm, steps)
+    eu, ev, ep, ed, info = run_oracle(o32, g, f, patch, prm, steps)
+    assert abs(st["time"] - info["time"]) <= 1e-12 * max(1.0, info["time"])
+    for name, a, b in (("u", eu, u), ("v", ev, v), ("p", ep, p), ("dye", ed, d)):
+        assert mismatch(a, b) == 0, "%s: %d values differ from the float32 oracle" % (name, mismatch(a, b))
+    # float64 trajectory drift: reported, loosely bounded
+    fu, fv, fp, fd, _ = run_oracle(o64, g, f, patch, prm, steps)
+    for name, a, b in (("u", fu, u), ("v", fv, v), ("dye", fd, d)):
+        diff = np.abs(a - b).max()
+        assert diff < 1e-3 * max(1.0, np.abs(a).max()), "%s drift %.3g" % (name, diff)
+
+
+def test_karman_steps_match_float32_oracle(o32):
+    g, f, patch = configs.karman(64, 48)
+    prm = configs.karman_params()
+    steps = 10
+    u, v, p, d, st = run_engine(g, f, patch, prm, steps)
+    eu, ev, ep, ed, info = run_oracle(o32, g, f, patch, prm, steps)
+    for name, a, b in (("u", eu, u), ("v", ev, v), ("p", ep, p), ("dye", ed, d)):
+        assert mismatch(a, b) == 0, "%s: %d values differ from the float32 oracle" % (name, mismatch(a, b))
+    # simulation.test.ts:22-39 — the outlet never takes inflow
+    U = u.reshape(g.ny, g.nx + 1)
+    assert (U[:, g.nx - 1] >= 0).all() and (U[:, g.nx] >= 0).all()
+
+
+def test_host_dt_step_matches_device_dt_step():
+    """fl_step with the caller's dt equals fl_step_auto when the caller passes
+    the dt the device would compute."""
+    g, f, patch = configs.plume(48)
+    prm = configs.plume_params(tol=1e-4, max_cycles=8)
+    ua, va, pa, da, st = run_engine(g, f, patch, prm, 1)
+    eng = native.Engine(g.nx, g.ny, g.h, params=prm)
+    try:
+        eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+        eng.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
+                 ptr(f32(f.dye)))
+        s0 = eng.stats()
+        keep = (ctypes.c_double * 3)(*[np.exp(-d * np.float64(np.float32(s0["dt"]))) if d > 0 else 1.0
+                                       for d in prm.dye_decay])
+        eng.call("fl_step", s0["dt"], s0["scale"], s0["grad_scale"], keep, None)
+        u = np.empty(eng.ufaces, np.float32)
+        v = np.empty(eng.vfaces, np.float32)
+        eng.call("fl_read_velocity", native.FL_F32, ptr(u), ptr(v))
+    finally:
+        eng.close()
+    assert mismatch(ua, u) == 0 and mismatch(va, v) == 0
+
+
+def test_uniform_through_flow_is_steady():
+    # emitters.test.ts:160-183 — u.fill(1) with an Air outlet is an exact
+    # steady solution; 20 steps leave it bit-for-bit unchanged.
+    g = sc.Grid(48, 32, 1 / 32)
+    spec = sc.SceneSpec(labels=sc.open_right(), seed=sc.uniform_flow(1.0))
+    f, _ = sc.reset_fields(g, g, spec)
+    prm = native.default_params(scheme=native.FL_MACCORMACK, solver=native.FL_SOLVER_MG, tol=1e-6, mg_max_cycles=5)
+    u, v, p, d, _ = run_engine(g, f, None, prm, 20)
+    assert np.array_equal(u, f32(f.u)) and np.array_equal(v, f32(f.v))
+
+
+def test_dye_decay_exponential_in_time():
+    # simulation.test.ts:69-82 — zero velocity, dye 1 decays as exp(-2 t)
+    g = sc.Grid(16, 16, 1 / 16)
+    f = sc.create_fields(g)
+    f.dye[:256] = 1.0
+    prm = native.default_params(dye_decay=(2.0, 0.0, 0.0), solver=native.FL_SOLVER_MG)
+    u, v, p, d, st = run_engine(g, f, None, prm, 30)
+    assert abs(d[0] - np.exp(-2 * st["time"])) < 1e-5
+    assert d[300] == 0
+
+
+def test_plume_reaches_relative_residual_target():
+    g, f, patch = configs.plume(128)
+    prm = configs.plume_params(tol=1e-5, max_cycles=40)
+    u, v, p, d, st = run_engine(g, f, patch, prm, 5)
+    assert 0 < st["rel_residual"] <= 1e-5, st
+    assert np.isfinite(u).all() and np.isfinite(d).all()
