@@ -1,0 +1,358 @@
+#!/usr/bin/env python
+"""Steps/s of the thermal-plume projection step at 1024^2, solved to a
+1e-6 relative residual, on one GB300 (or N independent replicas).
+
+Workload: the thermal-plume configuration at 1024^2 (closed box, two Gaussian
+heat+smoke sources of sigma 8 cells, beta 1, alpha 0.05, confinement 0.3,
+MacCormack advection, multigrid V(3,3) to an 8x8 coarsest level, every step
+solved to a relative residual of 1e-6 or the 20-cycle cap), float32 fields,
+synthetic seeded scene. One "step" is the whole projection step: advect u,v,
+body forces, divergence, pressure solve, gradient subtract + outflow, dye
+advection with decay and inlet, CFL reduction.
+
+  value   steps/s over K timed steps, fields resident in HBM, L2 flushed
+          (a 320 MB write) before every timed step, CUDA events on the
+          engine's stream; whole job = N ranks x K steps / max rank time.
+  e2e     the same steps through the C ABI with host buffers: every step
+          uploads u, v, p, label, dye from pinned host memory, steps, and
+          reads u, v, p, dye back.
+  roofline  the phase with the most device time, algorithmic bytes / its
+          event-timed duration, against MEASURED_PEAKS.json's HBM copy rate.
+  cpu_baseline  the float64 CPU port of the reference's step (the oracle),
+          one core, on a bounded sample of the same workload.
+
+--impl reference runs only that CPU port (rank 0) on the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = None
+BASELINE_PATH = os.path.join(ROOT, "BASELINE.json")
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def baseline_metric():
+    try:
+        with open(BASELINE_PATH) as fh:
+            return json.load(fh)["metric"]
+    except Exception:
+        return "steps/s at 1024^2 to 1e-6 relative residual (plain multigrid)"
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_PATH) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--max-cycles", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU-baseline sample")
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.samples = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append((time.time(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        sel = [p for t, p in self.samples if t0 - 0.25 <= t <= t1 + 0.25] or [p for _, p in self.samples]
+        if not sel:
+            return None
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(p[0]) for p in sel if num(p[0]) is not None]
+        mx = [num(p[1]) for p in sel if num(p[1]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for p in sel:
+            for k, n in enumerate(names):
+                if p[4 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sel)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------- CPU port
+
+def cpu_port_steps(size, tol, max_cycles, steps, warmup, state=None):
+    """Times `steps` steps of the float64 CPU port (the oracle's Simulation)
+    on the plume workload, after `warmup` untimed steps from `state` (host
+    fields) or from the reset scene. Returns (steps/s, seconds)."""
+    from flowlab_gb300 import configs
+    from oracle import Oracle, params_from_engine as oracle_params
+
+    g, f, patch = configs.plume(size)
+    prm = configs.plume_params(tol=tol, max_cycles=max_cycles)
+    sim = Oracle("f64").simulation(g.nx, g.ny, 1, **oracle_params(prm))
+    if state is not None:
+        u, v, p, dye = state
+        sim.set_fields(u, v, p, f.label, dye)
+    else:
+        sim.set_fields(f.u, f.v, f.p, f.label, f.dye)
+    sim.set_patch(patch.i0, patch.j0, patch.nx, patch.ny, patch.data)
+    for _ in range(warmup):
+        sim.step()
+    t = time.perf_counter()
+    for _ in range(steps):
+        sim.step()
+    dt = time.perf_counter() - t
+    return steps / dt, dt
+
+
+def run_reference(args, world, rank, pg):
+    metric = baseline_metric()
+    if rank != 0:
+        return
+    sps, secs = cpu_port_steps(args.size, args.tol, args.max_cycles, args.steps, args.warmup)
+    sample = "%d steps (after %d warm-up steps from the reset scene) of the %d^2 thermal plume, float64 CPU port of " \
+             "the reference's Simulation.step, one thread" % (args.steps, args.warmup, args.size)
+    line = {"metric": metric, "value": sps, "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / sps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args), "impl": "reference",
+            "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": sps, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    return {"workload": "thermal plume %dx%d, closed box, MacCormack, beta 1 / alpha 0.05 / confinement 0.3, "
+                        "multigrid V(3,3) coarsest 8x8, relative residual %.0e (cap %d cycles)"
+                        % (args.size, args.size, args.tol, args.max_cycles),
+            "grid": [args.size, args.size], "solver": "multigrid V(3,3), 32 coarse sweep pairs",
+            "tol": args.tol, "precision": "float32", "l2": "flushed (320 MB write) before every timed step",
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+# ------------------------------------------------------------ our engine
+
+def run_ours(args, world, rank, local, pg):
+    import numpy as np
+    import torch
+
+    from flowlab_gb300 import build, configs, native
+    from flowlab_gb300.native import f32, ptr
+
+    build.build()
+    torch.cuda.set_device(local)
+    g, f, patch = configs.plume(args.size)
+    prm = configs.plume_params(tol=args.tol, max_cycles=args.max_cycles)
+    eng = native.Engine(g.nx, g.ny, g.h, params=prm, device=local)
+    eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+    eng.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
+             ptr(f32(f.dye)))
+    iters = ctypes.c_int()
+    for _ in range(args.warmup):
+        eng.call("fl_step_auto", 1, ctypes.byref(iters))
+    eng.call("fl_synchronize")
+
+    # Host copy of the warmed-up state: the CPU baseline continues from it.
+    state = None
+    if rank == 0 and args.cpu_steps > 0:
+        su = np.empty(eng.ufaces, np.float32)
+        sv = np.empty(eng.vfaces, np.float32)
+        sp = np.empty(eng.cells, np.float32)
+        sd = np.empty(eng.dye_len, np.float32)
+        eng.call("fl_read_velocity", native.FL_F32, ptr(su), ptr(sv))
+        eng.call("fl_read_pressure", native.FL_F32, ptr(sp))
+        eng.call("fl_read_dye", native.FL_F32, ptr(sd))
+        state = (su.astype(np.float64), sv.astype(np.float64), sp.astype(np.float64), sd.astype(np.float64))
+
+    stream = torch.cuda.ExternalStream(eng.stream(), device=local)
+    flush = torch.empty(320 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:%d" % local)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    cycles, relres = [], []
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.5)
+    eng.profile(True)
+    barrier(pg)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        starts[k].record(stream)
+        eng.call("fl_step_auto", 1, ctypes.byref(iters))
+        ends[k].record(stream)
+        st = eng.stats()
+        cycles.append(st["cycles"])
+        relres.append(st["rel_residual"])
+    eng.call("fl_synchronize")
+    torch.cuda.synchronize()
+    barrier(pg)
+    t1 = time.time()
+    sampler.stop()
+    prof = eng.profile()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = max_over_ranks(pg, sum(step_ms))
+    value = world * args.steps / (total_ms / 1000.0)
+
+    # e2e: host buffers through the C ABI, copies inside the timed region
+    hu = torch.empty(eng.ufaces, dtype=torch.float32, pin_memory=True).numpy()
+    hv = torch.empty(eng.vfaces, dtype=torch.float32, pin_memory=True).numpy()
+    hp = torch.empty(eng.cells, dtype=torch.float32, pin_memory=True).numpy()
+    hd = torch.empty(eng.dye_len, dtype=torch.float32, pin_memory=True).numpy()
+    hl = torch.empty(eng.cells, dtype=torch.uint8, pin_memory=True).numpy()
+    eng.call("fl_read_velocity", native.FL_F32, ptr(hu), ptr(hv))
+    eng.call("fl_read_pressure", native.FL_F32, ptr(hp))
+    eng.call("fl_read_dye", native.FL_F32, ptr(hd))
+    hl[:] = f.label
+    barrier(pg)
+    te = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        eng.call("fl_upload_fields", native.FL_F32, ptr(hu), ptr(hv), ptr(hp), ptr(hl), ptr(hd))
+        eng.call("fl_step_auto", 1, ctypes.byref(iters))
+        eng.call("fl_read_velocity", native.FL_F32, ptr(hu), ptr(hv))
+        eng.call("fl_read_pressure", native.FL_F32, ptr(hp))
+        eng.call("fl_read_dye", native.FL_F32, ptr(hd))
+    e2e_s = max_over_ranks(pg, time.perf_counter() - te)
+    e2e_value = world * args.e2e_steps / e2e_s
+    h2d = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len) + eng.cells
+    d2h = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len)
+
+    cpu = None
+    if rank == 0 and args.cpu_steps > 0:
+        sps, secs = cpu_port_steps(args.size, args.tol, args.max_cycles, args.cpu_steps, 0, state)
+        cpu = {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
+               "sample": "%d steps of the %d^2 thermal plume continuing from the GPU's warmed-up state, float64 CPU "
+                         "port of the reference's Simulation.step, one thread (%.1f s)"
+                         % (args.cpu_steps, args.size, secs)}
+    eng.close()
+    if rank != 0:
+        return
+
+    peak, peak_kind = hbm_peak()
+    phases = {n: {"ms": ms, "launches": int(l), "gbytes": b / 1e9} for n, (ms, l, b) in prof.items() if l > 0}
+    dom = max(phases, key=lambda n: phases[n]["ms"])
+    d = phases[dom]
+    achieved = (d["gbytes"] / d["launches"]) / ((d["ms"] / d["launches"]) / 1000.0)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": d["gbytes"] * 1e9 / d["launches"],
+                "avg_launch_us": 1000.0 * d["ms"] / d["launches"]}
+    launches = int(sum(p["launches"] for p in phases.values()))
+    ms_per_step = total_ms / args.steps
+    line = {
+        "metric": baseline_metric(), "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded plume scene)",
+        "config": workload_config(args),
+        "cell_updates_per_s": value * args.size * args.size,
+        "vcycles_per_step": statistics.mean(cycles), "max_vcycles": max(cycles),
+        "rel_residual_max": max(relres), "converged_steps": sum(1 for r in relres if 0 <= r <= args.tol),
+        "roofline": roofline, "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": sampler.summary(t0, t1),
+        "phases_ms_per_step": {n: p["ms"] / args.steps for n, p in phases.items()},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local, pg = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, world, rank, pg)
+    else:
+        run_ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -21,6 +21,54 @@ struct fl_engine {
   Engine e;
 };
 
+namespace fl {
+
+int prof_begin(Engine& e, int phase) {
+  if (!e.profiling) return -1;
+  Engine::PendingPhase p;
+  p.phase = phase;
+  for (cudaEvent_t* ev : {&p.a, &p.b}) {
+    if (!e.event_pool.empty()) {
+      *ev = e.event_pool.back();
+      e.event_pool.pop_back();
+    } else if (cudaEventCreate(ev) != cudaSuccess) {
+      return -1;
+    }
+  }
+  p.bytes = 0;
+  p.launches = 0;
+  cudaEventRecord(p.a, e.stream);
+  e.pending.push_back(p);
+  return (int)e.pending.size() - 1;
+}
+
+void prof_end(Engine& e, int token, double bytes, int launches) {
+  if (token < 0 || token >= (int)e.pending.size()) return;
+  Engine::PendingPhase& p = e.pending[token];
+  p.bytes = bytes;
+  p.launches = launches;
+  cudaEventRecord(p.b, e.stream);
+}
+
+// Folds recorded phases into the counters (synchronises).
+static void prof_drain(Engine& e) {
+  if (e.pending.empty()) return;
+  cudaStreamSynchronize(e.stream);
+  for (auto& p : e.pending) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      e.prof_ms[p.phase] += ms;
+      e.prof_bytes[p.phase] += p.bytes;
+      e.prof_launches[p.phase] += p.launches;
+    }
+    e.event_pool.push_back(p.a);
+    e.event_pool.push_back(p.b);
+  }
+  e.pending.clear();
+}
+
+}  // namespace fl
+
 namespace {
 
 thread_local std::string g_create_error;
@@ -106,6 +154,11 @@ void free_all(Engine* e) {
   cudaFree(e->staging);
   if (!e->levels.empty()) cudaFree(e->levels[0].label);
   mg_free(*e);
+  for (auto& p : e->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
   if (e->acc_host) cudaFreeHost(e->acc_host);
   if (e->stream) cudaStreamDestroy(e->stream);
 }
@@ -138,8 +191,10 @@ StepScalars host_scalars(const Engine* e, float dt, float scale, float grad_scal
   return s;
 }
 
+// Ordered on the engine's (non-blocking) stream; a pageable source is staged
+// before the call returns, so `s` may be a temporary.
 int put_scalars(Engine* e, const StepScalars& s) {
-  return cuda_status(e, cudaMemcpy(e->sc, &s, sizeof s, cudaMemcpyHostToDevice), "scalars");
+  return cuda_status(e, cudaMemcpyAsync(e->sc, &s, sizeof s, cudaMemcpyHostToDevice, e->stream), "scalars");
 }
 
 int upload(Engine* e, void* dst, const void* src, long n, int dtype, const char* what) {
@@ -246,7 +301,9 @@ int rb_solve_device(Engine* e, float scale, int iterations, float omega, double 
   while (k < iterations) {
     int chunk = std::min(4, iterations - k);
     if (target >= 0) chunk = std::min(chunk, 12 - (k % 12));
+    const int tok = prof_begin(*e, FL_PH_RB_SWEEPS);
     launch_rb_sweeps(e->stream, L.nx, L.ny, L.x[src], L.x[1 - src], L.b, L.code, scale, omega, chunk);
+    prof_end(*e, tok, 13.0 * e->cells(), 1);
     TRY(check_launch(e, "red-black sweeps"));
     src = 1 - src;
     k += chunk;
@@ -282,8 +339,13 @@ int step_once(Engine* e, bool device_dt) {
   }
   const int mac = e->prm.scheme == FL_MACCORMACK;
   const int in = e->cur, out = 1 - e->cur;
+  const double N = (double)e->cells(), F = (double)(e->ufaces() + e->vfaces()), D = (double)e->dye_cells();
+  if (e->pending.size() > 8192) prof_drain(*e);
+  int tok = prof_begin(*e, FL_PH_ADVECT_VELOCITY);
   launch_advect_velocity(s, e->nx, e->ny, e->h, mac, e->u[in], e->v[in], e->u_hat, e->v_hat, e->u[out], e->v[out],
                          L0.label, e->sc);
+  // forward: carrier u,v + label in, faces out; correction: u,v + hat + label in, faces out
+  prof_end(*e, tok, mac ? (8 * F + N) + (12 * F + N) : 8 * F + N, mac ? 2 : 1);
   TRY(check_launch(e, "advect velocity"));
   e->cur = out;
   float* u = e->u[e->cur];
@@ -293,17 +355,28 @@ int step_once(Engine* e, bool device_dt) {
     e->stir_pending = false;
   }
   const bool conf = e->prm.confinement != 0;
+  const bool beta_on = e->prm.beta != 0, alpha_on = e->prm.alpha != 0;
+  tok = prof_begin(*e, FL_PH_BODY_FORCES);
+  double fbytes = 0;
+  int flaunch = 0;
   if (conf) {
     launch_vorticity(s, e->nx, e->ny, e->h, u, v, e->w);
     launch_confinement_force(s, e->nx, e->ny, e->h, e->w, L0.label, (float)e->prm.confinement, e->fx, e->fy);
+    fbytes += (4 * F + 4 * N) + (4 * N + N + 8 * N);
+    flaunch += 2;
   }
-  const bool beta_on = e->prm.beta != 0, alpha_on = e->prm.alpha != 0;
-  if (beta_on || alpha_on || conf)
+  if (beta_on || alpha_on || conf) {
     launch_forces(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, u, v, e->dye[e->dcur], L0.label, beta_on, alpha_on,
                   conf, e->fx, e->fy, e->sc);
+    fbytes += 8 * F + N + (beta_on ? 4 * D : 0) + (alpha_on ? 4 * D : 0) + (conf ? 8 * N : 0);
+    flaunch += 1;
+  }
+  prof_end(*e, tok, fbytes, flaunch);
   TRY(zero_solve_accum(e));
   const bool mg = e->prm.solver == FL_SOLVER_MG;
+  tok = prof_begin(*e, FL_PH_DIVERGENCE);
   launch_divergence(s, e->nx, e->ny, e->h, u, v, L0.b, mg, L0.label, e->sc, e->acc);
+  prof_end(*e, tok, 4 * F + N + 4 * N, 1);
   TRY(check_launch(e, "body forces / divergence"));
 
   int iters = 0;
@@ -316,7 +389,8 @@ int step_once(Engine* e, bool device_dt) {
     const double div_rms = rms(e->acc_host->b_sq, e->acc_host->n_fluid);
     e->last_div_rms = div_rms;
     StepScalars hs;
-    TRY(cuda_status(e, cudaMemcpy(&hs, e->sc, sizeof hs, cudaMemcpyDeviceToHost), "read scalars"));
+    TRY(cuda_status(e, cudaMemcpyAsync(&hs, e->sc, sizeof hs, cudaMemcpyDeviceToHost, s), "read scalars"));
+    TRY(sync(e, "read scalars"));
     if (div_rms == 0) {
       TRY(cuda_status(e, cudaMemsetAsync(L0.x[0], 0, e->cells() * sizeof(float), s), "zero p"));
     } else {
@@ -324,12 +398,19 @@ int step_once(Engine* e, bool device_dt) {
     }
   }
   e->last_iters = iters;
+  tok = prof_begin(*e, FL_PH_PROJECT);
   launch_subtract_outflow(s, e->nx, e->ny, L0.x[0], u, v, L0.label, e->sc, true, true);
+  prof_end(*e, tok, 4 * N + 4 * F + N + 4 * F, 1);
   const int din = e->dcur, dout = 1 - e->dcur;
+  tok = prof_begin(*e, FL_PH_ADVECT_DYE);
   launch_advect_dye(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, mac, u, v, e->dye[din], e->dye_hat, e->dye[dout],
                     L0.label, e->sc, true, e->patch, e->pi0, e->pj0, e->pnx, e->pny);
+  // forward: u,v + 3 planes + label in, 3 planes out; correction adds the hat planes
+  prof_end(*e, tok, mac ? (4 * F + 24 * D + N) + (4 * F + 36 * D + N) : 4 * F + 24 * D + N, mac ? 2 : 1);
   e->dcur = dout;
+  tok = prof_begin(*e, FL_PH_CFL);
   launch_max_speed(s, e->nx, e->ny, u, v, e->acc, e->sc, e->time_dev, &e->prm, e->h, device_dt, device_dt);
+  prof_end(*e, tok, 4 * F, 1);
   TRY(check_launch(e, "project / dye / CFL"));
   e->steps++;
   return FL_OK;
@@ -619,6 +700,30 @@ int fl_read_pressure(fl_engine* h, int dtype, void* p) {
   ENTER(h);
   TRY(download(e, p, e->levels[0].x[0], e->cells(), dtype, "read p"));
   return sync(e, "read pressure");
+}
+
+int fl_profile_enable(fl_engine* h, int on) {
+  ENTER(h);
+  prof_drain(*e);
+  for (int k = 0; k < FL_PHASES; k++) {
+    e->prof_ms[k] = 0;
+    e->prof_bytes[k] = 0;
+    e->prof_launches[k] = 0;
+  }
+  e->profiling = on != 0;
+  return FL_OK;
+}
+
+int fl_profile_read(fl_engine* h, fl_profile* out) {
+  ENTER(h);
+  if (!out) return fail(e, FL_EINVAL, "null profile");
+  prof_drain(*e);
+  for (int k = 0; k < FL_PHASES; k++) {
+    out->ms[k] = e->prof_ms[k];
+    out->bytes[k] = e->prof_bytes[k];
+    out->launches[k] = e->prof_launches[k];
+  }
+  return check_launch(e, "profile");
 }
 
 // ----------------------------------------------------------- Advector seam

@@ -71,6 +71,20 @@ struct Engine {
   bool labels_dirty = false;
   bool codes_valid = false;
 
+  // phase profiling (fl_profile_enable / fl_profile_read)
+  struct PendingPhase {
+    int phase;
+    cudaEvent_t a, b;
+    double bytes;
+    int launches;
+  };
+  bool profiling = false;
+  std::vector<PendingPhase> pending;
+  std::vector<cudaEvent_t> event_pool;
+  double prof_ms[FL_PHASES] = {};
+  double prof_bytes[FL_PHASES] = {};
+  long long prof_launches[FL_PHASES] = {};
+
   // report
   double time = 0;
   int steps = 0;
@@ -84,6 +98,12 @@ struct Engine {
   long vfaces() const { return (long)nx * (ny + 1); }
   long dye_cells() const { return (long)dnx * dny; }
 };
+
+// Phase timing: prof_begin records the start event (returns -1 when
+// profiling is off), prof_end the stop event with the phase's algorithmic
+// bytes and launch count. Defined in fl_engine.cu.
+int prof_begin(Engine& e, int phase);
+void prof_end(Engine& e, int token, double bytes, int launches);
 
 // ------------------------------------------------------------- launchers
 

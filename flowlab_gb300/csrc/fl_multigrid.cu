@@ -625,9 +625,12 @@ void mg_vcycle(Engine& e, StepAccum* acc) {
   cudaStream_t s = e.stream;
   const int lc = e.coarse_level;
   const float omega = (float)e.prm.mg_omega;
+  auto cells = [&](int l) { return (double)e.levels[l].nx * e.levels[l].ny; };
   for (int l = 0; l < lc; l++) {
     Level& L = e.levels[l];
     Level& C = e.levels[l + 1];
+    // x (level 0 only: coarser levels start from zero), b, code, x out, coarse b
+    const int tok = prof_begin(e, FL_PH_MG_DOWN);
     SmoothArgs a{};
     a.nx = L.nx;
     a.ny = L.ny;
@@ -642,8 +645,12 @@ void mg_vcycle(Engine& e, StepAccum* acc) {
     a.cny = C.ny;
     a.x_is_zero = l > 0;
     launch_smooth(s, a, e.prm.mg_pre, MODE_PRE);
+    prof_end(e, tok, (l == 0 ? 13.0 : 9.0) * cells(l) + 4.0 * cells(l + 1), 1);
   }
   {
+    const int tok = prof_begin(e, FL_PH_MG_COARSE);
+    double bytes = (lc == 0 ? 4.0 : 0.0) * cells(lc) + 8.0 * cells(lc);
+    for (int l = lc; l < (int)e.levels.size(); l++) bytes += cells(l);
     CoarseArgs a{};
     int ox[MAX_LEVELS], ob[MAX_LEVELS], oc[MAX_LEVELS];
     coarse_smem_bytes(e, lc, ox, ob, oc);
@@ -661,10 +668,13 @@ void mg_vcycle(Engine& e, StepAccum* acc) {
     a.omega = omega;
     a.acc = lc == 0 ? acc : nullptr;
     k_mg_coarse<<<1, COARSE_THREADS, e.coarse_smem, s>>>(a);
+    prof_end(e, tok, bytes, 1);
   }
   for (int l = lc - 1; l >= 0; l--) {
     Level& L = e.levels[l];
     Level& C = e.levels[l + 1];
+    // x in, b, code, coarse e, x out
+    const int tok = prof_begin(e, FL_PH_MG_UP);
     SmoothArgs a{};
     a.nx = L.nx;
     a.ny = L.ny;
@@ -679,6 +689,7 @@ void mg_vcycle(Engine& e, StepAccum* acc) {
     a.cny = C.ny;
     a.acc = l == 0 ? acc : nullptr;
     launch_smooth(s, a, e.prm.mg_post, MODE_POST);
+    prof_end(e, tok, 13.0 * cells(l) + 4.0 * cells(l + 1), 1);
   }
 }
 

@@ -73,6 +73,20 @@ class Stats(ctypes.Structure):
     ]
 
 
+PHASES = ["advect_velocity", "body_forces", "divergence", "mg_down", "mg_coarse", "mg_up", "rb_sweeps", "project",
+          "advect_dye", "cfl"]
+
+
+class Profile(ctypes.Structure):
+    """fl_profile."""
+
+    _fields_ = [
+        ("ms", ctypes.c_double * 10),
+        ("launches", ctypes.c_longlong * 10),
+        ("bytes", ctypes.c_double * 10),
+    ]
+
+
 # (name, restype, argtypes) for every entry point of include/flowlab_gb300.h
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -99,6 +113,8 @@ SIGNATURES = [
     ("fl_read_velocity", _I, [_P, _I, _P, _P]),
     ("fl_read_dye", _I, [_P, _I, _P]),
     ("fl_read_pressure", _I, [_P, _I, _P]),
+    ("fl_profile_enable", _I, [_P, _I]),
+    ("fl_profile_read", _I, [_P, _P]),
     ("fl_advect_velocity", _I, [_P, _I, _P, _P, _P, _P, _P, _F]),
     ("fl_advect_dye", _I, [_P, _I, _P, _P, _P, _P, _P, _F]),
     ("fl_rb_solve", _I, [_P, _P, _P, _P, _F, _I, _F, _D, _P]),
@@ -210,6 +226,15 @@ class Engine:
     def set_params(self, params):
         self.params = params
         self.call("fl_set_params", ctypes.byref(params))
+
+    def profile(self, enable=None):
+        """Per-phase {name: (ms, launches, bytes)} since profiling was enabled."""
+        if enable is not None:
+            self.call("fl_profile_enable", int(enable))
+            return None
+        p = Profile()
+        self.call("fl_profile_read", ctypes.byref(p))
+        return {n: (p.ms[k], p.launches[k], p.bytes[k]) for k, n in enumerate(PHASES)}
 
     def stats(self):
         s = Stats()

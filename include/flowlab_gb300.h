@@ -101,6 +101,24 @@ typedef struct fl_stats {
   double max_face_speed; /* max |u|,|v| after the last step (CFL input of the next one) */
 } fl_stats;
 
+/* Per-phase device timing of fused steps, from CUDA events recorded on the
+ * engine's stream around each phase while profiling is enabled. `bytes` is
+ * the algorithmic DRAM traffic the engine attributes to the phase: each
+ * array a kernel must read or write, counted once per launch. No
+ * counterpart in the reference (its profiler is host-side phase timing,
+ * src/core/profiler.ts:39-113). */
+#define FL_PHASES 10
+/* phase indices */
+enum fl_phase {
+  FL_PH_ADVECT_VELOCITY = 0, FL_PH_BODY_FORCES = 1, FL_PH_DIVERGENCE = 2, FL_PH_MG_DOWN = 3, FL_PH_MG_COARSE = 4,
+  FL_PH_MG_UP = 5, FL_PH_RB_SWEEPS = 6, FL_PH_PROJECT = 7, FL_PH_ADVECT_DYE = 8, FL_PH_CFL = 9
+};
+typedef struct fl_profile {
+  double ms[FL_PHASES];
+  long long launches[FL_PHASES];
+  double bytes[FL_PHASES];
+} fl_profile;
+
 /* Fills `p` with the reference defaults (simulation.ts:223-234,
  * pressureMultigrid.ts:47-67). */
 void fl_default_params(fl_params* p);
@@ -154,6 +172,11 @@ int fl_get_stats(fl_engine* e, fl_stats* out);
 int fl_read_velocity(fl_engine* e, int dtype, void* u, void* v);
 int fl_read_dye(fl_engine* e, int dtype, void* dye);
 int fl_read_pressure(fl_engine* e, int dtype, void* p);
+
+/* Enables (1) or disables (0) phase timing and clears the counters. */
+int fl_profile_enable(fl_engine* e, int on);
+/* Synchronises and returns the counters accumulated since enabling. */
+int fl_profile_read(fl_engine* e, fl_profile* out);
 
 /* ------------------------------------ Advector (advector.ts:28-63), float32 host arrays */
 

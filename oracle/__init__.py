@@ -76,6 +76,15 @@ def make_params(**kw):
     return p
 
 
+def params_from_engine(p):
+    """The oracle's StepParams for an engine fl_params (flowlab_gb300.native.Params)."""
+    return dict(cflTarget=p.cfl_target, dtMax=p.dt_max, rho=p.rho, macCormack=int(p.scheme == 1),
+                solver=SOLVER_MG if p.solver == 1 else SOLVER_RBSOR, pressureIters=p.pressure_iters,
+                mgMaxCycles=p.mg_max_cycles, omega=p.omega, tol=p.tol, dyeDecay=tuple(p.dye_decay), beta=p.beta,
+                alpha=p.alpha, confinement=p.confinement, mgPre=p.mg_pre, mgPost=p.mg_post,
+                mgCoarseSweeps=p.mg_coarse_sweeps, mgCoarsest=p.mg_coarsest, mgOmega=p.mg_omega)
+
+
 def lib():
     global _LIB
     if _LIB is None:

@@ -136,8 +136,15 @@ def test_mg_tiled_identical(o32, o64, nx, ny, pre, post, coarse, coarsest):
         eng.close()
     e32, _, _ = o32.mg_solve(nx, ny, warm, f32(div), label, 0.02, 3, 0.0, pre, post, coarse, coarsest)
     assert_identical(e32, p, "multigrid %dx%d" % (nx, ny))
+    # Precision: after 3 cycles the float32 iterate has drifted from the
+    # float64 one by O(eps) amplified by the unconverged smooth modes, so the
+    # bar is the reference's second one — the same residual to 1%
+    # (multigrid.gputest.ts:236-238).
     e64, _, _ = o64.mg_solve(nx, ny, warm.astype(np.float64), div, label, 0.02, 3, 0.0, pre, post, coarse, coarsest)
-    assert_close_rel(e64, p, "multigrid %dx%d vs float64" % (nx, ny), rel=1e-4)
+    r_cpu = o64.rms_remaining(nx, ny, e64, div, label, 0.02)
+    r_gpu = o64.rms_remaining(nx, ny, p.astype(np.float64), div, label, 0.02)
+    assert abs(r_gpu - r_cpu) < 0.01 * r_cpu, (r_gpu, r_cpu)
+    assert_close_rel(e64, p, "multigrid %dx%d vs float64" % (nx, ny), rel=2e-3)
 
 
 def test_mg_tolerance_matches_oracle(o32):
