@@ -18,7 +18,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libflowlab_gb300.so")
 
-SOURCES = ["fl_engine.cu", "fl_multigrid.cu", "fl_advect.cu", "fl_project.cu"]
+SOURCES = ["fl_engine.cu", "fl_multigrid.cu", "fl_advect.cu", "fl_project.cu", "fl_noalloc.cu"]
 HEADERS = ["fl_common.cuh", "fl_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [

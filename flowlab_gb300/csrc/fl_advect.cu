@@ -171,6 +171,13 @@ void launch_advect_velocity(cudaStream_t s, int nx, int ny, float h, int mac, co
   }
 }
 
+cudaError_t preload_advect_kernels() {
+  cudaFuncAttributes a;
+  cudaError_t err = cudaFuncGetAttributes(&a, k_advect_velocity<0>);
+  if (err == cudaSuccess) err = cudaFuncGetAttributes(&a, k_advect_velocity<1>);
+  return err;
+}
+
 void launch_advect_dye(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, int mac, const float* u,
                        const float* v, const float* q_in, float* q_hat, float* q_out, const uint8_t* label,
                        const StepScalars* sc, bool tail, const float* patch, int pi0, int pj0, int pnx, int pny) {

@@ -73,6 +73,19 @@ namespace {
 
 thread_local std::string g_create_error;
 
+}  // namespace
+
+void fl::set_global_error(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_create_error = buf;
+}
+
+namespace {
+
 int fail(Engine* e, int code, const char* fmt, ...) {
   char buf[512];
   va_list ap;

@@ -105,6 +105,10 @@ struct Engine {
 int prof_begin(Engine& e, int phase);
 void prof_end(Engine& e, int token, double bytes, int launches);
 
+// Message for fl_last_error(NULL) (calls that have no engine). Defined in
+// fl_engine.cu.
+void set_global_error(const char* fmt, ...);
+
 // ------------------------------------------------------------- launchers
 
 // fl_advect.cu
@@ -114,6 +118,8 @@ void launch_advect_velocity(cudaStream_t s, int nx, int ny, float h, int mac, co
 void launch_advect_dye(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, int mac, const float* u,
                        const float* v, const float* q_in, float* q_hat, float* q_out, const uint8_t* label,
                        const StepScalars* sc, bool tail, const float* patch, int pi0, int pj0, int pnx, int pny);
+// Loads the velocity-advection kernels (so that later launches need no module load).
+cudaError_t preload_advect_kernels();
 
 // fl_project.cu
 void launch_vorticity(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* w);

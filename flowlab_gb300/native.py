@@ -127,6 +127,7 @@ SIGNATURES = [
     ("fl_body_forces", _I, [_P, _P, _P, _P, _P, _F, _F, _F, _F]),
     ("fl_stir", _I, [_P, _P, _P, _P, _F, _F, _F, _F, _F]),
     ("fl_dye_patch", _I, [_P, _P, _I, _I, _I, _I, _P]),
+    ("fl_advect_velocity_noalloc", _I, [_I, _I, _I, _F, _F, _P, _P, _P, _P, _P, _P]),
 ]
 
 _lib = None

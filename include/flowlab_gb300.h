@@ -217,6 +217,28 @@ int fl_stir(fl_engine* e, float* u, float* v, const uint8_t* label, float x, flo
             float dy);                                                                /* stir.ts:49-83 */
 int fl_dye_patch(fl_engine* e, float* dye, int i0, int j0, int pnx, int pny, const float* data); /* dye.ts:158-175 */
 
+/* --------------------------------------------- no-allocation variant */
+
+/*
+ * Velocity advection (semi-Lagrangian or MacCormack, as fl_advect_velocity)
+ * on the caller's own DEVICE buffers, allocating nothing. This entry point has
+ * no counterpart in the reference. It is for callers that cannot call
+ * cudaMalloc where they advect: code recorded into a CUDA graph by stream
+ * capture, real-time or callback threads that must not block in an
+ * allocator, and hosts whose device memory comes from an arena they do not
+ * own. The MacCormack scratch lives in one fixed array of the library's
+ * device memory (about 8.8 MB on every GPU that loads the library, held until
+ * exit), so the grid may have at most 2,200,000 faces, (nx+1)*ny + nx*(ny+1)
+ * (1024x1024 fits); larger grids return FL_EINVAL. The first call on each
+ * device looks the array up and loads the kernels, so make it before any
+ * stream capture. Calls on one device share the array: calls whose work
+ * overlaps on the GPU race, so order them on one stream. Work is queued on
+ * `stream` (a cudaStream_t, NULL for the default stream) and not waited for.
+ * Errors are reported by fl_last_error(NULL).
+ */
+int fl_advect_velocity_noalloc(int scheme, int nx, int ny, float h, float dt, const float* u_in, const float* v_in,
+                               float* u_out, float* v_out, const uint8_t* label, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
