@@ -165,6 +165,9 @@ void free_all(Engine* e) {
   cudaFree(e->acc);
   cudaFree(e->time_dev);
   cudaFree(e->staging);
+  cudaFree(e->p64[0]);
+  cudaFree(e->p64[1]);
+  cudaFree(e->r32);
   if (!e->levels.empty()) cudaFree(e->levels[0].label);
   mg_free(*e);
   for (auto& p : e->pending) {
@@ -302,6 +305,50 @@ int mg_solve_device(Engine* e, int max_cycles, double tol, int* cycles, double* 
   return FL_OK;
 }
 
+// Float64 defect correction around the multigrid (the oracle's solveMixed):
+// p64[par] is the pressure, levels[0].b the float rhs with its fluid sums in
+// acc. Each pass: one float V-cycle on A e = r (from e = 0), then
+// p64 += e and r = b - A p64 in double; stop when the relative residual
+// reaches tol (tested before every pass, so a converged warm start costs no
+// cycle) or after max_cycles.
+int mg_solve_mixed_device(Engine* e, int max_cycles, double tol, int* cycles, double* relres) {
+  Level& L0 = e->levels[0];
+  cudaStream_t s = e->stream;
+  TRY(zero_residual_accum(e));
+  launch_update_resid64(s, e->nx, e->ny, e->p64[e->par], nullptr, L0.b, L0.code, nullptr, e->r32, e->acc);
+  TRY(check_launch(e, "residual"));
+  TRY(read_accum(e));
+  const double b_rms = rms(e->acc_host->b_sq, e->acc_host->n_fluid);
+  e->last_div_rms = b_rms;
+  *cycles = 0;
+  if (b_rms == 0) {
+    TRY(cuda_status(e, cudaMemsetAsync(e->p64[e->par], 0, e->cells() * sizeof(double), s), "zero p"));
+    *relres = 0;
+    return FL_OK;
+  }
+  if (!std::isfinite(b_rms)) return fail(e, FL_ENONFINITE, "non-finite divergence");
+  double rel = rms(e->acc_host->res_sq, e->acc_host->n_res) / b_rms;
+  *relres = rel;
+  int c = 0;
+  while (c < max_cycles && !(rel <= tol)) {
+    mg_vcycle_on(*e, e->r32, true, nullptr);
+    TRY(zero_residual_accum(e));
+    const int tok = prof_begin(*e, FL_PH_MG_UP);
+    launch_update_resid64(s, e->nx, e->ny, e->p64[e->par], L0.x[0], L0.b, L0.code, e->p64[1 - e->par], e->r32,
+                          e->acc);
+    prof_end(*e, tok, 29.0 * e->cells(), 1);
+    TRY(check_launch(e, "update + residual"));
+    e->par = 1 - e->par;
+    TRY(read_accum(e));
+    rel = rms(e->acc_host->res_sq, e->acc_host->n_res) / b_rms;
+    *relres = rel;
+    if (!std::isfinite(rel)) return fail(e, FL_ENONFINITE, "non-finite residual after %d V-cycles", c + 1);
+    c++;
+  }
+  *cycles = c;
+  return FL_OK;
+}
+
 // Red-black SOR to tolerance (pressureRedBlack.ts:88-113) on div in
 // levels[0].b with the warm start in levels[0].x[0]. Sweep pairs are grouped
 // up to four per launch (temporal blocking) and never across a 12-sweep check.
@@ -393,7 +440,12 @@ int step_once(Engine* e, bool device_dt) {
   TRY(check_launch(e, "body forces / divergence"));
 
   int iters = 0;
-  if (mg) {
+  const bool mixed = mg && e->prm.mixed;
+  if (mixed) {
+    double rr;
+    TRY(mg_solve_mixed_device(e, e->prm.mg_max_cycles, e->prm.tol, &iters, &rr));
+    e->last_relres = rr;
+  } else if (mg) {
     double rr;
     TRY(mg_solve_device(e, e->prm.mg_max_cycles, e->prm.tol, &iters, &rr));
     e->last_relres = rr;
@@ -412,8 +464,9 @@ int step_once(Engine* e, bool device_dt) {
   }
   e->last_iters = iters;
   tok = prof_begin(*e, FL_PH_PROJECT);
-  launch_subtract_outflow(s, e->nx, e->ny, L0.x[0], u, v, L0.label, e->sc, true, true);
-  prof_end(*e, tok, 4 * N + 4 * F + N + 4 * F, 1);
+  launch_subtract_outflow(s, e->nx, e->ny, L0.x[0], u, v, L0.label, e->sc, true, true,
+                          mixed ? e->p64[e->par] : nullptr);
+  prof_end(*e, tok, (mixed ? 8 : 4) * N + 4 * F + N + 4 * F, 1);
   const int din = e->dcur, dout = 1 - e->dcur;
   tok = prof_begin(*e, FL_PH_ADVECT_DYE);
   launch_advect_dye(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, mac, u, v, e->dye[din], e->dye_hat, e->dye[dout],
@@ -519,6 +572,9 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   s = s ? s : dalloc(e, (void**)&e->acc, sizeof(StepAccum), "accumulators");
   s = s ? s : dalloc(e, (void**)&e->time_dev, sizeof(double), "clock");
   s = s ? s : dalloc(e, &e->staging, e->staging_bytes, "staging");
+  s = s ? s : dalloc(e, (void**)&e->p64[0], (size_t)e->cells() * 8, "p64");
+  s = s ? s : dalloc(e, (void**)&e->p64[1], (size_t)e->cells() * 8, "p64");
+  s = s ? s : dalloc(e, (void**)&e->r32, cf, "residual");
   if (s) return bail(s);
   if (cudaMallocHost(&e->acc_host, sizeof(StepAccum)) != cudaSuccess) {
     fail(e, FL_ENOMEM, "pinned accumulator");
@@ -590,6 +646,13 @@ int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, cons
     TRY(upload(e, e->levels[0].x[0], p, e->cells(), dtype, "upload p"));
   else
     TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].x[0], 0, e->cells() * 4, e->stream), "zero p"));
+  // the float64 pressure of the defect-correction solve starts from the same p
+  e->par = 0;
+  if (p && dtype == FL_F64)
+    TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, e->cells() * sizeof(double), cudaMemcpyHostToDevice, e->stream),
+                    "upload p64"));
+  else
+    launch_convert(e->stream, e->levels[0].x[0], FL_F32, e->p64[0], FL_F64, e->cells());
   TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "upload label"));
   TRY(upload(e, e->dye[0], dye, 3 * e->dye_cells(), dtype, "upload dye"));
   mg_build_codes(*e);
@@ -711,6 +774,22 @@ int fl_read_dye(fl_engine* h, int dtype, void* dye) {
 
 int fl_read_pressure(fl_engine* h, int dtype, void* p) {
   ENTER(h);
+  if (e->prm.solver == FL_SOLVER_MG && e->prm.mixed) {
+    if (!p) return fail(e, FL_EINVAL, "read p: null pointer");
+    const long n = e->cells();
+    if (dtype == FL_F64) {
+      TRY(cuda_status(e, cudaMemcpyAsync(p, e->p64[e->par], n * sizeof(double), cudaMemcpyDeviceToHost, e->stream),
+                      "read p"));
+    } else if (dtype == FL_F32) {
+      launch_convert(e->stream, e->p64[e->par], FL_F64, e->staging, FL_F32, n);
+      TRY(check_launch(e, "read p"));
+      TRY(cuda_status(e, cudaMemcpyAsync(p, e->staging, n * sizeof(float), cudaMemcpyDeviceToHost, e->stream),
+                      "read p"));
+    } else {
+      return fail(e, FL_EINVAL, "read p: dtype %d", dtype);
+    }
+    return sync(e, "read pressure");
+  }
   TRY(download(e, p, e->levels[0].x[0], e->cells(), dtype, "read p"));
   return sync(e, "read pressure");
 }
@@ -823,6 +902,30 @@ int fl_mg_solve(fl_engine* h, float* p, const float* div, const uint8_t* label, 
   if (rel_residual) *rel_residual = rr;
   TRY(down32(e, p, L.x[0], n * 4, "p"));
   return sync(e, "mg solve");
+}
+
+int fl_mg_solve_mixed(fl_engine* h, double* p, const float* div, const uint8_t* label, float scale, int max_cycles,
+                      double tol, int* cycles_used, double* rel_residual) {
+  ENTER(h);
+  e->uploaded = false;
+  if (!p || !div || !label) return fail(e, FL_EINVAL, "null pointer");
+  const long n = e->cells();
+  Level& L = e->levels[0];
+  e->par = 0;
+  TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, n * sizeof(double), cudaMemcpyHostToDevice, e->stream), "p"));
+  TRY(up32(e, e->u_hat, div, n * 4, "div"));
+  TRY(up32(e, L.label, label, (size_t)n, "label"));
+  mg_build_codes(*e);
+  TRY(zero_solve_accum(e));
+  launch_scale_rhs(e->stream, n, e->u_hat, L.b, -scale, L.label, e->acc);
+  TRY(check_launch(e, "rhs"));
+  int cycles = 0;
+  double rr = -1;
+  TRY(mg_solve_mixed_device(e, max_cycles, tol, &cycles, &rr));
+  if (cycles_used) *cycles_used = cycles;
+  if (rel_residual) *rel_residual = rr;
+  TRY(cuda_status(e, cudaMemcpyAsync(p, e->p64[e->par], n * sizeof(double), cudaMemcpyDeviceToHost, e->stream), "p"));
+  return sync(e, "mg solve mixed");
 }
 
 // ------------------------------------------------------------ single passes

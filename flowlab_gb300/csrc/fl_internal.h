@@ -49,6 +49,12 @@ struct Engine {
   int coarse_level = 0;       // first level solved inside the single-CTA kernel
   size_t coarse_smem = 0;
 
+  // float64 pressure of the defect-correction solve (fl_params.mixed):
+  // p64[par] is the pressure, r32 the float residual fed to each V-cycle.
+  double* p64[2] = {nullptr, nullptr};
+  int par = 0;
+  float* r32 = nullptr;
+
   float* w = nullptr;   // vorticity scratch
   float* fx = nullptr;  // confinement force scratch
   float* fy = nullptr;
@@ -131,7 +137,8 @@ void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, fl
 void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
                        bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc);
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
-                             const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow);
+                             const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow,
+                             const double* p64 = nullptr);
 void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const float* v, StepAccum* acc,
                       StepScalars* sc_next, double* time_dev, const fl_params* prm, float h, bool write_scalars,
                       bool add_time);
@@ -151,6 +158,9 @@ void mg_setup(Engine& e);  // allocates levels for e.nx, e.ny and the coarsest s
 void mg_free(Engine& e);
 void mg_build_codes(Engine& e);  // label chain + stencil codes from levels[0].label
 void mg_vcycle(Engine& e, StepAccum* acc_for_residual);
+void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc_for_residual);
+void launch_update_resid64(cudaStream_t s, int nx, int ny, const double* p_in, const float* e, const float* b,
+                           const uint8_t* code, double* p_out, float* r32, StepAccum* acc);
 void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* x_out, const float* b,
                       const uint8_t* code, float scale, float omega, int pairs);
 void launch_rms_remaining(cudaStream_t s, int nx, int ny, const float* p, const float* div, const uint8_t* code,

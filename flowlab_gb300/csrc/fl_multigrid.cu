@@ -402,6 +402,53 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(CoarseArgs a) {
   for (int k = tid; k < n; k += COARSE_THREADS) a.x_top[k] = fs[T.off_x + k];
 }
 
+// Float64 defect correction (oracle: solveMixed). p_out = p_in + e (e may be
+// null: no update), then r = b - A p_out in double with the neighbour sum in
+// the order +x, -x, +y, -y; r is stored as float (the next V-cycle's rhs) and
+// its square summed over fluid cells with links. Each thread also forms its
+// four neighbours' updated values (the same additions their own threads
+// make), so the kernel needs no halo exchange; p_out must not alias p_in.
+__global__ void __launch_bounds__(256) k_update_resid64(int nx, int ny, const double* __restrict__ p_in,
+                                                        const float* __restrict__ e, const float* __restrict__ b,
+                                                        const uint8_t* __restrict__ code, double* __restrict__ p_out,
+                                                        float* __restrict__ r32, StepAccum* acc) {
+  __shared__ double red[32];
+  __shared__ unsigned long long redn[32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  double sq = 0.0;
+  unsigned long long n = 0;
+  if (i < nx && j < ny) {
+    const long k = i + (long)j * nx;
+    auto P = [&](long q) { return e ? p_in[q] + (double)e[q] : p_in[q]; };
+    const double pk = P(k);
+    if (p_out) p_out[k] = pk;
+    const uint8_t c = code[k];
+    float r = 0.0f;
+    if ((c & 3u) == FLUID) {
+      const int cnt = code_count(c);
+      if (cnt > 0) {
+        double sum = 0.0;
+        if (c & LINK_XP) sum += P(k + 1);
+        if (c & LINK_XM) sum += P(k - 1);
+        if (c & LINK_YP) sum += P(k + nx);
+        if (c & LINK_YM) sum += P(k - nx);
+        const double rd = (double)b[k] - ((double)cnt * pk - sum);
+        r = (float)rd;
+        sq = rd * rd;
+        n = 1;
+      }
+    }
+    r32[k] = r;
+  }
+  const double bs = block_sum(sq, red);
+  const unsigned long long bn = block_sum_u64(n, redn);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    atomicAdd(&acc->res_sq, bs);
+    atomicAdd(&acc->n_res, bn);
+  }
+}
+
 // Remaining divergence of the red-black solver's stopping test (pressure.ts:
 // 127-167): neighbour sum in the lexicographic order +x, +y, -x, -y, the
 // residual formed in double.
@@ -526,6 +573,12 @@ void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* 
   launch_smooth(s, a, pairs, MODE_PLAIN);
 }
 
+void launch_update_resid64(cudaStream_t s, int nx, int ny, const double* p_in, const float* e, const float* b,
+                           const uint8_t* code, double* p_out, float* r32, StepAccum* acc) {
+  dim3 bl(32, 8), g((nx + 31) / 32, (ny + 7) / 8);
+  k_update_resid64<<<g, bl, 0, s>>>(nx, ny, p_in, e, b, code, p_out, r32, acc);
+}
+
 void launch_rms_remaining(cudaStream_t s, int nx, int ny, const float* p, const float* div, const uint8_t* code,
                           float scale, StepAccum* acc) {
   dim3 b(32, 8), g((nx + 31) / 32, (ny + 7) / 8);
@@ -621,7 +674,12 @@ void mg_build_codes(Engine& e) {
 // start in levels[0].x[0]; the result lands back in levels[0].x[0]. When
 // `acc` is set, the finest level's residual sum of squares is accumulated
 // into it for the tolerance test.
-void mg_vcycle(Engine& e, StepAccum* acc) {
+void mg_vcycle(Engine& e, StepAccum* acc) { mg_vcycle_on(e, e.levels[0].b, false, acc); }
+
+// One V-cycle with level 0's rhs `b0`; with `zero_start` the level-0 unknown
+// starts from 0 (the correction equation of the defect-correction loop)
+// instead of the warm start in levels[0].x[0].
+void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc) {
   cudaStream_t s = e.stream;
   const int lc = e.coarse_level;
   const float omega = (float)e.prm.mg_omega;
@@ -636,14 +694,14 @@ void mg_vcycle(Engine& e, StepAccum* acc) {
     a.ny = L.ny;
     a.xin = L.x[0];
     a.xout = L.x[1];
-    a.b = L.b;
+    a.b = l == 0 ? b0 : L.b;
     a.code = L.code;
     a.scale = -1.0f;
     a.omega = omega;
     a.bc = C.b;
     a.cnx = C.nx;
     a.cny = C.ny;
-    a.x_is_zero = l > 0;
+    a.x_is_zero = l > 0 || zero_start;
     launch_smooth(s, a, e.prm.mg_pre, MODE_PRE);
     prof_end(e, tok, (l == 0 ? 13.0 : 9.0) * cells(l) + 4.0 * cells(l + 1), 1);
   }
@@ -659,9 +717,9 @@ void mg_vcycle(Engine& e, StepAccum* acc) {
       const Level& L = e.levels[lc + l];
       a.lv[l] = CoarseLevel{L.nx, L.ny, L.code, ox[l], ob[l], oc[l]};
     }
-    a.b_top = e.levels[lc].b;
+    a.b_top = lc == 0 ? b0 : e.levels[lc].b;
     a.x_top = e.levels[lc].x[0];
-    a.x_is_zero = lc > 0;
+    a.x_is_zero = lc > 0 || zero_start;
     a.pre = e.prm.mg_pre;
     a.post = e.prm.mg_post;
     a.coarse_sweeps = e.prm.mg_coarse_sweeps;
@@ -680,7 +738,7 @@ void mg_vcycle(Engine& e, StepAccum* acc) {
     a.ny = L.ny;
     a.xin = L.x[1];
     a.xout = L.x[0];
-    a.b = L.b;
+    a.b = l == 0 ? b0 : L.b;
     a.code = L.code;
     a.scale = -1.0f;
     a.omega = omega;

@@ -128,30 +128,36 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
 //   u(1,j) and u(0,j): thread (1,j); u(nx-1,j) and u(nx,j): thread (nx-1,j).
 // With nx == 2 both edges meet at face 1, handled left then right as the
 // reference's loop order does.
-__device__ __forceinline__ float projected_u(const float* __restrict__ p, const float* __restrict__ u,
-                                             const uint8_t* __restrict__ label, int nx, int ny, int i, int j,
-                                             float gs, bool subtract) {
+// Pressure difference between two cells: float32, or with a float64
+// pressure the difference formed in double and rounded once.
+__device__ __forceinline__ float pdiff(const float* __restrict__ p, const double* __restrict__ p64, long a, long b) {
+  return p64 ? (float)(p64[a] - p64[b]) : p[a] - p[b];
+}
+
+__device__ __forceinline__ float projected_u(const float* __restrict__ p, const double* __restrict__ p64,
+                                             const float* __restrict__ u, const uint8_t* __restrict__ label, int nx,
+                                             int ny, int i, int j, float gs, bool subtract) {
   float val = u[i + (long)j * (nx + 1)];
   if (subtract && i >= 1 && i < nx) {
     if (!(solid_or_outside(label, nx, ny, i - 1, j) || solid_or_outside(label, nx, ny, i, j)))
-      val -= gs * (p[i + (long)j * nx] - p[(i - 1) + (long)j * nx]);
+      val -= gs * pdiff(p, p64, i + (long)j * nx, (i - 1) + (long)j * nx);
   }
   return val;
 }
-__device__ __forceinline__ float projected_v(const float* __restrict__ p, const float* __restrict__ v,
-                                             const uint8_t* __restrict__ label, int nx, int ny, int i, int j,
-                                             float gs, bool subtract) {
+__device__ __forceinline__ float projected_v(const float* __restrict__ p, const double* __restrict__ p64,
+                                             const float* __restrict__ v, const uint8_t* __restrict__ label, int nx,
+                                             int ny, int i, int j, float gs, bool subtract) {
   float val = v[i + (long)j * nx];
   if (subtract && j >= 1 && j < ny) {
     if (!(solid_or_outside(label, nx, ny, i, j - 1) || solid_or_outside(label, nx, ny, i, j)))
-      val -= gs * (p[i + (long)j * nx] - p[i + (long)(j - 1) * nx]);
+      val -= gs * pdiff(p, p64, i + (long)j * nx, i + (long)(j - 1) * nx);
   }
   return val;
 }
 
 __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const float* __restrict__ p,
-                                                          float* __restrict__ u, float* __restrict__ v,
-                                                          const uint8_t* __restrict__ label,
+                                                          const double* __restrict__ p64, float* __restrict__ u,
+                                                          float* __restrict__ v, const uint8_t* __restrict__ label,
                                                           const StepScalars* __restrict__ sc, int subtract,
                                                           int outflow) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -159,7 +165,7 @@ __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const 
   const float gs = subtract ? sc->grad_scale : 0.0f;
   // u faces: threads 1..nx-1 write; faces 0 and nx are written only by outflow.
   if (j < ny && i >= 1 && i < nx) {
-    float val = projected_u(p, u, label, nx, ny, i, j, gs, subtract);
+    float val = projected_u(p, p64, u, label, nx, ny, i, j, gs, subtract);
     if (outflow) {
       if (i == 1 && label[0 + (long)j * nx] == AIR) {
         val = smin(val, 0.0f);
@@ -173,7 +179,7 @@ __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const 
     u[i + (long)j * (nx + 1)] = val;
   }
   if (i < nx && j >= 1 && j < ny) {
-    float val = projected_v(p, v, label, nx, ny, i, j, gs, subtract);
+    float val = projected_v(p, p64, v, label, nx, ny, i, j, gs, subtract);
     if (outflow) {
       if (j == 1 && label[i] == AIR) {
         val = smin(val, 0.0f);
@@ -372,9 +378,10 @@ void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, 
 }
 
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
-                             const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow) {
+                             const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow,
+                             const double* p64) {
   dim3 b(32, 8);
-  k_subtract_outflow<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, p, u, v, label, sc, subtract, outflow);
+  k_subtract_outflow<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, p, p64, u, v, label, sc, subtract, outflow);
 }
 
 void launch_scale_rhs(cudaStream_t s, long n, const float* div, float* b, float neg_scale, const uint8_t* label,

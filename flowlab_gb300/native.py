@@ -119,6 +119,7 @@ SIGNATURES = [
     ("fl_advect_dye", _I, [_P, _I, _P, _P, _P, _P, _P, _F]),
     ("fl_rb_solve", _I, [_P, _P, _P, _P, _F, _I, _F, _D, _P]),
     ("fl_mg_solve", _I, [_P, _P, _P, _P, _F, _I, _D, _P, _P]),
+    ("fl_mg_solve_mixed", _I, [_P, _P, _P, _P, _F, _I, _D, _P, _P]),
     ("fl_divergence", _I, [_P, _P, _P, _P]),
     ("fl_rb_sweep", _I, [_P, _P, _P, _P, _F, _F, _I]),
     ("fl_subtract_gradient", _I, [_P, _P, _P, _P, _P, _F]),

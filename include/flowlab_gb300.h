@@ -198,6 +198,14 @@ int fl_rb_solve(fl_engine* e, float* p, const float* div, const uint8_t* label, 
 int fl_mg_solve(fl_engine* e, float* p, const float* div, const uint8_t* label, float scale, int max_cycles,
                 double tol, int* cycles_used, double* rel_residual);
 
+/* The same multigrid wrapped in float64 defect correction (NEW, no reference
+ * counterpart): p is a float64 in/out warm start; each pass forms
+ * r = b - A p in float64, runs one float32 V-cycle on A e = r from e = 0 and
+ * adds e back in float64, until the relative residual <= tol or max_cycles.
+ * This is what reaches relative residuals below float32's ~1e-5 floor. */
+int fl_mg_solve_mixed(fl_engine* e, double* p, const float* div, const uint8_t* label, float scale, int max_cycles,
+                      double tol, int* cycles_used, double* rel_residual);
+
 /* ------------------------------------------- single passes, float32 host arrays */
 
 int fl_divergence(fl_engine* e, const float* u, const float* v, float* div);           /* divergence.ts:17-25 */

@@ -43,6 +43,7 @@ class Params(ctypes.Structure):
         ("mgCoarseSweeps", ctypes.c_int),
         ("mgCoarsest", ctypes.c_int),
         ("mgOmega", ctypes.c_double),
+        ("mixed", ctypes.c_int),
     ]
 
 
@@ -68,6 +69,7 @@ def make_params(**kw):
     p.confinement = 0.0
     p.mgPre, p.mgPost, p.mgCoarseSweeps, p.mgCoarsest = 2, 2, 8, 4
     p.mgOmega = 1.0
+    p.mixed = 0
     for k, v in kw.items():
         if k == "dyeDecay":
             p.dyeDecay[:] = list(v)
@@ -82,7 +84,7 @@ def params_from_engine(p):
                 solver=SOLVER_MG if p.solver == 1 else SOLVER_RBSOR, pressureIters=p.pressure_iters,
                 mgMaxCycles=p.mg_max_cycles, omega=p.omega, tol=p.tol, dyeDecay=tuple(p.dye_decay), beta=p.beta,
                 alpha=p.alpha, confinement=p.confinement, mgPre=p.mg_pre, mgPost=p.mg_post,
-                mgCoarseSweeps=p.mg_coarse_sweeps, mgCoarsest=p.mg_coarsest, mgOmega=p.mg_omega)
+                mgCoarseSweeps=p.mg_coarse_sweeps, mgCoarsest=p.mg_coarsest, mgOmega=p.mg_omega, mixed=p.mixed)
 
 
 def lib():
@@ -177,6 +179,17 @@ class Oracle:
         used = self._f("mg_solve")(nx, ny, _p(p), _p(div), _p(label), self.ct(scale), int(cycles), ctypes.c_double(tol),
                                    int(pre), int(post), int(coarse), int(coarsest), ctypes.c_double(omega), ctypes.byref(rr))
         return p, used, rr.value
+
+    def mg_solve_mixed(self, nx, ny, p64, div, label, scale, cycles, tol, pre=2, post=2, coarse=8, coarsest=4,
+                       omega=1.0):
+        """solveMixed: float64 pressure, defect correction around the multigrid."""
+        p64 = np.ascontiguousarray(p64, dtype=np.float64).copy()
+        div, label = self._arr(div), self._lab(label)
+        rr = ctypes.c_double(-1)
+        used = self._f("mg_solve_mixed")(nx, ny, _p(p64), _p(div), _p(label), self.ct(scale), int(cycles),
+                                         ctypes.c_double(tol), int(pre), int(post), int(coarse), int(coarsest),
+                                         ctypes.c_double(omega), ctypes.byref(rr))
+        return p64, used, rr.value
 
     def residual(self, nx, ny, x, b, label):
         x, b, label = self._arr(x), self._arr(b), self._lab(label)
@@ -292,6 +305,11 @@ class OracleSimulation:
         dye = np.zeros(3 * self.dnx * self.dny, self.o.dtype)
         self.o._f("sim_get_fields")(self.handle, _p(u), _p(v), _p(p), _p(dye))
         return u, v, p, dye
+
+    def get_p64(self):
+        p = np.zeros(self.nx * self.ny, np.float64)
+        self.o._f("sim_get_p64")(self.handle, _p(p))
+        return p
 
     def set_patch(self, i0, j0, pnx, pny, data):
         if data is None:

@@ -655,6 +655,72 @@ struct Multigrid {
   }
 };
 
+// NEW — float64 defect correction (iterative refinement) around the float32
+// multigrid: the pressure is kept in double; each outer pass
+// forms the residual r = b - A p in double (b = float32 rhs, neighbour sum
+// in the order +x, -x, +y, -y), runs ONE float32 V-cycle on A e = float(r)
+// from e = 0, and adds e back in double. The relative residual is
+// rms(r over fluid cells with links) / rms(b over fluid cells), tested
+// before each pass, so an already converged warm start costs no cycle.
+template <class T>
+double residual64(const Grid<T>& g, const double* p, const T* b, const uint8_t* label, T* r32, double& bSq, long& nb) {
+  double sumSq = 0;
+  long n = 0;
+  bSq = 0;
+  nb = 0;
+  for (int j = 0; j < g.ny; j++)
+    for (int i = 0; i < g.nx; i++) {
+      long k = idxP(g.nx, i, j);
+      r32[k] = 0;
+      if (label[k] != FLUID) continue;
+      bSq += (double)b[k] * (double)b[k];
+      nb += 1;
+      double count = 0, sum = 0;
+      if (!solidOrOutside(g, label, i + 1, j)) { count += 1.0; sum += p[k + 1]; }
+      if (!solidOrOutside(g, label, i - 1, j)) { count += 1.0; sum += p[k - 1]; }
+      if (!solidOrOutside(g, label, i, j + 1)) { count += 1.0; sum += p[k + g.nx]; }
+      if (!solidOrOutside(g, label, i, j - 1)) { count += 1.0; sum += p[k - g.nx]; }
+      if (count == 0) continue;
+      double r = (double)b[k] - (count * p[k] - sum);
+      r32[k] = (T)r;
+      sumSq += r * r;
+      n += 1;
+    }
+  return n > 0 ? std::sqrt(sumSq / (double)n) : 0.0;
+}
+
+template <class T>
+int solveMixed(Multigrid<T>& mg, const Grid<T>& g, double* p, const T* div, const uint8_t* label, T scale,
+               int cycles, double tol, double* relRes) {
+  const long n = (long)g.nx * g.ny;
+  mg.prepare(g, div, label, scale);  // labels + levels[0].b = -scale*div
+  std::vector<T> b(mg.levels[0].b);
+  std::vector<T> e(n);
+  double bSq;
+  long nb;
+  double rr = residual64(g, p, b.data(), label, mg.levels[0].b.data(), bSq, nb);
+  const double bRms = nb > 0 ? std::sqrt(bSq / (double)nb) : 0.0;
+  if (relRes) *relRes = -1;
+  if (bRms == 0) {
+    std::fill(p, p + n, 0.0);
+    if (relRes) *relRes = 0;
+    return 0;
+  }
+  double rel = rr / bRms;
+  if (relRes) *relRes = rel;
+  int c = 0;
+  while (c < cycles && !(rel <= tol)) {
+    std::fill(e.begin(), e.end(), T(0));
+    mg.vcycle(0, e.data());  // levels[0].b holds float(r)
+    for (long k = 0; k < n; k++) p[k] += (double)e[k];
+    rr = residual64(g, p, b.data(), label, mg.levels[0].b.data(), bSq, nb);
+    rel = rr / bRms;
+    if (relRes) *relRes = rel;
+    c++;
+  }
+  return c;
+}
+
 // ------------------------------------------------------------- projection
 
 // subtractGradient.ts:40-61
@@ -669,6 +735,22 @@ void subtractGradient(const Grid<T>& g, const T* p, T* u, T* v, const uint8_t* l
     for (int i = 0; i < g.nx; i++) {
       if (solidOrOutside(g, label, i, j - 1) || solidOrOutside(g, label, i, j)) continue;
       v[idxV(g.nx, i, j)] -= gradScale * (p[idxP(g.nx, i, j)] - p[idxP(g.nx, i, j - 1)]);
+    }
+}
+
+// subtractGradient with a float64 pressure: the difference is formed in
+// double and rounded once before the float update.
+template <class T>
+void subtractGradient64(const Grid<T>& g, const double* p, T* u, T* v, const uint8_t* label, T gradScale) {
+  for (int j = 0; j < g.ny; j++)
+    for (int i = 1; i < g.nx; i++) {
+      if (solidOrOutside(g, label, i - 1, j) || solidOrOutside(g, label, i, j)) continue;
+      u[idxU(g.nx, i, j)] -= gradScale * (T)(p[idxP(g.nx, i, j)] - p[idxP(g.nx, i - 1, j)]);
+    }
+  for (int j = 1; j < g.ny; j++)
+    for (int i = 0; i < g.nx; i++) {
+      if (solidOrOutside(g, label, i, j - 1) || solidOrOutside(g, label, i, j)) continue;
+      v[idxV(g.nx, i, j)] -= gradScale * (T)(p[idxP(g.nx, i, j)] - p[idxP(g.nx, i, j - 1)]);
     }
 }
 
@@ -879,6 +961,7 @@ struct StepParams {
   double beta = 0, alpha = 0, confinement = 0;
   MgShape mg;
   int mgMaxCycles = 3;
+  int mixed = 0;  // NEW: float64 pressure + defect correction around the multigrid
 };
 
 template <class T>
@@ -886,6 +969,7 @@ struct Simulation {
   Grid<T> g, dg;
   StepParams prm;
   std::vector<T> u, v, p, div, uNext, vNext, uHat, vHat, qHat, fx, fy;
+  std::vector<double> p64;  // the pressure when prm.mixed
   std::vector<uint8_t> label;
   std::vector<T> dye[DYE_CHANNELS], dyeNext[DYE_CHANNELS];
   std::vector<float> patch;
@@ -905,6 +989,7 @@ struct Simulation {
     uNext.assign(nu, 0); vNext.assign(nv, 0); uHat.assign(nu, 0); vHat.assign(nv, 0);
     qHat.assign(nd, 0); fx.assign(n, 0); fy.assign(n, 0);
     label.assign(n, FLUID);
+    p64.assign(n, 0.0);
     for (int c = 0; c < DYE_CHANNELS; c++) { dye[c].assign(nd, 0); dyeNext[c].assign(nd, 0); }
     mg.shape = prm.mg;
   }
@@ -942,14 +1027,20 @@ struct Simulation {
 
     computeDivergence(g, u.data(), v.data(), div.data());
     lastRelRes = -1;
-    if (prm.solver == 1) {
+    if (prm.solver == 1 && prm.mixed) {
+      iters = solveMixed(mg, g, p64.data(), div.data(), label.data(), scale, prm.mgMaxCycles, prm.tol, &lastRelRes);
+      for (size_t k = 0; k < p.size(); k++) p[k] = (T)p64[k];
+    } else if (prm.solver == 1) {
       iters = mg.solve(g, p.data(), div.data(), label.data(), scale, prm.mgMaxCycles, prm.tol, &lastRelRes);
     } else if (prm.solver == 0) {
       iters = solvePressureRedBlack(g, p.data(), div.data(), label.data(), scale, prm.pressureIters, T(prm.omega), prm.tol);
     } else {
       iters = solvePressure(g, p.data(), div.data(), label.data(), scale, prm.pressureIters, T(prm.omega), prm.tol);
     }
-    subtractGradient(g, p.data(), u.data(), v.data(), label.data(), gradScale);
+    if (prm.solver == 1 && prm.mixed)
+      subtractGradient64(g, p64.data(), u.data(), v.data(), label.data(), gradScale);
+    else
+      subtractGradient(g, p.data(), u.data(), v.data(), label.data(), gradScale);
     applyOutflow(g, u.data(), v.data(), label.data());
 
     for (int c = 0; c < DYE_CHANNELS; c++) {

@@ -18,6 +18,7 @@ struct orc_params {
   double beta, alpha, confinement;
   int mgPre, mgPost, mgCoarseSweeps, mgCoarsest;
   double mgOmega;
+  int mixed;
 };
 
 int orc_abi_version(void) { return 1; }
@@ -44,6 +45,7 @@ static StepParams toParams(const orc_params* c) {
   p.mg.coarseSweeps = c->mgCoarseSweeps;
   p.mg.coarsest = c->mgCoarsest;
   p.mg.omega = c->mgOmega;
+  p.mixed = c->mixed;
   return p;
 }
 
@@ -110,6 +112,21 @@ static StepParams toParams(const orc_params* c) {
     mg.shape.coarsest = coarsest;                                                                       \
     mg.shape.omega = omega;                                                                             \
     return mg.solve(Grid<T>{nx, ny, T(1)}, p, div, label, scale, cycles, tol, relRes);                  \
+  }                                                                                                     \
+  int orc_mg_solve_mixed_##SUF(int nx, int ny, double* p, const T* div, const uint8_t* label, T scale,         \
+                               int cycles, double tol, int pre, int post, int coarseSweeps, int coarsest,      \
+                               double omega, double* relRes) {                                                 \
+    Multigrid<T> mg;                                                                                    \
+    mg.shape.pre = pre;                                                                                 \
+    mg.shape.post = post;                                                                               \
+    mg.shape.coarseSweeps = coarseSweeps;                                                               \
+    mg.shape.coarsest = coarsest;                                                                       \
+    mg.shape.omega = omega;                                                                             \
+    return solveMixed(mg, Grid<T>{nx, ny, T(1)}, p, div, label, scale, cycles, tol, relRes);           \
+  }                                                                                                     \
+  void orc_sim_get_p64_##SUF(void* sp, double* p) {                                                     \
+    Simulation<T>* s = (Simulation<T>*)sp;                                                              \
+    std::copy(s->p64.begin(), s->p64.end(), p);                                                         \
   }                                                                                                     \
   void orc_residual_##SUF(int nx, int ny, const T* x, const T* b, const uint8_t* label, T* r) {         \
     computeResidual(Grid<T>{nx, ny, T(1)}, x, b, label, r);                                             \

@@ -164,6 +164,38 @@ def test_mg_tolerance_matches_oracle(o32):
     assert_identical(e32, p, "multigrid to tolerance")
 
 
+@pytest.mark.parametrize("closed", [True, False])
+def test_mg_mixed_identical(o32, o64, closed):
+    """Float64 defect correction (the oracle's solveMixed): identical float64
+    pressure, same pass count, relative residual 1e-6 reached where float32
+    alone stalls."""
+    nx, ny = 256, 192
+    if closed:
+        label = np.zeros(nx * ny, np.uint8)
+        div = fx.js_lcg_uniform(nx * ny, 99)
+        div -= div.mean()
+    else:
+        label = fx.scaled_block_labels(nx, ny)
+        div = fx.js_lcg_uniform(nx * ny, 4242)
+    prm = native.default_params(mg_pre=3, mg_post=3, mg_coarse_sweeps=32, mg_coarsest=8, mixed=1)
+    eng = native.Engine(nx, ny, params=prm)
+    try:
+        p = np.zeros(nx * ny)
+        used = native.ctypes.c_int()
+        rr = native.ctypes.c_double()
+        eng.call("fl_mg_solve_mixed", ptr(p), ptr(f32(div)), ptr(label), 0.02, 40, 1e-6, native.ctypes.byref(used),
+                 native.ctypes.byref(rr))
+    finally:
+        eng.close()
+    e32, used32, rr32 = o32.mg_solve_mixed(nx, ny, np.zeros(nx * ny), f32(div), label, 0.02, 40, 1e-6, 3, 3, 32, 8)
+    assert used.value == used32 and rr.value <= 1e-6, (used.value, used32, rr.value)
+    assert np.array_equal(e32, p), "%d values differ" % int((e32 != p).sum())
+    # the float64 solution solves the float64 problem to the same tolerance
+    r = o64.rms_remaining(nx, ny, p, f32(div).astype(np.float64), label, 0.02)
+    d = o64.fluid_div_rms(f32(div).astype(np.float64), label)
+    assert r / d < 2e-6
+
+
 # -------------------------------------------------------------- advection
 
 @pytest.mark.parametrize("mac", [False, True])

@@ -55,7 +55,7 @@ def mismatch(a, b):
 
 def test_plume_steps_match_float32_oracle(o32, o64):
     g, f, patch = configs.plume(64)
-    prm = configs.plume_params(tol=1e-4, max_cycles=12)
+    prm = configs.plume_params(tol=1e-4, max_cycles=12, mixed=0)
     steps = 12
     u, v, p, d, st = run_engine(g, f, patch, prm, steps)
     eu, ev, ep, ed, info = run_oracle(o32, g, f, patch, prm, steps)
@@ -127,9 +127,22 @@ def test_dye_decay_exponential_in_time():
     assert d[300] == 0
 
 
+def test_plume_mixed_steps_match_float32_oracle(o32):
+    """The plume with the float64 defect-correction solve to 1e-6, identical to
+    the oracle's float32-fields / float64-pressure step."""
+    g, f, patch = configs.plume(64)
+    prm = configs.plume_params(tol=1e-6, max_cycles=30, mixed=1)
+    steps = 8
+    u, v, p, d, st = run_engine(g, f, patch, prm, steps)
+    eu, ev, ep, ed, info = run_oracle(o32, g, f, patch, prm, steps)
+    for name, a, b in (("u", eu, u), ("v", ev, v), ("dye", ed, d)):
+        assert mismatch(a, b) == 0, "%s: %d values differ from the float32 oracle" % (name, mismatch(a, b))
+    assert 0 <= st["rel_residual"] <= 1e-6 and abs(st["rel_residual"] - info["rel_res"]) <= 1e-9 * info["rel_res"] + 1e-15
+
+
 def test_plume_reaches_relative_residual_target():
-    g, f, patch = configs.plume(128)
-    prm = configs.plume_params(tol=1e-5, max_cycles=40)
+    g, f, patch = configs.plume(256)
+    prm = configs.plume_params(tol=1e-6, max_cycles=40, mixed=1)
     u, v, p, d, st = run_engine(g, f, patch, prm, 5)
-    assert 0 < st["rel_residual"] <= 1e-5, st
+    assert 0 <= st["rel_residual"] <= 1e-6, st
     assert np.isfinite(u).all() and np.isfinite(d).all()
