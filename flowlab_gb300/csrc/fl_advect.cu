@@ -21,7 +21,7 @@ namespace fl {
 
 // advect.ts:41-55
 __device__ __forceinline__ void backtrace(const float* __restrict__ uc, const float* __restrict__ vc, int nx, int ny,
-                                          float h, float x, float y, float u0, float v0, float dt, float& bx,
+                                          const Spacing& h, float x, float y, float u0, float v0, float dt, float& bx,
                                           float& by) {
   float midX = x - 0.5f * dt * u0;
   float midY = y - 0.5f * dt * v0;
@@ -33,7 +33,7 @@ __device__ __forceinline__ void backtrace(const float* __restrict__ uc, const fl
 // MODE 1: MacCormack correction: `hat` is the forward result, `out` receives
 //         clamp(hat + 0.5*(in - reverse(hat))) (advect.ts:177-210).
 template <int MODE>
-__global__ void __launch_bounds__(256) k_advect_velocity(int nx, int ny, float h, const float* __restrict__ u_in,
+__global__ void __launch_bounds__(256) k_advect_velocity(int nx, int ny, Spacing h, const float* __restrict__ u_in,
                                                          const float* __restrict__ v_in,
                                                          const float* __restrict__ u_hat,
                                                          const float* __restrict__ v_hat, float* __restrict__ u_out,
@@ -48,8 +48,8 @@ __global__ void __launch_bounds__(256) k_advect_velocity(int nx, int ny, float h
     if (solid_or_outside(label, nx, ny, i - 1, j) || solid_or_outside(label, nx, ny, i, j)) {
       u_out[k] = u_in[k];
     } else {
-      const float x = (float)i * h;
-      const float y = ((float)j + 0.5f) * h;
+      const float x = (float)i * h.h;
+      const float y = ((float)j + 0.5f) * h.h;
       const float u0 = u_in[k];
       const float v0 = sample_v(v_in, nx, ny, h, x, y);
       float bx, by;
@@ -70,8 +70,8 @@ __global__ void __launch_bounds__(256) k_advect_velocity(int nx, int ny, float h
     if (solid_or_outside(label, nx, ny, i, j - 1) || solid_or_outside(label, nx, ny, i, j)) {
       v_out[k] = v_in[k];
     } else {
-      const float x = ((float)i + 0.5f) * h;
-      const float y = (float)j * h;
+      const float x = ((float)i + 0.5f) * h.h;
+      const float y = (float)j * h.h;
       const float u0 = sample_u(u_in, nx, ny, h, x, y);
       const float v0 = v_in[k];
       float bx, by;
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(256) k_advect_velocity(int nx, int ny, float h
 // 294-311). TAIL applies decay then the inlet patch (simulation.ts:569-581,
 // dye.ts:158-175) to the value this thread writes.
 template <int MODE, bool TAIL>
-__global__ void __launch_bounds__(256) k_advect_dye(int nx, int ny, float h, int dnx, int dny, float dh,
+__global__ void __launch_bounds__(256) k_advect_dye(int nx, int ny, Spacing h, int dnx, int dny, Spacing dh,
                                                     const float* __restrict__ u, const float* __restrict__ v,
                                                     const float* __restrict__ q_in, const float* __restrict__ q_hat,
                                                     float* __restrict__ q_out, const uint8_t* __restrict__ label,
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(256) k_advect_dye(int nx, int ny, float h, int
   const long cells = (long)dnx * dny;
   const long k = i + (long)j * dnx;
   const float dt = sc->dt;
-  const float ratio = dh / h;
+  const float ratio = dh.h / h.h;
   const int lj = (int)floorf(((float)j + 0.5f) * ratio);
   const int li = (int)floorf(((float)i + 0.5f) * ratio);
   float q[DYE_CHANNELS];
@@ -114,8 +114,8 @@ __global__ void __launch_bounds__(256) k_advect_dye(int nx, int ny, float h, int
 #pragma unroll
     for (int c = 0; c < DYE_CHANNELS; c++) q[c] = q_in[k + c * cells];
   } else {
-    const float x = ((float)i + 0.5f) * dh;
-    const float y = ((float)j + 0.5f) * dh;
+    const float x = ((float)i + 0.5f) * dh.h;
+    const float y = ((float)j + 0.5f) * dh.h;
     const float u0 = sample_u(u, nx, ny, h, x, y);
     const float v0 = sample_v(v, nx, ny, h, x, y);
     float bx, by;
@@ -161,13 +161,14 @@ __global__ void __launch_bounds__(256) k_advect_dye(int nx, int ny, float h, int
 void launch_advect_velocity(cudaStream_t s, int nx, int ny, float h, int mac, const float* u_in, const float* v_in,
                             float* u_hat, float* v_hat, float* u_out, float* v_out, const uint8_t* label,
                             const StepScalars* sc) {
+  const Spacing hs = make_spacing(h);
   dim3 blk(32, 8);
   dim3 grd((nx + 1 + blk.x - 1) / blk.x, (ny + 1 + blk.y - 1) / blk.y);
   if (mac) {
-    k_advect_velocity<0><<<grd, blk, 0, s>>>(nx, ny, h, u_in, v_in, nullptr, nullptr, u_hat, v_hat, label, sc);
-    k_advect_velocity<1><<<grd, blk, 0, s>>>(nx, ny, h, u_in, v_in, u_hat, v_hat, u_out, v_out, label, sc);
+    k_advect_velocity<0><<<grd, blk, 0, s>>>(nx, ny, hs, u_in, v_in, nullptr, nullptr, u_hat, v_hat, label, sc);
+    k_advect_velocity<1><<<grd, blk, 0, s>>>(nx, ny, hs, u_in, v_in, u_hat, v_hat, u_out, v_out, label, sc);
   } else {
-    k_advect_velocity<0><<<grd, blk, 0, s>>>(nx, ny, h, u_in, v_in, nullptr, nullptr, u_out, v_out, label, sc);
+    k_advect_velocity<0><<<grd, blk, 0, s>>>(nx, ny, hs, u_in, v_in, nullptr, nullptr, u_out, v_out, label, sc);
   }
 }
 
@@ -181,23 +182,24 @@ cudaError_t preload_advect_kernels() {
 void launch_advect_dye(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, int mac, const float* u,
                        const float* v, const float* q_in, float* q_hat, float* q_out, const uint8_t* label,
                        const StepScalars* sc, bool tail, const float* patch, int pi0, int pj0, int pnx, int pny) {
+  const Spacing hs = make_spacing(h), ds = make_spacing(dh);
   dim3 blk(32, 8);
   dim3 grd((dnx + blk.x - 1) / blk.x, (dny + blk.y - 1) / blk.y);
   if (mac) {
-    k_advect_dye<0, false><<<grd, blk, 0, s>>>(nx, ny, h, dnx, dny, dh, u, v, q_in, nullptr, q_hat, label, sc, nullptr,
+    k_advect_dye<0, false><<<grd, blk, 0, s>>>(nx, ny, hs, dnx, dny, ds, u, v, q_in, nullptr, q_hat, label, sc, nullptr,
                                                0, 0, 0, 0);
     if (tail)
-      k_advect_dye<1, true><<<grd, blk, 0, s>>>(nx, ny, h, dnx, dny, dh, u, v, q_in, q_hat, q_out, label, sc, patch,
+      k_advect_dye<1, true><<<grd, blk, 0, s>>>(nx, ny, hs, dnx, dny, ds, u, v, q_in, q_hat, q_out, label, sc, patch,
                                                 pi0, pj0, pnx, pny);
     else
-      k_advect_dye<1, false><<<grd, blk, 0, s>>>(nx, ny, h, dnx, dny, dh, u, v, q_in, q_hat, q_out, label, sc,
+      k_advect_dye<1, false><<<grd, blk, 0, s>>>(nx, ny, hs, dnx, dny, ds, u, v, q_in, q_hat, q_out, label, sc,
                                                  nullptr, 0, 0, 0, 0);
   } else {
     if (tail)
-      k_advect_dye<0, true><<<grd, blk, 0, s>>>(nx, ny, h, dnx, dny, dh, u, v, q_in, nullptr, q_out, label, sc, patch,
+      k_advect_dye<0, true><<<grd, blk, 0, s>>>(nx, ny, hs, dnx, dny, ds, u, v, q_in, nullptr, q_out, label, sc, patch,
                                                 pi0, pj0, pnx, pny);
     else
-      k_advect_dye<0, false><<<grd, blk, 0, s>>>(nx, ny, h, dnx, dny, dh, u, v, q_in, nullptr, q_out, label, sc,
+      k_advect_dye<0, false><<<grd, blk, 0, s>>>(nx, ny, hs, dnx, dny, ds, u, v, q_in, nullptr, q_out, label, sc,
                                                  nullptr, 0, 0, 0, 0);
   }
 }

@@ -61,6 +61,28 @@ struct StepAccum {
 
 // ------------------------------------------------------------ sampling
 
+// A cell size with its reciprocal. When h is a power of two, x / h and
+// x * (1/h) are the same float (both scale by an exact power of two), so the
+// samplers multiply instead of dividing; otherwise they divide as the
+// reference does.
+struct Spacing {
+  float h;
+  float inv;
+  int pow2;
+};
+
+__host__ inline Spacing make_spacing(float h) {
+  int ex = 0;
+  const float m = frexpf(h, &ex);
+  Spacing s;
+  s.h = h;
+  s.inv = 1.0f / h;
+  s.pow2 = (m == 0.5f) ? 1 : 0;
+  return s;
+}
+
+__device__ __forceinline__ float over(float x, const Spacing& s) { return s.pow2 ? x * s.inv : x / s.h; }
+
 struct AxisF {
   int i0;
   float f;
@@ -93,27 +115,27 @@ __device__ __forceinline__ float bilerp(float v00, float v10, float v01, float v
 __device__ __forceinline__ float ldg(const float* p) { return __ldg(p); }
 
 // grid.ts:197-208 sampleU: u[i,j] at (i*h, (j+0.5)*h), (nx+1) x ny values.
-__device__ __forceinline__ float sample_u(const float* __restrict__ u, int nx, int ny, float h, float x, float y) {
-  AxisF a = clamped_axis(x / h, nx + 1);
-  AxisF b = clamped_axis(y / h - 0.5f, ny);
+__device__ __forceinline__ float sample_u(const float* __restrict__ u, int nx, int ny, const Spacing& h, float x, float y) {
+  AxisF a = clamped_axis(over(x, h), nx + 1);
+  AxisF b = clamped_axis(over(y, h) - 0.5f, ny);
   long s = nx + 1;
   long k = a.i0 + (long)b.i0 * s;
   return bilerp(ldg(u + k), ldg(u + k + 1), ldg(u + k + s), ldg(u + k + s + 1), a.f, b.f);
 }
 
 // grid.ts:214-225 sampleV: v[i,j] at ((i+0.5)*h, j*h), nx x (ny+1) values.
-__device__ __forceinline__ float sample_v(const float* __restrict__ v, int nx, int ny, float h, float x, float y) {
-  AxisF a = clamped_axis(x / h - 0.5f, nx);
-  AxisF b = clamped_axis(y / h, ny + 1);
+__device__ __forceinline__ float sample_v(const float* __restrict__ v, int nx, int ny, const Spacing& h, float x, float y) {
+  AxisF a = clamped_axis(over(x, h) - 0.5f, nx);
+  AxisF b = clamped_axis(over(y, h), ny + 1);
   long s = nx;
   long k = a.i0 + (long)b.i0 * s;
   return bilerp(ldg(v + k), ldg(v + k + 1), ldg(v + k + s), ldg(v + k + s + 1), a.f, b.f);
 }
 
 // grid.ts:239-250 sampleP on a cell-centred field of nx x ny.
-__device__ __forceinline__ float sample_p(const float* __restrict__ q, int nx, int ny, float h, float x, float y) {
-  AxisF a = clamped_axis(x / h - 0.5f, nx);
-  AxisF b = clamped_axis(y / h - 0.5f, ny);
+__device__ __forceinline__ float sample_p(const float* __restrict__ q, int nx, int ny, const Spacing& h, float x, float y) {
+  AxisF a = clamped_axis(over(x, h) - 0.5f, nx);
+  AxisF b = clamped_axis(over(y, h) - 0.5f, ny);
   long s = nx;
   long k = a.i0 + (long)b.i0 * s;
   return bilerp(ldg(q + k), ldg(q + k + 1), ldg(q + k + s), ldg(q + k + s + 1), a.f, b.f);
@@ -127,26 +149,26 @@ __device__ __forceinline__ float clamp_to_range(float q, float a, float b, float
 }
 
 // grid.ts:273-315 clampToStencil{U,V,P}
-__device__ __forceinline__ float clamp_stencil_u(const float* __restrict__ u, int nx, int ny, float h, float x, float y,
+__device__ __forceinline__ float clamp_stencil_u(const float* __restrict__ u, int nx, int ny, const Spacing& h, float x, float y,
                                                  float q) {
-  int i0 = clamped_axis(x / h, nx + 1).i0;
-  int j0 = clamped_axis(y / h - 0.5f, ny).i0;
+  int i0 = clamped_axis(over(x, h), nx + 1).i0;
+  int j0 = clamped_axis(over(y, h) - 0.5f, ny).i0;
   long s = nx + 1;
   long k = i0 + (long)j0 * s;
   return clamp_to_range(q, ldg(u + k), ldg(u + k + 1), ldg(u + k + s), ldg(u + k + s + 1));
 }
-__device__ __forceinline__ float clamp_stencil_v(const float* __restrict__ v, int nx, int ny, float h, float x, float y,
+__device__ __forceinline__ float clamp_stencil_v(const float* __restrict__ v, int nx, int ny, const Spacing& h, float x, float y,
                                                  float q) {
-  int i0 = clamped_axis(x / h - 0.5f, nx).i0;
-  int j0 = clamped_axis(y / h, ny + 1).i0;
+  int i0 = clamped_axis(over(x, h) - 0.5f, nx).i0;
+  int j0 = clamped_axis(over(y, h), ny + 1).i0;
   long s = nx;
   long k = i0 + (long)j0 * s;
   return clamp_to_range(q, ldg(v + k), ldg(v + k + 1), ldg(v + k + s), ldg(v + k + s + 1));
 }
-__device__ __forceinline__ float clamp_stencil_p(const float* __restrict__ q, int nx, int ny, float h, float x, float y,
+__device__ __forceinline__ float clamp_stencil_p(const float* __restrict__ q, int nx, int ny, const Spacing& h, float x, float y,
                                                  float val) {
-  int i0 = clamped_axis(x / h - 0.5f, nx).i0;
-  int j0 = clamped_axis(y / h - 0.5f, ny).i0;
+  int i0 = clamped_axis(over(x, h) - 0.5f, nx).i0;
+  int j0 = clamped_axis(over(y, h) - 0.5f, ny).i0;
   long s = nx;
   long k = i0 + (long)j0 * s;
   return clamp_to_range(val, ldg(q + k), ldg(q + k + 1), ldg(q + k + s), ldg(q + k + s + 1));

@@ -29,7 +29,6 @@ namespace fl {
 
 constexpr int MODE_PLAIN = 0, MODE_PRE = 1, MODE_POST = 2;
 constexpr int MAX_LEVELS = 24;
-constexpr int SMOOTH_THREADS_X = 32, SMOOTH_THREADS_Y = 8;
 
 // ------------------------------------------------------------ label codes
 
@@ -109,92 +108,108 @@ struct SmoothArgs {
   int x_is_zero;    // PRE on a coarse level: x starts at zero (pressureMultigrid.ts:175)
 };
 
-template <int TW, int TH, int P, int MODE>
-struct SmoothGeom {
+// (sum - scale*b) / count with count in 1..4: a multiply by the exact
+// reciprocal for 1, 2 and 4 (the same float as the division, since scaling by
+// a power of two is exact) and a true division for 3.
+__device__ __forceinline__ float over_count(float s, int cnt) {
+  return cnt == 3 ? s / 3.0f : s * (cnt == 4 ? 0.25f : (cnt == 2 ? 0.5f : 1.0f));
+}
+
+// Temporally blocked red-black smoother. One 1024-thread CTA owns a 64x64
+// region: its tile plus a halo of H = 2*pairs (+1 when a residual follows).
+// Thread (tx, ty) owns the cells (2tx, ty), (2tx+1, ty), (2tx, ty+32),
+// (2tx+1, ty+32) — one of each colour per row — and keeps their stencil
+// code, rhs and value in registers for the whole launch. Neighbour values go
+// through shared memory split by local parity, xs[(li+lj)&1][lj][li>>1], so
+// a warp's reads and writes are unit-stride. Every half-sweep updates every
+// region cell of its colour except the region's outer ring: half-sweep s is
+// correct on the region shrunk by s+1 cells, so after 2*pairs half-sweeps the
+// tile (and, with the +1, a ring around it) holds exactly the values the
+// sequential sweeps produce; outer cells hold finite values nobody uses.
+constexpr int RGN = 64;
+constexpr int RGN_T = 32;
+
+template <int P, int MODE>
+struct Tile {
   static constexpr int H = (MODE == MODE_PLAIN) ? 2 * P : 2 * P + 1;
-  static constexpr int SW = TW + 2 * H, SH = TH + 2 * H;
-  // Coarse footprint of the region for prolongation: indices (GX>>1)-1 ..
-  // ((GX+SW-1)>>1)+1 with GX = X0-H and X0 even, i.e. TW/2 + H + 3 values.
-  static constexpr int CW = TW / 2 + H + 3, CH = TH / 2 + H + 3;
-  static constexpr size_t bytes() {
-    return sizeof(float) * (2 * SW * SH + (MODE == MODE_POST ? CW * CH : 0)) + ((SW * SH + 15) / 16) * 16;
-  }
+  static constexpr int T = RGN - 2 * H;  // tile side, even
 };
 
-template <int TW, int TH, int P, int MODE>
-__global__ void __launch_bounds__(SMOOTH_THREADS_X* SMOOTH_THREADS_Y) k_smooth(SmoothArgs a) {
-  using G = SmoothGeom<TW, TH, P, MODE>;
-  constexpr int H = G::H, SW = G::SW, SH = G::SH, CW = G::CW, CH = G::CH;
-  extern __shared__ __align__(16) unsigned char smem[];
-  float* xs = reinterpret_cast<float*>(smem);
-  float* bs = xs + SW * SH;
-  float* es = bs + SW * SH;
-  uint8_t* cs = reinterpret_cast<uint8_t*>(es + (MODE == MODE_POST ? CW * CH : 0));
+template <int P, int MODE>
+__global__ void __launch_bounds__(RGN_T* RGN_T, 1) k_smooth(SmoothArgs a) {
+  constexpr int H = Tile<P, MODE>::H;
+  constexpr int T = Tile<P, MODE>::T;
+  static_assert(T % 2 == 0 && T > 0, "tile must be even");
+  __shared__ float xs[2][RGN][RGN / 2];
+  __shared__ float rs[MODE == MODE_PRE ? RGN : 1][MODE == MODE_PRE ? RGN : 1];
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int X0 = blockIdx.x * TW, Y0 = blockIdx.y * TH;
+  const int X0 = blockIdx.x * T, Y0 = blockIdx.y * T;
   const int GX = X0 - H, GY = Y0 - H;
   const int nx = a.nx, ny = a.ny;
 
-  for (int lj = ty; lj < SH; lj += SMOOTH_THREADS_Y) {
+  uint8_t cd[2][2];
+  float bb[2][2], xx[2][2];
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    const int lj = ty + RGN_T * r;
     const int gj = GY + lj;
-    for (int li = tx; li < SW; li += SMOOTH_THREADS_X) {
+#pragma unroll
+    for (int o = 0; o < 2; o++) {
+      const int li = 2 * tx + o;
       const int gi = GX + li;
-      const int s = li + lj * SW;
       if (gi >= 0 && gj >= 0 && gi < nx && gj < ny) {
         const long k = gi + (long)gj * nx;
-        xs[s] = a.x_is_zero ? 0.0f : a.xin[k];
-        bs[s] = a.b[k];
-        cs[s] = a.code[k];
+        cd[r][o] = a.code[k];
+        bb[r][o] = a.b[k];
+        xx[r][o] = a.x_is_zero ? 0.0f : a.xin[k];
+        if (MODE == MODE_POST && (cd[r][o] & 3u) == FLUID) {
+          // pressureMultigrid.ts:192-207 — x += 9/16, 3/16, 3/16, 1/16 of e
+          const int I = gi >> 1, J = gj >> 1;
+          const int I2 = (gi & 1) ? min(I + 1, a.cnx - 1) : max(I - 1, 0);
+          const int J2 = (gj & 1) ? min(J + 1, a.cny - 1) : max(J - 1, 0);
+          const float* e = a.ec;
+          const long cs = a.cnx;
+          xx[r][o] += 0.5625f * __ldg(e + I + J * cs) + 0.1875f * (__ldg(e + I2 + J * cs) + __ldg(e + I + J2 * cs)) +
+                      0.0625f * __ldg(e + I2 + J2 * cs);
+        }
       } else {
-        xs[s] = 0.0f;
-        bs[s] = 0.0f;
-        cs[s] = CODE_OUTSIDE;
+        cd[r][o] = CODE_OUTSIDE;
+        bb[r][o] = 0.0f;
+        xx[r][o] = 0.0f;
       }
-    }
-  }
-
-  if (MODE == MODE_POST) {
-    // pressureMultigrid.ts:192-207 — x += 9/16, 3/16, 3/16, 1/16 of e.
-    const int cI0 = (GX >> 1) - 1, cJ0 = (GY >> 1) - 1;
-    for (int cj = ty; cj < CH; cj += SMOOTH_THREADS_Y)
-      for (int ci = tx; ci < CW; ci += SMOOTH_THREADS_X) {
-        const int I = cI0 + ci, J = cJ0 + cj;
-        es[ci + cj * CW] = (I >= 0 && J >= 0 && I < a.cnx && J < a.cny) ? a.ec[I + (long)J * a.cnx] : 0.0f;
-      }
-    __syncthreads();
-    for (int lj = ty; lj < SH; lj += SMOOTH_THREADS_Y) {
-      const int gj = GY + lj;
-      if (gj < 0 || gj >= ny) continue;
-      const int J = gj >> 1;
-      const int J2 = (gj & 1) ? min(J + 1, a.cny - 1) : max(J - 1, 0);
-      for (int li = tx; li < SW; li += SMOOTH_THREADS_X) {
-        const int gi = GX + li;
-        if (gi < 0 || gi >= nx) continue;
-        const int s = li + lj * SW;
-        if ((cs[s] & 3u) != FLUID) continue;
-        const int I = gi >> 1;
-        const int I2 = (gi & 1) ? min(I + 1, a.cnx - 1) : max(I - 1, 0);
-        const float e00 = es[(I - cI0) + (J - cJ0) * CW];
-        const float e20 = es[(I2 - cI0) + (J - cJ0) * CW];
-        const float e02 = es[(I - cI0) + (J2 - cJ0) * CW];
-        const float e22 = es[(I2 - cI0) + (J2 - cJ0) * CW];
-        xs[s] += 0.5625f * e00 + 0.1875f * (e20 + e02) + 0.0625f * e22;
-      }
+      xs[(li + lj) & 1][lj][tx] = xx[r][o];
     }
   }
   __syncthreads();
 
+  const float scale = a.scale, omega = a.omega, keep = 1.0f - omega;
 #pragma unroll 1
   for (int hs = 0; hs < 2 * P; hs++) {
-    const int color = hs & 1;
-    const int sh = hs + 1;
-    for (int lj = sh + ty; lj < SH - sh; lj += SMOOTH_THREADS_Y) {
-      const int gj = GY + lj;
-      const int first = sh + ((GX + sh + gj + color) & 1);
-      for (int li = first + 2 * tx; li < SW - sh; li += 2 * SMOOTH_THREADS_X) {
-        const int s = li + lj * SW;
-        rb_update(xs, bs, cs[s], s, SW, a.scale, a.omega);
-      }
+    // local parity of this half-sweep's colour ((gi + gj) & 1 == hs & 1)
+    const int qa = ((hs & 1) + GX + GY) & 1;
+    const float(*xo)[RGN / 2] = xs[1 - qa];
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const int lj = ty + RGN_T * r;
+      const int o = (qa + lj) & 1;
+      const int li = 2 * tx + o;
+      // select, not index: a runtime index would put the arrays in local memory
+      const uint8_t c = o ? cd[r][1] : cd[r][0];
+      if (li == 0 || li == RGN - 1 || lj == 0 || lj == RGN - 1 || (c & 3u) != FLUID) continue;
+      const int cnt = code_count(c);
+      if (cnt == 0) continue;
+      float sum = 0.0f;
+      if (c & LINK_XP) sum += xo[lj][tx + o];
+      if (c & LINK_XM) sum += xo[lj][tx + o - 1];
+      if (c & LINK_YP) sum += xo[lj + 1][tx];
+      if (c & LINK_YM) sum += xo[lj - 1][tx];
+      const float pgs = over_count(sum - scale * (o ? bb[r][1] : bb[r][0]), cnt);
+      const float nv = keep * (o ? xx[r][1] : xx[r][0]) + omega * pgs;
+      if (o)
+        xx[r][1] = nv;
+      else
+        xx[r][0] = nv;
+      xs[qa][lj][tx] = nv;
     }
     __syncthreads();
   }
@@ -202,37 +217,52 @@ __global__ void __launch_bounds__(SMOOTH_THREADS_X* SMOOTH_THREADS_Y) k_smooth(S
   if (MODE == MODE_PRE || (MODE == MODE_POST && a.acc != nullptr)) {
     double rsq = 0.0;
     unsigned long long rn = 0;
-    for (int lj = H + ty; lj < H + TH; lj += SMOOTH_THREADS_Y)
-      for (int li = H + tx; li < H + TW; li += SMOOTH_THREADS_X) {
-        const int s = li + lj * SW;
-        bool counted;
-        const float r = residual_at(xs, bs, cs[s], s, SW, counted);
-        if (MODE == MODE_PRE) {
-          // Each cell's b is read by that cell alone, so the residual can
-          // replace it in place for the restriction below.
-          bs[s] = r;
-        } else if (counted) {
-          rsq += (double)r * (double)r;
-          rn += 1;
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const int lj = ty + RGN_T * r;
+#pragma unroll
+      for (int o = 0; o < 2; o++) {
+        const int li = 2 * tx + o;
+        if (li < H || li >= H + T || lj < H || lj >= H + T) continue;
+        const uint8_t c = cd[r][o];
+        float res = 0.0f;
+        if ((c & 3u) == FLUID) {
+          const int cnt = code_count(c);
+          if (cnt > 0) {
+            // r = b - (count*x - sum), sum order +x, -x, +y, -y (pressureMultigrid.ts:117-151)
+            const float(*xq)[RGN / 2] = xs[1 - ((li + lj) & 1)];
+            float sum = 0.0f;
+            if (c & LINK_XP) sum += xq[lj][tx + o];
+            if (c & LINK_XM) sum += xq[lj][tx + o - 1];
+            if (c & LINK_YP) sum += xq[lj + 1][tx];
+            if (c & LINK_YM) sum += xq[lj - 1][tx];
+            res = bb[r][o] - ((float)cnt * xx[r][o] - sum);
+            rsq += (double)res * (double)res;
+            rn += 1;
+          }
         }
+        if (MODE == MODE_PRE) rs[lj][li] = res;
       }
+    }
     if (MODE == MODE_PRE) {
       __syncthreads();
-      // pressureMultigrid.ts:156-178: coarse b = sum of the (up to) four
-      // children's residuals. Tiles are even-aligned, so every child of this
-      // tile's coarse cells is one of its own cells.
-      for (int cj = ty; cj < TH / 2; cj += SMOOTH_THREADS_Y)
-        for (int ci = tx; ci < TW / 2; ci += SMOOTH_THREADS_X) {
-          const int I = (X0 >> 1) + ci, J = (Y0 >> 1) + cj;
-          if (I >= a.cnx || J >= a.cny) continue;
+      // pressureMultigrid.ts:156-178: coarse b = sum of the children's
+      // residuals; tiles start at even coordinates, so all children of the
+      // tile's coarse cells are tile cells.
+      const int t = tx + RGN_T * ty;
+      if (t < (T / 2) * (T / 2)) {
+        const int cj = t / (T / 2), ci = t - cj * (T / 2);
+        const int I = (X0 >> 1) + ci, J = (Y0 >> 1) + cj;
+        if (I < a.cnx && J < a.cny) {
           float sum = 0.0f;
           for (int dj = 0; dj < 2; dj++)
             for (int di = 0; di < 2; di++) {
               const int i = 2 * I + di, j = 2 * J + dj;
-              if (i < nx && j < ny) sum += bs[(i - GX) + (j - GY) * SW];
+              if (i < nx && j < ny) sum += rs[j - GY][i - GX];
             }
           a.bc[I + (long)J * a.cnx] = sum;
         }
+      }
     } else {
       __shared__ double red[32];
       __shared__ unsigned long long redn[32];
@@ -245,18 +275,30 @@ __global__ void __launch_bounds__(SMOOTH_THREADS_X* SMOOTH_THREADS_Y) k_smooth(S
     }
   }
 
-  for (int lj = H + ty; lj < H + TH; lj += SMOOTH_THREADS_Y) {
-    const int gj = GY + lj;
-    if (gj >= ny) break;
-    for (int li = H + tx; li < H + TW; li += SMOOTH_THREADS_X) {
-      const int gi = GX + li;
-      if (gi < nx) a.xout[gi + (long)gj * nx] = xs[li + lj * SW];
+  if (a.xout != nullptr) {
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const int lj = ty + RGN_T * r;
+      const int gj = GY + lj;
+      if (lj < H || lj >= H + T || gj >= ny) continue;
+#pragma unroll
+      for (int o = 0; o < 2; o++) {
+        const int li = 2 * tx + o;
+        const int gi = GX + li;
+        if (li < H || li >= H + T || gi >= nx) continue;
+        a.xout[gi + (long)gj * nx] = xx[r][o];
+      }
     }
   }
 }
 
 // ----------------------------------------------------- single-CTA coarse tail
 
+// Levels whose sides are both <= 64 run in ONE 1024-thread CTA, entirely in
+// shared memory. Thread (tx, ty) owns cells (2tx + o, ty + 32r) of every
+// level (o, r in {0, 1}), so no index needs a division. Per level: x split by
+// parity, xs[(i+j)&1][j][i>>1] (unit-stride warp access), b and the stencil
+// codes row-major.
 struct CoarseLevel {
   int nx, ny;
   const uint8_t* code;
@@ -272,124 +314,162 @@ struct CoarseArgs {
   int pre, post, coarse_sweeps;
   float omega;
   StepAccum* acc;
-  int code_bytes_off;  // byte offset of the code region
 };
 
-constexpr int COARSE_THREADS = 1024;
-constexpr int SMALL_LEVEL = 512;  // levels at or below this many cells run on one warp
+constexpr int COARSE_SIDE = 64;
 
-__device__ void coarse_smooth(float* x, const float* b, const uint8_t* c, int nx, int ny, int pairs, float omega) {
-  const int n = nx * ny;
-  const int tid = threadIdx.x;
-  if (n <= SMALL_LEVEL) {
-    if (tid < 32) {
-      for (int hs = 0; hs < 2 * pairs; hs++) {
-        const int color = hs & 1;
-        for (int k = tid; k < n; k += 32) {
-          const int j = k / nx, i = k - j * nx;
-          if (((i + j) & 1) != color) continue;
-          rb_update(x, b, c[k], k, nx, -1.0f, omega);
-        }
-        __syncwarp();
-      }
+struct CoarseView {
+  float* xs;  // 2 * ny * 32 floats
+  float* bs;
+  const uint8_t* cs;
+  int nx, ny;
+  __device__ float& x(int i, int j) const { return xs[((i + j) & 1) * ny * 32 + j * 32 + (i >> 1)]; }
+};
+
+__device__ __forceinline__ CoarseView coarse_view(unsigned char* smem, const CoarseLevel& L) {
+  float* fs = reinterpret_cast<float*>(smem);
+  CoarseView v;
+  v.xs = fs + L.off_x;
+  v.bs = fs + L.off_b;
+  v.cs = smem + L.off_c;
+  v.nx = L.nx;
+  v.ny = L.ny;
+  return v;
+}
+
+// r = b - (count*x - sum), 0 off-fluid (pressureMultigrid.ts:117-151)
+__device__ __forceinline__ float coarse_residual(const CoarseView& v, int i, int j, bool& counted) {
+  counted = false;
+  const int k = i + j * v.nx;
+  const uint8_t c = v.cs[k];
+  if ((c & 3u) != FLUID) return 0.0f;
+  const int cnt = code_count(c);
+  if (cnt == 0) return 0.0f;
+  float sum = 0.0f;
+  if (c & LINK_XP) sum += v.x(i + 1, j);
+  if (c & LINK_XM) sum += v.x(i - 1, j);
+  if (c & LINK_YP) sum += v.x(i, j + 1);
+  if (c & LINK_YM) sum += v.x(i, j - 1);
+  counted = true;
+  return v.bs[k] - ((float)cnt * v.x(i, j) - sum);
+}
+
+__device__ void coarse_smooth(const CoarseView& v, int pairs, float omega) {
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const float keep = 1.0f - omega;
+  for (int hs = 0; hs < 2 * pairs; hs++) {
+    const int color = hs & 1;
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const int j = ty + 32 * r;
+      const int i = 2 * tx + ((color + j) & 1);
+      if (j >= v.ny || i >= v.nx) continue;
+      const int k = i + j * v.nx;
+      const uint8_t c = v.cs[k];
+      if ((c & 3u) != FLUID) continue;
+      const int cnt = code_count(c);
+      if (cnt == 0) continue;
+      float sum = 0.0f;
+      if (c & LINK_XP) sum += v.x(i + 1, j);
+      if (c & LINK_XM) sum += v.x(i - 1, j);
+      if (c & LINK_YP) sum += v.x(i, j + 1);
+      if (c & LINK_YM) sum += v.x(i, j - 1);
+      const float pgs = over_count(sum - (-1.0f) * v.bs[k], cnt);
+      float& xr = v.x(i, j);
+      xr = keep * xr + omega * pgs;
     }
     __syncthreads();
-  } else {
-    for (int hs = 0; hs < 2 * pairs; hs++) {
-      const int color = hs & 1;
-      for (int k = tid; k < n; k += COARSE_THREADS) {
-        const int j = k / nx, i = k - j * nx;
-        if (((i + j) & 1) != color) continue;
-        rb_update(x, b, c[k], k, nx, -1.0f, omega);
-      }
-      __syncthreads();
-    }
   }
 }
 
-__global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(CoarseArgs a) {
+__global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  float* fs = reinterpret_cast<float*>(smem);
-  const int tid = threadIdx.x;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + 32 * ty;
   for (int l = 0; l < a.nlev; l++) {
     const CoarseLevel& L = a.lv[l];
     const int n = L.nx * L.ny;
     uint8_t* c = smem + L.off_c;
-    for (int k = tid; k < n; k += COARSE_THREADS) c[k] = L.code[k];
+    for (int k = tid; k < n; k += 1024) c[k] = L.code[k];
   }
-  {
-    const CoarseLevel& L = a.lv[0];
-    const int n = L.nx * L.ny;
-    for (int k = tid; k < n; k += COARSE_THREADS) {
-      fs[L.off_b + k] = a.b_top[k];
-      fs[L.off_x + k] = a.x_is_zero ? 0.0f : a.x_top[k];
-    }
-  }
-  __syncthreads();
-
-  // down: pre-smooth, residual + restriction (x_coarse = 0)
-  for (int l = 0; l < a.nlev - 1; l++) {
-    const CoarseLevel& L = a.lv[l];
-    const CoarseLevel& C = a.lv[l + 1];
-    float* x = fs + L.off_x;
-    float* b = fs + L.off_b;
-    const uint8_t* c = smem + L.off_c;
-    coarse_smooth(x, b, c, L.nx, L.ny, a.pre, a.omega);
-    const int cn = C.nx * C.ny;
-    for (int K = tid; K < cn; K += COARSE_THREADS) {
-      const int J = K / C.nx, I = K - J * C.nx;
-      float sum = 0.0f;
-      for (int dj = 0; dj < 2; dj++)
-        for (int di = 0; di < 2; di++) {
-          const int i = 2 * I + di, j = 2 * J + dj;
-          if (i < L.nx && j < L.ny) {
-            bool counted;
-            const int s = i + j * L.nx;
-            sum += residual_at(x, b, c[s], s, L.nx, counted);
-          }
-        }
-      fs[C.off_b + K] = sum;
-      fs[C.off_x + K] = 0.0f;
-    }
-    __syncthreads();
-  }
-  {
-    const CoarseLevel& L = a.lv[a.nlev - 1];
-    coarse_smooth(fs + L.off_x, fs + L.off_b, smem + L.off_c, L.nx, L.ny, a.coarse_sweeps, a.omega);
-  }
-  // up: prolong + post-smooth
-  for (int l = a.nlev - 2; l >= 0; l--) {
-    const CoarseLevel& L = a.lv[l];
-    const CoarseLevel& C = a.lv[l + 1];
-    float* x = fs + L.off_x;
-    const float* e = fs + C.off_x;
-    const uint8_t* c = smem + L.off_c;
-    const int n = L.nx * L.ny;
-    for (int k = tid; k < n; k += COARSE_THREADS) {
-      if ((c[k] & 3u) != FLUID) continue;
-      const int j = k / L.nx, i = k - j * L.nx;
-      const int J = j >> 1, I = i >> 1;
-      const int J2 = (j & 1) ? min(J + 1, C.ny - 1) : max(J - 1, 0);
-      const int I2 = (i & 1) ? min(I + 1, C.nx - 1) : max(I - 1, 0);
-      x[k] += 0.5625f * e[I + J * C.nx] + 0.1875f * (e[I2 + J * C.nx] + e[I + J2 * C.nx]) + 0.0625f * e[I2 + J2 * C.nx];
-    }
-    __syncthreads();
-    coarse_smooth(x, fs + L.off_b, c, L.nx, L.ny, a.post, a.omega);
-  }
-
-  const CoarseLevel& T = a.lv[0];
-  const int n = T.nx * T.ny;
-  if (a.acc != nullptr) {
-    double rsq = 0.0;
-    unsigned long long rn = 0;
-    for (int k = tid; k < n; k += COARSE_THREADS) {
-      bool counted;
-      const float r = residual_at(fs + T.off_x, fs + T.off_b, smem[T.off_c + k], k, T.nx, counted);
-      if (counted) {
-        rsq += (double)r * (double)r;
-        rn += 1;
+  const CoarseView T = coarse_view(smem, a.lv[0]);
+#pragma unroll
+  for (int r = 0; r < 2; r++)
+#pragma unroll
+    for (int o = 0; o < 2; o++) {
+      const int i = 2 * tx + o, j = ty + 32 * r;
+      if (i < T.nx && j < T.ny) {
+        const int k = i + j * T.nx;
+        T.bs[k] = a.b_top[k];
+        T.x(i, j) = a.x_is_zero ? 0.0f : a.x_top[k];
       }
     }
+  __syncthreads();
+
+  // down: pre-smooth, then residual + restriction with the coarse x set to 0
+  for (int l = 0; l < a.nlev - 1; l++) {
+    const CoarseView F = coarse_view(smem, a.lv[l]);
+    const CoarseView C = coarse_view(smem, a.lv[l + 1]);
+    coarse_smooth(F, a.pre, a.omega);
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int o = 0; o < 2; o++) {
+        const int I = 2 * tx + o, J = ty + 32 * r;
+        if (I >= C.nx || J >= C.ny) continue;
+        float sum = 0.0f;
+        for (int dj = 0; dj < 2; dj++)
+          for (int di = 0; di < 2; di++) {
+            const int i = 2 * I + di, j = 2 * J + dj;
+            if (i < F.nx && j < F.ny) {
+              bool counted;
+              sum += coarse_residual(F, i, j, counted);
+            }
+          }
+        C.bs[I + J * C.nx] = sum;
+        C.x(I, J) = 0.0f;
+      }
+    __syncthreads();
+  }
+  coarse_smooth(coarse_view(smem, a.lv[a.nlev - 1]), a.coarse_sweeps, a.omega);
+  // up: prolongation (9/16, 3/16, 3/16, 1/16), then post-smooth
+  for (int l = a.nlev - 2; l >= 0; l--) {
+    const CoarseView F = coarse_view(smem, a.lv[l]);
+    const CoarseView C = coarse_view(smem, a.lv[l + 1]);
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int o = 0; o < 2; o++) {
+        const int i = 2 * tx + o, j = ty + 32 * r;
+        if (i >= F.nx || j >= F.ny) continue;
+        if ((F.cs[i + j * F.nx] & 3u) != FLUID) continue;
+        const int I = i >> 1, J = j >> 1;
+        const int I2 = (i & 1) ? min(I + 1, C.nx - 1) : max(I - 1, 0);
+        const int J2 = (j & 1) ? min(J + 1, C.ny - 1) : max(J - 1, 0);
+        F.x(i, j) += 0.5625f * C.x(I, J) + 0.1875f * (C.x(I2, J) + C.x(I, J2)) + 0.0625f * C.x(I2, J2);
+      }
+    __syncthreads();
+    coarse_smooth(F, a.post, a.omega);
+  }
+
+  double rsq = 0.0;
+  unsigned long long rn = 0;
+#pragma unroll
+  for (int r = 0; r < 2; r++)
+#pragma unroll
+    for (int o = 0; o < 2; o++) {
+      const int i = 2 * tx + o, j = ty + 32 * r;
+      if (i >= T.nx || j >= T.ny) continue;
+      if (a.acc != nullptr) {
+        bool counted;
+        const float res = coarse_residual(T, i, j, counted);
+        if (counted) {
+          rsq += (double)res * (double)res;
+          rn += 1;
+        }
+      }
+      a.x_top[i + j * T.nx] = T.x(i, j);
+    }
+  if (a.acc != nullptr) {
     __shared__ double red[32];
     __shared__ unsigned long long redn[32];
     const double bsum = block_sum(rsq, red);
@@ -399,7 +479,6 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_mg_coarse(CoarseArgs a) {
       atomicAdd(&a.acc->n_res, bn);
     }
   }
-  for (int k = tid; k < n; k += COARSE_THREADS) a.x_top[k] = fs[T.off_x + k];
 }
 
 // Float64 defect correction (oracle: solveMixed). p_out = p_in + e (e may be
@@ -415,10 +494,10 @@ __global__ void __launch_bounds__(256) k_update_resid64(int nx, int ny, const do
   __shared__ double red[32];
   __shared__ unsigned long long redn[32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
   double sq = 0.0;
   unsigned long long n = 0;
-  if (i < nx && j < ny) {
+  for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
+    if (i >= nx) break;
     const long k = i + (long)j * nx;
     auto P = [&](long q) { return e ? p_in[q] + (double)e[q] : p_in[q]; };
     const double pk = P(k);
@@ -435,8 +514,8 @@ __global__ void __launch_bounds__(256) k_update_resid64(int nx, int ny, const do
         if (c & LINK_YM) sum += P(k - nx);
         const double rd = (double)b[k] - ((double)cnt * pk - sum);
         r = (float)rd;
-        sq = rd * rd;
-        n = 1;
+        sq += rd * rd;
+        n += 1;
       }
     }
     r32[k] = r;
@@ -459,10 +538,10 @@ __global__ void __launch_bounds__(256) k_rms_remaining(int nx, int ny, const flo
   __shared__ double red[32];
   __shared__ unsigned long long redn[32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
   double sq = 0.0;
   unsigned long long n = 0;
-  if (i < nx && j < ny) {
+  for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
+    if (i >= nx) break;
     const long k = i + (long)j * nx;
     const uint8_t c = code[k];
     if ((c & 3u) == FLUID && code_count(c) > 0) {
@@ -473,8 +552,8 @@ __global__ void __launch_bounds__(256) k_rms_remaining(int nx, int ny, const flo
       if (c & LINK_YM) sum += p[k - nx];
       const double r =
           (double)div[k] + ((double)(float)code_count(c) * (double)p[k] - (double)sum) / (double)scale;
-      sq = r * r;
-      n = 1;
+      sq += r * r;
+      n += 1;
     }
   }
   const double bs = block_sum(sq, red);
@@ -508,44 +587,30 @@ __global__ void k_rb_halfsweep(int nx, int ny, float* __restrict__ p, const floa
 
 // ------------------------------------------------------------- host side
 
-template <int TW, int TH, int P, int MODE>
+template <int P, int MODE>
 static void launch_smooth_t(cudaStream_t s, const SmoothArgs& a) {
-  using G = SmoothGeom<TW, TH, P, MODE>;
-  static bool configured = false;  // per-instantiation attribute, set once per process
-  const size_t bytes = G::bytes();
-  if (!configured) {
-    cudaFuncSetAttribute(k_smooth<TW, TH, P, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    configured = true;
-  }
-  dim3 blk(SMOOTH_THREADS_X, SMOOTH_THREADS_Y);
-  dim3 grd((a.nx + TW - 1) / TW, (a.ny + TH - 1) / TH);
-  k_smooth<TW, TH, P, MODE><<<grd, blk, bytes, s>>>(a);
+  constexpr int T = Tile<P, MODE>::T;
+  dim3 blk(RGN_T, RGN_T);
+  dim3 grd((a.nx + T - 1) / T, (a.ny + T - 1) / T);
+  k_smooth<P, MODE><<<grd, blk, 0, s>>>(a);
 }
 
-template <int TW, int TH, int MODE>
+template <int MODE>
 static bool launch_smooth_p(cudaStream_t s, const SmoothArgs& a, int pairs) {
   switch (pairs) {
-    case 0: if (MODE != MODE_PLAIN) { launch_smooth_t<TW, TH, 0, MODE>(s, a); return true; } return false;
-    case 1: launch_smooth_t<TW, TH, 1, MODE>(s, a); return true;
-    case 2: launch_smooth_t<TW, TH, 2, MODE>(s, a); return true;
-    case 3: launch_smooth_t<TW, TH, 3, MODE>(s, a); return true;
-    case 4: launch_smooth_t<TW, TH, 4, MODE>(s, a); return true;
+    case 0: if (MODE != MODE_PLAIN) { launch_smooth_t<0, MODE>(s, a); return true; } return false;
+    case 1: launch_smooth_t<1, MODE>(s, a); return true;
+    case 2: launch_smooth_t<2, MODE>(s, a); return true;
+    case 3: launch_smooth_t<3, MODE>(s, a); return true;
+    case 4: launch_smooth_t<4, MODE>(s, a); return true;
     default: return false;
   }
 }
 
-// Tile choice: large tiles where there are enough of them to fill 152 SMs,
-// smaller ones on coarser levels.
 static bool launch_smooth(cudaStream_t s, const SmoothArgs& a, int pairs, int mode) {
-  const bool big = (long)a.nx * a.ny >= 512L * 1024L;
-  if (big) {
-    if (mode == MODE_PLAIN) return launch_smooth_p<64, 32, MODE_PLAIN>(s, a, pairs);
-    if (mode == MODE_PRE) return launch_smooth_p<64, 32, MODE_PRE>(s, a, pairs);
-    return launch_smooth_p<64, 32, MODE_POST>(s, a, pairs);
-  }
-  if (mode == MODE_PLAIN) return launch_smooth_p<32, 16, MODE_PLAIN>(s, a, pairs);
-  if (mode == MODE_PRE) return launch_smooth_p<32, 16, MODE_PRE>(s, a, pairs);
-  return launch_smooth_p<32, 16, MODE_POST>(s, a, pairs);
+  if (mode == MODE_PLAIN) return launch_smooth_p<MODE_PLAIN>(s, a, pairs);
+  if (mode == MODE_PRE) return launch_smooth_p<MODE_PRE>(s, a, pairs);
+  return launch_smooth_p<MODE_POST>(s, a, pairs);
 }
 
 void launch_build_codes(cudaStream_t s, int nx, int ny, const uint8_t* label, uint8_t* code) {
@@ -576,25 +641,24 @@ void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* 
 void launch_update_resid64(cudaStream_t s, int nx, int ny, const double* p_in, const float* e, const float* b,
                            const uint8_t* code, double* p_out, float* r32, StepAccum* acc) {
   dim3 bl(32, 8), g((nx + 31) / 32, (ny + 7) / 8);
+  g.y = std::min(g.y, std::max(1u, 1024u / g.x));
   k_update_resid64<<<g, bl, 0, s>>>(nx, ny, p_in, e, b, code, p_out, r32, acc);
 }
 
 void launch_rms_remaining(cudaStream_t s, int nx, int ny, const float* p, const float* div, const uint8_t* code,
                           float scale, StepAccum* acc) {
   dim3 b(32, 8), g((nx + 31) / 32, (ny + 7) / 8);
+  g.y = std::min(g.y, std::max(1u, 1024u / g.x));
   k_rms_remaining<<<g, b, 0, s>>>(nx, ny, p, div, code, scale, acc);
 }
 
-// Levels that the single-CTA tail holds in shared memory: from the first
-// level at or below this many cells.
-static long coarse_cells_limit() { return 64L * 64L; }
-
+// Shared-memory layout of the single-CTA tail for levels from..end.
 static size_t coarse_smem_bytes(const Engine& e, int from, int* off_x, int* off_b, int* off_c) {
   size_t floats = 0;
   for (int l = from; l < (int)e.levels.size(); l++) {
     const long n = (long)e.levels[l].nx * e.levels[l].ny;
     if (off_x) off_x[l - from] = (int)floats;
-    floats += n;
+    floats += 2 * 32 * (size_t)e.levels[l].ny;
     if (off_b) off_b[l - from] = (int)floats;
     floats += n;
   }
@@ -643,15 +707,13 @@ void mg_setup(Engine& e) {
     cudaMemsetAsync(L.x[1], 0, n * sizeof(float), e.stream);
     cudaMemsetAsync(L.b, 0, n * sizeof(float), e.stream);
   }
+  // the tail starts at the first level with both sides <= 64
   int lc = (int)e.levels.size() - 1;
   for (int l = 0; l < (int)e.levels.size(); l++)
-    if ((long)e.levels[l].nx * e.levels[l].ny <= coarse_cells_limit()) {
+    if (e.levels[l].nx <= COARSE_SIDE && e.levels[l].ny <= COARSE_SIDE) {
       lc = l;
       break;
     }
-  // The tiled kernels need even-aligned tiles on the level they restrict
-  // from; any level works. Keep the tail within shared memory.
-  while (coarse_smem_bytes(e, lc, nullptr, nullptr, nullptr) > 200 * 1024 && lc < (int)e.levels.size() - 1) lc++;
   e.coarse_level = lc;
   e.coarse_smem = coarse_smem_bytes(e, lc, nullptr, nullptr, nullptr);
   cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.coarse_smem);
@@ -725,7 +787,7 @@ void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc) {
     a.coarse_sweeps = e.prm.mg_coarse_sweeps;
     a.omega = omega;
     a.acc = lc == 0 ? acc : nullptr;
-    k_mg_coarse<<<1, COARSE_THREADS, e.coarse_smem, s>>>(a);
+    k_mg_coarse<<<1, dim3(32, 32), e.coarse_smem, s>>>(a);
     prof_end(e, tok, bytes, 1);
   }
   for (int l = lc - 1; l >= 0; l--) {

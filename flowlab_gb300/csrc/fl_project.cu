@@ -2,6 +2,7 @@
 // boundaries.ts, buoyancy.ts, stir.ts, dye.ts, vorticity.ts; WGSL twin
 // src/gpu/project.wgsl) plus the NEW vorticity confinement and the device-
 // side CFL reduction that sets the next step's dt.
+#include <algorithm>
 #include <cmath>
 
 #include "fl_internal.h"
@@ -10,13 +11,13 @@ namespace fl {
 
 // vorticity.ts:9-14
 __device__ __forceinline__ float curl_at_corner(const float* __restrict__ u, const float* __restrict__ v, int nx,
-                                                float h, int i, int j) {
-  return (v[i + (long)j * nx] - v[(i - 1) + (long)j * nx]) / h -
-         (u[i + (long)j * (nx + 1)] - u[i + (long)(j - 1) * (nx + 1)]) / h;
+                                                const Spacing& h, int i, int j) {
+  return over(v[i + (long)j * nx] - v[(i - 1) + (long)j * nx], h) -
+         over(u[i + (long)j * (nx + 1)] - u[i + (long)(j - 1) * (nx + 1)], h);
 }
 
 // vorticity.ts:24-42 — corner curls averaged to the centre, clamped at walls.
-__global__ void k_vorticity(int nx, int ny, float h, const float* __restrict__ u, const float* __restrict__ v,
+__global__ void k_vorticity(int nx, int ny, Spacing h, const float* __restrict__ u, const float* __restrict__ v,
                             float* __restrict__ w) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -31,7 +32,7 @@ __global__ void k_vorticity(int nx, int ny, float h, const float* __restrict__ u
 // NEW — vorticity confinement force at cell centres (Fedkiw, Stam & Jensen
 // 2001): N = grad|w| / (|grad|w|| + 1e-20), f = eps*h * (N_y w, -N_x w),
 // zero in solid cells. Centred differences, one-sided at the walls.
-__global__ void k_confinement_force(int nx, int ny, float h, const float* __restrict__ w,
+__global__ void k_confinement_force(int nx, int ny, Spacing h1, Spacing h2, const float* __restrict__ w,
                                     const uint8_t* __restrict__ label, float epsh, float* __restrict__ fx,
                                     float* __restrict__ fy) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -45,8 +46,9 @@ __global__ void k_confinement_force(int nx, int ny, float h, const float* __rest
   }
   const int ie = min(i + 1, nx - 1), iw = max(i - 1, 0);
   const int jn = min(j + 1, ny - 1), js = max(j - 1, 0);
-  const float gx = (fabsf(w[ie + (long)j * nx]) - fabsf(w[iw + (long)j * nx])) / ((float)(ie - iw) * h);
-  const float gy = (fabsf(w[i + (long)jn * nx]) - fabsf(w[i + (long)js * nx])) / ((float)(jn - js) * h);
+  // (ie-iw)*h is h or 2h: both powers of two when h is one
+  const float gx = over(fabsf(w[ie + (long)j * nx]) - fabsf(w[iw + (long)j * nx]), ie - iw == 2 ? h2 : h1);
+  const float gy = over(fabsf(w[i + (long)jn * nx]) - fabsf(w[i + (long)js * nx]), jn - js == 2 ? h2 : h1);
   const float mag = sqrtf(gx * gx + gy * gy) + 1e-20f;
   const float Nx = gx / mag, Ny = gy / mag;
   const float wk = w[k];
@@ -58,7 +60,7 @@ __global__ void k_confinement_force(int nx, int ny, float h, const float* __rest
 // stir.ts:49-83 bounds for u): v += (beta*dt)*T + (-alpha*dt)*s, then the
 // confinement face average. One thread per (u face, v face) pair, in place:
 // every write depends only on the thread's own face.
-__global__ void __launch_bounds__(256) k_forces(int nx, int ny, float h, int dnx, int dny, float dh,
+__global__ void __launch_bounds__(256) k_forces(int nx, int ny, float h, int dnx, int dny, Spacing dh,
                                                 float* __restrict__ u, float* __restrict__ v,
                                                 const float* __restrict__ dye, const uint8_t* __restrict__ label,
                                                 int beta_on, int alpha_on, int conf_on,
@@ -97,19 +99,21 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
   __shared__ double red[32];
   __shared__ unsigned long long redn[32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
   double sq = 0.0;
   unsigned long long n = 0;
-  if (i < nx && j < ny) {
-    const float coef = 1.0f / h;
+  const float coef = 1.0f / h;
+  const float ns = as_rhs ? sc->neg_scale : 0.0f;
+  // rows strided over a bounded grid, so that few blocks feed the atomics
+  for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
+    if (i >= nx) break;
     const long k = i + (long)j * nx;
     const float d = coef * (u[(i + 1) + (long)j * (nx + 1)] - u[i + (long)j * (nx + 1)] + v[i + (long)(j + 1) * nx] -
                             v[i + (long)j * nx]);
-    const float o = as_rhs ? sc->neg_scale * d : d;
+    const float o = as_rhs ? ns * d : d;
     out[k] = o;
     if (label != nullptr && label[k] == FLUID) {
-      sq = (double)o * (double)o;
-      n = 1;
+      sq += (double)o * (double)o;
+      n += 1;
     }
   }
   if (acc == nullptr) return;
@@ -354,27 +358,30 @@ static dim3 grid2(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + 
 
 void launch_vorticity(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* w) {
   dim3 b(32, 8);
-  k_vorticity<<<grid2(nx, ny, b), b, 0, s>>>(nx, ny, h, u, v, w);
+  k_vorticity<<<grid2(nx, ny, b), b, 0, s>>>(nx, ny, make_spacing(h), u, v, w);
 }
 
 void launch_confinement_force(cudaStream_t s, int nx, int ny, float h, const float* w, const uint8_t* label,
                               float eps, float* fx, float* fy) {
   dim3 b(32, 8);
-  k_confinement_force<<<grid2(nx, ny, b), b, 0, s>>>(nx, ny, h, w, label, eps * h, fx, fy);
+  k_confinement_force<<<grid2(nx, ny, b), b, 0, s>>>(nx, ny, make_spacing(1.0f * h), make_spacing(2.0f * h), w,
+                                                     label, eps * h, fx, fy);
 }
 
 void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, float* u, float* v,
                    const float* dye, const uint8_t* label, bool beta_on, bool alpha_on, bool conf_on,
                    const float* fx, const float* fy, const StepScalars* sc) {
   dim3 b(32, 8);
-  k_forces<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, h, dnx, dny, dh, u, v, dye, label, beta_on, alpha_on,
+  k_forces<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, h, dnx, dny, make_spacing(dh), u, v, dye, label, beta_on, alpha_on,
                                                   conf_on, fx, fy, sc);
 }
 
 void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
                        bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc) {
   dim3 b(32, 8);
-  k_divergence<<<grid2(nx, ny, b), b, 0, s>>>(nx, ny, h, u, v, out, as_rhs, label, sc, acc);
+  dim3 g = grid2(nx, ny, b);
+  g.y = std::min(g.y, std::max(1u, 1024u / g.x));
+  k_divergence<<<g, b, 0, s>>>(nx, ny, h, u, v, out, as_rhs, label, sc, acc);
 }
 
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
