@@ -59,6 +59,25 @@ struct StepAccum {
   unsigned int nonfinite;
 };
 
+// Device-side state of one pressure solve, so that the cycle loop can run
+// without the host: the begin/check kernels decide whether another cycle
+// runs (a CUDA-graph WHILE condition, or a flag the host reads), count
+// cycles, and keep the float64 pressure's buffer parity.
+struct SolveCtl {
+  double tol;        // relative-residual target (<= 0: run max_cycles)
+  double b_rms;      // RMS of the rhs over fluid cells
+  double rel;        // last relative residual (-1: not evaluated)
+  int max_cycles;
+  int mode;          // SOLVE_MG, SOLVE_MIXED, SOLVE_RB
+  int cycles;        // cycles run in this solve
+  int cont;          // 1: run another cycle
+  int zero_p;        // the rhs vanished: p = 0 is the answer
+  int nonfinite;     // a NaN/Inf showed up in the rhs or the residual
+  int par;           // which float64 pressure buffer holds p
+  int pad;
+};
+constexpr int SOLVE_MG = 0, SOLVE_MIXED = 1, SOLVE_RB = 2;
+
 // ------------------------------------------------------------ sampling
 
 // A cell size with its reciprocal. When h is a power of two, x / h and

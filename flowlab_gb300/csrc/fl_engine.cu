@@ -25,6 +25,7 @@ namespace fl {
 
 int prof_begin(Engine& e, int phase) {
   if (!e.profiling) return -1;
+  launch_hold(e.stream);
   Engine::PendingPhase p;
   p.phase = phase;
   for (cudaEvent_t* ev : {&p.a, &p.b}) {
@@ -147,6 +148,8 @@ int dalloc(Engine* e, void** p, size_t bytes, const char* what) {
   return cudaMemsetAsync(*p, 0, bytes, e->stream) == cudaSuccess ? FL_OK : cuda_status(e, cudaGetLastError(), what);
 }
 
+void destroy_graphs(Engine* e);
+
 void free_all(Engine* e) {
   cudaFree(e->u[0]);
   cudaFree(e->u[1]);
@@ -168,6 +171,8 @@ void free_all(Engine* e) {
   cudaFree(e->p64[0]);
   cudaFree(e->p64[1]);
   cudaFree(e->r32);
+  cudaFree(e->ctl);
+  destroy_graphs(e);
   if (!e->levels.empty()) cudaFree(e->levels[0].label);
   mg_free(*e);
   for (auto& p : e->pending) {
@@ -176,6 +181,8 @@ void free_all(Engine* e) {
   }
   for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
   if (e->acc_host) cudaFreeHost(e->acc_host);
+  if (e->ctl_host) cudaFreeHost(e->ctl_host);
+  if (e->stream2) cudaStreamDestroy(e->stream2);
   if (e->stream) cudaStreamDestroy(e->stream);
 }
 
@@ -273,85 +280,175 @@ double host_fluid_div_rms(const float* div, const uint8_t* label, long n) {
   return c > 0 ? std::sqrt(s / (double)c) : 0.0;
 }
 
-// Multigrid to tolerance on levels[0].b (pressureMultigrid.ts:284-319): the
-// warm start is levels[0].x[0]; b's fluid sums must already be in acc.
-int mg_solve_device(Engine* e, int max_cycles, double tol, int* cycles, double* relres) {
-  TRY(read_accum(e));
-  const double b_rms = rms(e->acc_host->b_sq, e->acc_host->n_fluid);
-  e->last_div_rms = b_rms;
-  *relres = -1;
-  *cycles = 0;
-  if (b_rms == 0) {
-    // p = 0 is the exact answer; a warm-started leftover would re-inject
-    // divergence (pressureMultigrid.ts:294-300).
-    TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].x[0], 0, e->cells() * sizeof(float), e->stream), "zero p"));
-    *relres = 0;
-    return FL_OK;
-  }
-  if (!std::isfinite(b_rms)) return fail(e, FL_ENONFINITE, "non-finite divergence");
-  for (int c = 0; c < max_cycles; c++) {
-    if (tol > 0) TRY(zero_residual_accum(e));
-    mg_vcycle(*e, tol > 0 ? e->acc : nullptr);
-    TRY(check_launch(e, "v-cycle"));
-    *cycles = c + 1;
-    if (tol > 0) {
-      TRY(read_accum(e));
-      const double rel = rms(e->acc_host->res_sq, e->acc_host->n_res) / b_rms;
-      *relres = rel;
-      if (!std::isfinite(rel)) return fail(e, FL_ENONFINITE, "non-finite residual after %d V-cycles", c + 1);
-      if (rel <= tol) break;
-    }
-  }
-  return FL_OK;
+// ------------------------------------------------------------ the step
+//
+// A step is enqueued in three parts: the pre-solve passes, the pressure solve
+// (prologue, a cycle body repeated while the device says so, epilogue) and the
+// post-solve passes. The eager path repeats the body while a flag read back
+// from the device is set; the graph path captures the same kernels once, with
+// the body inside a CUDA-graph WHILE node that the check kernel drives, so a
+// whole step is one graph launch with no host round trip.
+
+bool solve_on_device(const Engine* e) { return e->prm.solver == FL_SOLVER_MG || e->prm.tol <= 0; }
+
+// Writes the solve parameters into the device control block. The float64
+// buffer parity is state, not a parameter: it is kept unless reset_par.
+int put_ctl(Engine* e, int mode, double tol, int max_cycles, bool reset_par) {
+  TRY(cuda_status(e, cudaMemcpyAsync(e->ctl_host, e->ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, e->stream),
+                  "read solve state"));
+  TRY(sync(e, "read solve state"));
+  SolveCtl c{};
+  c.tol = tol;
+  c.max_cycles = max_cycles;
+  c.mode = mode;
+  c.rel = -1;
+  c.par = reset_par ? 0 : e->ctl_host->par;
+  *e->ctl_host = c;
+  TRY(cuda_status(e, cudaMemcpyAsync(e->ctl, e->ctl_host, sizeof(SolveCtl), cudaMemcpyHostToDevice, e->stream),
+                  "solve state"));
+  return sync(e, "solve state");
 }
 
-// Float64 defect correction around the multigrid (the oracle's solveMixed):
-// p64[par] is the pressure, levels[0].b the float rhs with its fluid sums in
-// acc. Each pass: one float V-cycle on A e = r (from e = 0), then
-// p64 += e and r = b - A p64 in double; stop when the relative residual
-// reaches tol (tested before every pass, so a converged warm start costs no
-// cycle) or after max_cycles.
-int mg_solve_mixed_device(Engine* e, int max_cycles, double tol, int* cycles, double* relres) {
+bool step_mixed(const Engine* e) { return e->prm.solver == FL_SOLVER_MG && e->prm.mixed; }
+
+// The step's solve settings from the engine parameters.
+int put_step_ctl(Engine* e, bool reset_par) {
+  if (e->prm.solver == FL_SOLVER_MG)
+    return put_ctl(e, e->prm.mixed ? SOLVE_MIXED : SOLVE_MG, e->prm.tol, e->prm.mg_max_cycles, reset_par);
+  return put_ctl(e, SOLVE_RB, e->prm.tol, e->prm.pressure_iters, reset_par);
+}
+
+int read_ctl(Engine* e) {
+  TRY(cuda_status(e, cudaMemcpyAsync(e->ctl_host, e->ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, e->stream),
+                  "read solve state"));
+  return sync(e, "read solve state");
+}
+
+// advect u,v -> [stir] -> [confinement] -> body forces -> divergence
+void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
   Level& L0 = e->levels[0];
-  cudaStream_t s = e->stream;
-  TRY(zero_residual_accum(e));
-  launch_update_resid64(s, e->nx, e->ny, e->p64[e->par], nullptr, L0.b, L0.code, nullptr, e->r32, e->acc);
-  TRY(check_launch(e, "residual"));
-  TRY(read_accum(e));
-  const double b_rms = rms(e->acc_host->b_sq, e->acc_host->n_fluid);
-  e->last_div_rms = b_rms;
-  *cycles = 0;
-  if (b_rms == 0) {
-    TRY(cuda_status(e, cudaMemsetAsync(e->p64[e->par], 0, e->cells() * sizeof(double), s), "zero p"));
-    *relres = 0;
-    return FL_OK;
+  const int mac = e->prm.scheme == FL_MACCORMACK;
+  const double N = (double)e->cells(), F = (double)(e->ufaces() + e->vfaces()), D = (double)e->dye_cells();
+  int tok = prof_begin(*e, FL_PH_ADVECT_VELOCITY);
+  launch_advect_velocity(s, e->nx, e->ny, e->h, mac, e->u[par], e->v[par], e->u_hat, e->v_hat, e->u[1 - par],
+                         e->v[1 - par], L0.label, e->sc);
+  // forward: carrier u,v + label in, faces out; correction: u,v + hat + label in, faces out
+  prof_end(*e, tok, mac ? (8 * F + N) + (12 * F + N) : 8 * F + N, mac ? 2 : 1);
+  float* u = e->u[1 - par];
+  float* v = e->v[1 - par];
+  if (stir) launch_stir(s, e->nx, e->ny, e->h, u, v, L0.label, e->stir);
+  const bool conf = e->prm.confinement != 0;
+  const bool beta_on = e->prm.beta != 0, alpha_on = e->prm.alpha != 0;
+  tok = prof_begin(*e, FL_PH_BODY_FORCES);
+  double fbytes = 0;
+  int flaunch = 0;
+  if (conf) {
+    launch_vorticity(s, e->nx, e->ny, e->h, u, v, e->w);
+    launch_confinement_force(s, e->nx, e->ny, e->h, e->w, L0.label, (float)e->prm.confinement, e->fx, e->fy);
+    fbytes += (4 * F + 4 * N) + (4 * N + N + 8 * N);
+    flaunch += 2;
   }
-  if (!std::isfinite(b_rms)) return fail(e, FL_ENONFINITE, "non-finite divergence");
-  double rel = rms(e->acc_host->res_sq, e->acc_host->n_res) / b_rms;
-  *relres = rel;
-  int c = 0;
-  while (c < max_cycles && !(rel <= tol)) {
-    mg_vcycle_on(*e, e->r32, true, nullptr);
-    TRY(zero_residual_accum(e));
-    const int tok = prof_begin(*e, FL_PH_MG_UP);
-    launch_update_resid64(s, e->nx, e->ny, e->p64[e->par], L0.x[0], L0.b, L0.code, e->p64[1 - e->par], e->r32,
-                          e->acc);
-    prof_end(*e, tok, 29.0 * e->cells(), 1);
-    TRY(check_launch(e, "update + residual"));
-    e->par = 1 - e->par;
-    TRY(read_accum(e));
-    rel = rms(e->acc_host->res_sq, e->acc_host->n_res) / b_rms;
-    *relres = rel;
-    if (!std::isfinite(rel)) return fail(e, FL_ENONFINITE, "non-finite residual after %d V-cycles", c + 1);
-    c++;
+  if (beta_on || alpha_on || conf) {
+    launch_forces(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, u, v, e->dye[par], L0.label, beta_on, alpha_on, conf,
+                  e->fx, e->fy, e->sc);
+    fbytes += 8 * F + N + (beta_on ? 4 * D : 0) + (alpha_on ? 4 * D : 0) + (conf ? 8 * N : 0);
+    flaunch += 1;
   }
-  *cycles = c;
-  return FL_OK;
+  prof_end(*e, tok, fbytes, flaunch);
+  cudaMemsetAsync(e->acc, 0, 4 * sizeof(double), s);
+  tok = prof_begin(*e, FL_PH_DIVERGENCE);
+  launch_divergence(s, e->nx, e->ny, e->h, u, v, L0.b, e->prm.solver == FL_SOLVER_MG, L0.label, e->sc, e->acc);
+  prof_end(*e, tok, 4 * F + N + 4 * N, 1);
 }
 
-// Red-black SOR to tolerance (pressureRedBlack.ts:88-113) on div in
-// levels[0].b with the warm start in levels[0].x[0]. Sweep pairs are grouped
-// up to four per launch (temporal blocking) and never across a 12-sweep check.
+// Solve prologue: the float64 path's initial residual, then the begin test.
+void enqueue_solve_prologue(Engine* e, cudaStream_t s, bool mixed, bool use_cond, cudaGraphConditionalHandle h) {
+  Level& L0 = e->levels[0];
+  if (mixed) {
+    const int tok = prof_begin(*e, FL_PH_DEFECT64);
+    launch_update_resid64(s, e->nx, e->ny, e->p64[0], e->p64[1], e->ctl, nullptr, L0.b, L0.code, false, e->r32,
+                          e->acc);
+    // p64, b, code in; r32 out
+    prof_end(*e, tok, 17.0 * e->cells(), 1);
+  }
+  const int tok = prof_begin(*e, FL_PH_CONTROL);
+  launch_solve_begin(s, e->acc, e->ctl, use_cond, h);
+  prof_end(*e, tok, 0, 1);
+}
+
+// One multigrid cycle: a V-cycle on b (float32 path, warm start in
+// levels[0].x[0], residual accumulated by its last kernel) or on the float64
+// path's residual followed by p64 += e and the new float64 residual.
+void enqueue_solve_body(Engine* e, cudaStream_t s, bool mixed, bool use_cond, cudaGraphConditionalHandle h) {
+  Level& L0 = e->levels[0];
+  if (mixed) {
+    mg_vcycle_on(*e, e->r32, true, nullptr);
+    const int tok = prof_begin(*e, FL_PH_DEFECT64);
+    launch_update_resid64(s, e->nx, e->ny, e->p64[0], e->p64[1], e->ctl, L0.x[0], L0.b, L0.code, true, e->r32,
+                          e->acc);
+    // p64, e, b, code in; p64 (other buffer), r32 out
+    prof_end(*e, tok, 29.0 * e->cells(), 1);
+  } else {
+    mg_vcycle_on(*e, L0.b, false, e->acc);
+  }
+  const int tok = prof_begin(*e, FL_PH_CONTROL);
+  launch_solve_check(s, e->acc, e->ctl, use_cond, h);
+  prof_end(*e, tok, 0, 1);
+}
+
+void enqueue_solve_epilogue(Engine* e, cudaStream_t s, bool mixed) {
+  const int tok = prof_begin(*e, FL_PH_CONTROL);
+  launch_zero_if(s, e->ctl, mixed ? nullptr : e->levels[0].x[0], mixed ? e->p64[0] : nullptr,
+                 mixed ? e->p64[1] : nullptr, e->cells());
+  prof_end(*e, tok, 0, 1);
+}
+
+// Red-black SOR with a fixed budget (tol <= 0, the reference's browser
+// setting): sweep pairs grouped up to four per launch, scale read from the
+// step's scalars on the device, result back in levels[0].x[0].
+void enqueue_rb_fixed(Engine* e, cudaStream_t s) {
+  Level& L = e->levels[0];
+  launch_solve_begin(s, e->acc, e->ctl, false, 0);
+  int k = 0, src = 0;
+  const int iters = e->prm.pressure_iters;
+  while (k < iters) {
+    const int chunk = std::min(4, iters - k);
+    const int tok = prof_begin(*e, FL_PH_RB_SWEEPS);
+    launch_rb_sweeps(s, L.nx, L.ny, L.x[src], L.x[1 - src], L.b, L.code, 0.0f, (float)e->prm.omega, chunk,
+                     &e->sc->scale);
+    prof_end(*e, tok, 13.0 * e->cells(), 1);
+    src = 1 - src;
+    k += chunk;
+  }
+  if (src == 1) cudaMemcpyAsync(L.x[0], L.x[1], e->cells() * sizeof(float), cudaMemcpyDeviceToDevice, s);
+  launch_zero_if(s, e->ctl, L.x[0], nullptr, nullptr, e->cells());
+}
+
+// subtract gradient + outflow -> dye (advect, decay, inlet) -> CFL
+void enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
+  Level& L0 = e->levels[0];
+  const int mac = e->prm.scheme == FL_MACCORMACK;
+  const double N = (double)e->cells(), F = (double)(e->ufaces() + e->vfaces()), D = (double)e->dye_cells();
+  const bool mixed = step_mixed(e);
+  float* u = e->u[1 - par];
+  float* v = e->v[1 - par];
+  int tok = prof_begin(*e, FL_PH_PROJECT);
+  launch_subtract_outflow(s, e->nx, e->ny, L0.x[0], u, v, L0.label, e->sc, true, true, mixed ? e->p64[0] : nullptr,
+                          mixed ? e->p64[1] : nullptr, e->ctl);
+  prof_end(*e, tok, (mixed ? 8 : 4) * N + 4 * F + N + 4 * F, 1);
+  tok = prof_begin(*e, FL_PH_ADVECT_DYE);
+  launch_advect_dye(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, mac, u, v, e->dye[par], e->dye_hat, e->dye[1 - par],
+                    L0.label, e->sc, true, e->patch, e->pi0, e->pj0, e->pnx, e->pny);
+  // forward: u,v + 3 planes + label in, 3 planes out; correction adds the hat planes
+  prof_end(*e, tok, mac ? (4 * F + 24 * D + N) + (4 * F + 36 * D + N) : 4 * F + 24 * D + N, mac ? 2 : 1);
+  tok = prof_begin(*e, FL_PH_CFL);
+  launch_max_speed(s, e->nx, e->ny, u, v, e->acc, e->sc, e->time_dev, &e->prm, e->h, device_dt, device_dt);
+  prof_end(*e, tok, 4 * F, 1);
+}
+
+// Red-black SOR to a tolerance (pressureRedBlack.ts:88-113): checked every
+// 12 sweeps on the host, pairs grouped up to four per launch and never
+// across a check.
 int rb_solve_device(Engine* e, float scale, int iterations, float omega, double tol, double div_rms, int* used) {
   Level& L = e->levels[0];
   *used = iterations;
@@ -386,69 +483,45 @@ int rb_solve_device(Engine* e, float scale, int iterations, float omega, double 
   return FL_OK;
 }
 
-// One fused step. host_dt: scalars already in e->sc from the caller.
-int step_once(Engine* e, bool device_dt) {
+// The multigrid solve, eager: the same kernels as the graph's, with the host
+// reading the device's decision after each cycle.
+int solve_mg_eager(Engine* e, bool mixed, int max_cycles) {
+  cudaStream_t s = e->stream;
+  enqueue_solve_prologue(e, s, mixed, false, 0);
+  TRY(check_launch(e, "solve"));
+  for (int guard = 0; guard <= max_cycles + 1; guard++) {
+    TRY(read_ctl(e));
+    if (e->ctl_host->nonfinite)
+      return fail(e, FL_ENONFINITE, "non-finite %s", e->ctl_host->cycles ? "residual" : "divergence");
+    if (!e->ctl_host->cont) break;
+    enqueue_solve_body(e, s, mixed, false, 0);
+    TRY(check_launch(e, "V-cycle"));
+  }
+  enqueue_solve_epilogue(e, s, mixed);
+  return check_launch(e, "solve");
+}
+
+// One step, eager. device_dt: scalars from the previous CFL reduction;
+// otherwise the caller put them in e->sc.
+int step_eager(Engine* e, bool device_dt) {
   cudaStream_t s = e->stream;
   Level& L0 = e->levels[0];
+  const int par = e->cur;
   if (e->labels_dirty) {
-    launch_commit_labels(s, e->nx, e->ny, L0.label, L0.x[0], e->u[e->cur], e->v[e->cur], e->dye[e->dcur],
-                         e->dye_cells());
+    launch_commit_labels(s, e->nx, e->ny, L0.label, L0.x[0], e->u[par], e->v[par], e->dye[par], e->dye_cells());
     mg_build_codes(*e);
     TRY(check_launch(e, "commit labels"));
     e->labels_dirty = false;
   }
-  const int mac = e->prm.scheme == FL_MACCORMACK;
-  const int in = e->cur, out = 1 - e->cur;
-  const double N = (double)e->cells(), F = (double)(e->ufaces() + e->vfaces()), D = (double)e->dye_cells();
   if (e->pending.size() > 8192) prof_drain(*e);
-  int tok = prof_begin(*e, FL_PH_ADVECT_VELOCITY);
-  launch_advect_velocity(s, e->nx, e->ny, e->h, mac, e->u[in], e->v[in], e->u_hat, e->v_hat, e->u[out], e->v[out],
-                         L0.label, e->sc);
-  // forward: carrier u,v + label in, faces out; correction: u,v + hat + label in, faces out
-  prof_end(*e, tok, mac ? (8 * F + N) + (12 * F + N) : 8 * F + N, mac ? 2 : 1);
-  TRY(check_launch(e, "advect velocity"));
-  e->cur = out;
-  float* u = e->u[e->cur];
-  float* v = e->v[e->cur];
-  if (e->stir_pending) {
-    launch_stir(s, e->nx, e->ny, e->h, u, v, L0.label, e->stir);
-    e->stir_pending = false;
-  }
-  const bool conf = e->prm.confinement != 0;
-  const bool beta_on = e->prm.beta != 0, alpha_on = e->prm.alpha != 0;
-  tok = prof_begin(*e, FL_PH_BODY_FORCES);
-  double fbytes = 0;
-  int flaunch = 0;
-  if (conf) {
-    launch_vorticity(s, e->nx, e->ny, e->h, u, v, e->w);
-    launch_confinement_force(s, e->nx, e->ny, e->h, e->w, L0.label, (float)e->prm.confinement, e->fx, e->fy);
-    fbytes += (4 * F + 4 * N) + (4 * N + N + 8 * N);
-    flaunch += 2;
-  }
-  if (beta_on || alpha_on || conf) {
-    launch_forces(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, u, v, e->dye[e->dcur], L0.label, beta_on, alpha_on,
-                  conf, e->fx, e->fy, e->sc);
-    fbytes += 8 * F + N + (beta_on ? 4 * D : 0) + (alpha_on ? 4 * D : 0) + (conf ? 8 * N : 0);
-    flaunch += 1;
-  }
-  prof_end(*e, tok, fbytes, flaunch);
-  TRY(zero_solve_accum(e));
-  const bool mg = e->prm.solver == FL_SOLVER_MG;
-  tok = prof_begin(*e, FL_PH_DIVERGENCE);
-  launch_divergence(s, e->nx, e->ny, e->h, u, v, L0.b, mg, L0.label, e->sc, e->acc);
-  prof_end(*e, tok, 4 * F + N + 4 * N, 1);
-  TRY(check_launch(e, "body forces / divergence"));
-
-  int iters = 0;
-  const bool mixed = mg && e->prm.mixed;
-  if (mixed) {
-    double rr;
-    TRY(mg_solve_mixed_device(e, e->prm.mg_max_cycles, e->prm.tol, &iters, &rr));
-    e->last_relres = rr;
-  } else if (mg) {
-    double rr;
-    TRY(mg_solve_device(e, e->prm.mg_max_cycles, e->prm.tol, &iters, &rr));
-    e->last_relres = rr;
+  enqueue_pre(e, s, par, e->stir_pending);
+  e->stir_pending = false;
+  TRY(check_launch(e, "advect / forces / divergence"));
+  e->stats_on_device = solve_on_device(e);
+  if (e->prm.solver == FL_SOLVER_MG) {
+    TRY(solve_mg_eager(e, step_mixed(e), e->prm.mg_max_cycles));
+  } else if (e->prm.tol <= 0) {
+    enqueue_rb_fixed(e, s);
   } else {
     TRY(read_accum(e));
     const double div_rms = rms(e->acc_host->b_sq, e->acc_host->n_fluid);
@@ -456,29 +529,117 @@ int step_once(Engine* e, bool device_dt) {
     StepScalars hs;
     TRY(cuda_status(e, cudaMemcpyAsync(&hs, e->sc, sizeof hs, cudaMemcpyDeviceToHost, s), "read scalars"));
     TRY(sync(e, "read scalars"));
-    if (div_rms == 0) {
+    int iters = 0;
+    if (div_rms == 0)
       TRY(cuda_status(e, cudaMemsetAsync(L0.x[0], 0, e->cells() * sizeof(float), s), "zero p"));
-    } else {
+    else
       TRY(rb_solve_device(e, hs.scale, e->prm.pressure_iters, (float)e->prm.omega, e->prm.tol, div_rms, &iters));
-    }
+    e->last_iters = iters;
   }
-  e->last_iters = iters;
-  tok = prof_begin(*e, FL_PH_PROJECT);
-  launch_subtract_outflow(s, e->nx, e->ny, L0.x[0], u, v, L0.label, e->sc, true, true,
-                          mixed ? e->p64[e->par] : nullptr);
-  prof_end(*e, tok, (mixed ? 8 : 4) * N + 4 * F + N + 4 * F, 1);
-  const int din = e->dcur, dout = 1 - e->dcur;
-  tok = prof_begin(*e, FL_PH_ADVECT_DYE);
-  launch_advect_dye(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, mac, u, v, e->dye[din], e->dye_hat, e->dye[dout],
-                    L0.label, e->sc, true, e->patch, e->pi0, e->pj0, e->pnx, e->pny);
-  // forward: u,v + 3 planes + label in, 3 planes out; correction adds the hat planes
-  prof_end(*e, tok, mac ? (4 * F + 24 * D + N) + (4 * F + 36 * D + N) : 4 * F + 24 * D + N, mac ? 2 : 1);
-  e->dcur = dout;
-  tok = prof_begin(*e, FL_PH_CFL);
-  launch_max_speed(s, e->nx, e->ny, u, v, e->acc, e->sc, e->time_dev, &e->prm, e->h, device_dt, device_dt);
-  prof_end(*e, tok, 4 * F, 1);
+  enqueue_post(e, s, par, device_dt);
   TRY(check_launch(e, "project / dye / CFL"));
+  e->cur = 1 - par;
   e->steps++;
+  return FL_OK;
+}
+
+void destroy_graphs(Engine* e) {
+  for (auto& g : e->graph) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  e->graphs_valid = false;
+}
+
+// Captures the whole step for buffer parity `par` into an executable graph.
+int build_graph(Engine* e, int par, cudaGraphExec_t* out) {
+  cudaStream_t s = e->stream;
+  cudaError_t err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (err != cudaSuccess) return cuda_status(e, err, "begin capture");
+  enqueue_pre(e, s, par, false);
+  if (e->prm.solver == FL_SOLVER_MG) {
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t cap = nullptr;
+    err = cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap, nullptr, nullptr, nullptr);
+    cudaGraphConditionalHandle h = 0;
+    if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&h, cap, 0, cudaGraphCondAssignDefault);
+    if (err == cudaSuccess) {
+      enqueue_solve_prologue(e, s, step_mixed(e), true, h);
+      const cudaGraphNode_t* deps = nullptr;
+      size_t ndeps = 0;
+      err = cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap, &deps, nullptr, &ndeps);
+      cudaGraphNodeParams cp{};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node = nullptr;
+      if (err == cudaSuccess) err = cudaGraphAddNode(&node, cap, deps, nullptr, ndeps, &cp);
+      if (err == cudaSuccess) err = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+      if (err == cudaSuccess) {
+        // the body is captured from the second stream; the V-cycle launchers
+        // enqueue on e->stream, so it points there meanwhile
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        e->stream = e->stream2;
+        err = cudaStreamBeginCaptureToGraph(e->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (err == cudaSuccess) {
+          enqueue_solve_body(e, e->stream, step_mixed(e), true, h);
+          cudaGraph_t done = nullptr;
+          err = cudaStreamEndCapture(e->stream, &done);
+        }
+        e->stream = s;
+      }
+    }
+    if (err == cudaSuccess) enqueue_solve_epilogue(e, s, step_mixed(e));
+  } else {
+    enqueue_rb_fixed(e, s);
+  }
+  if (err == cudaSuccess) enqueue_post(e, s, par, true);
+  cudaGraph_t graph = nullptr;
+  cudaError_t end = cudaStreamEndCapture(s, &graph);
+  if (err == cudaSuccess) err = end;
+  if (err == cudaSuccess) err = cudaGetLastError();
+  if (err == cudaSuccess) err = cudaGraphInstantiate(out, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (err != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_status(e, err, "step graph");
+  }
+  return FL_OK;
+}
+
+bool graph_eligible(const Engine* e) {
+  return e->use_graphs && !e->profiling && !e->stir_pending && !e->labels_dirty && solve_on_device(e);
+}
+
+int step_graph(Engine* e) {
+  if (!e->graphs_valid) {
+    destroy_graphs(e);
+    for (int par = 0; par < 2; par++) TRY(build_graph(e, par, &e->graph[par]));
+    e->graphs_valid = true;
+  }
+  TRY(cuda_status(e, cudaGraphLaunch(e->graph[e->cur], e->stream), "graph launch"));
+  e->cur = 1 - e->cur;
+  e->steps++;
+  e->stats_on_device = true;
+  return FL_OK;
+}
+
+// Fills last_iters / last_relres / last_div_rms from the control block when
+// the last solve ran under the device's control (synchronises).
+int solve_stats(Engine* e) {
+  if (!e->stats_on_device) return FL_OK;
+  TRY(read_ctl(e));
+  const SolveCtl& c = *e->ctl_host;
+  e->last_div_rms = c.b_rms;
+  if (c.mode == SOLVE_RB) {
+    e->last_iters = c.zero_p ? 0 : e->prm.pressure_iters;
+    e->last_relres = -1;
+  } else {
+    e->last_iters = c.cycles;
+    e->last_relres = c.rel;
+  }
+  if (c.nonfinite) return fail(e, FL_ENONFINITE, "non-finite %s", c.cycles ? "residual" : "divergence");
   return FL_OK;
 }
 
@@ -575,10 +736,16 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   s = s ? s : dalloc(e, (void**)&e->p64[0], (size_t)e->cells() * 8, "p64");
   s = s ? s : dalloc(e, (void**)&e->p64[1], (size_t)e->cells() * 8, "p64");
   s = s ? s : dalloc(e, (void**)&e->r32, cf, "residual");
+  s = s ? s : dalloc(e, (void**)&e->ctl, sizeof(SolveCtl), "solve control");
   if (s) return bail(s);
-  if (cudaMallocHost(&e->acc_host, sizeof(StepAccum)) != cudaSuccess) {
+  if (cudaMallocHost(&e->acc_host, sizeof(StepAccum)) != cudaSuccess ||
+      cudaMallocHost(&e->ctl_host, sizeof(SolveCtl)) != cudaSuccess) {
     fail(e, FL_ENOMEM, "pinned accumulator");
     return bail(FL_ENOMEM);
+  }
+  if (cudaStreamCreateWithFlags(&e->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+    fail(e, FL_EDEVICE, "stream creation failed");
+    return bail(FL_EDEVICE);
   }
   mg_setup(*e);
   uint8_t* label0 = nullptr;
@@ -587,6 +754,7 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   if (s) return bail(s);
   e->levels[0].label = label0;
   if (sync(e, "create")) return bail(FL_EDEVICE);
+  if (put_step_ctl(e, true)) return bail(FL_EDEVICE);
   *out = H;
   return FL_OK;
 }
@@ -606,6 +774,8 @@ int fl_set_params(fl_engine* h, const fl_params* p) {
   TRY(validate_params(e, p));
   const bool reshape = p->mg_coarsest != e->prm.mg_coarsest;
   e->prm = *p;
+  destroy_graphs(e);
+  TRY(put_step_ctl(e, false));
   if (reshape) {
     uint8_t* label0 = e->levels[0].label;
     float* p0 = nullptr;
@@ -639,7 +809,8 @@ int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, cons
                      const void* dye) {
   ENTER(h);
   e->cur = 0;
-  e->dcur = 0;
+  e->stats_on_device = false;
+  TRY(put_step_ctl(e, true));
   TRY(upload(e, e->u[0], u, e->ufaces(), dtype, "upload u"));
   TRY(upload(e, e->v[0], v, e->vfaces(), dtype, "upload v"));
   if (p)
@@ -647,7 +818,6 @@ int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, cons
   else
     TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].x[0], 0, e->cells() * 4, e->stream), "zero p"));
   // the float64 pressure of the defect-correction solve starts from the same p
-  e->par = 0;
   if (p && dtype == FL_F64)
     TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, e->cells() * sizeof(double), cudaMemcpyHostToDevice, e->stream),
                     "upload p64"));
@@ -678,6 +848,7 @@ int fl_set_dye_patch(fl_engine* h, int i0, int j0, int pnx, int pny, const float
   cudaFree(e->patch);
   e->patch = nullptr;
   e->pnx = e->pny = 0;
+  destroy_graphs(e);
   if (!data) return FL_OK;
   if (pnx <= 0 || pny <= 0) return fail(e, FL_EINVAL, "patch %dx%d", pnx, pny);
   const size_t bytes = (size_t)4 * pnx * pny * sizeof(float);
@@ -694,6 +865,7 @@ int fl_set_buoyancy(fl_engine* h, double beta, double alpha) {
   ENTER(h);
   e->prm.beta = beta;
   e->prm.alpha = alpha;
+  destroy_graphs(e);
   if (e->uploaded)
     launch_max_speed(e->stream, e->nx, e->ny, e->u[e->cur], e->v[e->cur], e->acc, e->sc, e->time_dev, &e->prm, e->h,
                      true, false);
@@ -703,6 +875,7 @@ int fl_set_buoyancy(fl_engine* h, double beta, double alpha) {
 int fl_set_confinement(fl_engine* h, double eps) {
   ENTER(h);
   e->prm.confinement = eps;
+  destroy_graphs(e);
   return FL_OK;
 }
 
@@ -719,18 +892,23 @@ int fl_step(fl_engine* h, double dt, double scale, double grad_scale, const doub
   if (!e->uploaded) return fail(e, FL_ESTATE, "step before fl_upload_fields");
   if (!(dt > 0)) return fail(e, FL_EINVAL, "dt must be positive");
   TRY(put_scalars(e, host_scalars(e, (float)dt, (float)scale, (float)grad_scale, keep)));
-  TRY(step_once(e, false));
+  TRY(step_eager(e, false));
   e->time += dt;
+  TRY(sync(e, "step"));
+  TRY(solve_stats(e));
   if (iters) *iters = e->last_iters;
-  return sync(e, "step");
+  return FL_OK;
 }
 
 int fl_step_auto(fl_engine* h, int nsteps, int* iters_last) {
   ENTER(h);
   if (!e->uploaded) return fail(e, FL_ESTATE, "step before fl_upload_fields");
   if (nsteps < 0) return fail(e, FL_EINVAL, "nsteps < 0");
-  for (int n = 0; n < nsteps; n++) TRY(step_once(e, true));
-  if (iters_last) *iters_last = e->last_iters;
+  for (int n = 0; n < nsteps; n++) TRY(graph_eligible(e) ? step_graph(e) : step_eager(e, true));
+  if (iters_last) {
+    TRY(solve_stats(e));
+    *iters_last = e->last_iters;
+  }
   return check_launch(e, "step");
 }
 
@@ -743,6 +921,8 @@ int fl_get_stats(fl_engine* h, fl_stats* out) {
   TRY(cuda_status(e, cudaMemcpy(&s, e->sc, sizeof s, cudaMemcpyDeviceToHost), "stats"));
   TRY(cuda_status(e, cudaMemcpy(&t, e->time_dev, sizeof t, cudaMemcpyDeviceToHost), "stats"));
   TRY(read_accum(e));
+  const int st = solve_stats(e);
+  if (st && st != FL_ENONFINITE) return st;
   std::memset(out, 0, sizeof *out);
   out->dt = s.dt;
   out->scale = s.scale;
@@ -768,20 +948,21 @@ int fl_read_velocity(fl_engine* h, int dtype, void* u, void* v) {
 
 int fl_read_dye(fl_engine* h, int dtype, void* dye) {
   ENTER(h);
-  TRY(download(e, dye, e->dye[e->dcur], 3 * e->dye_cells(), dtype, "read dye"));
+  TRY(download(e, dye, e->dye[e->cur], 3 * e->dye_cells(), dtype, "read dye"));
   return sync(e, "read dye");
 }
 
 int fl_read_pressure(fl_engine* h, int dtype, void* p) {
   ENTER(h);
-  if (e->prm.solver == FL_SOLVER_MG && e->prm.mixed) {
+  if (step_mixed(e) && e->uploaded) {
     if (!p) return fail(e, FL_EINVAL, "read p: null pointer");
     const long n = e->cells();
+    TRY(read_ctl(e));
+    const double* p64 = e->p64[e->ctl_host->par];
     if (dtype == FL_F64) {
-      TRY(cuda_status(e, cudaMemcpyAsync(p, e->p64[e->par], n * sizeof(double), cudaMemcpyDeviceToHost, e->stream),
-                      "read p"));
+      TRY(cuda_status(e, cudaMemcpyAsync(p, p64, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream), "read p"));
     } else if (dtype == FL_F32) {
-      launch_convert(e->stream, e->p64[e->par], FL_F64, e->staging, FL_F32, n);
+      launch_convert(e->stream, p64, FL_F64, e->staging, FL_F32, n);
       TRY(check_launch(e, "read p"));
       TRY(cuda_status(e, cudaMemcpyAsync(p, e->staging, n * sizeof(float), cudaMemcpyDeviceToHost, e->stream),
                       "read p"));
@@ -895,11 +1076,10 @@ int fl_mg_solve(fl_engine* h, float* p, const float* div, const uint8_t* label, 
   TRY(zero_solve_accum(e));
   launch_scale_rhs(e->stream, n, e->u_hat, L.b, -scale, L.label, e->acc);
   TRY(check_launch(e, "rhs"));
-  int cycles = 0;
-  double rr = -1;
-  TRY(mg_solve_device(e, max_cycles, tol, &cycles, &rr));
-  if (cycles_used) *cycles_used = cycles;
-  if (rel_residual) *rel_residual = rr;
+  TRY(put_ctl(e, SOLVE_MG, tol, max_cycles, true));
+  TRY(solve_mg_eager(e, false, max_cycles));
+  if (cycles_used) *cycles_used = e->ctl_host->cycles;
+  if (rel_residual) *rel_residual = e->ctl_host->rel;
   TRY(down32(e, p, L.x[0], n * 4, "p"));
   return sync(e, "mg solve");
 }
@@ -911,7 +1091,7 @@ int fl_mg_solve_mixed(fl_engine* h, double* p, const float* div, const uint8_t* 
   if (!p || !div || !label) return fail(e, FL_EINVAL, "null pointer");
   const long n = e->cells();
   Level& L = e->levels[0];
-  e->par = 0;
+  TRY(put_ctl(e, SOLVE_MIXED, tol, max_cycles, true));
   TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, n * sizeof(double), cudaMemcpyHostToDevice, e->stream), "p"));
   TRY(up32(e, e->u_hat, div, n * 4, "div"));
   TRY(up32(e, L.label, label, (size_t)n, "label"));
@@ -919,12 +1099,12 @@ int fl_mg_solve_mixed(fl_engine* h, double* p, const float* div, const uint8_t* 
   TRY(zero_solve_accum(e));
   launch_scale_rhs(e->stream, n, e->u_hat, L.b, -scale, L.label, e->acc);
   TRY(check_launch(e, "rhs"));
-  int cycles = 0;
-  double rr = -1;
-  TRY(mg_solve_mixed_device(e, max_cycles, tol, &cycles, &rr));
-  if (cycles_used) *cycles_used = cycles;
-  if (rel_residual) *rel_residual = rr;
-  TRY(cuda_status(e, cudaMemcpyAsync(p, e->p64[e->par], n * sizeof(double), cudaMemcpyDeviceToHost, e->stream), "p"));
+  TRY(solve_mg_eager(e, true, max_cycles));
+  TRY(read_ctl(e));
+  if (cycles_used) *cycles_used = e->ctl_host->cycles;
+  if (rel_residual) *rel_residual = e->ctl_host->rel;
+  TRY(cuda_status(e, cudaMemcpyAsync(p, e->p64[e->ctl_host->par], n * sizeof(double), cudaMemcpyDeviceToHost, e->stream),
+                  "p"));
   return sync(e, "mg solve mixed");
 }
 

@@ -34,7 +34,8 @@ struct Engine {
   std::atomic<int> busy{0};
   std::string err;
 
-  // velocity: u[cur]/v[cur] is the field; the other is the advection target
+  // velocity and dye: u[cur]/v[cur]/dye[cur] are the fields; the others are
+  // the advection targets
   float* u[2] = {nullptr, nullptr};
   float* v[2] = {nullptr, nullptr};
   float* u_hat = nullptr;
@@ -43,17 +44,24 @@ struct Engine {
   // dye: 3 planes of dnx*dny each
   float* dye[2] = {nullptr, nullptr};
   float* dye_hat = nullptr;
-  int dcur = 0;
 
   std::vector<Level> levels;  // levels[0].x[0] is the resident pressure
   int coarse_level = 0;       // first level solved inside the single-CTA kernel
   size_t coarse_smem = 0;
 
   // float64 pressure of the defect-correction solve (fl_params.mixed):
-  // p64[par] is the pressure, r32 the float residual fed to each V-cycle.
+  // p64[ctl->par] is the pressure, r32 the float residual fed to each V-cycle.
   double* p64[2] = {nullptr, nullptr};
-  int par = 0;
   float* r32 = nullptr;
+  SolveCtl* ctl = nullptr;       // device
+  SolveCtl* ctl_host = nullptr;  // pinned mirror
+
+  // whole-step CUDA graphs, one per velocity/dye buffer parity
+  cudaStream_t stream2 = nullptr;  // capture stream of the cycle-loop body
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  bool graphs_valid = false;
+  bool use_graphs = true;
+  bool stats_on_device = false;  // the last solve's statistics live in ctl
 
   float* w = nullptr;   // vorticity scratch
   float* fx = nullptr;  // confinement force scratch
@@ -138,7 +146,8 @@ void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, 
                        bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc);
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
                              const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow,
-                             const double* p64 = nullptr);
+                             const double* p64a = nullptr, const double* p64b = nullptr,
+                             const SolveCtl* ctl = nullptr);
 void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const float* v, StepAccum* acc,
                       StepScalars* sc_next, double* time_dev, const fl_params* prm, float h, bool write_scalars,
                       bool add_time);
@@ -151,6 +160,7 @@ void launch_stir(cudaStream_t s, int nx, int ny, float h, float* u, float* v, co
                  const float* stir5);
 void launch_dye_patch(cudaStream_t s, int dnx, int dny, float* dye, const float* patch, int pi0, int pj0, int pnx,
                       int pny);
+void launch_hold(cudaStream_t s);
 void launch_convert(cudaStream_t s, const void* src, int src_dtype, void* dst, int dst_dtype, long n);
 
 // fl_multigrid.cu
@@ -159,10 +169,14 @@ void mg_free(Engine& e);
 void mg_build_codes(Engine& e);  // label chain + stencil codes from levels[0].label
 void mg_vcycle(Engine& e, StepAccum* acc_for_residual);
 void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc_for_residual);
-void launch_update_resid64(cudaStream_t s, int nx, int ny, const double* p_in, const float* e, const float* b,
-                           const uint8_t* code, double* p_out, float* r32, StepAccum* acc);
+void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, const SolveCtl* ctl,
+                           const float* e, const float* b, const uint8_t* code, bool update, float* r32,
+                           StepAccum* acc);
+void launch_solve_begin(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h);
+void launch_solve_check(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h);
+void launch_zero_if(cudaStream_t s, const SolveCtl* ctl, float* p32, double* p64a, double* p64b, long n);
 void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* x_out, const float* b,
-                      const uint8_t* code, float scale, float omega, int pairs);
+                      const uint8_t* code, float scale, float omega, int pairs, const float* scale_dev = nullptr);
 void launch_rms_remaining(cudaStream_t s, int nx, int ny, const float* p, const float* div, const uint8_t* code,
                           float scale, StepAccum* acc);
 void launch_build_codes(cudaStream_t s, int nx, int ny, const uint8_t* label, uint8_t* code);

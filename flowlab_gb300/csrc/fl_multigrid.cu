@@ -101,6 +101,7 @@ struct SmoothArgs {
   const float* b;
   const uint8_t* code;
   float scale, omega;
+  const float* scale_dev;  // PLAIN: when set, the scale is read here (the step's scalars)
   float* bc;  // PRE: coarse rhs target
   int cnx, cny;
   const float* ec;  // POST: coarse correction
@@ -182,7 +183,7 @@ __global__ void __launch_bounds__(RGN_T* RGN_T, 1) k_smooth(SmoothArgs a) {
   }
   __syncthreads();
 
-  const float scale = a.scale, omega = a.omega, keep = 1.0f - omega;
+  const float scale = a.scale_dev ? *a.scale_dev : a.scale, omega = a.omega, keep = 1.0f - omega;
 #pragma unroll 1
   for (int hs = 0; hs < 2 * P; hs++) {
     // local parity of this half-sweep's colour ((gi + gj) & 1 == hs & 1)
@@ -481,27 +482,32 @@ __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
   }
 }
 
-// Float64 defect correction (oracle: solveMixed). p_out = p_in + e (e may be
-// null: no update), then r = b - A p_out in double with the neighbour sum in
-// the order +x, -x, +y, -y; r is stored as float (the next V-cycle's rhs) and
-// its square summed over fluid cells with links. Each thread also forms its
-// four neighbours' updated values (the same additions their own threads
-// make), so the kernel needs no halo exchange; p_out must not alias p_in.
-__global__ void __launch_bounds__(256) k_update_resid64(int nx, int ny, const double* __restrict__ p_in,
+// Float64 defect correction (oracle: solveMixed). With update, p_out =
+// p_in + e; then r = b - A p in double with the neighbour sum in the order
+// +x, -x, +y, -y; r is stored as float (the next V-cycle's rhs) and its
+// square summed over fluid cells with links. p_in/p_out are the two float64
+// buffers chosen by ctl->par (the check kernel flips it after an update).
+// Each thread forms its four neighbours' updated values itself (the same
+// additions their own threads make), so no halo exchange is needed.
+__global__ void __launch_bounds__(256) k_update_resid64(int nx, int ny, double* __restrict__ p64a,
+                                                        double* __restrict__ p64b, const SolveCtl* __restrict__ ctl,
                                                         const float* __restrict__ e, const float* __restrict__ b,
-                                                        const uint8_t* __restrict__ code, double* __restrict__ p_out,
+                                                        const uint8_t* __restrict__ code, int update,
                                                         float* __restrict__ r32, StepAccum* acc) {
   __shared__ double red[32];
   __shared__ unsigned long long redn[32];
+  const int par = ctl->par;
+  const double* p_in = par ? p64b : p64a;
+  double* p_out = par ? p64a : p64b;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double sq = 0.0;
   unsigned long long n = 0;
   for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
     if (i >= nx) break;
     const long k = i + (long)j * nx;
-    auto P = [&](long q) { return e ? p_in[q] + (double)e[q] : p_in[q]; };
+    auto P = [&](long q) { return update ? p_in[q] + (double)e[q] : p_in[q]; };
     const double pk = P(k);
-    if (p_out) p_out[k] = pk;
+    if (update) p_out[k] = pk;
     const uint8_t c = code[k];
     float r = 0.0f;
     if ((c & 3u) == FLUID) {
@@ -525,6 +531,71 @@ __global__ void __launch_bounds__(256) k_update_resid64(int nx, int ny, const do
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     atomicAdd(&acc->res_sq, bs);
     atomicAdd(&acc->n_res, bn);
+  }
+}
+
+__device__ __forceinline__ double acc_rms(double sq, unsigned long long n) { return n ? sqrt(sq / (double)n) : 0.0; }
+
+// Before the cycle loop (pressureMultigrid.ts:294-300, solveMixed): the rhs
+// RMS; a vanishing rhs means p = 0 and no cycle; the float64 path also tests
+// its initial residual, so a converged warm start costs no cycle.
+__global__ void k_solve_begin(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaGraphConditionalHandle h) {
+  const double b_rms = acc_rms(acc->b_sq, acc->n_fluid);
+  ctl->b_rms = b_rms;
+  ctl->cycles = 0;
+  ctl->zero_p = b_rms == 0.0;
+  ctl->nonfinite = !isfinite(b_rms);
+  int cont = 0;
+  if (ctl->zero_p) {
+    ctl->rel = 0.0;
+  } else if (ctl->nonfinite) {
+    ctl->rel = -1.0;
+  } else if (ctl->mode == SOLVE_MIXED) {
+    const double rel = acc_rms(acc->res_sq, acc->n_res) / b_rms;
+    ctl->rel = rel;
+    cont = ctl->max_cycles > 0 && !(rel <= ctl->tol);
+  } else {
+    ctl->rel = -1.0;
+    cont = ctl->max_cycles > 0;
+  }
+  acc->res_sq = 0.0;
+  acc->n_res = 0ull;
+  ctl->cont = cont;
+  if (use_cond) cudaGraphSetConditional(h, cont);
+}
+
+// After each cycle: count it, evaluate the relative residual the cycle's
+// last kernel accumulated, and decide on another (pressureMultigrid.ts:
+// 314-317 for float32, solveMixed for float64 defect correction).
+__global__ void k_solve_check(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaGraphConditionalHandle h) {
+  ctl->cycles += 1;
+  if (ctl->mode == SOLVE_MIXED) ctl->par = 1 - ctl->par;
+  const double rel = acc_rms(acc->res_sq, acc->n_res) / ctl->b_rms;
+  ctl->rel = rel;
+  int cont = ctl->cycles < ctl->max_cycles;
+  if (!isfinite(rel)) {
+    ctl->nonfinite = 1;
+    cont = 0;
+  } else if (ctl->mode == SOLVE_MIXED) {
+    cont = cont && !(rel <= ctl->tol);
+  } else if (ctl->tol > 0) {
+    cont = cont && !(rel <= ctl->tol);
+  }
+  acc->res_sq = 0.0;
+  acc->n_res = 0ull;
+  ctl->cont = cont;
+  if (use_cond) cudaGraphSetConditional(h, cont);
+}
+
+// After the loop: when the rhs vanished the answer is p = 0 (float32 field
+// or the current float64 buffer).
+__global__ void k_zero_if(const SolveCtl* __restrict__ ctl, float* __restrict__ p32, double* __restrict__ p64a,
+                          double* __restrict__ p64b, long n) {
+  if (!ctl->zero_p) return;
+  double* p64 = p64a ? (ctl->par ? p64b : p64a) : nullptr;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    if (p32) p32[k] = 0.0f;
+    if (p64) p64[k] = 0.0;
   }
 }
 
@@ -625,8 +696,9 @@ void launch_rb_halfsweep(cudaStream_t s, int nx, int ny, float* p, const float* 
 }
 
 void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* x_out, const float* b,
-                      const uint8_t* code, float scale, float omega, int pairs) {
+                      const uint8_t* code, float scale, float omega, int pairs, const float* scale_dev) {
   SmoothArgs a{};
+  a.scale_dev = scale_dev;
   a.nx = nx;
   a.ny = ny;
   a.xin = x_in;
@@ -638,11 +710,25 @@ void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* 
   launch_smooth(s, a, pairs, MODE_PLAIN);
 }
 
-void launch_update_resid64(cudaStream_t s, int nx, int ny, const double* p_in, const float* e, const float* b,
-                           const uint8_t* code, double* p_out, float* r32, StepAccum* acc) {
+void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, const SolveCtl* ctl,
+                           const float* e, const float* b, const uint8_t* code, bool update, float* r32,
+                           StepAccum* acc) {
   dim3 bl(32, 8), g((nx + 31) / 32, (ny + 7) / 8);
   g.y = std::min(g.y, std::max(1u, 1024u / g.x));
-  k_update_resid64<<<g, bl, 0, s>>>(nx, ny, p_in, e, b, code, p_out, r32, acc);
+  k_update_resid64<<<g, bl, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, code, update, r32, acc);
+}
+
+void launch_solve_begin(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h) {
+  k_solve_begin<<<1, 1, 0, s>>>(acc, ctl, use_cond, h);
+}
+
+void launch_solve_check(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h) {
+  k_solve_check<<<1, 1, 0, s>>>(acc, ctl, use_cond, h);
+}
+
+void launch_zero_if(cudaStream_t s, const SolveCtl* ctl, float* p32, double* p64a, double* p64b, long n) {
+  long blocks = std::min((n + 255) / 256, 152L * 4);
+  k_zero_if<<<(unsigned)std::max(1L, blocks), 256, 0, s>>>(ctl, p32, p64a, p64b, n);
 }
 
 void launch_rms_remaining(cudaStream_t s, int nx, int ny, const float* p, const float* div, const uint8_t* code,
@@ -750,7 +836,7 @@ void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc) {
     Level& L = e.levels[l];
     Level& C = e.levels[l + 1];
     // x (level 0 only: coarser levels start from zero), b, code, x out, coarse b
-    const int tok = prof_begin(e, FL_PH_MG_DOWN);
+    const int tok = prof_begin(e, l == 0 ? FL_PH_MG_PRE_FINE : FL_PH_MG_PRE);
     SmoothArgs a{};
     a.nx = L.nx;
     a.ny = L.ny;
@@ -794,7 +880,7 @@ void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc) {
     Level& L = e.levels[l];
     Level& C = e.levels[l + 1];
     // x in, b, code, coarse e, x out
-    const int tok = prof_begin(e, FL_PH_MG_UP);
+    const int tok = prof_begin(e, l == 0 ? FL_PH_MG_POST_FINE : FL_PH_MG_POST);
     SmoothArgs a{};
     a.nx = L.nx;
     a.ny = L.ny;

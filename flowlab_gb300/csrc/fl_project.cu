@@ -160,10 +160,14 @@ __device__ __forceinline__ float projected_v(const float* __restrict__ p, const 
 }
 
 __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const float* __restrict__ p,
-                                                          const double* __restrict__ p64, float* __restrict__ u,
+                                                          const double* __restrict__ p64a,
+                                                          const double* __restrict__ p64b,
+                                                          const SolveCtl* __restrict__ ctl, float* __restrict__ u,
                                                           float* __restrict__ v, const uint8_t* __restrict__ label,
                                                           const StepScalars* __restrict__ sc, int subtract,
                                                           int outflow) {
+  // the float64 pressure, when there is one, is the buffer ctl->par names
+  const double* p64 = p64a ? (ctl->par ? p64b : p64a) : nullptr;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const float gs = subtract ? sc->grad_scale : 0.0f;
@@ -386,9 +390,10 @@ void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, 
 
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
                              const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow,
-                             const double* p64) {
+                             const double* p64a, const double* p64b, const SolveCtl* ctl) {
   dim3 b(32, 8);
-  k_subtract_outflow<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, p, p64, u, v, label, sc, subtract, outflow);
+  k_subtract_outflow<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, p, p64a, p64b, ctl, u, v, label, sc, subtract,
+                                                            outflow);
 }
 
 void launch_scale_rhs(cudaStream_t s, long n, const float* div, float* b, float neg_scale, const uint8_t* label,
@@ -440,5 +445,14 @@ void launch_convert(cudaStream_t s, const void* src, int src_dtype, void* dst, i
   else if (src_dtype == FL_F32 && dst_dtype == FL_F64)
     k_convert_f32_f64<<<(unsigned)blocks, 256, 0, s>>>((const float*)src, (double*)dst, n);
 }
+
+// A fixed-duration single-thread kernel (about 40 us, bounded by its loop
+// count) queued ahead of each profiled phase, so that the phase's launches
+// are submitted before the device reaches its start event.
+__global__ void k_hold() {
+  for (int k = 0; k < 40; k++) __nanosleep(1000);
+}
+
+void launch_hold(cudaStream_t s) { k_hold<<<1, 1, 0, s>>>(); }
 
 }  // namespace fl

@@ -73,17 +73,19 @@ class Stats(ctypes.Structure):
     ]
 
 
-PHASES = ["advect_velocity", "body_forces", "divergence", "mg_down", "mg_coarse", "mg_up", "rb_sweeps", "project",
-          "advect_dye", "cfl"]
+ABI_VERSION = 2  # FL_ABI_VERSION
+
+PHASES = ["advect_velocity", "body_forces", "divergence", "mg_pre_fine", "mg_pre", "mg_coarse", "mg_post",
+          "mg_post_fine", "defect64", "rb_sweeps", "project", "advect_dye", "cfl", "control"]
 
 
 class Profile(ctypes.Structure):
     """fl_profile."""
 
     _fields_ = [
-        ("ms", ctypes.c_double * 10),
-        ("launches", ctypes.c_longlong * 10),
-        ("bytes", ctypes.c_double * 10),
+        ("ms", ctypes.c_double * len(PHASES)),
+        ("launches", ctypes.c_longlong * len(PHASES)),
+        ("bytes", ctypes.c_double * len(PHASES)),
     ]
 
 
@@ -147,7 +149,7 @@ def load():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.fl_abi_version() != 1:
+    if lib.fl_abi_version() != ABI_VERSION:
         raise RuntimeError("flowlab_gb300 ABI version mismatch")
     _lib = lib
     return lib

@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define FL_ABI_VERSION 1
+#define FL_ABI_VERSION 2
 
 typedef struct fl_engine fl_engine;
 
@@ -102,16 +102,22 @@ typedef struct fl_stats {
 } fl_stats;
 
 /* Per-phase device timing of fused steps, from CUDA events recorded on the
- * engine's stream around each phase while profiling is enabled. `bytes` is
- * the algorithmic DRAM traffic the engine attributes to the phase: each
- * array a kernel must read or write, counted once per launch. No
- * counterpart in the reference (its profiler is host-side phase timing,
- * src/core/profiler.ts:39-113). */
-#define FL_PHASES 10
-/* phase indices */
+ * engine's stream around each phase while profiling is enabled. Profiled
+ * steps run eagerly (not as a graph), and each phase is preceded by a short
+ * fixed-duration hold kernel so that the phase's launches are queued before
+ * the device reaches its first event: the events then bracket device work
+ * only, not host submission. `bytes` is the algorithmic DRAM traffic the
+ * engine attributes to the phase: each array a kernel must read or write,
+ * counted once per launch. No counterpart in the reference (its profiler is
+ * host-side phase timing, src/core/profiler.ts:39-113). */
+#define FL_PHASES 14
+/* phase indices: the multigrid phases separate the finest level's smoother
+ * launches from the coarser levels'; CONTROL is the one-thread solve-control
+ * kernels (tolerance test, cycle decision) and the p = 0 fill. */
 enum fl_phase {
-  FL_PH_ADVECT_VELOCITY = 0, FL_PH_BODY_FORCES = 1, FL_PH_DIVERGENCE = 2, FL_PH_MG_DOWN = 3, FL_PH_MG_COARSE = 4,
-  FL_PH_MG_UP = 5, FL_PH_RB_SWEEPS = 6, FL_PH_PROJECT = 7, FL_PH_ADVECT_DYE = 8, FL_PH_CFL = 9
+  FL_PH_ADVECT_VELOCITY = 0, FL_PH_BODY_FORCES = 1, FL_PH_DIVERGENCE = 2, FL_PH_MG_PRE_FINE = 3, FL_PH_MG_PRE = 4,
+  FL_PH_MG_COARSE = 5, FL_PH_MG_POST = 6, FL_PH_MG_POST_FINE = 7, FL_PH_DEFECT64 = 8, FL_PH_RB_SWEEPS = 9,
+  FL_PH_PROJECT = 10, FL_PH_ADVECT_DYE = 11, FL_PH_CFL = 12, FL_PH_CONTROL = 13
 };
 typedef struct fl_profile {
   double ms[FL_PHASES];

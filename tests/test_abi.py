@@ -36,7 +36,7 @@ def test_bindings_cover_the_header():
 
 
 def test_abi_version_and_defaults(lib):
-    assert lib.fl_abi_version() == 1
+    assert lib.fl_abi_version() == native.ABI_VERSION == 2
     p = native.default_params()
     # simulation.ts:223-234 and pressureMultigrid.ts:47-67
     assert p.cfl_target == 2.0 and abs(p.dt_max - 1 / 30) < 1e-15 and p.tol == 5e-3
@@ -56,3 +56,13 @@ def test_create_fails_loudly_without_a_device(lib):
 
 def test_null_engine_is_rejected(lib):
     assert lib.fl_synchronize(None) == native.FL_EINVAL
+
+
+def test_profile_phases_match_the_header():
+    src = open(HEADER).read()
+    n = int(re.search(r"#define FL_PHASES (\d+)", src).group(1))
+    enum = re.search(r"enum fl_phase \{(.*?)\};", src, flags=re.S).group(1)
+    names = re.findall(r"FL_PH_([A-Z0-9_]+) = (\d+)", enum)
+    assert [int(k) for _, k in names] == list(range(n))
+    assert [nm.lower() for nm, _ in names] == native.PHASES
+    assert ctypes.sizeof(native.Profile) == n * 24

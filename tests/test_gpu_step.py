@@ -146,3 +146,98 @@ def test_plume_reaches_relative_residual_target():
     u, v, p, d, st = run_engine(g, f, patch, prm, 5)
     assert 0 <= st["rel_residual"] <= 1e-6, st
     assert np.isfinite(u).all() and np.isfinite(d).all()
+
+
+def run_steps(g, f, patch, prm, steps, eager):
+    """fl_step_auto one step at a time; with `eager` the phases are profiled,
+    which keeps the step off the CUDA-graph path."""
+    eng = native.Engine(g.nx, g.ny, g.h, params=prm)
+    try:
+        if patch is not None:
+            eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+        eng.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
+                 ptr(f32(f.dye)))
+        if eager:
+            eng.profile(True)
+        cyc = []
+        for _ in range(steps):
+            eng.call("fl_step_auto", 1, None)
+            st = eng.stats()
+            cyc.append((st["cycles"], st["rel_residual"], st["div_rms"]))
+        prof = eng.profile() if eager else None
+        u = np.empty(eng.ufaces, np.float32)
+        v = np.empty(eng.vfaces, np.float32)
+        p = np.empty(eng.cells, np.float32)
+        d = np.empty(eng.dye_len, np.float32)
+        eng.call("fl_read_velocity", native.FL_F32, ptr(u), ptr(v))
+        eng.call("fl_read_pressure", native.FL_F32, ptr(p))
+        eng.call("fl_read_dye", native.FL_F32, ptr(d))
+    finally:
+        eng.close()
+    return (u, v, p, d), cyc, prof
+
+
+@pytest.mark.parametrize("case", ["plume_mixed", "plume_float32", "karman_rb"])
+def test_graph_steps_equal_eager_steps(case):
+    """The whole-step CUDA graph (device-side V-cycle loop) performs exactly
+    the eager path's kernels: identical fields and identical cycle counts and
+    residuals, step by step."""
+    if case == "karman_rb":
+        g, f, patch = configs.karman(96, 64)
+        prm = configs.karman_params()
+    else:
+        g, f, patch = configs.plume(96)
+        prm = configs.plume_params(tol=1e-6 if case == "plume_mixed" else 1e-4, max_cycles=20,
+                                   mixed=int(case == "plume_mixed"))
+    a, ca, _ = run_steps(g, f, patch, prm, 6, eager=False)
+    b, cb, prof = run_steps(g, f, patch, prm, 6, eager=True)
+    for name, x, y in zip(("u", "v", "p", "dye"), a, b):
+        assert mismatch(x, y) == 0, "%s: %d values differ between graph and eager steps" % (name, mismatch(x, y))
+    # cycle counts identical; the residual norms are sums accumulated with
+    # atomics in block order, so they agree to rounding, not bit for bit
+    assert [c[0] for c in ca] == [c[0] for c in cb]
+    for x, y in zip(ca, cb):
+        assert np.allclose(x[1:], y[1:], rtol=1e-12, atol=0)
+    assert sum(prof[n][1] for n in prof) > 0
+
+
+def test_graph_rebuilt_after_parameter_change(o32):
+    """Buoyancy, confinement and dye-patch changes rebuild the step graph: a
+    run that changes them mid-way equals the oracle doing the same."""
+    g, f, patch = configs.plume(64)
+    prm = configs.plume_params(tol=1e-4, max_cycles=12, mixed=0)
+    eng = native.Engine(g.nx, g.ny, g.h, params=prm)
+    sim = o32.simulation(g.nx, g.ny, 1, **oracle_params(prm))
+    try:
+        eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+        eng.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
+                 ptr(f32(f.dye)))
+        sim.set_fields(f.u, f.v, f.p, f.label, f.dye)
+        sim.set_patch(patch.i0, patch.j0, patch.nx, patch.ny, patch.data)
+        eng.call("fl_step_auto", 3, None)
+        for _ in range(3):
+            sim.step()
+        eng.call("fl_set_buoyancy", 2.0, 0.0)
+        eng.call("fl_set_confinement", 0.0)
+        prm2 = configs.plume_params(tol=1e-4, max_cycles=12, mixed=0)
+        prm2.beta, prm2.alpha, prm2.confinement = 2.0, 0.0, 0.0
+        sim2_params = oracle_params(prm2)
+        u = np.empty(eng.ufaces, np.float32)
+        v = np.empty(eng.vfaces, np.float32)
+        p = np.empty(eng.cells, np.float32)
+        d = np.empty(eng.dye_len, np.float32)
+        eng.call("fl_step_auto", 3, None)
+        eng.call("fl_read_velocity", native.FL_F32, ptr(u), ptr(v))
+        eng.call("fl_read_pressure", native.FL_F32, ptr(p))
+        eng.call("fl_read_dye", native.FL_F32, ptr(d))
+    finally:
+        eng.close()
+    su, sv, sp, sd = sim.get_fields()
+    sim2 = o32.simulation(g.nx, g.ny, 1, **sim2_params)
+    sim2.set_fields(su, sv, sp, f.label, sd)
+    sim2.set_patch(patch.i0, patch.j0, patch.nx, patch.ny, patch.data)
+    for _ in range(3):
+        sim2.step()
+    eu, ev, ep, ed = sim2.get_fields()
+    for name, x, y in (("u", eu, u), ("v", ev, v), ("p", ep, p), ("dye", ed, d)):
+        assert mismatch(x, y) == 0, "%s: %d values differ from the float32 oracle" % (name, mismatch(x, y))
