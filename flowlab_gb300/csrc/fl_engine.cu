@@ -193,7 +193,8 @@ int validate_params(Engine* e, const fl_params* p) {
     return fail(e, FL_EINVAL, "mg_pre/mg_post must be in [0, 4] (got %d, %d)", p->mg_pre, p->mg_post);
   if (p->mg_coarse_sweeps < 0 || p->mg_max_cycles < 0 || p->pressure_iters < 0)
     return fail(e, FL_EINVAL, "negative sweep or cycle count");
-  if (p->mg_coarsest < 1) return fail(e, FL_EINVAL, "mg_coarsest must be >= 1");
+  // the coarsest level is solved inside the single-CTA tail (sides <= 64)
+  if (p->mg_coarsest < 1 || p->mg_coarsest > 64) return fail(e, FL_EINVAL, "mg_coarsest must be in [1, 64]");
   if (!(p->cfl_target > 0) || !(p->dt_max > 0) || !(p->rho > 0))
     return fail(e, FL_EINVAL, "cfl_target, dt_max and rho must be positive");
   return FL_OK;

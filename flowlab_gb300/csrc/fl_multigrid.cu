@@ -184,35 +184,62 @@ __global__ void __launch_bounds__(RGN_T* RGN_T, 1) k_smooth(SmoothArgs a) {
   __syncthreads();
 
   const float scale = a.scale_dev ? *a.scale_dev : a.scale, omega = a.omega, keep = 1.0f - omega;
-#pragma unroll 1
-  for (int hs = 0; hs < 2 * P; hs++) {
-    // local parity of this half-sweep's colour ((gi + gj) & 1 == hs & 1)
-    const int qa = ((hs & 1) + GX + GY) & 1;
-    const float(*xo)[RGN / 2] = xs[1 - qa];
+  {
+    // Colour view of the thread's cells: in row r the colour-c cell is
+    // column 2tx + oc[c] (the same for both rows), kept in registers with
+    // what its updates need precomputed once: whether it is updated at all
+    // (fluid, linked, off the region's outer ring), scale*b, the exact
+    // reciprocal of its link count (0 marks a count of 3: true division).
+    const int g = (GX + GY) & 1;
+    int oc[2];
+    oc[0] = (g + ty) & 1;
+    oc[1] = 1 - oc[0];
+    uint8_t cc[2][2];
+    bool act[2][2];
+    float sb[2][2], rc[2][2], xc[2][2];
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int c = 0; c < 2; c++) {
+        const int o = oc[c];
+        const int lj = ty + RGN_T * r, li = 2 * tx + o;
+        const uint8_t code = o ? cd[r][1] : cd[r][0];
+        const int cnt = code_count(code);
+        cc[r][c] = code;
+        act[r][c] = li != 0 && li != RGN - 1 && lj != 0 && lj != RGN - 1 && (code & 3u) == FLUID && cnt > 0;
+        sb[r][c] = scale * (o ? bb[r][1] : bb[r][0]);
+        rc[r][c] = cnt == 4 ? 0.25f : (cnt == 2 ? 0.5f : (cnt == 1 ? 1.0f : 0.0f));
+        xc[r][c] = o ? xx[r][1] : xx[r][0];
+      }
+#pragma unroll
+    for (int hs = 0; hs < 2 * P; hs++) {
+      const int c = hs & 1;
+      const int q = c ^ g;  // local parity plane of colour c
+      const float(*xo)[RGN / 2] = xs[1 - q];
+#pragma unroll
+      for (int r = 0; r < 2; r++) {
+        if (!act[r][c]) continue;
+        const int lj = ty + RGN_T * r;
+        const int o = oc[c];
+        const uint8_t code = cc[r][c];
+        float sum = 0.0f;
+        if (code & LINK_XP) sum += xo[lj][tx + o];
+        if (code & LINK_XM) sum += xo[lj][tx + o - 1];
+        if (code & LINK_YP) sum += xo[lj + 1][tx];
+        if (code & LINK_YM) sum += xo[lj - 1][tx];
+        const float d = sum - sb[r][c];
+        const float pgs = rc[r][c] != 0.0f ? d * rc[r][c] : d / 3.0f;
+        const float nv = keep * xc[r][c] + omega * pgs;
+        xc[r][c] = nv;
+        xs[q][lj][tx] = nv;
+      }
+      __syncthreads();
+    }
 #pragma unroll
     for (int r = 0; r < 2; r++) {
-      const int lj = ty + RGN_T * r;
-      const int o = (qa + lj) & 1;
-      const int li = 2 * tx + o;
-      // select, not index: a runtime index would put the arrays in local memory
-      const uint8_t c = o ? cd[r][1] : cd[r][0];
-      if (li == 0 || li == RGN - 1 || lj == 0 || lj == RGN - 1 || (c & 3u) != FLUID) continue;
-      const int cnt = code_count(c);
-      if (cnt == 0) continue;
-      float sum = 0.0f;
-      if (c & LINK_XP) sum += xo[lj][tx + o];
-      if (c & LINK_XM) sum += xo[lj][tx + o - 1];
-      if (c & LINK_YP) sum += xo[lj + 1][tx];
-      if (c & LINK_YM) sum += xo[lj - 1][tx];
-      const float pgs = over_count(sum - scale * (o ? bb[r][1] : bb[r][0]), cnt);
-      const float nv = keep * (o ? xx[r][1] : xx[r][0]) + omega * pgs;
-      if (o)
-        xx[r][1] = nv;
-      else
-        xx[r][0] = nv;
-      xs[qa][lj][tx] = nv;
+      xx[r][0] = oc[0] == 0 ? xc[r][0] : xc[r][1];
+      xx[r][1] = oc[0] == 0 ? xc[r][1] : xc[r][0];
     }
-    __syncthreads();
   }
 
   if (MODE == MODE_PRE || (MODE == MODE_POST && a.acc != nullptr)) {
@@ -296,14 +323,22 @@ __global__ void __launch_bounds__(RGN_T* RGN_T, 1) k_smooth(SmoothArgs a) {
 // ----------------------------------------------------- single-CTA coarse tail
 
 // Levels whose sides are both <= 64 run in ONE 1024-thread CTA, entirely in
-// shared memory. Thread (tx, ty) owns cells (2tx + o, ty + 32r) of every
-// level (o, r in {0, 1}), so no index needs a division. Per level: x split by
-// parity, xs[(i+j)&1][j][i>>1] (unit-stride warp access), b and the stencil
-// codes row-major.
+// shared memory: per level x split by parity, xs[(i+j)&1][j][i>>1] (row
+// stride 32), b and the stencil codes row-major. The CTA is bound by how
+// many instructions its warps issue, so each level is owned by as few warps
+// as hold its cells: a row of colour-c cells gets LPR = 2^lsh lanes (the
+// power of two >= ceil(nx/2)), a warp covers 32/LPR rows, and only the first
+// `nwarps` warps (at most 32; a 64-row level gives each of them two row
+// groups) take part in that level's phases, synchronising on the level's own
+// named barrier. Coarser levels are owned by a subset of the finer level's
+// warps, so the barrier that ends a phase on a level also orders it before
+// every coarser-level phase.
 struct CoarseLevel {
   int nx, ny;
   const uint8_t* code;
   int off_x, off_b, off_c;  // shared-memory offsets: floats, floats, bytes
+  int lsh;                  // log2 of the lanes per row
+  int nwarps;               // owner warps
 };
 
 struct CoarseArgs {
@@ -338,6 +373,17 @@ __device__ __forceinline__ CoarseView coarse_view(unsigned char* smem, const Coa
   return v;
 }
 
+// The cell of colour c in row group w + 32 s owned by `lane`.
+__device__ __forceinline__ void tail_cell(const CoarseLevel& L, int w, int lane, int s, int c, int& i, int& j) {
+  j = ((w + 32 * s) << (5 - L.lsh)) + (lane >> L.lsh);
+  i = 2 * (lane & ((1 << L.lsh) - 1)) + ((c + j) & 1);
+}
+
+// Named barrier `l + 1` over the owner warps of tail level l.
+__device__ __forceinline__ void tail_bar(int l, int nwarps) {
+  asm volatile("bar.sync %0, %1;" ::"r"(l + 1), "r"(nwarps * 32) : "memory");
+}
+
 // r = b - (count*x - sum), 0 off-fluid (pressureMultigrid.ts:117-151)
 __device__ __forceinline__ float coarse_residual(const CoarseView& v, int i, int j, bool& counted) {
   counted = false;
@@ -355,67 +401,105 @@ __device__ __forceinline__ float coarse_residual(const CoarseView& v, int i, int
   return v.bs[k] - ((float)cnt * v.x(i, j) - sum);
 }
 
-__device__ void coarse_smooth(const CoarseView& v, int pairs, float omega) {
-  const int tx = threadIdx.x, ty = threadIdx.y;
+// `pairs` red-black sweep pairs on tail level l by its owner warps; ends
+// with the level's barrier (also when pairs is 0). Each thread keeps its
+// cells' code, rhs, value and neighbour offsets in registers.
+__device__ void tail_smooth(unsigned char* smem, const CoarseLevel& L, int l, int pairs, float omega, int w,
+                            int lane) {
+  if (w >= L.nwarps) return;
+  float* xs = reinterpret_cast<float*>(smem) + L.off_x;
+  const float* bs = reinterpret_cast<const float*>(smem) + L.off_b;
+  const uint8_t* cs = smem + L.off_c;
+  const int plane = L.ny * 32;
+  uint8_t cq[2][2];
+  int own[2][2], oth[2][2], dd[2][2];
+  float bq[2][2], xq[2][2];
+#pragma unroll
+  for (int s = 0; s < 2; s++)
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      int i, j;
+      tail_cell(L, w, lane, s, c, i, j);
+      const bool ok = i < L.nx && j < L.ny;
+      cq[s][c] = ok ? cs[i + j * L.nx] : (uint8_t)CODE_OUTSIDE;
+      own[s][c] = c * plane + j * 32 + (i >> 1);
+      oth[s][c] = (1 - c) * plane + j * 32 + (i >> 1);
+      dd[s][c] = i & 1;
+      bq[s][c] = ok ? bs[i + j * L.nx] : 0.0f;
+      xq[s][c] = ok ? xs[own[s][c]] : 0.0f;
+    }
   const float keep = 1.0f - omega;
+#pragma unroll 1
   for (int hs = 0; hs < 2 * pairs; hs++) {
     const int color = hs & 1;
 #pragma unroll
-    for (int r = 0; r < 2; r++) {
-      const int j = ty + 32 * r;
-      const int i = 2 * tx + ((color + j) & 1);
-      if (j >= v.ny || i >= v.nx) continue;
-      const int k = i + j * v.nx;
-      const uint8_t c = v.cs[k];
-      if ((c & 3u) != FLUID) continue;
-      const int cnt = code_count(c);
-      if (cnt == 0) continue;
-      float sum = 0.0f;
-      if (c & LINK_XP) sum += v.x(i + 1, j);
-      if (c & LINK_XM) sum += v.x(i - 1, j);
-      if (c & LINK_YP) sum += v.x(i, j + 1);
-      if (c & LINK_YM) sum += v.x(i, j - 1);
-      const float pgs = over_count(sum - (-1.0f) * v.bs[k], cnt);
-      float& xr = v.x(i, j);
-      xr = keep * xr + omega * pgs;
-    }
-    __syncthreads();
+    for (int s = 0; s < 2; s++)
+#pragma unroll
+      for (int c = 0; c < 2; c++) {
+        if (c != color) continue;
+        const uint8_t code = cq[s][c];
+        if ((code & 3u) != FLUID) continue;
+        const int cnt = code_count(code);
+        if (cnt == 0) continue;
+        const int o = oth[s][c], d = dd[s][c];
+        float sum = 0.0f;
+        if (code & LINK_XP) sum += xs[o + d];
+        if (code & LINK_XM) sum += xs[o + d - 1];
+        if (code & LINK_YP) sum += xs[o + 32];
+        if (code & LINK_YM) sum += xs[o - 32];
+        const float pgs = over_count(sum - (-1.0f) * bq[s][c], cnt);
+        const float nv = keep * xq[s][c] + omega * pgs;
+        xq[s][c] = nv;
+        xs[own[s][c]] = nv;
+      }
+    tail_bar(l, L.nwarps);
   }
+  if (pairs <= 0) tail_bar(l, L.nwarps);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + 32 * ty;
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  const int lane = tid & 31, w = tid >> 5;
   for (int l = 0; l < a.nlev; l++) {
     const CoarseLevel& L = a.lv[l];
     const int n = L.nx * L.ny;
     uint8_t* c = smem + L.off_c;
     for (int k = tid; k < n; k += 1024) c[k] = L.code[k];
   }
-  const CoarseView T = coarse_view(smem, a.lv[0]);
+  const CoarseLevel& TL = a.lv[0];
+  const CoarseView T = coarse_view(smem, TL);
+  if (w < TL.nwarps) {
 #pragma unroll
-  for (int r = 0; r < 2; r++)
+    for (int s = 0; s < 2; s++)
 #pragma unroll
-    for (int o = 0; o < 2; o++) {
-      const int i = 2 * tx + o, j = ty + 32 * r;
-      if (i < T.nx && j < T.ny) {
-        const int k = i + j * T.nx;
-        T.bs[k] = a.b_top[k];
-        T.x(i, j) = a.x_is_zero ? 0.0f : a.x_top[k];
+      for (int c = 0; c < 2; c++) {
+        int i, j;
+        tail_cell(TL, w, lane, s, c, i, j);
+        if (i < T.nx && j < T.ny) {
+          const int k = i + j * T.nx;
+          T.bs[k] = a.b_top[k];
+          T.x(i, j) = a.x_is_zero ? 0.0f : a.x_top[k];
+        }
       }
-    }
+  }
   __syncthreads();
 
-  // down: pre-smooth, then residual + restriction with the coarse x set to 0
+  // down: pre-smooth, then residual + restriction (by the coarse level's
+  // owners) with the coarse x set to 0
   for (int l = 0; l < a.nlev - 1; l++) {
-    const CoarseView F = coarse_view(smem, a.lv[l]);
-    const CoarseView C = coarse_view(smem, a.lv[l + 1]);
-    coarse_smooth(F, a.pre, a.omega);
+    const CoarseLevel& FL = a.lv[l];
+    const CoarseLevel& CL = a.lv[l + 1];
+    tail_smooth(smem, FL, l, a.pre, a.omega, w, lane);
+    if (w >= CL.nwarps) continue;
+    const CoarseView F = coarse_view(smem, FL);
+    const CoarseView C = coarse_view(smem, CL);
 #pragma unroll
-    for (int r = 0; r < 2; r++)
+    for (int s = 0; s < 2; s++)
 #pragma unroll
-      for (int o = 0; o < 2; o++) {
-        const int I = 2 * tx + o, J = ty + 32 * r;
+      for (int c = 0; c < 2; c++) {
+        int I, J;
+        tail_cell(CL, w, lane, s, c, I, J);
         if (I >= C.nx || J >= C.ny) continue;
         float sum = 0.0f;
         for (int dj = 0; dj < 2; dj++)
@@ -429,18 +513,22 @@ __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
         C.bs[I + J * C.nx] = sum;
         C.x(I, J) = 0.0f;
       }
-    __syncthreads();
+    tail_bar(l + 1, CL.nwarps);
   }
-  coarse_smooth(coarse_view(smem, a.lv[a.nlev - 1]), a.coarse_sweeps, a.omega);
+  tail_smooth(smem, a.lv[a.nlev - 1], a.nlev - 1, a.coarse_sweeps, a.omega, w, lane);
   // up: prolongation (9/16, 3/16, 3/16, 1/16), then post-smooth
   for (int l = a.nlev - 2; l >= 0; l--) {
-    const CoarseView F = coarse_view(smem, a.lv[l]);
+    const CoarseLevel& FL = a.lv[l];
+    if (w >= FL.nwarps) continue;
+    tail_bar(l, FL.nwarps);  // the coarse level's owners are done with it
+    const CoarseView F = coarse_view(smem, FL);
     const CoarseView C = coarse_view(smem, a.lv[l + 1]);
 #pragma unroll
-    for (int r = 0; r < 2; r++)
+    for (int s = 0; s < 2; s++)
 #pragma unroll
-      for (int o = 0; o < 2; o++) {
-        const int i = 2 * tx + o, j = ty + 32 * r;
+      for (int c = 0; c < 2; c++) {
+        int i, j;
+        tail_cell(FL, w, lane, s, c, i, j);
         if (i >= F.nx || j >= F.ny) continue;
         if ((F.cs[i + j * F.nx] & 3u) != FLUID) continue;
         const int I = i >> 1, J = j >> 1;
@@ -448,28 +536,31 @@ __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
         const int J2 = (j & 1) ? min(J + 1, C.ny - 1) : max(J - 1, 0);
         F.x(i, j) += 0.5625f * C.x(I, J) + 0.1875f * (C.x(I2, J) + C.x(I, J2)) + 0.0625f * C.x(I2, J2);
       }
-    __syncthreads();
-    coarse_smooth(F, a.post, a.omega);
+    tail_bar(l, FL.nwarps);
+    tail_smooth(smem, FL, l, a.post, a.omega, w, lane);
   }
 
   double rsq = 0.0;
   unsigned long long rn = 0;
+  if (w < TL.nwarps) {
 #pragma unroll
-  for (int r = 0; r < 2; r++)
+    for (int s = 0; s < 2; s++)
 #pragma unroll
-    for (int o = 0; o < 2; o++) {
-      const int i = 2 * tx + o, j = ty + 32 * r;
-      if (i >= T.nx || j >= T.ny) continue;
-      if (a.acc != nullptr) {
-        bool counted;
-        const float res = coarse_residual(T, i, j, counted);
-        if (counted) {
-          rsq += (double)res * (double)res;
-          rn += 1;
+      for (int c = 0; c < 2; c++) {
+        int i, j;
+        tail_cell(TL, w, lane, s, c, i, j);
+        if (i >= T.nx || j >= T.ny) continue;
+        if (a.acc != nullptr) {
+          bool counted;
+          const float res = coarse_residual(T, i, j, counted);
+          if (counted) {
+            rsq += (double)res * (double)res;
+            rn += 1;
+          }
         }
+        a.x_top[i + j * T.nx] = T.x(i, j);
       }
-      a.x_top[i + j * T.nx] = T.x(i, j);
-    }
+  }
   if (a.acc != nullptr) {
     __shared__ double red[32];
     __shared__ unsigned long long redn[32];
@@ -482,45 +573,132 @@ __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
   }
 }
 
-// Float64 defect correction (oracle: solveMixed). With update, p_out =
-// p_in + e; then r = b - A p in double with the neighbour sum in the order
-// +x, -x, +y, -y; r is stored as float (the next V-cycle's rhs) and its
-// square summed over fluid cells with links. p_in/p_out are the two float64
-// buffers chosen by ctl->par (the check kernel flips it after an update).
-// Each thread forms its four neighbours' updated values itself (the same
-// additions their own threads make), so no halo exchange is needed.
-__global__ void __launch_bounds__(256) k_update_resid64(int nx, int ny, double* __restrict__ p64a,
-                                                        double* __restrict__ p64b, const SolveCtl* __restrict__ ctl,
-                                                        const float* __restrict__ e, const float* __restrict__ b,
-                                                        const uint8_t* __restrict__ code, int update,
-                                                        float* __restrict__ r32, StepAccum* acc) {
+// Exact float -> double by bit manipulation (integer pipe) for zero and
+// normal floats; subnormals, infinities and NaN take the conversion
+// instruction. The result equals (double)f in every case.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ex = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  if (ex != 0u && ex != 0xffu) {
+    const unsigned long long bits =
+        sign | ((unsigned long long)(ex + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+  }
+  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)sign);
+  return (double)f;
+}
+
+// x * 2^k (k = 1, 2) by an exponent increment when x is normal and the
+// product stays normal; zero returns itself (as x * 2^k does); otherwise
+// the multiply. Equal to x * 2^k in every case.
+__device__ __forceinline__ double scale_pow2(double x, int k) {
+  const long long bits = __double_as_longlong(x);
+  const long long ex = (bits >> 52) & 0x7ff;
+  if (ex != 0 && ex < 0x7ff - k) return __longlong_as_double(bits + ((long long)k << 52));
+  if ((bits & 0x7fffffffffffffffll) == 0) return x;
+  return x * (double)(1 << k);
+}
+
+// 0.0 + x: x itself except that -0.0 becomes +0.0.
+__device__ __forceinline__ double zero_plus(double x) {
+  const long long bits = __double_as_longlong(x);
+  return bits == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+
+// The float64 defect-correction pass (iterative refinement, solveMixed):
+// p64' = p64 + e (when `update`), then r = b - (count*p64' - sum) in double
+// with the neighbour sum in the order +x, -x, +y, -y, r32 = float(r), and
+// the squared norm of r accumulated. GB300 issues few float64 operations per
+// clock, so this pass is bound by its float64 arithmetic, not by memory. It
+// spends float64 instructions only where the result needs them: each p64' is
+// formed once and handed to its neighbours in registers (the rows above and
+// below, a rolling column) and by warp shuffles (left and right); the exact
+// float -> double widenings, the first addition to 0.0 and the products by 2
+// and 4 are done on the integer pipe with identical results. A warp owns 30
+// interior columns (lanes 1..30; lanes 0 and 31 are the halo) and UR_ROWS
+// rows; the halo rows and columns are formed redundantly.
+constexpr int UR_ROWS = 16;
+constexpr int UR_WARPS = 8;
+
+template <bool UPDATE>
+__global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny, double* __restrict__ p64a,
+                                                                double* __restrict__ p64b,
+                                                                const SolveCtl* __restrict__ ctl,
+                                                                const float* __restrict__ e,
+                                                                const float* __restrict__ b,
+                                                                const uint8_t* __restrict__ code,
+                                                                float* __restrict__ r32, StepAccum* acc) {
   __shared__ double red[32];
   __shared__ unsigned long long redn[32];
   const int par = ctl->par;
   const double* p_in = par ? p64b : p64a;
   double* p_out = par ? p64a : p64b;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gx = blockIdx.x * 30 - 1 + lane;
+  const int y0 = (blockIdx.y * UR_WARPS + w) * UR_ROWS;
+  const bool col = gx >= 0 && gx < nx;
+  const bool own = col && lane != 0 && lane != 31;
+
+  double pn[UR_ROWS + 2];
+  float bv[UR_ROWS];
+  uint8_t cv[UR_ROWS];
+#pragma unroll
+  for (int t = 0; t < UR_ROWS + 2; t++) {
+    const int gy = y0 - 1 + t;
+    double v = 0.0;
+    if (col && gy >= 0 && gy < ny) {
+      const long k = gx + (long)gy * nx;
+      v = p_in[k];
+      if (UPDATE) v += f2d_exact(e[k]);
+    }
+    pn[t] = v;
+    if (t >= 1 && t <= UR_ROWS) {
+      const bool in = own && gy < ny;
+      const long k = gx + (long)gy * nx;
+      bv[t - 1] = in ? b[k] : 0.0f;
+      cv[t - 1] = in ? code[k] : (uint8_t)CODE_OUTSIDE;
+    }
+  }
+
   double sq = 0.0;
   unsigned long long n = 0;
-  for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
-    if (i >= nx) break;
-    const long k = i + (long)j * nx;
-    auto P = [&](long q) { return update ? p_in[q] + (double)e[q] : p_in[q]; };
-    const double pk = P(k);
-    if (update) p_out[k] = pk;
-    const uint8_t c = code[k];
+#pragma unroll
+  for (int t = 1; t <= UR_ROWS; t++) {
+    const double left = __shfl_up_sync(0xffffffffu, pn[t], 1);
+    const double right = __shfl_down_sync(0xffffffffu, pn[t], 1);
+    const int gy = y0 - 1 + t;
+    if (!own || gy >= ny) continue;
+    const long k = gx + (long)gy * nx;
+    if (UPDATE) p_out[k] = pn[t];
+    const uint8_t c = cv[t - 1];
     float r = 0.0f;
     if ((c & 3u) == FLUID) {
       const int cnt = code_count(c);
       if (cnt > 0) {
-        double sum = 0.0;
-        if (c & LINK_XP) sum += P(k + 1);
-        if (c & LINK_XM) sum += P(k - 1);
-        if (c & LINK_YP) sum += P(k + nx);
-        if (c & LINK_YM) sum += P(k - nx);
-        const double rd = (double)b[k] - ((double)cnt * pk - sum);
+        // the first linked term enters as 0.0 + term
+        double sum;
+        bool first = true;
+        if (c & LINK_XP) {
+          sum = zero_plus(right);
+          first = false;
+        }
+        if (c & LINK_XM) {
+          sum = first ? zero_plus(left) : sum + left;
+          first = false;
+        }
+        if (c & LINK_YP) {
+          sum = first ? zero_plus(pn[t + 1]) : sum + pn[t + 1];
+          first = false;
+        }
+        if (c & LINK_YM) sum = first ? zero_plus(pn[t - 1]) : sum + pn[t - 1];
+        const double cp = cnt == 4 ? scale_pow2(pn[t], 2)
+                          : cnt == 2 ? scale_pow2(pn[t], 1)
+                          : cnt == 1 ? pn[t]
+                                     : 3.0 * pn[t];
+        const double rd = f2d_exact(bv[t - 1]) - (cp - sum);
         r = (float)rd;
-        sq += rd * rd;
+        sq = fma(rd, rd, sq);
         n += 1;
       }
     }
@@ -528,7 +706,7 @@ __global__ void __launch_bounds__(256) k_update_resid64(int nx, int ny, double* 
   }
   const double bs = block_sum(sq, red);
   const unsigned long long bn = block_sum_u64(n, redn);
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
+  if (threadIdx.x == 0) {
     atomicAdd(&acc->res_sq, bs);
     atomicAdd(&acc->n_res, bn);
   }
@@ -713,9 +891,11 @@ void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* 
 void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, const SolveCtl* ctl,
                            const float* e, const float* b, const uint8_t* code, bool update, float* r32,
                            StepAccum* acc) {
-  dim3 bl(32, 8), g((nx + 31) / 32, (ny + 7) / 8);
-  g.y = std::min(g.y, std::max(1u, 1024u / g.x));
-  k_update_resid64<<<g, bl, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, code, update, r32, acc);
+  dim3 g((nx + 29) / 30, (ny + UR_WARPS * UR_ROWS - 1) / (UR_WARPS * UR_ROWS));
+  if (update)
+    k_update_resid64<true><<<g, 32 * UR_WARPS, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, code, r32, acc);
+  else
+    k_update_resid64<false><<<g, 32 * UR_WARPS, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, code, r32, acc);
 }
 
 void launch_solve_begin(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h) {
@@ -863,7 +1043,14 @@ void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc) {
     a.nlev = (int)e.levels.size() - lc;
     for (int l = 0; l < a.nlev; l++) {
       const Level& L = e.levels[lc + l];
-      a.lv[l] = CoarseLevel{L.nx, L.ny, L.code, ox[l], ob[l], oc[l]};
+      int lpr = 1, lsh = 0;
+      while (lpr < (L.nx + 1) / 2) {
+        lpr <<= 1;
+        lsh++;
+      }
+      const int rows_per_warp = 32 >> lsh;
+      const int groups = (L.ny + rows_per_warp - 1) / rows_per_warp;
+      a.lv[l] = CoarseLevel{L.nx, L.ny, L.code, ox[l], ob[l], oc[l], lsh, std::min(32, groups)};
     }
     a.b_top = lc == 0 ? b0 : e.levels[lc].b;
     a.x_top = e.levels[lc].x[0];

@@ -83,7 +83,7 @@ typedef struct fl_params {
   double confinement;    /* vorticity confinement epsilon; 0 = off */
   int mg_pre, mg_post;   /* smoothing sweep pairs per level (reference 2, 2) */
   int mg_coarse_sweeps;  /* sweep pairs on the coarsest level (reference 8) */
-  int mg_coarsest;       /* stop coarsening at <= this many cells a side (reference 4) */
+  int mg_coarsest;       /* stop coarsening at <= this many cells a side (reference 4; at most 64) */
   double mg_omega;       /* smoother relaxation (reference 1.0) */
   int mixed;             /* 1: float64 fine pressure + float64 residual (defect correction) */
   int reserved[7];
