@@ -25,6 +25,9 @@ advection with decay and inlet, CFL reduction.
           one core, on a bounded sample of the same workload.
 
 --impl reference runs only that CPU port (rank 0) on the same workload.
+--workload turbulence measures the turbulence grid instead: 2048^2, u = 1
+inflow through a 16x16 lattice of solid squares, multigrid to a relative
+residual of 1e-8 through the float64 defect correction.
 """
 import argparse
 import ctypes
@@ -67,13 +70,35 @@ def parse():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--size", type=int, default=1024)
-    ap.add_argument("--tol", type=float, default=1e-6)
-    ap.add_argument("--max-cycles", type=int, default=20)
+    ap.add_argument("--workload", choices=["plume", "turbulence"], default="plume",
+                    help="plume: thermal plume 1024^2 to 1e-6 (the headline); turbulence: turbulence grid 2048^2 "
+                         "to 1e-8 through the float64 defect correction")
+    ap.add_argument("--size", type=int, default=None)
+    ap.add_argument("--tol", type=float, default=None)
+    ap.add_argument("--max-cycles", type=int, default=None)
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU-baseline sample")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--profile-steps", type=int, default=8, help="eager steps with phase events, after the timed ones")
-    return ap.parse_args()
+    args = ap.parse_args()
+    plume = args.workload == "plume"
+    if args.size is None:
+        args.size = 1024 if plume else 2048
+    if args.tol is None:
+        args.tol = 1e-6 if plume else 1e-8
+    if args.max_cycles is None:
+        args.max_cycles = 20 if plume else 40
+    return args
+
+
+def workload(args):
+    """(grid, fields, dye patch, engine params) of the selected workload."""
+    from flowlab_gb300 import configs
+
+    if args.workload == "plume":
+        g, f, patch = configs.plume(args.size)
+        return g, f, patch, configs.plume_params(tol=args.tol, max_cycles=args.max_cycles)
+    g, f, patch = configs.turbulence(args.size)
+    return g, f, patch, configs.turbulence_params(tol=args.tol, max_cycles=args.max_cycles)
 
 
 class ClockSampler:
@@ -170,22 +195,21 @@ def max_over_ranks(pg, x):
 
 # ------------------------------------------------------------- CPU port
 
-def cpu_port_steps(size, tol, max_cycles, steps, warmup, state=None):
+def cpu_port_steps(args, steps, warmup, state=None):
     """Times `steps` steps of the float64 CPU port (the oracle's Simulation)
-    on the plume workload, after `warmup` untimed steps from `state` (host
+    on the selected workload, after `warmup` untimed steps from `state` (host
     fields) or from the reset scene. Returns (steps/s, seconds)."""
-    from flowlab_gb300 import configs
     from oracle import Oracle, params_from_engine as oracle_params
 
-    g, f, patch = configs.plume(size)
-    prm = configs.plume_params(tol=tol, max_cycles=max_cycles)
+    g, f, patch, prm = workload(args)
     sim = Oracle("f64").simulation(g.nx, g.ny, 1, **oracle_params(prm))
     if state is not None:
         u, v, p, dye = state
         sim.set_fields(u, v, p, f.label, dye)
     else:
         sim.set_fields(f.u, f.v, f.p, f.label, f.dye)
-    sim.set_patch(patch.i0, patch.j0, patch.nx, patch.ny, patch.data)
+    if patch is not None:
+        sim.set_patch(patch.i0, patch.j0, patch.nx, patch.ny, patch.data)
     for _ in range(warmup):
         sim.step()
     t = time.perf_counter()
@@ -199,9 +223,9 @@ def run_reference(args, world, rank, pg):
     metric = baseline_metric()
     if rank != 0:
         return
-    sps, secs = cpu_port_steps(args.size, args.tol, args.max_cycles, args.steps, args.warmup)
-    sample = "%d steps (after %d warm-up steps from the reset scene) of the %d^2 thermal plume, float64 CPU port of " \
-             "the reference's Simulation.step, one thread" % (args.steps, args.warmup, args.size)
+    sps, secs = cpu_port_steps(args, args.steps, args.warmup)
+    sample = "%d steps (after %d warm-up steps from the reset scene) of the %d^2 %s, float64 CPU port of " \
+             "the reference's Simulation.step, one thread" % (args.steps, args.warmup, args.size, workload_name(args))
     line = {"metric": metric, "value": sps, "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 / sps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -211,12 +235,23 @@ def run_reference(args, world, rank, pg):
     print(json.dumps(line), flush=True)
 
 
+def workload_name(args):
+    return "thermal plume" if args.workload == "plume" else "turbulence grid"
+
+
 def workload_config(args):
-    return {"workload": "thermal plume %dx%d, closed box, MacCormack, beta 1 / alpha 0.05 / confinement 0.3, "
-                        "multigrid V(3,3) coarsest 8x8, relative residual %.0e (cap %d cycles)"
-                        % (args.size, args.size, args.tol, args.max_cycles),
-            "grid": [args.size, args.size], "solver": "multigrid V(3,3), 32 coarse sweep pairs",
-            "tol": args.tol, "precision": "float32", "l2": "flushed (320 MB write) before every timed step",
+    n = args.size
+    if args.workload == "plume":
+        desc = ("thermal plume %dx%d, closed box, MacCormack, beta 1 / alpha 0.05 / confinement 0.3, "
+                "multigrid V(3,3) coarsest 8x8 in a float64 defect-correction loop, relative residual %.0e "
+                "(cap %d cycles)" % (n, n, args.tol, args.max_cycles))
+    else:
+        desc = ("turbulence grid %dx%d, u = 1 inflow through a 16x16 lattice of solid squares, MacCormack, CFL 0.5, "
+                "multigrid V(3,3) coarsest 8x8 in a float64 defect-correction loop, relative residual %.0e "
+                "(cap %d cycles)" % (n, n, args.tol, args.max_cycles))
+    return {"workload": desc, "grid": [n, n], "solver": "multigrid V(3,3), 32 coarse sweep pairs",
+            "tol": args.tol, "precision": "float32 fields and smoothing, float64 residual and correction",
+            "l2": "flushed (320 MB write) before every timed step",
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 
 
@@ -231,10 +266,10 @@ def run_ours(args, world, rank, local, pg):
 
     build.build()
     torch.cuda.set_device(local)
-    g, f, patch = configs.plume(args.size)
-    prm = configs.plume_params(tol=args.tol, max_cycles=args.max_cycles)
+    g, f, patch, prm = workload(args)
     eng = native.Engine(g.nx, g.ny, g.h, params=prm, device=local)
-    eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+    if patch is not None:
+        eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
     eng.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
              ptr(f32(f.dye)))
     iters = ctypes.c_int()
@@ -320,11 +355,11 @@ def run_ours(args, world, rank, local, pg):
 
     cpu = None
     if rank == 0 and args.cpu_steps > 0:
-        sps, secs = cpu_port_steps(args.size, args.tol, args.max_cycles, args.cpu_steps, 0, state)
+        sps, secs = cpu_port_steps(args, args.cpu_steps, 0, state)
         cpu = {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
-               "sample": "%d steps of the %d^2 thermal plume continuing from the GPU's warmed-up state, float64 CPU "
+               "sample": "%d steps of the %d^2 %s continuing from the GPU's warmed-up state, float64 CPU "
                          "port of the reference's Simulation.step, one thread (%.1f s)"
-                         % (args.cpu_steps, args.size, secs)}
+                         % (args.cpu_steps, args.size, workload_name(args), secs)}
     eng.close()
     if rank != 0:
         return
@@ -352,7 +387,7 @@ def run_ours(args, world, rank, local, pg):
     line = {
         "metric": baseline_metric(), "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded plume scene)",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded %s scene)" % workload_name(args),
         "config": workload_config(args),
         "cell_updates_per_s": value * args.size * args.size,
         "vcycles_per_step": statistics.mean(cycles), "max_vcycles": max(cycles),

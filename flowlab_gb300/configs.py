@@ -11,6 +11,12 @@
                MacCormack, multigrid V(3,3) to an 8x8 coarsest level inside a
                float64 defect-correction loop, solved to a relative residual
                of 1e-6 (float32 alone stalls near 3e-5 at 1024^2).
+  turbulence(...)  turbulence grid: inflow u = 1 at the left wall, Air outlet
+               column, a 16 x 16 lattice of solid squares of side 24 cells (at
+               2048^2; scaled with the grid) in the inlet's first ~40% of the
+               width, seeded 1e-3 noise and dye stripes; MacCormack, CFL 0.5,
+               multigrid V(3,3) to an 8x8 coarsest level inside the float64
+               defect-correction loop, solved to a relative residual of 1e-8.
 Scenes come from flowlab_gb300.scenes (float64 host arrays, the reference's
 helpers); parameters are fl_params for the engine.
 """
@@ -50,3 +56,33 @@ def karman(nx=128, ny=128, noise=1e-3):
 def karman_params(iters=60, omega=1.9):
     return native.default_params(cfl_target=0.5, dt_max=1 / 30, scheme=native.FL_MACCORMACK,
                                  solver=native.FL_SOLVER_RBSOR, pressure_iters=iters, omega=omega, tol=0.0)
+
+
+def turbulence_lattice(n, count=16, side_cells=24):
+    """Square centres and side (cells) of the turbulence-grid lattice on an
+    n x n grid: `count` rows spread evenly over the height, `count` columns
+    at a pitch of twice the side starting 5% of the width from the inlet;
+    the side is 24 cells at 2048^2 and scales with n (at least 2 cells)."""
+    side = max(2, int(round(side_cells * n / 2048)))
+    pitch_x, pitch_y = 2 * side, n / count
+    x0 = 0.05 * n
+    return [(x0 + (a + 0.5) * pitch_x, (b + 0.5) * pitch_y) for a in range(count) for b in range(count)], side
+
+
+def turbulence(n=2048, count=16, noise=1e-3):
+    g = sc.Grid(n, n, 1.0 / n)
+    centres, side = turbulence_lattice(n, count)
+    half = 0.5 * side * g.h
+    rects = [sc.solid_rect(cx * g.h - half, cy * g.h - half, cx * g.h + half, cy * g.h + half) for cx, cy in centres]
+    spec = sc.SceneSpec(
+        labels=sc.all_labels(sc.open_right(), *rects),
+        seed=sc.chain_seeds(sc.uniform_flow(1.0), sc.lcg_noise(noise)),
+        dye=lambda dg, dye: sc.add_dye_stripes(dg, dye))
+    f, patch = sc.reset_fields(g, g, spec)
+    return g, f, patch
+
+
+def turbulence_params(tol=1e-8, max_cycles=40, mixed=1, coarse_sweeps=32):
+    return native.default_params(
+        cfl_target=0.5, dt_max=1 / 30, scheme=native.FL_MACCORMACK, solver=native.FL_SOLVER_MG, tol=tol,
+        mg_max_cycles=max_cycles, mg_pre=3, mg_post=3, mg_coarse_sweeps=coarse_sweeps, mg_coarsest=8, mixed=mixed)
