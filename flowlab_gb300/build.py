@@ -18,8 +18,9 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libflowlab_gb300.so")
 
-SOURCES = ["fl_engine.cu", "fl_multigrid.cu", "fl_advect.cu", "fl_project.cu", "fl_noalloc.cu"]
-HEADERS = ["fl_common.cuh", "fl_internal.h"]
+SOURCES = ["fl_engine.cu", "fl_multigrid.cu", "fl_advect.cu", "fl_project.cu", "fl_noalloc.cu", "fl_unet.cu",
+           "fl_unet_tc.cu", "fl_unet_abi.cu"]
+HEADERS = ["fl_common.cuh", "fl_internal.h", "fl_unet.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",

@@ -14,8 +14,13 @@
 #include <new>
 
 #include "fl_internal.h"
+#include "fl_unet.h"
 
 using namespace fl;
+
+namespace fl {
+Unet* unet_of(fl_unet* h);
+}
 
 struct fl_engine {
   Engine e;
@@ -172,6 +177,7 @@ void free_all(Engine* e) {
   cudaFree(e->p64[1]);
   cudaFree(e->r32);
   cudaFree(e->ctl);
+  cudaFree(e->ws_scales);
   destroy_graphs(e);
   if (!e->levels.empty()) cudaFree(e->levels[0].label);
   mg_free(*e);
@@ -360,6 +366,15 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
   tok = prof_begin(*e, FL_PH_DIVERGENCE);
   launch_divergence(s, e->nx, e->ny, e->h, u, v, L0.b, e->prm.solver == FL_SOLVER_MG, L0.label, e->sc, e->acc);
   prof_end(*e, tok, 4 * F + N + 4 * N, 1);
+  if (e->warm != nullptr && e->prm.solver == FL_SOLVER_MG) {
+    // p_prev -> p_guess in place: the float64 pressure of the defect
+    // correction, or the float32 warm start of the plain multigrid
+    const bool mixed = e->prm.mixed != 0;
+    tok = prof_begin(*e, FL_PH_WARM_START);
+    unet_warm_start(*e->warm, s, e->nx, e->ny, L0.b, L0.label, e->acc, mixed ? nullptr : L0.x[0],
+                    mixed ? e->p64[0] : nullptr, mixed ? e->p64[1] : nullptr, &e->ctl->par, e->ws_scales);
+    prof_end(*e, tok, 0, 0);
+  }
 }
 
 // Solve prologue: the float64 path's initial residual, then the begin test.
@@ -738,6 +753,7 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   s = s ? s : dalloc(e, (void**)&e->p64[1], (size_t)e->cells() * 8, "p64");
   s = s ? s : dalloc(e, (void**)&e->r32, cf, "residual");
   s = s ? s : dalloc(e, (void**)&e->ctl, sizeof(SolveCtl), "solve control");
+  s = s ? s : dalloc(e, (void**)&e->ws_scales, 4 * sizeof(float), "warm-start scales");
   if (s) return bail(s);
   if (cudaMallocHost(&e->acc_host, sizeof(StepAccum)) != cudaSuccess ||
       cudaMallocHost(&e->ctl_host, sizeof(SolveCtl)) != cudaSuccess) {
@@ -1243,6 +1259,27 @@ int fl_dye_patch(fl_engine* h, float* dye, int i0, int j0, int pnx, int pny, con
   TRY(check_launch(e, "dye patch"));
   TRY(down32(e, dye, e->dye[0], 3 * e->dye_cells() * 4, "dye"));
   return sync(e, "dye patch");
+}
+
+// ------------------------------------------------------ learned warm start
+
+int fl_set_warm_start(fl_engine* h, fl_unet* net) {
+  ENTER(h);
+  Unet* u = unet_of(net);
+  if (u != nullptr) {
+    if (e->nx % 8 || e->ny % 8) return fail(e, FL_EINVAL, "warm start needs sides that are multiples of 8");
+    if ((long)e->nx * e->ny > u->cap) return fail(e, FL_EINVAL, "grid exceeds the network's capacity");
+    if (u->device != e->device) return fail(e, FL_EINVAL, "network and engine are on different devices");
+  }
+  e->warm = u;
+  destroy_graphs(e);
+  return FL_OK;
+}
+
+int fl_read_rhs(fl_engine* h, int dtype, void* b) {
+  ENTER(h);
+  TRY(download(e, b, e->levels[0].b, e->cells(), dtype, "read rhs"));
+  return sync(e, "read rhs");
 }
 
 }  // extern "C"

@@ -63,6 +63,10 @@ struct Engine {
   bool use_graphs = true;
   bool stats_on_device = false;  // the last solve's statistics live in ctl
 
+  // learned warm start (fl_set_warm_start), run between divergence and solve
+  struct Unet* warm = nullptr;
+  float* ws_scales = nullptr;  // device: s_b, s_p, 1/s_b, 1/s_p of the last step
+
   float* w = nullptr;   // vorticity scratch
   float* fx = nullptr;  // confinement force scratch
   float* fy = nullptr;

@@ -76,7 +76,7 @@ class Stats(ctypes.Structure):
 ABI_VERSION = 2  # FL_ABI_VERSION
 
 PHASES = ["advect_velocity", "body_forces", "divergence", "mg_pre_fine", "mg_pre", "mg_coarse", "mg_post",
-          "mg_post_fine", "defect64", "rb_sweeps", "project", "advect_dye", "cfl", "control"]
+          "mg_post_fine", "defect64", "rb_sweeps", "project", "advect_dye", "cfl", "control", "warm_start"]
 
 
 class Profile(ctypes.Structure):
@@ -131,6 +131,17 @@ SIGNATURES = [
     ("fl_stir", _I, [_P, _P, _P, _P, _F, _F, _F, _F, _F]),
     ("fl_dye_patch", _I, [_P, _P, _I, _I, _I, _I, _P]),
     ("fl_advect_velocity_noalloc", _I, [_I, _I, _I, _F, _F, _P, _P, _P, _P, _P, _P]),
+    ("fl_unet_create", _I, [ctypes.c_longlong, _I, ctypes.POINTER(_P)]),
+    ("fl_unet_destroy", _I, [_P]),
+    ("fl_unet_last_error", ctypes.c_char_p, [_P]),
+    ("fl_unet_num_params", ctypes.c_longlong, []),
+    ("fl_unet_set_params", _I, [_P, _P]),
+    ("fl_unet_get_params", _I, [_P, _P]),
+    ("fl_unet_forward", _I, [_P, _I, _I, _I, _P, _P]),
+    ("fl_unet_train_step", _I, [_P, _I, _I, _I, _P, _P, _P, _D, _I, _P, _P]),
+    ("fl_unet_use_tensor_cores", _I, [_I]),
+    ("fl_set_warm_start", _I, [_P, _P]),
+    ("fl_read_rhs", _I, [_P, _I, _P]),
 ]
 
 _lib = None
@@ -244,3 +255,57 @@ class Engine:
         s = Stats()
         self.call("fl_get_stats", ctypes.byref(s))
         return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+
+class Unet:
+    """The pressure warm-start network (fl_unet_*): a handle plus helpers
+    taking numpy arrays."""
+
+    def __init__(self, max_pixels, device=0):
+        lib = load()
+        h = ctypes.c_void_p()
+        st = lib.fl_unet_create(int(max_pixels), device, ctypes.byref(h))
+        if st != FL_OK:
+            raise FlowlabError(st, lib.fl_last_error(None).decode())
+        self.lib, self.h = lib, h
+        self.n = int(lib.fl_unet_num_params())
+
+    def close(self):
+        if self.h:
+            self.lib.fl_unet_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def call(self, name, *args):
+        st = getattr(self.lib, name)(self.h, *args)
+        if st != FL_OK:
+            raise FlowlabError(st, self.lib.fl_unet_last_error(self.h).decode())
+
+    def set_params(self, theta):
+        self.call("fl_unet_set_params", ptr(f32(theta)))
+
+    def get_params(self):
+        out = np.empty(self.n, np.float32)
+        self.call("fl_unet_get_params", ptr(out))
+        return out
+
+    def forward(self, x):
+        x = f32(x)
+        B, H, W, _ = x.shape
+        out = np.empty((B, H, W), np.float32)
+        self.call("fl_unet_forward", B, H, W, ptr(x), ptr(out))
+        return out
+
+    def train_step(self, x, target, mask, lr=1e-3, update=True, want_grad=False):
+        x, target, mask = f32(x), f32(target), f32(mask)
+        B, H, W, _ = x.shape
+        loss = ctypes.c_double()
+        grad = np.empty(self.n, np.float32) if want_grad else None
+        self.call("fl_unet_train_step", B, H, W, ptr(x), ptr(target), ptr(mask), float(lr), int(update),
+                  ctypes.byref(loss), ptr(grad) if grad is not None else None)
+        return (loss.value, grad) if want_grad else loss.value

@@ -110,14 +110,15 @@ typedef struct fl_stats {
  * engine attributes to the phase: each array a kernel must read or write,
  * counted once per launch. No counterpart in the reference (its profiler is
  * host-side phase timing, src/core/profiler.ts:39-113). */
-#define FL_PHASES 14
+#define FL_PHASES 15
 /* phase indices: the multigrid phases separate the finest level's smoother
  * launches from the coarser levels'; CONTROL is the one-thread solve-control
- * kernels (tolerance test, cycle decision) and the p = 0 fill. */
+ * kernels (tolerance test, cycle decision) and the p = 0 fill; WARM_START
+ * is the learned warm start (input, network, correction) when attached. */
 enum fl_phase {
   FL_PH_ADVECT_VELOCITY = 0, FL_PH_BODY_FORCES = 1, FL_PH_DIVERGENCE = 2, FL_PH_MG_PRE_FINE = 3, FL_PH_MG_PRE = 4,
   FL_PH_MG_COARSE = 5, FL_PH_MG_POST = 6, FL_PH_MG_POST_FINE = 7, FL_PH_DEFECT64 = 8, FL_PH_RB_SWEEPS = 9,
-  FL_PH_PROJECT = 10, FL_PH_ADVECT_DYE = 11, FL_PH_CFL = 12, FL_PH_CONTROL = 13
+  FL_PH_PROJECT = 10, FL_PH_ADVECT_DYE = 11, FL_PH_CFL = 12, FL_PH_CONTROL = 13, FL_PH_WARM_START = 14
 };
 typedef struct fl_profile {
   double ms[FL_PHASES];
@@ -252,6 +253,53 @@ int fl_dye_patch(fl_engine* e, float* dye, int i0, int j0, int pnx, int pny, con
  */
 int fl_advect_velocity_noalloc(int scheme, int nx, int ny, float h, float dt, const float* u_in, const float* v_in,
                                float* u_out, float* v_out, const uint8_t* label, void* stream);
+
+/* ------------------------------------------------ learned warm start
+ * No counterpart in the reference, whose warm start is the previous step's
+ * pressure (src/core/pressureSolver.ts:28-30). A U-Net (4 levels of two
+ * 3x3 convolutions + ReLU, 32/64/96/128 channels, average pooling down,
+ * nearest upsampling with concatenated skips up, a 1x1 head; bf16 weights
+ * and activations, float32 arithmetic) maps, per cell,
+ *   x = (b / s_b, 1 if Fluid else 0, p_prev / s_p)     (NHWC, 3 channels)
+ * to a correction: p_guess = p_prev + s_p * net(x) on Fluid cells, where
+ * b = -scale * div, s_b = RMS of b and s_p = RMS of p_prev over Fluid cells
+ * (s_p = s_b when p_prev vanishes). The multigrid then runs from p_guess to
+ * the same tolerance as without it. Parameters are one float32 vector:
+ * per layer the weights [cout][ky][kx][cin], then the biases, in the order
+ * enc0a enc0b enc1a enc1b enc2a enc2b mida midb dec2a dec2b dec1a dec1b
+ * dec0a dec0b head. */
+typedef struct fl_unet fl_unet;
+
+/* A network able to run batches of up to max_pixels = batch * height * width
+ * (a multiple of 64) on `device`; parameters start at zero. */
+int fl_unet_create(long long max_pixels, int device, fl_unet** out);
+int fl_unet_destroy(fl_unet* u);
+const char* fl_unet_last_error(const fl_unet* u);
+long long fl_unet_num_params(void);
+/* Parameters from / to a host float32 vector of fl_unet_num_params()
+ * values; setting them also resets the Adam state. */
+int fl_unet_set_params(fl_unet* u, const float* theta);
+int fl_unet_get_params(fl_unet* u, float* theta);
+/* x: batch*h*w*3 host floats (NHWC), out: batch*h*w; h and w multiples of 8. */
+int fl_unet_forward(fl_unet* u, int batch, int h, int w, const float* x, float* out);
+/* One training step on the masked mean squared error between the output and
+ * `target` (mask: 1 to count a pixel, 0 to skip it): forward, backward and,
+ * when `update` is nonzero, one Adam step (beta 0.9 / 0.999, eps 1e-8) with
+ * learning rate lr. Returns the loss; `grad` (optional, host) receives the
+ * gradient. */
+int fl_unet_train_step(fl_unet* u, int batch, int h, int w, const float* x, const float* target, const float* mask,
+                       double lr, int update, double* loss, float* grad);
+/* Process-wide switch between the tensor-core (tcgen05) and CUDA-core
+ * forward convolutions (default: tensor cores where the shape allows). */
+int fl_unet_use_tensor_cores(int on);
+/* Attaches (or, with NULL, detaches) the network as the engine's warm start:
+ * every multigrid step then runs it between the divergence and the solve.
+ * The grid's sides must be multiples of 8 and fit the network's capacity;
+ * the network must not be used elsewhere while the engine steps. */
+int fl_set_warm_start(fl_engine* e, fl_unet* u);
+/* The right-hand side b = -scale * div of the last multigrid step (or solve),
+ * nx*ny values: the training input of the warm start. */
+int fl_read_rhs(fl_engine* e, int dtype, void* b);
 
 #ifdef __cplusplus
 }

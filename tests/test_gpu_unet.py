@@ -1,0 +1,133 @@
+"""The warm-start U-Net on the GPU (fl_unet_*) against its numpy oracle
+(oracle/unet_oracle.py): forward, gradients, Adam; and the engine hook."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from flowlab_gb300 import configs, native
+from flowlab_gb300.native import f32, ptr
+from oracle import unet_oracle as U
+
+pytestmark = pytest.mark.gpu
+
+
+def random_params(seed=0):
+    rng = np.random.default_rng(seed)
+    th = U.init_params(seed + 1)
+    layout, _ = U.param_layout()
+    for name, wo, nw, bo, cout in layout:
+        th[bo:bo + cout] = rng.standard_normal(cout).astype(np.float32) * 0.05
+    _, wo, nw, bo, _ = layout[-1]
+    th[wo:wo + nw] = rng.standard_normal(nw).astype(np.float32) * 0.2
+    return th
+
+
+def batch(seed=0, B=2, H=32, W=48):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((B, H, W, 3)).astype(np.float32)
+    x[..., 1] = (rng.random((B, H, W)) > 0.3)
+    t = rng.standard_normal((B, H, W)).astype(np.float32)
+    m = (rng.random((B, H, W)) > 0.2).astype(np.float32)
+    return x, t, m
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(1e-30, np.linalg.norm(b)))
+
+
+@pytest.fixture(scope="module")
+def net():
+    n = native.Unet(4 * 64 * 64)
+    yield n
+    n.close()
+
+
+@pytest.mark.parametrize("tc", [0, 1])
+def test_forward_matches_oracle(net, tc):
+    """bf16 activations: equal up to roundings that land on the other side
+    of a bf16 step (relative L2 error < 1e-2)."""
+    native.load().fl_unet_use_tensor_cores(tc)
+    try:
+        th = random_params(1)
+        net.set_params(th)
+        x, _, _ = batch(2)
+        out = net.forward(x)
+        ref = U.Net(th, bf16=True).forward(x)
+        assert rel(out, ref) < 1e-2, rel(out, ref)
+    finally:
+        native.load().fl_unet_use_tensor_cores(1)
+
+
+def test_gradient_matches_oracle(net):
+    th = random_params(3)
+    net.set_params(th)
+    x, t, m = batch(4)
+    loss, g = net.train_step(x, t, m, update=False, want_grad=True)
+    ref_net = U.Net(th, bf16=True)
+    ref_loss, dout, _ = U.loss_and_grad(ref_net, x, t, m)
+    ref = ref_net.backward(dout)
+    assert abs(loss - ref_loss) <= 1e-2 * ref_loss
+    layout, _ = U.param_layout()
+    for name, wo, nw, bo, cout in layout:
+        assert rel(g[wo:wo + nw], ref[wo:wo + nw]) < 3e-2, (name, rel(g[wo:wo + nw], ref[wo:wo + nw]))
+        assert rel(g[bo:bo + cout], ref[bo:bo + cout]) < 3e-2, name
+
+
+def test_adam_step_matches_oracle(net):
+    th = random_params(5)
+    net.set_params(th)
+    x, t, m = batch(6)
+    _, g = net.train_step(x, t, m, lr=1e-3, update=True, want_grad=True)
+    new = net.get_params()
+    ref, _, _ = U.adam(th, np.zeros_like(th), np.zeros_like(th), g, 1, lr=1e-3)
+    assert np.abs(new - ref).max() <= 1e-6
+
+
+def test_training_reduces_the_loss(net):
+    net.set_params(random_params(7))
+    x, t, m = batch(8, B=1, H=32, W=32)
+    t = np.tanh(x[..., 0] + 0.5 * x[..., 2]).astype(np.float32)  # a learnable target
+    first = net.train_step(x, t, m, lr=1e-3)
+    for _ in range(30):
+        last = net.train_step(x, t, m, lr=1e-3)
+    assert last < 0.5 * first, (first, last)
+
+
+def run_plume(steps, net=None, n=64):
+    g, f, patch = configs.plume(n)
+    prm = configs.plume_params(tol=1e-6, max_cycles=30, mixed=1)
+    eng = native.Engine(g.nx, g.ny, g.h, params=prm)
+    try:
+        eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+        eng.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
+                 ptr(f32(f.dye)))
+        if net is not None:
+            eng.call("fl_set_warm_start", net.h)
+        cyc = []
+        for _ in range(steps):
+            eng.call("fl_step_auto", 1, None)
+            st = eng.stats()
+            cyc.append((st["cycles"], st["rel_residual"]))
+        u = np.empty(eng.ufaces, np.float32)
+        v = np.empty(eng.vfaces, np.float32)
+        eng.call("fl_read_velocity", native.FL_F32, ptr(u), ptr(v))
+    finally:
+        eng.close()
+    return u, v, cyc
+
+
+def test_zero_network_leaves_the_step_unchanged(net):
+    """A network whose head is zero predicts no correction: the step with it
+    attached equals the step without it, bit for bit."""
+    net.set_params(U.init_params(0))
+    a = run_plume(4)
+    b = run_plume(4, net)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert [c[0] for c in a[2]] == [c[0] for c in b[2]]
+
+
+def test_warm_started_solve_reaches_the_tolerance(net):
+    net.set_params(random_params(9))
+    _, _, cyc = run_plume(4, net)
+    assert all(0 <= r <= 1e-6 for _, r in cyc), cyc
