@@ -56,6 +56,14 @@ def baseline_metric():
         return "steps/s at 1024^2 to 1e-6 relative residual (plain multigrid)"
 
 
+def bf16_peak():
+    try:
+        with open(PEAKS_PATH) as fh:
+            return float(json.load(fh)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
 def hbm_peak():
     try:
         with open(PEAKS_PATH) as fh:
@@ -79,6 +87,9 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU-baseline sample")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--profile-steps", type=int, default=8, help="eager steps with phase events, after the timed ones")
+    ap.add_argument("--cnn-steps", type=int, default=30,
+                    help="timed steps of the same workload with the trained U-Net warm start attached (0: skip)")
+    ap.add_argument("--cnn-weights", default=None, help="U-Net parameters (.npz); default: the packaged ones")
     args = ap.parse_args()
     plume = args.workload == "plume"
     if args.size is None:
@@ -257,6 +268,79 @@ def workload_config(args):
 
 # ------------------------------------------------------------ our engine
 
+def cnn_arm(args, local, stream_unused, flush, state0):
+    """The same workload from the same reset scene, stepped with the trained
+    U-Net warm start and without it, to the same tolerance: V-cycles per step
+    and device-timed steps/s (L2 flushed before every timed step) of both."""
+    import torch
+
+    from flowlab_gb300 import native, warmstart
+    from flowlab_gb300.native import f32, ptr
+
+    path = args.cnn_weights or warmstart.DEFAULT_WEIGHTS
+    if not os.path.exists(path):
+        return {"unavailable": "no trained U-Net parameters at %s" % os.path.relpath(path, ROOT)}
+    params, meta = warmstart.load(path)
+    g, f, patch, prm = workload(args)
+    if g.nx % 8 or g.ny % 8:
+        return {"unavailable": "grid sides are not multiples of 8"}
+    net = native.Unet(g.nx * g.ny, device=local)
+    net.set_params(params)
+    out = {}
+    try:
+        for arm in ("plain", "cnn"):
+            eng = native.Engine(g.nx, g.ny, g.h, params=prm, device=local)
+            try:
+                if patch is not None:
+                    eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+                eng.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)),
+                         ptr(f.label), ptr(f32(f.dye)))
+                if arm == "cnn":
+                    eng.call("fl_set_warm_start", net.h)
+                for _ in range(args.warmup):
+                    eng.call("fl_step_auto", 1, None)
+                eng.call("fl_synchronize")
+                st_ = torch.cuda.ExternalStream(eng.stream(), device=local)
+                ms, cyc, rr = [], [], []
+                for _ in range(args.cnn_steps):
+                    with torch.cuda.stream(st_):
+                        flush.zero_()
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(st_)
+                    eng.call("fl_step_auto", 1, None)
+                    b.record(st_)
+                    st = eng.stats()
+                    cyc.append(st["cycles"])
+                    rr.append(st["rel_residual"])
+                    ms.append(a.elapsed_time(b))
+                out[arm] = {"steps_per_s": 1000.0 * len(ms) / sum(ms), "vcycles_per_step": statistics.mean(cyc),
+                            "rel_residual_max": max(rr)}
+                if arm == "cnn":
+                    # the network's own device time, from phase events on a few eager steps
+                    eng.profile(True)
+                    for _ in range(3):
+                        eng.call("fl_step_auto", 1, None)
+                    ph = eng.profile()["warm_start"]
+                    eng.profile(False)
+                    fwd_ms = ph[0] / 3
+                    flops, tc_flops = warmstart.forward_flops(g.nx, g.ny)
+                    peak = bf16_peak()
+                    out["unet_forward_ms"] = fwd_ms
+                    out["unet_forward_flops"] = flops
+                    out["unet_tflops"] = flops / (fwd_ms * 1e-3) / 1e12
+                    out["unet_frac_of_bf16_peak"] = out["unet_tflops"] / peak[0] if peak[0] else None
+                    out["bf16_peak_source"] = peak[1]
+            finally:
+                eng.close()
+    finally:
+        net.close()
+    out["vcycles_saved_per_step"] = out["plain"]["vcycles_per_step"] - out["cnn"]["vcycles_per_step"]
+    out["steps"] = args.cnn_steps
+    out["training"] = {k: meta[k] for k in ("pairs", "size", "batch", "lr", "train_seconds") if k in meta}
+    return out
+
+
 def run_ours(args, world, rank, local, pg):
     import numpy as np
     import torch
@@ -353,6 +437,8 @@ def run_ours(args, world, rank, local, pg):
     h2d = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len) + eng.cells
     d2h = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len)
 
+    cnn = cnn_arm(args, local, stream, flush, state0=(f, patch)) if args.cnn_steps > 0 else None
+
     cpu = None
     if rank == 0 and args.cpu_steps > 0:
         sps, secs = cpu_port_steps(args, args.cpu_steps, 0, state)
@@ -395,6 +481,7 @@ def run_ours(args, world, rank, local, pg):
         "roofline": roofline, "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
+        "cnn_warm_start": cnn,
         "clocks": sampler.summary(t0, t1),
         "phases_ms_per_step": {n: p["ms"] / len(prof_cycles) for n, p in phases.items()},
         "phase_sample": "%d eager profiled steps after the timed region" % len(prof_cycles),

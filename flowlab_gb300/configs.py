@@ -17,6 +17,11 @@
                width, seeded 1e-3 noise and dye stripes; MacCormack, CFL 0.5,
                multigrid V(3,3) to an 8x8 coarsest level inside the float64
                defect-correction loop, solved to a relative residual of 1e-8.
+  random_scene(side, seed)  batched-scenes member: a closed box of the given
+               side with 0-12 seeded solid discs (radius 2-10% of the side),
+               a divergence-free velocity (curl of Gaussian-smoothed seeded
+               noise, scaled to an RMS face speed of 0.5) and a dye blob;
+               MacCormack, CFL 2, multigrid V(3,3) to 1e-6, float32.
 Scenes come from flowlab_gb300.scenes (float64 host arrays, the reference's
 helpers); parameters are fl_params for the engine.
 """
@@ -86,3 +91,37 @@ def turbulence_params(tol=1e-8, max_cycles=40, mixed=1, coarse_sweeps=32):
     return native.default_params(
         cfl_target=0.5, dt_max=1 / 30, scheme=native.FL_MACCORMACK, solver=native.FL_SOLVER_MG, tol=tol,
         mg_max_cycles=max_cycles, mg_pre=3, mg_post=3, mg_coarse_sweeps=coarse_sweeps, mg_coarsest=8, mixed=mixed)
+
+
+def random_scene(side, seed):
+    """A closed box of `side` cells with seeded discs, a smoothed-noise
+    stream function and a dye blob (all from numpy's PCG64 seeded by `seed`)."""
+    import numpy as np
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed)
+    g = sc.Grid(side, side, 1.0 / side)
+    discs = []
+    for _ in range(int(rng.integers(0, 13))):
+        r = float(rng.uniform(0.02, 0.10))
+        discs.append(sc.solid_disk(float(rng.uniform(r, 1 - r)), float(rng.uniform(r, 1 - r)), r))
+    psi = gaussian_filter(rng.standard_normal((side + 1, side + 1)), sigma=max(1.0, side / 16.0), mode="wrap")
+
+    def seed_velocity(g, u, v):
+        sc.add_curl_of_stream(g, u, v, lambda i, j: psi[np.minimum(j, side), np.minimum(i, side)], 1.0)
+        rms = np.sqrt(np.mean(np.concatenate([u, v]) ** 2))
+        if rms > 0:
+            u *= 0.5 / rms
+            v *= 0.5 / rms
+
+    cx, cy = (float(x) for x in rng.uniform(0.2, 0.8, 2))
+    spec = sc.SceneSpec(labels=sc.all_labels(*discs) if discs else None, seed=seed_velocity,
+                        dye=lambda dg, dye: sc.add_dye_disk(dg, dye[:dg.nx * dg.ny], r=0.1, cx=cx, cy=cy))
+    f, patch = sc.reset_fields(g, g, spec)
+    return g, f, patch
+
+
+def random_scene_params(tol=1e-6, max_cycles=20, mixed=0):
+    return native.default_params(
+        cfl_target=2.0, dt_max=1 / 30, scheme=native.FL_MACCORMACK, solver=native.FL_SOLVER_MG, tol=tol,
+        mg_max_cycles=max_cycles, mg_pre=3, mg_post=3, mg_coarse_sweeps=32, mg_coarsest=8, mixed=mixed)

@@ -65,8 +65,11 @@ struct Unet {
 // CUDA-core kernel.
 bool unet_tc_conv_fwd(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* w,
                       const float* bias, int Cout, __nv_bfloat16* y);
+void unet_tc_setup();
 void unet_tc_enable(bool on);
 bool unet_tc_enabled();
+// Nonzero (and cleared) when a tensor-core launch gave up a bounded wait.
+int unet_tc_take_error();
 
 // Warm start inside the engine's step: input from (b, labels, p_prev), the
 // forward pass, p = p_prev + s_p * out on fluid cells. p_prev is float

@@ -102,6 +102,7 @@ int fl_unet_create(long long max_pixels, int device, fl_unet** out) {
     delete h;
     return st;
   }
+  unet_tc_setup();
   cudaMemset(h->u.theta, 0, h->u.nparam * 4);
   h->u.refresh_bf16(h->u.stream);
   if (cudaStreamSynchronize(h->u.stream) != cudaSuccess) {
@@ -160,7 +161,9 @@ int fl_unet_forward(fl_unet* h, int B, int H, int W, const float* x, float* out)
   u.forward(u.stream, B, H, W);
   UTRY(ucuda(h, cudaGetLastError(), "forward"));
   UTRY(ucuda(h, cudaMemcpyAsync(out, u.out, P * 4, cudaMemcpyDeviceToHost, u.stream), "output"));
-  return usync(h, "forward");
+  UTRY(usync(h, "forward"));
+  if (unet_tc_take_error()) return ufail(h, FL_ETIMEOUT, "a tensor-core convolution gave up a bounded wait");
+  return FL_OK;
 }
 
 int fl_unet_train_step(fl_unet* h, int B, int H, int W, const float* x, const float* target, const float* mask,
@@ -186,6 +189,7 @@ int fl_unet_train_step(fl_unet* h, int B, int H, int W, const float* x, const fl
   UTRY(ucuda(h, cudaMemcpyAsync(&l, u.loss_dev, sizeof l, cudaMemcpyDeviceToHost, s), "loss"));
   if (grad) UTRY(ucuda(h, cudaMemcpyAsync(grad, u.grad, u.nparam * 4, cudaMemcpyDeviceToHost, s), "gradient"));
   UTRY(usync(h, "train step"));
+  if (unet_tc_take_error()) return ufail(h, FL_ETIMEOUT, "a tensor-core convolution gave up a bounded wait");
   if (loss) *loss = l;
   return FL_OK;
 }

@@ -57,3 +57,30 @@ def test_untrained_head_returns_zero():
     x = np.random.default_rng(0).standard_normal((1, 16, 16, 3))
     out = U.Net(U.init_params(0), bf16=True).forward(x)
     assert not out.any()
+
+
+def test_host_init_layout_matches_the_oracle():
+    from flowlab_gb300 import warmstart
+
+    th = warmstart.he_init(0)
+    assert th.size == U.num_params()
+    layout, _ = U.param_layout()
+    _, wo, nw, bo, _ = layout[-1]
+    assert not th[wo:].any()  # zero head: the untrained network predicts no correction
+
+
+def test_features_follow_the_engine_normalisation():
+    from flowlab_gb300 import warmstart
+
+    rng = np.random.default_rng(0)
+    b = rng.standard_normal((8, 8)).astype(np.float32)
+    p = rng.standard_normal((8, 8)).astype(np.float32)
+    label = np.zeros((8, 8), np.uint8)
+    label[0, :] = 2
+    x, sb, sp = warmstart.features(b, label, p)
+    fl = label == 0
+    assert abs(sb - np.sqrt(np.mean(b[fl].astype(np.float64) ** 2))) < 1e-12
+    assert np.allclose(x[..., 0][fl], b[fl] / sb, rtol=1e-6) and (x[..., 0][~fl] == 0).all()
+    assert (x[..., 1] == fl).all()
+    _, sb2, sp2 = warmstart.features(b, label, np.zeros_like(p))
+    assert sp2 == sb2
