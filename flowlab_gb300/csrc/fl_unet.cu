@@ -188,40 +188,50 @@ __global__ void __launch_bounds__(256) k_conv3_wgrad(const __nv_bfloat16* __rest
   }
 }
 
-// 2x2 average pooling, bf16 -> bf16 (the mean in float32).
+// 2x2 average pooling, bf16 -> bf16 (the mean in float32). One thread per
+// coarse pixel and group of 8 channels (C is a multiple of 8).
 __global__ void k_pool(const __nv_bfloat16* __restrict__ x, int B, int H, int W, int C, __nv_bfloat16* __restrict__ y) {
-  const int h = H / 2, w = W / 2;
-  const long n = (long)B * h * w * C;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(e % C);
-    long r = e / C;
-    const int i = (int)(r % w);
-    r /= w;
-    const int j = (int)(r % h);
-    const int b = (int)(r / h);
-    const long base = (((long)b * H + 2 * j) * W + 2 * i) * C + c;
-    const float s = (__bfloat162float(x[base]) + __bfloat162float(x[base + C])) +
-                    (__bfloat162float(x[base + (long)W * C]) + __bfloat162float(x[base + (long)W * C + C]));
-    y[e] = __float2bfloat16_rn(s * 0.25f);
+  const int h = H / 2, w = W / 2, cg = C / 8;
+  const int n = B * h * w * cg;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int g = e % cg, q = e / cg;
+    const int i = q % w, r = q / w, j = r % h, b = r / h;
+    const long base = (((long)b * H + 2 * j) * W + 2 * i) * C + 8 * g;
+    const uint4 v00 = *reinterpret_cast<const uint4*>(x + base);
+    const uint4 v01 = *reinterpret_cast<const uint4*>(x + base + C);
+    const uint4 v10 = *reinterpret_cast<const uint4*>(x + base + (long)W * C);
+    const uint4 v11 = *reinterpret_cast<const uint4*>(x + base + (long)W * C + C);
+    const __nv_bfloat16* a00 = reinterpret_cast<const __nv_bfloat16*>(&v00);
+    const __nv_bfloat16* a01 = reinterpret_cast<const __nv_bfloat16*>(&v01);
+    const __nv_bfloat16* a10 = reinterpret_cast<const __nv_bfloat16*>(&v10);
+    const __nv_bfloat16* a11 = reinterpret_cast<const __nv_bfloat16*>(&v11);
+    __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const float s2 = (__bfloat162float(a00[k]) + __bfloat162float(a01[k])) +
+                       (__bfloat162float(a10[k]) + __bfloat162float(a11[k]));
+      o[k] = __float2bfloat16_rn(s2 * 0.25f);
+    }
+    *reinterpret_cast<uint4*>(y + (long)q * C + 8 * g) = *reinterpret_cast<const uint4*>(o);
   }
 }
 
-// c[p][0:Cu] = u[p/2] (nearest upsampling), c[p][Cu:Cu+Cs] = s[p].
+// c[p][0:Cu] = u[p/2] (nearest upsampling), c[p][Cu:Cu+Cs] = s[p]; one
+// thread per pixel and group of 8 channels (Cu, Cs multiples of 8).
 __global__ void k_up_concat(const __nv_bfloat16* __restrict__ u, int Cu, const __nv_bfloat16* __restrict__ s, int Cs,
                             int B, int H, int W, __nv_bfloat16* __restrict__ c) {
-  const int C = Cu + Cs;
-  const long n = (long)B * H * W * C;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-    const int ch = (int)(e % C);
-    const long p = e / C;
-    if (ch < Cu) {
-      const int i = (int)(p % W);
-      const long r = p / W;
-      const int j = (int)(r % H), b = (int)(r / H);
-      c[e] = u[(((long)b * (H / 2) + j / 2) * (W / 2) + i / 2) * Cu + ch];
+  const int C = Cu + Cs, cg = C / 8;
+  const int n = B * H * W * cg;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int g = e % cg, p = e / cg;
+    uint4 v;
+    if (8 * g < Cu) {
+      const int i = p % W, r = p / W, j = r % H, b = r / H;
+      v = *reinterpret_cast<const uint4*>(u + (((long)b * (H / 2) + j / 2) * (W / 2) + i / 2) * Cu + 8 * g);
     } else {
-      c[e] = s[p * Cs + ch - Cu];
+      v = *reinterpret_cast<const uint4*>(s + (long)p * Cs + 8 * g - Cu);
     }
+    *reinterpret_cast<uint4*>(c + (long)p * C + 8 * g) = v;
   }
 }
 
@@ -267,13 +277,18 @@ __global__ void k_pool_bwd_mask(const float* __restrict__ skip, const float* __r
   }
 }
 
-// 1x1 head: out[p] = sum_c d0[p][c] * w[c] + b.
+// 1x1 head: out[p] = sum_c d0[p][c] * w[c] + b (C = 32: four 16-byte loads).
 __global__ void k_head(const __nv_bfloat16* __restrict__ d0, int C, long P, const __nv_bfloat16* __restrict__ w,
                        const float* __restrict__ b, float* __restrict__ out) {
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < P; p += (long)gridDim.x * blockDim.x) {
-    float s = 0.0f;
-    for (int c = 0; c < C; c++) s = __fmaf_rn(__bfloat162float(d0[p * C + c]), __bfloat162float(w[c]), s);
-    out[p] = s + b[0];
+    float s2 = 0.0f;
+    for (int c0 = 0; c0 < C; c0 += 8) {
+      const uint4 v = *reinterpret_cast<const uint4*>(d0 + p * C + c0);
+      const __nv_bfloat16* a = reinterpret_cast<const __nv_bfloat16*>(&v);
+#pragma unroll
+      for (int k = 0; k < 8; k++) s2 = __fmaf_rn(__bfloat162float(a[k]), __bfloat162float(w[c0 + k]), s2);
+    }
+    out[p] = s2 + b[0];
   }
 }
 

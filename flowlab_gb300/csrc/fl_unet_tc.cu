@@ -33,9 +33,9 @@ constexpr int KC = 32;       // input channels per chunk
 constexpr int STAGE_A = TM * KC * 2;        // bytes
 constexpr int STAGE_B_MAX = 128 * KC * 2;   // bytes, N <= 128
 constexpr int SMEM_TILES = 2 * STAGE_A + 2 * STAGE_B_MAX;  // 32 KB
-// slack so that every offset a descriptor of these tiles can reach, read
-// either way round (LBO and SBO exchanged), stays inside the allocation
-constexpr int SLACK = 32768;
+// every offset the descriptors reach lies inside the tiles (checked on the
+// host for every N); the barriers and the TMEM slot follow
+constexpr int SLACK = 0;
 constexpr int SMEM_BYTES = SMEM_TILES + SLACK + 64;
 constexpr long WAIT_LIMIT = 1L << 22;
 
@@ -164,6 +164,26 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
   bool failed = false;
   int issued = 0;  // chunks committed
 
+  // chunk loads go through registers one chunk ahead: the global (L2)
+  // latency of chunk it+1 overlaps the barrier and MMA issue of chunk it
+  uint4 ra[KC / 8], rb[4];
+  auto load_chunk = [&](int it) {
+    const int tap = it / cchunks, c0 = (it % cchunks) * KC;
+    const int ky = tap / 3, kx = tap % 3;
+    const int yy = py + ky - 1, xx = px + kx - 1;
+    const bool ok = pix_ok && yy >= 0 && yy < H && xx >= 0 && xx < W;
+    const uint4* src = reinterpret_cast<const uint4*>(x + (img + (long)(ok ? yy : 0) * W + (ok ? xx : 0)) * Cin + c0);
+#pragma unroll
+    for (int g = 0; g < KC / 8; g++) ra[g] = ok ? src[g] : make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int e = tid + 128 * q;
+      const int n = e / (KC / 8), g = e % (KC / 8);
+      rb[q] = n < N ? *reinterpret_cast<const uint4*>(w + ((long)n * 9 + tap) * Cin + c0 + 8 * g)
+                    : make_uint4(0, 0, 0, 0);
+    }
+  };
+  load_chunk(0);
   for (int it = 0; it < niter; it++) {
     const int buf = it & 1;
     unsigned char* A = tiles + buf * STAGE_A;
@@ -176,26 +196,15 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
       failed = true;
       break;
     }
-    const int tap = it / cchunks, c0 = (it % cchunks) * KC;
-    const int ky = tap / 3, kx = tap % 3;
-    // A: 128 pixels x 32 channels (4 groups of 8)
-    {
-      const int yy = py + ky - 1, xx = px + kx - 1;
-      const bool ok = pix_ok && yy >= 0 && yy < H && xx >= 0 && xx < W;
-      const uint4* src = reinterpret_cast<const uint4*>(x + (img + (long)yy * W + xx) * Cin + c0);
 #pragma unroll
-      for (int g = 0; g < KC / 8; g++) {
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (ok) v = src[g];
-        *reinterpret_cast<uint4*>(A + tile_off(tid, g, TM)) = v;
-      }
-    }
-    // B: N output channels x 32 channels of this tap
-    for (int e = tid; e < N * (KC / 8); e += 128) {
+    for (int g = 0; g < KC / 8; g++) *reinterpret_cast<uint4*>(A + tile_off(tid, g, TM)) = ra[g];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int e = tid + 128 * q;
       const int n = e / (KC / 8), g = e % (KC / 8);
-      const uint4 v = *reinterpret_cast<const uint4*>(w + ((long)n * 9 + tap) * Cin + c0 + 8 * g);
-      *reinterpret_cast<uint4*>(B + tile_off(n, g, N)) = v;
+      if (n < N) *reinterpret_cast<uint4*>(B + tile_off(n, g, N)) = rb[q];
     }
+    if (it + 1 < niter) load_chunk(it + 1);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (tid == 0) {
