@@ -21,7 +21,8 @@
                side with 0-12 seeded solid discs (radius 2-10% of the side),
                a divergence-free velocity (curl of Gaussian-smoothed seeded
                noise, scaled to an RMS face speed of 0.5) and a dye blob;
-               MacCormack, CFL 2, multigrid V(3,3) to 1e-6, float32.
+               MacCormack, CFL 2, multigrid V(3,3) to 1e-6 (float32; with
+               mixed=1 the float64 defect correction, which 1e-6 needs).
 Scenes come from flowlab_gb300.scenes (float64 host arrays, the reference's
 helpers); parameters are fl_params for the engine.
 """
@@ -98,13 +99,23 @@ def random_scene(side, seed):
     stream function and a dye blob (all from numpy's PCG64 seeded by `seed`)."""
     import numpy as np
     from scipy.ndimage import gaussian_filter
+    from scipy.ndimage import label as connected
 
     rng = np.random.default_rng(seed)
     g = sc.Grid(side, side, 1.0 / side)
-    discs = []
-    for _ in range(int(rng.integers(0, 13))):
-        r = float(rng.uniform(0.02, 0.10))
-        discs.append(sc.solid_disk(float(rng.uniform(r, 1 - r)), float(rng.uniform(r, 1 - r)), r))
+    # redraw the discs until the fluid is one connected region: a pocket
+    # sealed off by discs and walls has no solution for a nonzero net
+    # divergence, and the solve would stall there
+    while True:
+        discs = []
+        for _ in range(int(rng.integers(0, 13))):
+            r = float(rng.uniform(0.02, 0.10))
+            discs.append(sc.solid_disk(float(rng.uniform(r, 1 - r)), float(rng.uniform(r, 1 - r)), r))
+        lab = np.zeros(side * side, np.uint8)
+        for d in discs:
+            d(g, lab)
+        if connected(lab.reshape(side, side) == 0)[1] <= 1:
+            break
     psi = gaussian_filter(rng.standard_normal((side + 1, side + 1)), sigma=max(1.0, side / 16.0), mode="wrap")
 
     def seed_velocity(g, u, v):

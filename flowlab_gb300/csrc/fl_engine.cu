@@ -567,11 +567,13 @@ void destroy_graphs(Engine* e) {
   e->graphs_valid = false;
 }
 
-// Captures the whole step for buffer parity `par` into an executable graph.
-int build_graph(Engine* e, int par, cudaGraphExec_t* out) {
+// Enqueues one whole step for buffer parity `par` on e->stream while that
+// stream is being captured (into a graph of its own or a branch of a batch
+// graph); the pressure solve becomes a WHILE node whose body is captured
+// from e->stream2.
+cudaError_t capture_step(Engine* e, int par) {
   cudaStream_t s = e->stream;
-  cudaError_t err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-  if (err != cudaSuccess) return cuda_status(e, err, "begin capture");
+  cudaError_t err = cudaSuccess;
   enqueue_pre(e, s, par, false);
   if (e->prm.solver == FL_SOLVER_MG) {
     cudaStreamCaptureStatus cst;
@@ -611,6 +613,15 @@ int build_graph(Engine* e, int par, cudaGraphExec_t* out) {
     enqueue_rb_fixed(e, s);
   }
   if (err == cudaSuccess) enqueue_post(e, s, par, true);
+  return err;
+}
+
+// Captures the whole step for buffer parity `par` into an executable graph.
+int build_graph(Engine* e, int par, cudaGraphExec_t* out) {
+  cudaStream_t s = e->stream;
+  cudaError_t err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (err != cudaSuccess) return cuda_status(e, err, "begin capture");
+  err = capture_step(e, par);
   cudaGraph_t graph = nullptr;
   cudaError_t end = cudaStreamEndCapture(s, &graph);
   if (err == cudaSuccess) err = end;
@@ -1280,6 +1291,150 @@ int fl_read_rhs(fl_engine* h, int dtype, void* b) {
   ENTER(h);
   TRY(download(e, b, e->levels[0].b, e->cells(), dtype, "read rhs"));
   return sync(e, "read rhs");
+}
+
+// ------------------------------------------------------- batched scenes
+
+}  // extern "C"
+
+struct fl_batch {
+  std::vector<fl_engine*> engines;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  std::vector<cudaEvent_t> events;
+  std::string err;
+};
+
+namespace {
+
+int bfail(fl_batch* b, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (b)
+    b->err = buf;
+  else
+    set_global_error("%s", buf);
+  return code;
+}
+
+// One graph per buffer parity: a fork from the batch stream to every
+// engine's stream, each engine's whole step (its own WHILE node), a join.
+cudaError_t capture_batch(fl_batch* b, int par, cudaGraphExec_t* out) {
+  cudaError_t err = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+  if (err != cudaSuccess) return err;
+  const size_t n = b->engines.size();
+  for (size_t k = 0; k < n && err == cudaSuccess; k++) {
+    Engine* e = &b->engines[k]->e;
+    err = cudaEventRecord(b->events[2 * k], b->stream);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(e->stream, b->events[2 * k], 0);
+    if (err == cudaSuccess) err = capture_step(e, par);
+    if (err == cudaSuccess) err = cudaEventRecord(b->events[2 * k + 1], e->stream);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(b->stream, b->events[2 * k + 1], 0);
+  }
+  cudaGraph_t graph = nullptr;
+  cudaError_t end = cudaStreamEndCapture(b->stream, &graph);
+  if (err == cudaSuccess) err = end;
+  if (err == cudaSuccess) err = cudaGetLastError();
+  if (err == cudaSuccess) err = cudaGraphInstantiate(out, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (err != cudaSuccess) cudaGetLastError();
+  return err;
+}
+
+void batch_free(fl_batch* b) {
+  for (auto& g : b->graph)
+    if (g) cudaGraphExecDestroy(g);
+  for (cudaEvent_t ev : b->events) cudaEventDestroy(ev);
+  if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fl_batch_create(fl_engine* const* engines, int count, fl_batch** out) {
+  if (!out) return bfail(nullptr, FL_EINVAL, "null output pointer");
+  *out = nullptr;
+  if (!engines || count < 1) return bfail(nullptr, FL_EINVAL, "empty batch");
+  fl_batch* b = new (std::nothrow) fl_batch();
+  if (!b) return bfail(nullptr, FL_ENOMEM, "host allocation");
+  b->device = engines[0]->e.device;
+  const int par = engines[0]->e.cur;
+  for (int k = 0; k < count; k++) {
+    Engine* e = engines[k] ? &engines[k]->e : nullptr;
+    const char* why = !e                        ? "null engine"
+                      : e->device != b->device  ? "engines on different devices"
+                      : !e->uploaded            ? "engine without fields"
+                      : !graph_eligible(e)      ? "engine not eligible for graph steps (profiling, stir, label edit "
+                                                  "or a host-checked red-black tolerance)"
+                      : e->cur != par           ? "engines at different buffer parities"
+                                                : nullptr;
+    if (why) {
+      delete b;
+      return bfail(nullptr, FL_EINVAL, "engine %d: %s", k, why);
+    }
+    b->engines.push_back(engines[k]);
+  }
+  cudaSetDevice(b->device);
+  cudaError_t err = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  b->events.resize(2 * count, nullptr);
+  for (int k = 0; k < 2 * count && err == cudaSuccess; k++)
+    err = cudaEventCreateWithFlags(&b->events[k], cudaEventDisableTiming);
+  for (int p = 0; p < 2 && err == cudaSuccess; p++) err = capture_batch(b, p, &b->graph[p]);
+  if (err != cudaSuccess) {
+    batch_free(b);
+    delete b;
+    return bfail(nullptr, err == cudaErrorMemoryAllocation ? FL_ENOMEM : FL_EDEVICE, "batch graph: %s",
+                 cudaGetErrorString(err));
+  }
+  *out = b;
+  return FL_OK;
+}
+
+int fl_batch_destroy(fl_batch* b) {
+  if (!b) return FL_OK;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  batch_free(b);
+  delete b;
+  return FL_OK;
+}
+
+const char* fl_batch_last_error(const fl_batch* b) { return b ? b->err.c_str() : fl_last_error(nullptr); }
+
+void* fl_batch_stream(fl_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+int fl_batch_step(fl_batch* b, int nsteps) {
+  if (!b) return bfail(nullptr, FL_EINVAL, "null batch");
+  if (nsteps < 0) return bfail(b, FL_EINVAL, "nsteps < 0");
+  cudaSetDevice(b->device);
+  // every engine's earlier work is ordered before the batch's first step
+  for (size_t k = 0; k < b->engines.size(); k++) {
+    Engine* e = &b->engines[k]->e;
+    if (e->busy.load() != 0) return bfail(b, FL_EBUSY, "engine %zu is inside a call", k);
+    cudaEventRecord(b->events[2 * k], e->stream);
+    cudaStreamWaitEvent(b->stream, b->events[2 * k], 0);
+  }
+  const int par0 = b->engines[0]->e.cur;
+  for (int n = 0; n < nsteps; n++) {
+    cudaError_t err = cudaGraphLaunch(b->graph[(par0 + n) & 1], b->stream);
+    if (err != cudaSuccess) return bfail(b, FL_EDEVICE, "batch launch: %s", cudaGetErrorString(err));
+  }
+  // and the engines' later work after the batch's last step
+  for (size_t k = 0; k < b->engines.size(); k++) {
+    Engine* e = &b->engines[k]->e;
+    cudaEventRecord(b->events[2 * k + 1], b->stream);
+    cudaStreamWaitEvent(e->stream, b->events[2 * k + 1], 0);
+    e->cur = (e->cur + nsteps) & 1;
+    e->steps += nsteps;
+    e->stats_on_device = true;
+  }
+  cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? FL_OK : bfail(b, FL_EDEVICE, "batch step: %s", cudaGetErrorString(err));
 }
 
 }  // extern "C"

@@ -20,6 +20,7 @@
 //   * Labels become one byte per cell of stencil links (fl_common.cuh), built
 //     per level when labels change (pressureMultigrid.ts:302-310 rebuilt them
 //     every solve; stepGpu.ts:498 only on change, as here).
+#include <mutex>
 #include <algorithm>
 #include <cstdio>
 
@@ -948,6 +949,19 @@ void mg_free(Engine& e) {
   e.levels.clear();
 }
 
+// The dynamic shared-memory limit of k_mg_coarse is a per-device property
+// of the function, shared by every engine in the process: it only ever grows
+// to the largest tail any engine on the device needs (an engine with a
+// smaller tail must not lower it under another engine's launches).
+static void raise_coarse_smem_limit(int device, size_t bytes) {
+  static std::mutex mu;
+  static size_t limit[256] = {};
+  std::lock_guard<std::mutex> lock(mu);
+  if (device < 0 || device >= 256 || bytes <= limit[device]) return;
+  if (cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess)
+    limit[device] = bytes;
+}
+
 void mg_setup(Engine& e) {
   mg_free(e);
   // pressureMultigrid.ts:71-78
@@ -982,7 +996,7 @@ void mg_setup(Engine& e) {
     }
   e.coarse_level = lc;
   e.coarse_smem = coarse_smem_bytes(e, lc, nullptr, nullptr, nullptr);
-  cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.coarse_smem);
+  raise_coarse_smem_limit(e.device, e.coarse_smem);
   e.codes_valid = false;
 }
 

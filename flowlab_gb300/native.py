@@ -142,6 +142,11 @@ SIGNATURES = [
     ("fl_unet_use_tensor_cores", _I, [_I]),
     ("fl_set_warm_start", _I, [_P, _P]),
     ("fl_read_rhs", _I, [_P, _I, _P]),
+    ("fl_batch_create", _I, [_P, _I, ctypes.POINTER(_P)]),
+    ("fl_batch_destroy", _I, [_P]),
+    ("fl_batch_last_error", ctypes.c_char_p, [_P]),
+    ("fl_batch_stream", _P, [_P]),
+    ("fl_batch_step", _I, [_P, _I]),
 ]
 
 _lib = None
@@ -309,3 +314,37 @@ class Unet:
         self.call("fl_unet_train_step", B, H, W, ptr(x), ptr(target), ptr(mask), float(lr), int(update),
                   ctypes.byref(loss), ptr(grad) if grad is not None else None)
         return (loss.value, grad) if want_grad else loss.value
+
+
+class Batch:
+    """Several engines stepped by one graph launch per step (fl_batch_*)."""
+
+    def __init__(self, engines):
+        lib = load()
+        self.lib = lib
+        self.engines = list(engines)
+        arr = (ctypes.c_void_p * len(self.engines))(*[e.handle for e in self.engines])
+        h = ctypes.c_void_p()
+        st = lib.fl_batch_create(arr, len(self.engines), ctypes.byref(h))
+        if st != FL_OK:
+            raise FlowlabError(st, lib.fl_last_error(None).decode())
+        self.h = h
+
+    def step(self, n=1):
+        st = self.lib.fl_batch_step(self.h, int(n))
+        if st != FL_OK:
+            raise FlowlabError(st, self.lib.fl_batch_last_error(self.h).decode())
+
+    def stream(self):
+        return self.lib.fl_batch_stream(self.h)
+
+    def close(self):
+        if self.h:
+            self.lib.fl_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,84 @@
+"""Batched scenes (fl_batch_*): one graph launch steps every engine; each
+engine's result equals stepping it alone, bit for bit."""
+import numpy as np
+import pytest
+
+from flowlab_gb300 import batch, configs, native
+from flowlab_gb300.native import f32, ptr
+
+pytestmark = pytest.mark.gpu
+
+
+def karman_engine():
+    g, f, patch = configs.karman(96, 64)
+    e = native.Engine(g.nx, g.ny, g.h, params=configs.karman_params())
+    e.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
+           ptr(f32(f.dye)))
+    return e
+
+
+def fields(e):
+    u = np.empty(e.ufaces, np.float32)
+    v = np.empty(e.vfaces, np.float32)
+    p = np.empty(e.cells, np.float32)
+    d = np.empty(e.dye_len, np.float32)
+    e.call("fl_read_velocity", native.FL_F32, ptr(u), ptr(v))
+    e.call("fl_read_pressure", native.FL_F32, ptr(p))
+    e.call("fl_read_dye", native.FL_F32, ptr(d))
+    return u, v, p, d
+
+
+def test_batch_equals_engines_stepped_alone():
+    sides = [64, 128, 64, 256]
+    steps = 5
+    alone = batch.make_engines(sides, seed=11) + [karman_engine()]
+    together = batch.make_engines(sides, seed=11) + [karman_engine()]
+    try:
+        ref = []
+        for e in alone:
+            e.call("fl_step_auto", steps, None)
+            ref.append((fields(e), e.stats()))
+        b = native.Batch(together)
+        try:
+            b.step(steps)
+        finally:
+            b.close()
+        for k, e in enumerate(together):
+            got = fields(e)
+            st = e.stats()
+            for name, x, y in zip(("u", "v", "p", "dye"), ref[k][0], got):
+                assert np.array_equal(x, y), "scene %d: %s differs" % (k, name)
+            assert st["cycles"] == ref[k][1]["cycles"] and st["steps"] == ref[k][1]["steps"]
+            assert abs(st["time"] - ref[k][1]["time"]) <= 1e-12
+    finally:
+        batch.close_all(alone + together)
+
+
+def test_batch_then_single_steps_stay_ordered():
+    """Steps through the batch, then through each engine, equal the same
+    number of single steps."""
+    a = batch.make_engines([64, 128], seed=3)
+    c = batch.make_engines([64, 128], seed=3)
+    try:
+        for e in a:
+            e.call("fl_step_auto", 4, None)
+        b = native.Batch(c)
+        b.step(2)
+        b.close()
+        for e in c:
+            e.call("fl_step_auto", 2, None)
+        for x, y in zip(a, c):
+            for fx, fy in zip(fields(x), fields(y)):
+                assert np.array_equal(fx, fy)
+    finally:
+        batch.close_all(a + c)
+
+
+def test_engines_at_different_parities_are_refused():
+    es = batch.make_engines([64, 64], seed=5)
+    try:
+        es[0].call("fl_step_auto", 1, None)
+        with pytest.raises(native.FlowlabError):
+            native.Batch(es)
+    finally:
+        batch.close_all(es)

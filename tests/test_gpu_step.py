@@ -241,3 +241,20 @@ def test_graph_rebuilt_after_parameter_change(o32):
     eu, ev, ep, ed = sim2.get_fields()
     for name, x, y in (("u", eu, u), ("v", ev, v), ("p", ep, p), ("dye", ed, d)):
         assert mismatch(x, y) == 0, "%s: %d values differ from the float32 oracle" % (name, mismatch(x, y))
+
+
+def test_engines_with_different_coarse_tails_coexist():
+    """The coarse tail's shared-memory limit is per device and function:
+    creating an engine with a smaller tail must not break a larger one."""
+    g, f, patch = configs.plume(64)
+    big = native.Engine(g.nx, g.ny, g.h, params=configs.plume_params(tol=1e-4, max_cycles=8, mixed=0))
+    small = native.Engine(24, 16, 1 / 16, params=native.default_params(solver=native.FL_SOLVER_MG, mg_coarsest=2))
+    try:
+        big.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+        big.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
+                 ptr(f32(f.dye)))
+        big.call("fl_step_auto", 2, None)
+        assert big.stats()["cycles"] > 0
+    finally:
+        small.close()
+        big.close()
