@@ -201,6 +201,7 @@ int validate_params(Engine* e, const fl_params* p) {
     return fail(e, FL_EINVAL, "negative sweep or cycle count");
   // the coarsest level is solved inside the single-CTA tail (sides <= 64)
   if (p->mg_coarsest < 1 || p->mg_coarsest > 64) return fail(e, FL_EINVAL, "mg_coarsest must be in [1, 64]");
+  if (p->rb_pairs < 0 || p->rb_pairs > 4) return fail(e, FL_EINVAL, "rb_pairs must be in [0, 4]");
   if (!(p->cfl_target > 0) || !(p->dt_max > 0) || !(p->rho > 0))
     return fail(e, FL_EINVAL, "cfl_target, dt_max and rho must be positive");
   return FL_OK;
@@ -427,8 +428,9 @@ void enqueue_rb_fixed(Engine* e, cudaStream_t s) {
   launch_solve_begin(s, e->acc, e->ctl, false, 0);
   int k = 0, src = 0;
   const int iters = e->prm.pressure_iters;
+  const int per = e->prm.rb_pairs > 0 ? e->prm.rb_pairs : 4;
   while (k < iters) {
-    const int chunk = std::min(4, iters - k);
+    const int chunk = std::min(per, iters - k);
     const int tok = prof_begin(*e, FL_PH_RB_SWEEPS);
     launch_rb_sweeps(s, L.nx, L.ny, L.x[src], L.x[1 - src], L.b, L.code, 0.0f, (float)e->prm.omega, chunk,
                      &e->sc->scale);
@@ -471,8 +473,9 @@ int rb_solve_device(Engine* e, float scale, int iterations, float omega, double 
   const double target = tol > 0 ? tol * div_rms : -1;
   int k = 0;
   int src = 0;
+  const int per = e->prm.rb_pairs > 0 ? e->prm.rb_pairs : 4;
   while (k < iterations) {
-    int chunk = std::min(4, iterations - k);
+    int chunk = std::min(per, iterations - k);
     if (target >= 0) chunk = std::min(chunk, 12 - (k % 12));
     const int tok = prof_begin(*e, FL_PH_RB_SWEEPS);
     launch_rb_sweeps(e->stream, L.nx, L.ny, L.x[src], L.x[1 - src], L.b, L.code, scale, omega, chunk);
@@ -1071,6 +1074,10 @@ int fl_rb_solve(fl_engine* h, float* p, const float* div, const uint8_t* label, 
   const long n = e->cells();
   // pressureRedBlack.ts:335-339 — zero divergence: p = 0, no sweeps.
   const double div_rms = host_fluid_div_rms(div, label, n);
+  e->stats_on_device = false;
+  e->last_div_rms = div_rms;
+  e->last_relres = div_rms == 0 ? 0.0 : -1.0;
+  e->last_iters = 0;
   if (used) *used = 0;
   if (div_rms == 0) {
     std::memset(p, 0, n * sizeof(float));
@@ -1085,6 +1092,7 @@ int fl_rb_solve(fl_engine* h, float* p, const float* div, const uint8_t* label, 
   e->codes_valid = false;
   int u = 0;
   TRY(rb_solve_device(e, scale, iterations, omega, tol, div_rms, &u));
+  e->last_iters = u;
   if (used) *used = u;
   TRY(down32(e, p, L.x[0], n * 4, "p"));
   return sync(e, "rb solve");
@@ -1105,6 +1113,7 @@ int fl_mg_solve(fl_engine* h, float* p, const float* div, const uint8_t* label, 
   launch_scale_rhs(e->stream, n, e->u_hat, L.b, -scale, L.label, e->acc);
   TRY(check_launch(e, "rhs"));
   TRY(put_ctl(e, SOLVE_MG, tol, max_cycles, true));
+  e->stats_on_device = true;
   TRY(solve_mg_eager(e, false, max_cycles));
   if (cycles_used) *cycles_used = e->ctl_host->cycles;
   if (rel_residual) *rel_residual = e->ctl_host->rel;
@@ -1120,6 +1129,7 @@ int fl_mg_solve_mixed(fl_engine* h, double* p, const float* div, const uint8_t* 
   const long n = e->cells();
   Level& L = e->levels[0];
   TRY(put_ctl(e, SOLVE_MIXED, tol, max_cycles, true));
+  e->stats_on_device = true;
   TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, n * sizeof(double), cudaMemcpyHostToDevice, e->stream), "p"));
   TRY(up32(e, e->u_hat, div, n * 4, "div"));
   TRY(up32(e, L.label, label, (size_t)n, "label"));

@@ -53,7 +53,8 @@ class Params(ctypes.Structure):
         ("mg_coarsest", ctypes.c_int),
         ("mg_omega", ctypes.c_double),
         ("mixed", ctypes.c_int),
-        ("reserved", ctypes.c_int * 7),
+        ("rb_pairs", ctypes.c_int),
+        ("reserved", ctypes.c_int * 6),
     ]
 
 

@@ -86,7 +86,9 @@ typedef struct fl_params {
   int mg_coarsest;       /* stop coarsening at <= this many cells a side (reference 4; at most 64) */
   double mg_omega;       /* smoother relaxation (reference 1.0) */
   int mixed;             /* 1: float64 fine pressure + float64 residual (defect correction) */
-  int reserved[7];
+  int rb_pairs;          /* red-black sweep pairs per launch, 1..4 (0: 4): the temporal-blocking
+                            depth, i.e. the tile/halo shape; results do not depend on it */
+  int reserved[6];
 } fl_params;
 
 /* Per-step report (the reference's sim.iters / sim.dt plus the residual the
@@ -297,8 +299,9 @@ int fl_unet_use_tensor_cores(int on);
  * The grid's sides must be multiples of 8 and fit the network's capacity;
  * the network must not be used elsewhere while the engine steps. */
 int fl_set_warm_start(fl_engine* e, fl_unet* u);
-/* The right-hand side b = -scale * div of the last multigrid step (or solve),
- * nx*ny values: the training input of the warm start. */
+/* The last step's (or solve's) pressure right-hand side, nx*ny values:
+ * b = -scale * div for the multigrid (the training input of the warm
+ * start), div itself for the red-black solver. */
 int fl_read_rhs(fl_engine* e, int dtype, void* b);
 
 /* ------------------------------------------------------- batched scenes

@@ -1,0 +1,25 @@
+"""The autotuner's selection rules (CPU): fastest candidate that reaches the
+tolerance; smallest residual for omega; parameter copies."""
+from flowlab_gb300 import autotune, configs, native
+
+
+def test_fastest_converged_candidate_wins():
+    res = [({"mg_coarsest": 4}, {"ms": 1.0, "rel_max": 2e-6, "cycles": 5}),
+           ({"mg_coarsest": 8}, {"ms": 1.2, "rel_max": 9e-7, "cycles": 4}),
+           ({"mg_coarsest": 16}, {"ms": 1.1, "rel_max": 8e-7, "cycles": 4}),
+           ({"mg_coarsest": 32}, {"ms": 0.9, "rel_max": -1.0, "cycles": 20})]
+    best = autotune.pick_multigrid(res, 1e-6)
+    assert best[0] == {"mg_coarsest": 16}
+    assert autotune.pick_multigrid(res[:1], 1e-6) is None
+
+
+def test_omega_by_residual():
+    assert autotune.pick_omega([(1.7, 1e-3), (1.9, 2e-4), (1.95, 2e-4)]) == 1.9
+
+
+def test_with_params_copies():
+    base = configs.plume_params()
+    p = autotune.with_params(base, mg_coarsest=16)
+    assert p.mg_coarsest == 16 and base.mg_coarsest == 8 and p.tol == base.tol
+    assert autotune.cache_key(p, 256, 128) == "mg:256x128:mixed"
+    assert autotune.cache_key(configs.karman_params(), 128, 128) == "rb:128x128:f32"
