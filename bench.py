@@ -103,15 +103,20 @@ def parse():
     return args
 
 
+def workload_params(args):
+    from flowlab_gb300 import configs
+
+    if args.workload == "plume":
+        return configs.plume_params(tol=args.tol, max_cycles=args.max_cycles)
+    return configs.turbulence_params(tol=args.tol, max_cycles=args.max_cycles)
+
+
 def workload(args):
     """(grid, fields, dye patch, engine params) of the selected workload."""
     from flowlab_gb300 import configs
 
-    if args.workload == "plume":
-        g, f, patch = configs.plume(args.size)
-        return g, f, patch, configs.plume_params(tol=args.tol, max_cycles=args.max_cycles)
-    g, f, patch = configs.turbulence(args.size)
-    return g, f, patch, configs.turbulence_params(tol=args.tol, max_cycles=args.max_cycles)
+    scene = configs.plume(args.size) if args.workload == "plume" else configs.turbulence(args.size)
+    return scene + (workload_params(args),)
 
 
 class ClockSampler:
@@ -299,7 +304,9 @@ def workload_config(args):
         desc = ("turbulence grid %dx%d, u = 1 inflow through a 16x16 lattice of solid squares, MacCormack, CFL 0.5, "
                 "multigrid V(3,3) coarsest 8x8 in a float64 defect-correction loop, relative residual %.0e "
                 "(cap %d cycles)" % (n, n, args.tol, args.max_cycles))
-    return {"workload": desc, "grid": [n, n], "solver": "multigrid V(3,3), 32 coarse sweep pairs",
+    prm = workload_params(args)
+    return {"workload": desc, "grid": [n, n],
+            "solver": "multigrid V(3,3), %d coarse sweep pairs" % prm.mg_coarse_sweeps,
             "tol": args.tol, "precision": "float32 fields and smoothing, float64 residual and correction",
             "l2": "flushed (320 MB write) before every timed step",
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}

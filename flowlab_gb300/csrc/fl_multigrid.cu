@@ -128,19 +128,20 @@ __device__ __forceinline__ float over_count(float s, int cnt) {
 // correct on the region shrunk by s+1 cells, so after 2*pairs half-sweeps the
 // tile (and, with the +1, a ring around it) holds exactly the values the
 // sequential sweeps produce; outer cells hold finite values nobody uses.
-constexpr int RGN = 64;
-constexpr int RGN_T = 32;
-
-template <int P, int MODE>
+// The region side R is 64 (1024 threads) on large levels and 32 (256
+// threads, more CTAs for levels too small to fill the GPU with 64^2 regions).
+template <int P, int MODE, int R>
 struct Tile {
   static constexpr int H = (MODE == MODE_PLAIN) ? 2 * P : 2 * P + 1;
-  static constexpr int T = RGN - 2 * H;  // tile side, even
+  static constexpr int T = R - 2 * H;  // tile side, even
 };
 
-template <int P, int MODE>
-__global__ void __launch_bounds__(RGN_T* RGN_T, 1) k_smooth(SmoothArgs a) {
-  constexpr int H = Tile<P, MODE>::H;
-  constexpr int T = Tile<P, MODE>::T;
+template <int P, int MODE, int R>
+__global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs a) {
+  constexpr int RGN = R;
+  constexpr int RGN_T = R / 2;
+  constexpr int H = Tile<P, MODE, R>::H;
+  constexpr int T = Tile<P, MODE, R>::T;
   static_assert(T % 2 == 0 && T > 0, "tile must be even");
   __shared__ float xs[2][RGN][RGN / 2];
   __shared__ float rs[MODE == MODE_PRE ? RGN : 1][MODE == MODE_PRE ? RGN : 1];
@@ -837,12 +838,25 @@ __global__ void k_rb_halfsweep(int nx, int ny, float* __restrict__ p, const floa
 
 // ------------------------------------------------------------- host side
 
+template <int P, int MODE, int R>
+static void launch_smooth_r(cudaStream_t s, const SmoothArgs& a) {
+  constexpr int T = Tile<P, MODE, R>::T;
+  dim3 blk(R / 2, R / 2);
+  dim3 grd((a.nx + T - 1) / T, (a.ny + T - 1) / T);
+  k_smooth<P, MODE, R><<<grd, blk, 0, s>>>(a);
+}
+
+// 64^2 regions unless they would leave most SMs idle: below 64 such CTAs
+// (levels of about 400^2 and smaller) the 32^2 regions' extra CTAs win over
+// their larger halo share (measured: 256^2 and 128^2 faster, 512^2 slower).
 template <int P, int MODE>
 static void launch_smooth_t(cudaStream_t s, const SmoothArgs& a) {
-  constexpr int T = Tile<P, MODE>::T;
-  dim3 blk(RGN_T, RGN_T);
-  dim3 grd((a.nx + T - 1) / T, (a.ny + T - 1) / T);
-  k_smooth<P, MODE><<<grd, blk, 0, s>>>(a);
+  constexpr int T = Tile<P, MODE, 64>::T;
+  const long blocks64 = (long)((a.nx + T - 1) / T) * ((a.ny + T - 1) / T);
+  if (blocks64 < 64)
+    launch_smooth_r<P, MODE, 32>(s, a);
+  else
+    launch_smooth_r<P, MODE, 64>(s, a);
 }
 
 template <int MODE>
