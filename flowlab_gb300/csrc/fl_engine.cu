@@ -527,7 +527,9 @@ int step_eager(Engine* e, bool device_dt) {
   Level& L0 = e->levels[0];
   const int par = e->cur;
   if (e->labels_dirty) {
-    launch_commit_labels(s, e->nx, e->ny, L0.label, L0.x[0], e->u[par], e->v[par], e->dye[par], e->dye_cells());
+    const bool mixed = step_mixed(e);
+    launch_commit_labels(s, e->nx, e->ny, L0.label, L0.x[0], e->u[par], e->v[par], e->dye[par], e->dye_cells(),
+                         mixed ? e->p64[0] : nullptr, mixed ? e->p64[1] : nullptr, e->ctl);
     mg_build_codes(*e);
     TRY(check_launch(e, "commit labels"));
     e->labels_dirty = false;

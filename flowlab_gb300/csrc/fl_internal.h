@@ -159,7 +159,8 @@ void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const floa
 void launch_scale_rhs(cudaStream_t s, long n, const float* div, float* b, float neg_scale, const uint8_t* label,
                       StepAccum* acc);
 void launch_commit_labels(cudaStream_t s, int nx, int ny, const uint8_t* label, float* p, float* u, float* v,
-                          float* dye, long dye_cells);
+                          float* dye, long dye_cells, double* p64a = nullptr, double* p64b = nullptr,
+                          const SolveCtl* ctl = nullptr);
 void launch_stir(cudaStream_t s, int nx, int ny, float h, float* u, float* v, const uint8_t* label,
                  const float* stir5);
 void launch_dye_patch(cudaStream_t s, int dnx, int dny, float* dye, const float* patch, int pi0, int pj0, int pnx,

@@ -280,7 +280,8 @@ __global__ void __launch_bounds__(256) k_scale_rhs(long n, const float* __restri
 // extended to p and dye as the host version does.
 __global__ void k_commit_labels(int nx, int ny, const uint8_t* __restrict__ label, float* __restrict__ p,
                                 float* __restrict__ u, float* __restrict__ v, float* __restrict__ dye,
-                                long dye_cells) {
+                                long dye_cells, double* __restrict__ p64a, double* __restrict__ p64b,
+                                const SolveCtl* __restrict__ ctl) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i < nx && j < ny) {
@@ -288,6 +289,8 @@ __global__ void k_commit_labels(int nx, int ny, const uint8_t* __restrict__ labe
     const uint8_t l = label[k];
     if (l != FLUID) {
       if (p) p[k] = 0.0f;
+      // the float64 pressure of the defect correction keeps the same rule
+      if (p64a) (ctl->par ? p64b : p64a)[k] = 0.0;
       if (l == SOLID && dye && k < dye_cells)
         for (int c = 0; c < DYE_CHANNELS; c++) dye[k + c * dye_cells] = 0.0f;
     }
@@ -418,9 +421,9 @@ void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const floa
 }
 
 void launch_commit_labels(cudaStream_t s, int nx, int ny, const uint8_t* label, float* p, float* u, float* v,
-                          float* dye, long dye_cells) {
+                          float* dye, long dye_cells, double* p64a, double* p64b, const SolveCtl* ctl) {
   dim3 b(32, 8);
-  k_commit_labels<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, label, p, u, v, dye, dye_cells);
+  k_commit_labels<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, label, p, u, v, dye, dye_cells, p64a, p64b, ctl);
 }
 
 void launch_stir(cudaStream_t s, int nx, int ny, float h, float* u, float* v, const uint8_t* label,

@@ -311,6 +311,14 @@ class OracleSimulation:
         self.o._f("sim_get_p64")(self.handle, _p(p))
         return p
 
+    def set_stir(self, st):
+        """A one-shot stir (x, y, r, dx, dy) taken by the next step."""
+        if st is None:
+            self.o._f("sim_set_stir")(self.handle, None)
+        else:
+            a = np.asarray(st, np.float64)
+            self.o._f("sim_set_stir")(self.handle, _p(a))
+
     def set_patch(self, i0, j0, pnx, pny, data):
         if data is None:
             self.o._f("sim_set_patch")(self.handle, 0, 0, 0, 0, None)

@@ -979,6 +979,9 @@ struct Simulation {
   T dt = 0;
   int iters = 0;
   double lastRelRes = -1;
+  // simulation.ts:468-472, 504: a one-shot stir taken by the next step
+  bool stirPending = false;
+  T stir[5] = {0, 0, 0, 0, 0};
 
   Simulation(int nx, int ny, int dyeScale, const StepParams& p_) : prm(p_) {
     g = {nx, ny, T(1.0 / ny)};  // simulation.ts:365, h = 1/ny
@@ -1018,6 +1021,11 @@ struct Simulation {
       advectVelocity(g, u.data(), v.data(), uNext.data(), vNext.data(), label.data(), dt);
     std::swap(u, uNext);
     std::swap(v, vNext);
+    // simulation.ts:504 — between advection and the body forces
+    if (stirPending) {
+      applyStir(g, u.data(), v.data(), label.data(), stir[0], stir[1], stir[2], stir[3], stir[4]);
+      stirPending = false;
+    }
 
     // Body forces: confinement is evaluated on the advected velocity, before
     // buoyancy changes it, then both are added (buoyancy first).

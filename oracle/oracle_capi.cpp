@@ -218,6 +218,11 @@ static StepParams toParams(const orc_params* c) {
     s->pny = data ? pny : 0;                                                                            \
     s->patch.assign(data, data ? data + (size_t)4 * pnx * pny : data);                                  \
   }                                                                                                     \
+  void orc_sim_set_stir_##SUF(void* sp, const double* st) {                                            \
+    Simulation<T>* s = (Simulation<T>*)sp;                                                              \
+    s->stirPending = st != nullptr;                                                                     \
+    for (int k = 0; k < 5; k++) s->stir[k] = st ? (T)st[k] : T(0);                                      \
+  }                                                                                                     \
   int orc_sim_step_##SUF(void* sp) { return ((Simulation<T>*)sp)->step(); }                             \
   void orc_sim_info_##SUF(void* sp, double* dt, double* time, double* relRes) {                         \
     Simulation<T>* s = (Simulation<T>*)sp;                                                              \
