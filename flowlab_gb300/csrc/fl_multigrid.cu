@@ -113,8 +113,24 @@ struct SmoothArgs {
 // (sum - scale*b) / count with count in 1..4: a multiply by the exact
 // reciprocal for 1, 2 and 4 (the same float as the division, since scaling by
 // a power of two is exact) and a true division for 3.
+//
+// The division by 3 is the correctly rounded quotient formed with two FMAs
+// (the correction step for a divisor known in advance: Markstein; Brisebarre,
+// Muller and Raina, IEEE Trans. Computers 2004): q0 = RN(s * RN(1/3)),
+// r = s - 3 q0 (exact), q = RN(q0 + r * RN(1/3)); zero and infinities take
+// q0. It equals IEEE s / 3 for every float (checked exhaustively), at a
+// fraction of the division's latency.
+__device__ __forceinline__ float div3(float s) {
+  const float y = 0x1.555556p-2f;  // RN(1/3)
+  const float q0 = __fmul_rn(s, y);
+  const float r = __fmaf_rn(-3.0f, q0, s);
+  const float q1 = __fmaf_rn(r, y, q0);
+  return (s == 0.0f || fabsf(s) == __int_as_float(0x7f800000)) ? q0 : q1;
+}
+
 __device__ __forceinline__ float over_count(float s, int cnt) {
-  return cnt == 3 ? s / 3.0f : s * (cnt == 4 ? 0.25f : (cnt == 2 ? 0.5f : 1.0f));
+  const float third = div3(s);
+  return cnt == 3 ? third : s * (cnt == 4 ? 0.25f : (cnt == 2 ? 0.5f : 1.0f));
 }
 
 // Temporally blocked red-black smoother. One 1024-thread CTA owns a 64x64
@@ -230,7 +246,8 @@ __global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs
         if (code & LINK_YP) sum += xo[lj + 1][tx];
         if (code & LINK_YM) sum += xo[lj - 1][tx];
         const float d = sum - sb[r][c];
-        const float pgs = rc[r][c] != 0.0f ? d * rc[r][c] : d / 3.0f;
+        const float third = div3(d);
+        const float pgs = rc[r][c] != 0.0f ? d * rc[r][c] : third;
         const float nv = keep * xc[r][c] + omega * pgs;
         xc[r][c] = nv;
         xs[q][lj][tx] = nv;
@@ -341,6 +358,7 @@ struct CoarseLevel {
   int off_x, off_b, off_c;  // shared-memory offsets: floats, floats, bytes
   int lsh;                  // log2 of the lanes per row
   int nwarps;               // owner warps
+  int slots;                // row groups per warp: 2 when the level has more than 32 groups
 };
 
 struct CoarseArgs {
@@ -357,11 +375,11 @@ struct CoarseArgs {
 constexpr int COARSE_SIDE = 64;
 
 struct CoarseView {
-  float* xs;  // 2 * ny * 32 floats
+  float* xs;  // 2 * ny * rs floats
   float* bs;
   const uint8_t* cs;
-  int nx, ny;
-  __device__ float& x(int i, int j) const { return xs[((i + j) & 1) * ny * 32 + j * 32 + (i >> 1)]; }
+  int nx, ny, rs;
+  __device__ float& x(int i, int j) const { return xs[((i + j) & 1) * ny * rs + j * rs + (i >> 1)]; }
 };
 
 __device__ __forceinline__ CoarseView coarse_view(unsigned char* smem, const CoarseLevel& L) {
@@ -372,6 +390,7 @@ __device__ __forceinline__ CoarseView coarse_view(unsigned char* smem, const Coa
   v.cs = smem + L.off_c;
   v.nx = L.nx;
   v.ny = L.ny;
+  v.rs = 1 << L.lsh;
   return v;
 }
 
@@ -381,41 +400,74 @@ __device__ __forceinline__ void tail_cell(const CoarseLevel& L, int w, int lane,
   i = 2 * (lane & ((1 << L.lsh) - 1)) + ((c + j) & 1);
 }
 
-// Named barrier `l + 1` over the owner warps of tail level l.
+// Named barrier `l + 1` over the owner warps of tail level l (a warp
+// barrier when one warp owns the level).
 __device__ __forceinline__ void tail_bar(int l, int nwarps) {
+  if (nwarps == 1) {
+    __syncwarp();
+    return;
+  }
   asm volatile("bar.sync %0, %1;" ::"r"(l + 1), "r"(nwarps * 32) : "memory");
 }
 
-// r = b - (count*x - sum), 0 off-fluid (pressureMultigrid.ts:117-151)
+// r = b - (count*x - sum), 0 off-fluid (pressureMultigrid.ts:117-151).
+// Branch-free for the same reason as tail_smooth: every neighbour is read
+// (an unlinked one at the cell itself) and an unlinked one adds +0.0.
 __device__ __forceinline__ float coarse_residual(const CoarseView& v, int i, int j, bool& counted) {
-  counted = false;
   const int k = i + j * v.nx;
   const uint8_t c = v.cs[k];
-  if ((c & 3u) != FLUID) return 0.0f;
   const int cnt = code_count(c);
-  if (cnt == 0) return 0.0f;
+  counted = (c & 3u) == FLUID && cnt > 0;
+  const int pl = v.ny * v.rs;
+  const int own = ((i + j) & 1) * pl + j * v.rs + (i >> 1);
+  const int oth = (1 - ((i + j) & 1)) * pl + j * v.rs;
+  const float x0 = v.xs[own];
+  const float vxp = v.xs[(c & LINK_XP) ? oth + ((i + 1) >> 1) : own];
+  const float vxm = v.xs[(c & LINK_XM) ? oth + ((i - 1) >> 1) : own];
+  const float vyp = v.xs[(c & LINK_YP) ? oth + v.rs + (i >> 1) : own];
+  const float vym = v.xs[(c & LINK_YM) ? oth - v.rs + (i >> 1) : own];
   float sum = 0.0f;
-  if (c & LINK_XP) sum += v.x(i + 1, j);
-  if (c & LINK_XM) sum += v.x(i - 1, j);
-  if (c & LINK_YP) sum += v.x(i, j + 1);
-  if (c & LINK_YM) sum += v.x(i, j - 1);
-  counted = true;
-  return v.bs[k] - ((float)cnt * v.x(i, j) - sum);
+  sum += (c & LINK_XP) ? vxp : 0.0f;
+  sum += (c & LINK_XM) ? vxm : 0.0f;
+  sum += (c & LINK_YP) ? vyp : 0.0f;
+  sum += (c & LINK_YM) ? vym : 0.0f;
+  const float r = v.bs[k] - ((float)cnt * x0 - sum);
+  return counted ? r : 0.0f;
 }
 
 // `pairs` red-black sweep pairs on tail level l by its owner warps; ends
 // with the level's barrier (also when pairs is 0). Each thread keeps its
-// cells' code, rhs, value and neighbour offsets in registers.
+// cells' rhs, value, link mask and the shared-memory addresses of their
+// four neighbours in registers. The update has no branches: on these small
+// levels most warps hold boundary cells, and a lane-divergent branch around
+// each neighbour load serialised the warp (measured: a one-warp half-sweep
+// took ~630 cycles that way, ~270 with unconditional loads). An unlinked
+// neighbour is read at the cell's own address and contributes +0.0, which
+// leaves the sum's bits unchanged: a running sum that starts at +0.0 never
+// becomes -0.0.
+__device__ __forceinline__ float lds_f32(uint32_t addr) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ void sts_f32(uint32_t addr, float v) {
+  asm volatile("st.shared.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+
 __device__ void tail_smooth(unsigned char* smem, const CoarseLevel& L, int l, int pairs, float omega, int w,
                             int lane) {
   if (w >= L.nwarps) return;
   float* xs = reinterpret_cast<float*>(smem) + L.off_x;
+  const uint32_t xs_sh = static_cast<uint32_t>(__cvta_generic_to_shared(xs));
   const float* bs = reinterpret_cast<const float*>(smem) + L.off_b;
   const uint8_t* cs = smem + L.off_c;
-  const int plane = L.ny * 32;
-  uint8_t cq[2][2];
-  int own[2][2], oth[2][2], dd[2][2];
-  float bq[2][2], xq[2][2];
+  // row stride: the lanes per row (a power of two), so that the rows a warp
+  // covers fall in distinct shared-memory banks
+  const int rs = 1 << L.lsh;
+  const int plane = L.ny * rs;
+  unsigned mask[2][2];  // bits 0-3: neighbour links; bit 4: the cell is updated
+  int own[2][2], nb[2][2][4];
+  float bq[2][2], xq[2][2], rc[2][2];
 #pragma unroll
   for (int s = 0; s < 2; s++)
 #pragma unroll
@@ -423,38 +475,59 @@ __device__ void tail_smooth(unsigned char* smem, const CoarseLevel& L, int l, in
       int i, j;
       tail_cell(L, w, lane, s, c, i, j);
       const bool ok = i < L.nx && j < L.ny;
-      cq[s][c] = ok ? cs[i + j * L.nx] : (uint8_t)CODE_OUTSIDE;
-      own[s][c] = c * plane + j * 32 + (i >> 1);
-      oth[s][c] = (1 - c) * plane + j * 32 + (i >> 1);
-      dd[s][c] = i & 1;
+      const uint8_t code = ok ? cs[i + j * L.nx] : (uint8_t)CODE_OUTSIDE;
+      const int cnt = code_count(code);
+      const bool act = ok && (code & 3u) == FLUID && cnt > 0;
+      const int ow = ok ? c * plane + j * rs + (i >> 1) : 0;
+      const int o = (1 - c) * plane + j * rs + (i >> 1), d = i & 1;
+      own[s][c] = ow;
+      nb[s][c][0] = (ok && (code & LINK_XP)) ? o + d : ow;
+      nb[s][c][1] = (ok && (code & LINK_XM)) ? o + d - 1 : ow;
+      nb[s][c][2] = (ok && (code & LINK_YP)) ? o + rs : ow;
+      nb[s][c][3] = (ok && (code & LINK_YM)) ? o - rs : ow;
+      mask[s][c] = (act ? 16u : 0u) | ((code & LINK_XP) ? 1u : 0u) | ((code & LINK_XM) ? 2u : 0u) |
+                   ((code & LINK_YP) ? 4u : 0u) | ((code & LINK_YM) ? 8u : 0u);
+      rc[s][c] = cnt == 4 ? 0.25f : (cnt == 2 ? 0.5f : (cnt == 1 ? 1.0f : 0.0f));
       bq[s][c] = ok ? bs[i + j * L.nx] : 0.0f;
-      xq[s][c] = ok ? xs[own[s][c]] : 0.0f;
+      xq[s][c] = ok ? xs[ow] : 0.0f;
     }
+  // shared-space byte addresses (explicit ld/st.shared)
+#pragma unroll
+  for (int s = 0; s < 2; s++)
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      own[s][c] = (int)(xs_sh + 4u * (uint32_t)own[s][c]);
+#pragma unroll
+      for (int k = 0; k < 4; k++) nb[s][c][k] = (int)(xs_sh + 4u * (uint32_t)nb[s][c][k]);
+    }
+  const bool two = L.slots == 2;
   const float keep = 1.0f - omega;
 #pragma unroll 1
-  for (int hs = 0; hs < 2 * pairs; hs++) {
-    const int color = hs & 1;
+  for (int hs = 0; hs < 2 * pairs; hs += 2) {
 #pragma unroll
-    for (int s = 0; s < 2; s++)
+    for (int c = 0; c < 2; c++) {
 #pragma unroll
-      for (int c = 0; c < 2; c++) {
-        if (c != color) continue;
-        const uint8_t code = cq[s][c];
-        if ((code & 3u) != FLUID) continue;
-        const int cnt = code_count(code);
-        if (cnt == 0) continue;
-        const int o = oth[s][c], d = dd[s][c];
+      for (int s = 0; s < 2; s++) {
+        if (s == 1 && !two) continue;  // warp-uniform: the level has one row group per warp
+        const unsigned m = mask[s][c];
+        const float v0 = lds_f32((uint32_t)nb[s][c][0]), v1 = lds_f32((uint32_t)nb[s][c][1]);
+        const float v2 = lds_f32((uint32_t)nb[s][c][2]), v3 = lds_f32((uint32_t)nb[s][c][3]);
         float sum = 0.0f;
-        if (code & LINK_XP) sum += xs[o + d];
-        if (code & LINK_XM) sum += xs[o + d - 1];
-        if (code & LINK_YP) sum += xs[o + 32];
-        if (code & LINK_YM) sum += xs[o - 32];
-        const float pgs = over_count(sum - (-1.0f) * bq[s][c], cnt);
+        sum += (m & 1u) ? v0 : 0.0f;
+        sum += (m & 2u) ? v1 : 0.0f;
+        sum += (m & 4u) ? v2 : 0.0f;
+        sum += (m & 8u) ? v3 : 0.0f;
+        const float dv = sum - (-1.0f) * bq[s][c];
+        const float third = div3(dv);
+        const float pgs = rc[s][c] != 0.0f ? dv * rc[s][c] : third;
         const float nv = keep * xq[s][c] + omega * pgs;
-        xq[s][c] = nv;
-        xs[own[s][c]] = nv;
+        if (m & 16u) {
+          xq[s][c] = nv;
+          sts_f32((uint32_t)own[s][c], nv);
+        }
       }
-    tail_bar(l, L.nwarps);
+      tail_bar(l, L.nwarps);
+    }
   }
   if (pairs <= 0) tail_bar(l, L.nwarps);
 }
@@ -934,12 +1007,23 @@ void launch_rms_remaining(cudaStream_t s, int nx, int ny, const float* p, const 
 }
 
 // Shared-memory layout of the single-CTA tail for levels from..end.
+// log2 of the lanes a tail level gives one row of one colour: the power of
+// two >= ceil(nx / 2); also the row stride of its parity planes.
+static int tail_lsh(int nx) {
+  int lpr = 1, lsh = 0;
+  while (lpr < (nx + 1) / 2) {
+    lpr <<= 1;
+    lsh++;
+  }
+  return lsh;
+}
+
 static size_t coarse_smem_bytes(const Engine& e, int from, int* off_x, int* off_b, int* off_c) {
   size_t floats = 0;
   for (int l = from; l < (int)e.levels.size(); l++) {
     const long n = (long)e.levels[l].nx * e.levels[l].ny;
     if (off_x) off_x[l - from] = (int)floats;
-    floats += 2 * 32 * (size_t)e.levels[l].ny;
+    floats += 2 * ((size_t)1 << tail_lsh(e.levels[l].nx)) * (size_t)e.levels[l].ny;
     if (off_b) off_b[l - from] = (int)floats;
     floats += n;
   }
@@ -1071,14 +1155,10 @@ void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc) {
     a.nlev = (int)e.levels.size() - lc;
     for (int l = 0; l < a.nlev; l++) {
       const Level& L = e.levels[lc + l];
-      int lpr = 1, lsh = 0;
-      while (lpr < (L.nx + 1) / 2) {
-        lpr <<= 1;
-        lsh++;
-      }
+      const int lsh = tail_lsh(L.nx);
       const int rows_per_warp = 32 >> lsh;
       const int groups = (L.ny + rows_per_warp - 1) / rows_per_warp;
-      a.lv[l] = CoarseLevel{L.nx, L.ny, L.code, ox[l], ob[l], oc[l], lsh, std::min(32, groups)};
+      a.lv[l] = CoarseLevel{L.nx, L.ny, L.code, ox[l], ob[l], oc[l], lsh, std::min(32, groups), groups > 32 ? 2 : 1};
     }
     a.b_top = lc == 0 ? b0 : e.levels[lc].b;
     a.x_top = e.levels[lc].x[0];
