@@ -334,8 +334,14 @@ def cnn_arm(args, local, stream_unused, flush, state0):
     net.set_params(params)
     out = {}
     try:
-        for arm in ("plain", "cnn"):
-            eng = native.Engine(g.nx, g.ny, g.h, params=prm, device=local)
+        for arm in ("plain", "cnn", "extrapolated"):
+            p_arm = prm
+            if arm == "extrapolated":
+                # the analytic second-order warm start 2 p(n) - p(n-1), for scale
+                p_arm = native.Params()
+                ctypes.pointer(p_arm)[0] = prm
+                p_arm.warm_extrapolate = 1
+            eng = native.Engine(g.nx, g.ny, g.h, params=p_arm, device=local)
             try:
                 if patch is not None:
                     eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
@@ -382,6 +388,8 @@ def cnn_arm(args, local, stream_unused, flush, state0):
     finally:
         net.close()
     out["vcycles_saved_per_step"] = out["plain"]["vcycles_per_step"] - out["cnn"]["vcycles_per_step"]
+    out["extrapolated_vcycles_saved_per_step"] = (out["plain"]["vcycles_per_step"]
+                                                  - out["extrapolated"]["vcycles_per_step"])
     out["steps"] = args.cnn_steps
     out["training"] = {k: meta[k] for k in ("pairs", "size", "batch", "lr", "train_seconds") if k in meta}
     return out

@@ -176,6 +176,8 @@ void free_all(Engine* e) {
   cudaFree(e->p64[0]);
   cudaFree(e->p64[1]);
   cudaFree(e->r32);
+  cudaFree(e->pprev32);
+  cudaFree(e->pprev64);
   cudaFree(e->ctl);
   cudaFree(e->ws_scales);
   destroy_graphs(e);
@@ -367,6 +369,11 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
   tok = prof_begin(*e, FL_PH_DIVERGENCE);
   launch_divergence(s, e->nx, e->ny, e->h, u, v, L0.b, e->prm.solver == FL_SOLVER_MG, L0.label, e->sc, e->acc);
   prof_end(*e, tok, 4 * F + N + 4 * N, 1);
+  if (e->prm.warm_extrapolate && e->prm.solver == FL_SOLVER_MG) {
+    const bool mixed = e->prm.mixed != 0;
+    launch_extrapolate(s, e->cells(), L0.label, L0.x[0], e->pprev32, mixed ? e->p64[0] : nullptr,
+                       mixed ? e->p64[1] : nullptr, e->pprev64, e->ctl);
+  }
   if (e->warm != nullptr && e->prm.solver == FL_SOLVER_MG) {
     // p_prev -> p_guess in place: the float64 pressure of the defect
     // correction, or the float32 warm start of the plain multigrid
@@ -768,6 +775,8 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   s = s ? s : dalloc(e, (void**)&e->p64[0], (size_t)e->cells() * 8, "p64");
   s = s ? s : dalloc(e, (void**)&e->p64[1], (size_t)e->cells() * 8, "p64");
   s = s ? s : dalloc(e, (void**)&e->r32, cf, "residual");
+  s = s ? s : dalloc(e, (void**)&e->pprev32, cf, "previous pressure");
+  s = s ? s : dalloc(e, (void**)&e->pprev64, (size_t)e->cells() * 8, "previous pressure");
   s = s ? s : dalloc(e, (void**)&e->ctl, sizeof(SolveCtl), "solve control");
   s = s ? s : dalloc(e, (void**)&e->ws_scales, 4 * sizeof(float), "warm-start scales");
   if (s) return bail(s);
@@ -858,6 +867,11 @@ int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, cons
     launch_convert(e->stream, e->levels[0].x[0], FL_F32, e->p64[0], FL_F64, e->cells());
   TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "upload label"));
   TRY(upload(e, e->dye[0], dye, 3 * e->dye_cells(), dtype, "upload dye"));
+  // the second-order warm start's history starts at the uploaded pressure
+  TRY(cuda_status(e, cudaMemcpyAsync(e->pprev32, e->levels[0].x[0], e->cells() * 4, cudaMemcpyDeviceToDevice,
+                                     e->stream), "previous pressure"));
+  TRY(cuda_status(e, cudaMemcpyAsync(e->pprev64, e->p64[0], e->cells() * 8, cudaMemcpyDeviceToDevice, e->stream),
+                  "previous pressure"));
   mg_build_codes(*e);
   TRY(cuda_status(e, cudaMemsetAsync(e->time_dev, 0, sizeof(double), e->stream), "clock"));
   launch_max_speed(e->stream, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);

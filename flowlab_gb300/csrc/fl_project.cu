@@ -458,4 +458,32 @@ __global__ void k_hold() {
 
 void launch_hold(cudaStream_t s) { k_hold<<<1, 1, 0, s>>>(); }
 
+// Second-order warm start (no reference counterpart): on fluid cells
+// p = p + (p - p_prev) and p_prev = the old p, in float (the plain
+// multigrid's pressure) or float64 (the defect correction's current buffer,
+// chosen by the device parity).
+__global__ void k_extrapolate(long n, const uint8_t* __restrict__ label, float* __restrict__ p32,
+                              float* __restrict__ pp32, double* __restrict__ p64a, double* __restrict__ p64b,
+                              double* __restrict__ pp64, const SolveCtl* __restrict__ ctl) {
+  double* p64 = p64a ? (ctl->par ? p64b : p64a) : nullptr;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    if (label[k] != FLUID) continue;
+    if (p64) {
+      const double t = p64[k];
+      p64[k] = t + (t - pp64[k]);
+      pp64[k] = t;
+    } else {
+      const float t = p32[k];
+      p32[k] = t + (t - pp32[k]);
+      pp32[k] = t;
+    }
+  }
+}
+
+void launch_extrapolate(cudaStream_t s, long n, const uint8_t* label, float* p32, float* pp32, double* p64a,
+                        double* p64b, double* pp64, const SolveCtl* ctl) {
+  long blocks = std::min((n + 255) / 256, 152L * 8);
+  k_extrapolate<<<(unsigned)std::max(1L, blocks), 256, 0, s>>>(n, label, p32, pp32, p64a, p64b, pp64, ctl);
+}
+
 }  // namespace fl

@@ -54,7 +54,8 @@ class Params(ctypes.Structure):
         ("mg_omega", ctypes.c_double),
         ("mixed", ctypes.c_int),
         ("rb_pairs", ctypes.c_int),
-        ("reserved", ctypes.c_int * 6),
+        ("warm_extrapolate", ctypes.c_int),
+        ("reserved", ctypes.c_int * 5),
     ]
 
 

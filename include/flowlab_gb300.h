@@ -88,7 +88,9 @@ typedef struct fl_params {
   int mixed;             /* 1: float64 fine pressure + float64 residual (defect correction) */
   int rb_pairs;          /* red-black sweep pairs per launch, 1..4 (0: 4): the temporal-blocking
                             depth, i.e. the tile/halo shape; results do not depend on it */
-  int reserved[6];
+  int warm_extrapolate;  /* 1: the multigrid starts from 2 p(n) - p(n-1) on Fluid cells instead of
+                            p(n) (no reference counterpart; pressureSolver.ts:28-30 uses p(n)) */
+  int reserved[5];
 } fl_params;
 
 /* Per-step report (the reference's sim.iters / sim.dt plus the residual the

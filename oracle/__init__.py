@@ -44,6 +44,7 @@ class Params(ctypes.Structure):
         ("mgCoarsest", ctypes.c_int),
         ("mgOmega", ctypes.c_double),
         ("mixed", ctypes.c_int),
+        ("warmExtrapolate", ctypes.c_int),
     ]
 
 
@@ -84,7 +85,8 @@ def params_from_engine(p):
                 solver=SOLVER_MG if p.solver == 1 else SOLVER_RBSOR, pressureIters=p.pressure_iters,
                 mgMaxCycles=p.mg_max_cycles, omega=p.omega, tol=p.tol, dyeDecay=tuple(p.dye_decay), beta=p.beta,
                 alpha=p.alpha, confinement=p.confinement, mgPre=p.mg_pre, mgPost=p.mg_post,
-                mgCoarseSweeps=p.mg_coarse_sweeps, mgCoarsest=p.mg_coarsest, mgOmega=p.mg_omega, mixed=p.mixed)
+                mgCoarseSweeps=p.mg_coarse_sweeps, mgCoarsest=p.mg_coarsest, mgOmega=p.mg_omega, mixed=p.mixed,
+                warmExtrapolate=p.warm_extrapolate)
 
 
 def lib():

@@ -962,6 +962,7 @@ struct StepParams {
   MgShape mg;
   int mgMaxCycles = 3;
   int mixed = 0;  // NEW: float64 pressure + defect correction around the multigrid
+  int warmExtrapolate = 0;  // NEW: the multigrid starts from 2 p(n) - p(n-1) on fluid cells
 };
 
 template <class T>
@@ -970,6 +971,8 @@ struct Simulation {
   StepParams prm;
   std::vector<T> u, v, p, div, uNext, vNext, uHat, vHat, qHat, fx, fy;
   std::vector<double> p64;  // the pressure when prm.mixed
+  std::vector<double> pPrev64;  // the previous step's pressure (warmExtrapolate, mixed)
+  std::vector<T> pPrev;         // the previous step's pressure (warmExtrapolate)
   std::vector<uint8_t> label;
   std::vector<T> dye[DYE_CHANNELS], dyeNext[DYE_CHANNELS];
   std::vector<float> patch;
@@ -993,6 +996,8 @@ struct Simulation {
     qHat.assign(nd, 0); fx.assign(n, 0); fy.assign(n, 0);
     label.assign(n, FLUID);
     p64.assign(n, 0.0);
+    pPrev64.assign(n, 0.0);
+    pPrev.assign(n, 0);
     for (int c = 0; c < DYE_CHANNELS; c++) { dye[c].assign(nd, 0); dyeNext[c].assign(nd, 0); }
     mg.shape = prm.mg;
   }
@@ -1035,6 +1040,22 @@ struct Simulation {
 
     computeDivergence(g, u.data(), v.data(), div.data());
     lastRelRes = -1;
+    // NEW: second-order warm start p(n) + (p(n) - p(n-1)) on fluid cells
+    if (prm.warmExtrapolate && prm.solver == 1) {
+      const long n = (long)g.nx * g.ny;
+      for (long k = 0; k < n; k++) {
+        if (label[k] != FLUID) continue;
+        if (prm.mixed) {
+          const double t = p64[k];
+          p64[k] = t + (t - pPrev64[k]);
+          pPrev64[k] = t;
+        } else {
+          const T t = p[k];
+          p[k] = t + (t - pPrev[k]);
+          pPrev[k] = t;
+        }
+      }
+    }
     if (prm.solver == 1 && prm.mixed) {
       iters = solveMixed(mg, g, p64.data(), div.data(), label.data(), scale, prm.mgMaxCycles, prm.tol, &lastRelRes);
       for (size_t k = 0; k < p.size(); k++) p[k] = (T)p64[k];

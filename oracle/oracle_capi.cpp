@@ -19,6 +19,7 @@ struct orc_params {
   int mgPre, mgPost, mgCoarseSweeps, mgCoarsest;
   double mgOmega;
   int mixed;
+  int warmExtrapolate;
 };
 
 int orc_abi_version(void) { return 1; }
@@ -46,6 +47,7 @@ static StepParams toParams(const orc_params* c) {
   p.mg.coarsest = c->mgCoarsest;
   p.mg.omega = c->mgOmega;
   p.mixed = c->mixed;
+  p.warmExtrapolate = c->warmExtrapolate;
   return p;
 }
 
@@ -198,6 +200,8 @@ static StepParams toParams(const orc_params* c) {
     std::copy(v, v + s->v.size(), s->v.begin());                                                       \
     std::copy(p, p + s->p.size(), s->p.begin());                                                       \
     std::copy(label, label + s->label.size(), s->label.begin());                                       \
+    std::copy(p, p + s->p.size(), s->pPrev.begin());                                                   \
+    std::copy(s->p64.begin(), s->p64.end(), s->pPrev64.begin());                                       \
     long cells = (long)s->dye[0].size();                                                                \
     for (int c = 0; c < DYE_CHANNELS; c++)                                                              \
       std::copy(dye + c * cells, dye + (c + 1) * cells, s->dye[c].begin());                             \

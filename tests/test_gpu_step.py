@@ -369,3 +369,18 @@ def test_stir_step_matches_oracle(o32):
     assert np.abs(np.asarray(base[0]) - eu).max() > 1e-3  # the stir mattered
     for a, b in ((eu, u), (ev, v)):
         assert np.abs(np.asarray(a, np.float64) - b).max() <= 1e-5 * np.abs(a).max()
+
+
+@pytest.mark.parametrize("mixed", [0, 1])
+def test_extrapolated_warm_start_matches_float32_oracle(o32, mixed):
+    """The second-order warm start 2 p(n) - p(n-1) (no reference
+    counterpart) on the float32 and the float64 pressure."""
+    g, f, patch = configs.plume(64)
+    prm = configs.plume_params(tol=1e-6 if mixed else 1e-4, max_cycles=20, mixed=mixed)
+    prm.warm_extrapolate = 1
+    u, v, p, d, st = run_engine(g, f, patch, prm, 8)
+    eu, ev, ep, ed, info = run_oracle(o32, g, f, patch, prm, 8)
+    for name, a, b in (("u", eu, u), ("v", ev, v), ("dye", ed, d)):
+        assert mismatch(a, b) == 0, "%s: %d values differ from the float32 oracle" % (name, mismatch(a, b))
+    if not mixed:
+        assert mismatch(ep, p) == 0
