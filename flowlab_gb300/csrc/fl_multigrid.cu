@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs
             if (c & LINK_YP) sum += xq[lj + 1][tx];
             if (c & LINK_YM) sum += xq[lj - 1][tx];
             res = bb[r][o] - ((float)cnt * xx[r][o] - sum);
-            rsq += (double)res * (double)res;
+            rsq = fma(f2d_exact(res), f2d_exact(res), rsq);
             rn += 1;
           }
         }
@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
           bool counted;
           const float res = coarse_residual(T, i, j, counted);
           if (counted) {
-            rsq += (double)res * (double)res;
+            rsq = fma(f2d_exact(res), f2d_exact(res), rsq);
             rn += 1;
           }
         }
@@ -646,39 +646,6 @@ __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
       atomicAdd(&a.acc->n_res, bn);
     }
   }
-}
-
-// Exact float -> double by bit manipulation (integer pipe) for zero and
-// normal floats; subnormals, infinities and NaN take the conversion
-// instruction. The result equals (double)f in every case.
-__device__ __forceinline__ double f2d_exact(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned ex = (u >> 23) & 0xffu;
-  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
-  if (ex != 0u && ex != 0xffu) {
-    const unsigned long long bits =
-        sign | ((unsigned long long)(ex + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)bits);
-  }
-  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)sign);
-  return (double)f;
-}
-
-// x * 2^k (k = 1, 2) by an exponent increment when x is normal and the
-// product stays normal; zero returns itself (as x * 2^k does); otherwise
-// the multiply. Equal to x * 2^k in every case.
-__device__ __forceinline__ double scale_pow2(double x, int k) {
-  const long long bits = __double_as_longlong(x);
-  const long long ex = (bits >> 52) & 0x7ff;
-  if (ex != 0 && ex < 0x7ff - k) return __longlong_as_double(bits + ((long long)k << 52));
-  if ((bits & 0x7fffffffffffffffll) == 0) return x;
-  return x * (double)(1 << k);
-}
-
-// 0.0 + x: x itself except that -0.0 becomes +0.0.
-__device__ __forceinline__ double zero_plus(double x) {
-  const long long bits = __double_as_longlong(x);
-  return bits == (long long)0x8000000000000000ull ? 0.0 : x;
 }
 
 // The float64 defect-correction pass (iterative refinement, solveMixed):

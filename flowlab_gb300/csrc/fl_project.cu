@@ -112,7 +112,9 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
     const float o = as_rhs ? ns * d : d;
     out[k] = o;
     if (label != nullptr && label[k] == FLUID) {
-      sq += (double)o * (double)o;
+      // one float64 operation per cell (the widening is exact on the integer pipe)
+      const double od = f2d_exact(o);
+      sq = fma(od, od, sq);
       n += 1;
     }
   }
@@ -264,7 +266,7 @@ __global__ void __launch_bounds__(256) k_scale_rhs(long n, const float* __restri
     const float o = b ? neg_scale * div[k] : div[k];
     if (b) b[k] = o;
     if (label[k] == FLUID) {
-      sq += (double)o * (double)o;
+      sq = fma(f2d_exact(o), f2d_exact(o), sq);
       cnt += 1;
     }
   }
