@@ -215,8 +215,21 @@ __global__ void __launch_bounds__(256) k_max_speed(long nu, long nv, const float
   __shared__ float red[32];
   float m = 0.0f;
   const long stride = (long)gridDim.x * blockDim.x;
-  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < nu; k += stride) m = smax(m, fabsf(u[k]));
-  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < nv; k += stride) m = smax(m, fabsf(v[k]));
+  const long t0 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  // 16-byte loads over the aligned body of each array (the max does not
+  // depend on the order), the few trailing faces one by one
+  const float4* u4 = reinterpret_cast<const float4*>(u);
+  const float4* v4 = reinterpret_cast<const float4*>(v);
+  for (long k = t0; k < nu / 4; k += stride) {
+    const float4 q = u4[k];
+    m = smax(m, smax(smax(fabsf(q.x), fabsf(q.y)), smax(fabsf(q.z), fabsf(q.w))));
+  }
+  for (long k = t0; k < nv / 4; k += stride) {
+    const float4 q = v4[k];
+    m = smax(m, smax(smax(fabsf(q.x), fabsf(q.y)), smax(fabsf(q.z), fabsf(q.w))));
+  }
+  for (long k = 4 * (nu / 4) + t0; k < nu; k += stride) m = smax(m, fabsf(u[k]));
+  for (long k = 4 * (nv / 4) + t0; k < nv; k += stride) m = smax(m, fabsf(v[k]));
   float bm = block_max(m, red);
   __shared__ bool last;
   if (threadIdx.x == 0) {
