@@ -128,6 +128,60 @@ __global__ void __launch_bounds__(CT* CT) k_conv3(const TI* __restrict__ x, int 
   }
 }
 
+// The input layer (3 channels in, 32 out): 27 inputs per pixel held in
+// registers, the 27 x 32 weights in shared memory read four output channels
+// at a time; the generic kernel's 8-channel chunks would be 5/8 empty here.
+__global__ void __launch_bounds__(CT* CT) k_conv3_in3(const __nv_bfloat16* __restrict__ x, int H, int W,
+                                                       const __nv_bfloat16* __restrict__ w,
+                                                       const float* __restrict__ bias, __nv_bfloat16* __restrict__ y) {
+  constexpr int CI = 3, CO = 32;
+  __shared__ float xs[CI][CT + 2][CT + 3];
+  __shared__ __align__(16) float ws[9 * CI][CO];
+  const int tx = threadIdx.x % CT, ty = threadIdx.x / CT;
+  const int tiles_x = (W + CT - 1) / CT;
+  const int X0 = (blockIdx.x % tiles_x) * CT, Y0 = (blockIdx.x / tiles_x) * CT;
+  const long img = (long)blockIdx.y * H * W;
+  for (int e = threadIdx.x; e < CI * (CT + 2) * (CT + 2); e += CT * CT) {
+    const int ci = e % CI, r = e / CI, lx = r % (CT + 2), ly = r / (CT + 2);
+    const int gx = X0 + lx - 1, gy = Y0 + ly - 1;
+    float v = 0.0f;
+    if (gx >= 0 && gy >= 0 && gx < W && gy < H) v = __bfloat162float(x[(img + (long)gy * W + gx) * CI + ci]);
+    xs[ci][ly][lx] = v;
+  }
+  for (int e = threadIdx.x; e < 9 * CI * CO; e += CT * CT) {
+    const int co = e % CO, k = e / CO;  // k = tap * CI + ci, the weights' [ky][kx][ci] order
+    ws[k][co] = __bfloat162float(w[(long)co * 9 * CI + k]);
+  }
+  __syncthreads();
+  float acc[CO];
+#pragma unroll
+  for (int c = 0; c < CO; c++) acc[c] = 0.0f;
+#pragma unroll
+  for (int tap = 0; tap < 9; tap++) {
+#pragma unroll
+    for (int ci = 0; ci < CI; ci++) {
+      const float xv = xs[ci][ty + tap / 3][tx + tap % 3];
+      const float4* wv = reinterpret_cast<const float4*>(ws[tap * CI + ci]);
+#pragma unroll
+      for (int q = 0; q < CO / 4; q++) {
+        const float4 f = wv[q];
+        acc[4 * q + 0] = __fmaf_rn(xv, f.x, acc[4 * q + 0]);
+        acc[4 * q + 1] = __fmaf_rn(xv, f.y, acc[4 * q + 1]);
+        acc[4 * q + 2] = __fmaf_rn(xv, f.z, acc[4 * q + 2]);
+        acc[4 * q + 3] = __fmaf_rn(xv, f.w, acc[4 * q + 3]);
+      }
+    }
+  }
+  const int gx = X0 + tx, gy = Y0 + ty;
+  if (gx >= W || gy >= H) return;
+  __align__(16) __nv_bfloat16 o[CO];
+#pragma unroll
+  for (int c = 0; c < CO; c++) o[c] = __float2bfloat16_rn(fmaxf(acc[c] + bias[c], 0.0f));
+  uint4* dst = reinterpret_cast<uint4*>(y + (img + (long)gy * W + gx) * CO);
+#pragma unroll
+  for (int q = 0; q < CO / 8; q++) dst[q] = reinterpret_cast<const uint4*>(o)[q];
+}
+
 // W'[ci][2-ky][2-kx][co] = W[co][ky][kx][ci]: the data gradient of a 3x3
 // convolution is the convolution of the output gradient with W'.
 __global__ void k_flip_weights(const __nv_bfloat16* __restrict__ w, int Cin, int Cout,
@@ -425,6 +479,11 @@ void Unet::release() {
 void Unet::conv_fwd(cudaStream_t s, int l, const __nv_bfloat16* x, int B, int H, int W, __nv_bfloat16* y) {
   const UnetLayer& L = kUnetLayers[l];
   if (unet_tc_conv_fwd(s, x, B, H, W, L.cin, theta16 + woff[l], theta + boff[l], L.cout, y)) return;
+  if (L.cin == 3 && L.cout == 32 && L.k == 3) {
+    dim3 g((unsigned)(((W + CT - 1) / CT) * ((H + CT - 1) / CT)), (unsigned)B);
+    k_conv3_in3<<<g, CT * CT, 0, s>>>(x, H, W, theta16 + woff[l], theta + boff[l], y);
+    return;
+  }
   dim3 g((unsigned)(((W + CT - 1) / CT) * ((H + CT - 1) / CT)), (unsigned)(B * ((L.cout + CO_T - 1) / CO_T)));
   k_conv3<__nv_bfloat16, EPI_ACT><<<g, CT * CT, 0, s>>>(x, H, W, L.cin, theta16 + woff[l], theta + boff[l], L.cout, y,
                                                         nullptr, nullptr);
