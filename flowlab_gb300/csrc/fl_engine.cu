@@ -304,19 +304,22 @@ bool solve_on_device(const Engine* e) { return e->prm.solver == FL_SOLVER_MG || 
 // Writes the solve parameters into the device control block. The float64
 // buffer parity is state, not a parameter: it is kept unless reset_par.
 int put_ctl(Engine* e, int mode, double tol, int max_cycles, bool reset_par) {
-  TRY(cuda_status(e, cudaMemcpyAsync(e->ctl_host, e->ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, e->stream),
-                  "read solve state"));
-  TRY(sync(e, "read solve state"));
+  int par = 0;
+  if (!reset_par) {
+    TRY(cuda_status(e, cudaMemcpyAsync(e->ctl_host, e->ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, e->stream),
+                    "read solve state"));
+    TRY(sync(e, "read solve state"));
+    par = e->ctl_host->par;
+  }
   SolveCtl c{};
   c.tol = tol;
   c.max_cycles = max_cycles;
   c.mode = mode;
   c.rel = -1;
-  c.par = reset_par ? 0 : e->ctl_host->par;
-  *e->ctl_host = c;
-  TRY(cuda_status(e, cudaMemcpyAsync(e->ctl, e->ctl_host, sizeof(SolveCtl), cudaMemcpyHostToDevice, e->stream),
-                  "solve state"));
-  return sync(e, "solve state");
+  c.par = par;
+  // a pageable source is staged before the call returns: no synchronisation
+  return cuda_status(e, cudaMemcpyAsync(e->ctl, &c, sizeof(SolveCtl), cudaMemcpyHostToDevice, e->stream),
+                     "solve state");
 }
 
 bool step_mixed(const Engine* e) { return e->prm.solver == FL_SOLVER_MG && e->prm.mixed; }
@@ -1003,19 +1006,14 @@ int fl_read_pressure(fl_engine* h, int dtype, void* p) {
   ENTER(h);
   if (step_mixed(e) && e->uploaded) {
     if (!p) return fail(e, FL_EINVAL, "read p: null pointer");
+    if (dtype != FL_F32 && dtype != FL_F64) return fail(e, FL_EINVAL, "read p: dtype %d", dtype);
     const long n = e->cells();
-    TRY(read_ctl(e));
-    const double* p64 = e->p64[e->ctl_host->par];
-    if (dtype == FL_F64) {
-      TRY(cuda_status(e, cudaMemcpyAsync(p, p64, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream), "read p"));
-    } else if (dtype == FL_F32) {
-      launch_convert(e->stream, p64, FL_F64, e->staging, FL_F32, n);
-      TRY(check_launch(e, "read p"));
-      TRY(cuda_status(e, cudaMemcpyAsync(p, e->staging, n * sizeof(float), cudaMemcpyDeviceToHost, e->stream),
-                      "read p"));
-    } else {
-      return fail(e, FL_EINVAL, "read p: dtype %d", dtype);
-    }
+    // the current float64 buffer is chosen on the device (no parity round trip)
+    launch_select_p64(e->stream, e->ctl, e->p64[0], e->p64[1], e->staging, dtype == FL_F64, n);
+    TRY(check_launch(e, "read p"));
+    TRY(cuda_status(e, cudaMemcpyAsync(p, e->staging, n * (dtype == FL_F64 ? sizeof(double) : sizeof(float)),
+                                       cudaMemcpyDeviceToHost, e->stream),
+                    "read p"));
     return sync(e, "read pressure");
   }
   TRY(download(e, p, e->levels[0].x[0], e->cells(), dtype, "read p"));

@@ -169,6 +169,8 @@ void launch_stir(cudaStream_t s, int nx, int ny, float h, float* u, float* v, co
 void launch_dye_patch(cudaStream_t s, int dnx, int dny, float* dye, const float* patch, int pi0, int pj0, int pnx,
                       int pny);
 void launch_hold(cudaStream_t s);
+void launch_select_p64(cudaStream_t s, const SolveCtl* ctl, const double* p64a, const double* p64b, void* out,
+                       bool as_f64, long n);
 void launch_extrapolate(cudaStream_t s, long n, const uint8_t* label, float* p32, float* pp32, double* p64a,
                         double* p64b, double* pp64, const SolveCtl* ctl);
 void launch_convert(cudaStream_t s, const void* src, int src_dtype, void* dst, int dst_dtype, long n);

@@ -501,4 +501,22 @@ void launch_extrapolate(cudaStream_t s, long n, const uint8_t* label, float* p32
   k_extrapolate<<<(unsigned)std::max(1L, blocks), 256, 0, s>>>(n, label, p32, pp32, p64a, p64b, pp64, ctl);
 }
 
+// out = p64[ctl->par] as float64 or rounded to float32.
+__global__ void k_select_p64(const SolveCtl* __restrict__ ctl, const double* __restrict__ p64a,
+                             const double* __restrict__ p64b, void* __restrict__ out, int as_f64, long n) {
+  const double* src = ctl->par ? p64b : p64a;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    if (as_f64)
+      static_cast<double*>(out)[k] = src[k];
+    else
+      static_cast<float*>(out)[k] = (float)src[k];
+  }
+}
+
+void launch_select_p64(cudaStream_t s, const SolveCtl* ctl, const double* p64a, const double* p64b, void* out,
+                       bool as_f64, long n) {
+  long blocks = std::min((n + 255) / 256, 152L * 8);
+  k_select_p64<<<(unsigned)std::max(1L, blocks), 256, 0, s>>>(ctl, p64a, p64b, out, as_f64, n);
+}
+
 }  // namespace fl
