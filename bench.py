@@ -42,18 +42,25 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = None
-BASELINE_PATH = os.path.join(ROOT, "BASELINE.json")
+# The headline metric: steps/s of the 1024^2 plume solved to a 1e-6 relative
+# residual, plain multigrid against the U-Net warm start, with HBM GB/s.
+METRIC = "steps/s at 1024\u00b2 to 1e-6 residual: plain MG vs CNN warm-start MG; HBM GB/s"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
 
 def baseline_metric():
-    try:
-        with open(BASELINE_PATH) as fh:
-            return json.load(fh)["metric"]
-    except Exception:
-        return "steps/s at 1024^2 to 1e-6 relative residual (plain multigrid)"
+    return METRIC
+
+
+# What bounds each phase's kernels at 1024^2 when it is not HBM (ncu summaries
+# under profiles/): the roofline line names it beside the HBM fraction.
+LIMITERS = {
+    "defect64": "float64 pipe (ncu: 71-74% of peak float64 issue), not memory",
+    "mg_coarse": "latency: one CTA, a chain of dependent barrier phases",
+    "mg_pre": "latency: small levels, few CTAs per launch",
+    "mg_post": "latency: small levels, few CTAs per launch",
+}
 
 
 def bf16_peak():
@@ -512,7 +519,8 @@ def run_ours(args, world, rank, local, pg):
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
                 "algorithmic_bytes_per_launch": d["gbytes"] * 1e9 / d["launches"],
-                "avg_launch_us": 1000.0 * d["ms"] / d["launches"]}
+                "avg_launch_us": 1000.0 * d["ms"] / d["launches"],
+                "limiter": LIMITERS.get(dom, "instruction issue (working set resident in L2)")}
     # Launches in the timed region: the profiled steps give the launches per
     # V-cycle (smoothers, coarse tail, float64 update, cycle test) and per
     # step (the rest); the timed steps' own cycle counts scale them.

@@ -656,7 +656,7 @@ struct Multigrid {
 };
 
 // NEW — float64 defect correction (iterative refinement) around the float32
-// multigrid (SURVEY a13): the pressure is kept in double; each outer pass
+// multigrid: the pressure is kept in double; each outer pass
 // forms the residual r = b - A p in double (b = float32 rhs, neighbour sum
 // in the order +x, -x, +y, -y), runs ONE float32 V-cycle on A e = float(r)
 // from e = 0, and adds e back in double. The relative residual is
