@@ -13,9 +13,10 @@ advection with decay and inlet, CFL reduction.
   value   steps/s over K timed steps, fields resident in HBM, L2 flushed
           (a 320 MB write) before every timed step, CUDA events on the
           engine's stream; whole job = N ranks x K steps / max rank time.
-  e2e     the same steps through the C ABI with host buffers: every step
-          uploads u, v, p, label, dye from pinned host memory, steps, and
-          reads u, v, p, dye back.
+  e2e     the same steps through the C ABI with host buffers, as the
+          GpuStep seam runs them with invalidate() before every step: upload
+          u, v, p, label and dye from pinned host memory, step, read u and v
+          back (stepGpu.ts:521-522, 591-592: p and dye stay on the device).
   roofline  the phase with the most device time, algorithmic bytes / its
           event-timed duration, against MEASURED_PEAKS.json's HBM copy rate.
           Timed steps run as one CUDA graph each (the V-cycle loop is a
@@ -46,6 +47,8 @@ sys.path.insert(0, ROOT)
 # residual, plain multigrid against the U-Net warm start, with HBM GB/s.
 METRIC = "steps/s at 1024\u00b2 to 1e-6 residual: plain MG vs CNN warm-start MG; HBM GB/s"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+REF_WARMUP = 2       # the CPU reference arm's warm-up steps at most
+REF_BUDGET_S = 60.0  # and its timed seconds (about)
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -82,7 +85,8 @@ def hbm_peak():
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 1000 plume, 200 turbulence, 10 batch)")
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["plume", "turbulence", "batch"], default="plume",
@@ -101,6 +105,8 @@ def parse():
     ap.add_argument("--cnn-weights", default=None, help="U-Net parameters (.npz); default: the packaged ones")
     args = ap.parse_args()
     plume = args.workload == "plume"
+    if args.steps is None:
+        args.steps = {"plume": 1000, "turbulence": 200, "batch": 10}[args.workload]
     if args.size is None:
         args.size = 1024 if plume else 2048
     if args.tol is None:
@@ -127,7 +133,7 @@ def workload(args):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons, sampled every 100 ms."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -142,7 +148,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
             return
@@ -220,10 +226,12 @@ def max_over_ranks(pg, x):
 
 # ------------------------------------------------------------- CPU port
 
-def cpu_port_steps(args, steps, warmup, state=None):
+def cpu_port_steps(args, steps, warmup, state=None, budget_s=None):
     """Times `steps` steps of the float64 CPU port (the oracle's Simulation)
     on the selected workload, after `warmup` untimed steps from `state` (host
-    fields) or from the reset scene. Returns (steps/s, seconds)."""
+    fields) or from the reset scene; with `budget_s`, the timed loop stops
+    after the first step that ends past that many seconds. Returns
+    (steps/s, seconds, steps timed)."""
     from oracle import Oracle, params_from_engine as oracle_params
 
     g, f, patch, prm = workload(args)
@@ -238,10 +246,14 @@ def cpu_port_steps(args, steps, warmup, state=None):
     for _ in range(warmup):
         sim.step()
     t = time.perf_counter()
-    for _ in range(steps):
+    done = 0
+    while done < steps:
         sim.step()
+        done += 1
+        if budget_s is not None and time.perf_counter() - t > budget_s:
+            break
     dt = time.perf_counter() - t
-    return steps / dt, dt
+    return done / dt, dt, done
 
 
 def run_reference_batch(args):
@@ -285,11 +297,15 @@ def run_reference(args, world, rank, pg):
         return
     if args.workload == "batch":
         return run_reference_batch(args)
-    sps, secs = cpu_port_steps(args, args.steps, args.warmup)
-    sample = "%d steps (after %d warm-up steps from the reset scene) of the %d^2 %s, float64 CPU port of " \
-             "the reference's Simulation.step, one thread" % (args.steps, args.warmup, args.size, workload_name(args))
-    line = {"metric": metric, "value": sps, "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 / sps, "higher_is_better": True, "scaling": "weak",
+    # bounded: at most REF_WARMUP warm-up steps and REF_BUDGET_S seconds of
+    # timed steps, whatever --steps / --warmup ask for
+    warm = min(args.warmup, REF_WARMUP)
+    sps, secs, done = cpu_port_steps(args, args.steps, warm, budget_s=REF_BUDGET_S)
+    sample = "%d of %d requested steps (%.1f s, after %d warm-up steps from the reset scene) of the %d^2 %s, " \
+             "float64 CPU port of the reference's Simulation.step, one thread" % (
+                 done, args.steps, secs, warm, args.size, workload_name(args))
+    line = {"metric": metric, "value": sps, "unit": "steps/s", "n_gpus": args.gpus, "steps": done,
+            "warmup": warm, "ms_per_step": 1000.0 / sps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(args), "impl": "reference",
             "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
@@ -491,18 +507,16 @@ def run_ours(args, world, rank, local, pg):
         eng.call("fl_upload_fields", native.FL_F32, ptr(hu), ptr(hv), ptr(hp), ptr(hl), ptr(hd))
         eng.call("fl_step_auto", 1, ctypes.byref(iters))
         eng.call("fl_read_velocity", native.FL_F32, ptr(hu), ptr(hv))
-        eng.call("fl_read_pressure", native.FL_F32, ptr(hp))
-        eng.call("fl_read_dye", native.FL_F32, ptr(hd))
     e2e_s = max_over_ranks(pg, time.perf_counter() - te)
     e2e_value = world * args.e2e_steps / e2e_s
     h2d = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len) + eng.cells
-    d2h = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len)
+    d2h = 4 * (eng.ufaces + eng.vfaces)
 
     cnn = cnn_arm(args, local, stream, flush, state0=(f, patch)) if args.cnn_steps > 0 else None
 
     cpu = None
     if rank == 0 and args.cpu_steps > 0:
-        sps, secs = cpu_port_steps(args, args.cpu_steps, 0, state)
+        sps, secs, _ = cpu_port_steps(args, args.cpu_steps, 0, state)
         cpu = {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
                "sample": "%d steps of the %d^2 %s continuing from the GPU's warmed-up state, float64 CPU "
                          "port of the reference's Simulation.step, one thread (%.1f s)"

@@ -442,7 +442,7 @@ int Unet::alloc(long max_pixels, std::string* err) {
   }
   bool ok = A((void**)&theta, nparam * 4, "weights") && A((void**)&m, nparam * 4, "adam m") &&
             A((void**)&v, nparam * 4, "adam v") && A((void**)&grad, nparam * 4, "gradient") &&
-            A((void**)&theta16, nparam * 2, "bf16 weights") && A((void**)&wflip, 9L * 224 * 96 * 2, "flipped weights") &&
+            A((void**)&theta16, nparam * 2, "bf16 weights") && A((void**)&wimg, nparam * 2, "weight images") && A((void**)&wflip, 9L * 224 * 96 * 2, "flipped weights") &&
             A((void**)&loss_dev, sizeof(double), "loss");
   if (!ok) return FL_ENOMEM;
   const long P = max_pixels;
@@ -470,7 +470,7 @@ int Unet::alloc(long max_pixels, std::string* err) {
 }
 
 void Unet::release() {
-  void* ps[] = {theta, m, v, grad, theta16, wflip, loss_dev, gbuf[0], gbuf[1], gskip[0], gskip[1], gskip[2], gpool,
+  void* ps[] = {theta, m, v, grad, theta16, wimg, wflip, loss_dev, gbuf[0], gbuf[1], gskip[0], gskip[1], gskip[2], gpool,
                 out, dout, target, mask, input, ws_acc};
   for (void* p : ps) cudaFree(p);
   for (auto* a : act) cudaFree(a);
@@ -478,7 +478,7 @@ void Unet::release() {
 
 void Unet::conv_fwd(cudaStream_t s, int l, const __nv_bfloat16* x, int B, int H, int W, __nv_bfloat16* y) {
   const UnetLayer& L = kUnetLayers[l];
-  if (unet_tc_conv_fwd(s, x, B, H, W, L.cin, theta16 + woff[l], theta + boff[l], L.cout, y)) return;
+  if (unet_tc_conv_fwd(s, x, B, H, W, L.cin, theta16 + woff[l], wimg + woff[l], theta + boff[l], L.cout, y)) return;
   if (L.cin == 3 && L.cout == 32 && L.k == 3) {
     dim3 g((unsigned)(((W + CT - 1) / CT) * ((H + CT - 1) / CT)), (unsigned)B);
     k_conv3_in3<<<g, CT * CT, 0, s>>>(x, H, W, theta16 + woff[l], theta + boff[l], y);
@@ -577,9 +577,22 @@ void Unet::adam(cudaStream_t s, float lr) {
   const float b1 = 0.9f, b2 = 0.999f;
   const float c1 = 1.0f - std::pow(b1, (float)step_count), c2 = 1.0f - std::pow(b2, (float)step_count);
   k_adam<<<grid_for(nparam), 256, 0, s>>>(theta, m, v, grad, nparam, lr, b1, b2, c1, c2, 1e-8f, theta16);
+  refresh_weight_images(s);
 }
 
-void Unet::refresh_bf16(cudaStream_t s) { k_to_bf16<<<grid_for(nparam), 256, 0, s>>>(theta, nparam, theta16); }
+void Unet::refresh_bf16(cudaStream_t s) {
+  k_to_bf16<<<grid_for(nparam), 256, 0, s>>>(theta, nparam, theta16);
+  refresh_weight_images(s);
+}
+
+// The halo-form tensor-core convolutions read their weights as per-chunk
+// images (all 9 taps' B tiles of 32 input channels, contiguous).
+void Unet::refresh_weight_images(cudaStream_t s) {
+  for (int l = 0; l < UNET_LAYERS; l++) {
+    const UnetLayer& L = kUnetLayers[l];
+    if (L.k == 3 && L.cin % 32 == 0) unet_tc_weight_image(s, theta16 + woff[l], L.cin, L.cout, wimg + woff[l]);
+  }
+}
 
 // ------------------------------------------------------------- warm start
 

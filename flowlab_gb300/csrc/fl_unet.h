@@ -32,6 +32,7 @@ struct Unet {
   float* grad = nullptr;
   __nv_bfloat16* theta16 = nullptr;  // bf16 copies used by the kernels
   __nv_bfloat16* wflip = nullptr;    // flipped/transposed weights of one layer
+  __nv_bfloat16* wimg = nullptr;     // tensor-core weight images (offsets woff)
   double* loss_dev = nullptr;
   __nv_bfloat16* act[ACT_COUNT] = {};
   long act_size[ACT_COUNT] = {};
@@ -54,6 +55,7 @@ struct Unet {
   void loss(cudaStream_t s, long P, float inv_n);
   void adam(cudaStream_t s, float lr);
   void refresh_bf16(cudaStream_t s);
+  void refresh_weight_images(cudaStream_t s);
   void conv_fwd(cudaStream_t s, int l, const __nv_bfloat16* x, int B, int H, int W, __nv_bfloat16* y);
   void conv_bwd(cudaStream_t s, int l, const __nv_bfloat16* x, const float* g, int B, int H, int W, float* gx,
                 const __nv_bfloat16* act_x);
@@ -63,10 +65,16 @@ struct Unet {
 // false (and launches nothing) when the shape is not covered or the
 // tensor-core path is switched off, in which case the caller runs the
 // CUDA-core kernel.
+// w: [Cout][3][3][Cin]; wimg: the same weights arranged by
+// unet_tc_weight_image (read by the halo form).
 bool unet_tc_conv_fwd(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* w,
-                      const float* bias, int Cout, __nv_bfloat16* y);
+                      const __nv_bfloat16* wimg, const float* bias, int Cout, __nv_bfloat16* y);
+void unet_tc_weight_image(cudaStream_t s, const __nv_bfloat16* w, int Cin, int Cout, __nv_bfloat16* img);
 void unet_tc_setup();
 void unet_tc_enable(bool on);
+// true: the halo form (TMA halo tiles) where it applies; false: always the
+// chunked-gather form
+void unet_tc_halo(bool on);
 bool unet_tc_enabled();
 // Nonzero (and cleared) when a tensor-core launch gave up a bounded wait.
 int unet_tc_take_error();

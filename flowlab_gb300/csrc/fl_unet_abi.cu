@@ -194,8 +194,10 @@ int fl_unet_train_step(fl_unet* h, int B, int H, int W, const float* x, const fl
   return FL_OK;
 }
 
-int fl_unet_use_tensor_cores(int on) {
-  unet_tc_enable(on != 0);
+int fl_unet_use_tensor_cores(int mode) {
+  if (mode < 0 || mode > 2) return ufail(nullptr, FL_EINVAL, "tensor-core mode %d", mode);
+  unet_tc_enable(mode != 0);
+  unet_tc_halo(mode == 1);
   return FL_OK;
 }
 

@@ -19,6 +19,9 @@
 // for what it issued, frees its TMEM and returns.
 #include <cstdint>
 
+#include <cuda.h>  // CUtensorMap and its enums; the encoder is fetched through the runtime
+#include <cudaTypedefs.h>
+
 #include "fl_internal.h"
 #include "fl_unet.h"
 
@@ -27,6 +30,7 @@ namespace fl {
 namespace {
 
 bool g_tc_on = true;
+bool g_tc_halo = true;  // the halo form where it applies; false: the chunked-gather form
 
 constexpr int TM = 128;      // pixels per CTA (the MMA's M)
 constexpr int KC = 32;       // input channels per chunk
@@ -255,7 +259,229 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
   }
 }
 
+// ---------------------------------------------------------------- halo form
+//
+// The main forward form. A CTA computes TR image rows x 128 columns of one
+// image (TR accumulators of 128 pixels x N channels in TMEM). Per chunk of
+// 32 input channels it loads, once, the (TR+2) x 130 pixel halo of the tile
+// with four TMA tensor loads (one per 8-channel group; zero fill outside
+// the image) into four "planes" [halo row][halo column][8 channels] of
+// 16-byte rows, and the chunk's weights for all 9 taps with one bulk copy
+// of a pre-arranged weight image. In a plane the pixels sit 16 bytes apart,
+// which is the no-swizzle K-major layout with its 8-row groups 128 bytes
+// apart; so the A operand of tap (ky, kx) for output row r is the same
+// halo with the descriptor's start moved by ((r + ky) * 130 + kx) * 16
+// bytes. No tap is re-gathered: per chunk the tensor core runs 9 x TR x 2
+// MMAs (128 x N x 16) from one copy of the halo.
+//
+// Roles: thread 0 issues the copies into a ring of 1 or 2 stages (waiting
+// on the stage's "empty" barrier, which the MMAs' commit arrives on), lane 0
+// of warp 1 issues the MMAs once a stage's "full" barrier (transaction
+// bytes) completes, warp 2 owns the TMEM allocation, and all four warps run
+// the epilogue (bias, ReLU, bf16 NHWC) after the last commit. Every wait is
+// bounded; before the CTA ends every copy it issued has landed and every
+// MMA has completed.
+constexpr int HALO_TW = 128;            // output columns per tile (the MMA's M)
+constexpr int HALO_W = HALO_TW + 2;     // halo columns
+constexpr int HALO_SMEM_MAX = 227 * 1024;
+
+__host__ __device__ constexpr int halo_plane_bytes(int tr) { return ((tr + 2) * HALO_W * 16 + 127) / 128 * 128; }
+__host__ __device__ constexpr int halo_stage_bytes(int tr, int n) { return 4 * halo_plane_bytes(tr) + 9 * n * 64; }
+constexpr int HALO_BAR_BYTES = 64;  // 2 full + 2 empty + done barriers and the TMEM slot
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(128) k_conv3_halo(const __grid_constant__ CUtensorMap xmap, int H, int W,
+                                                    const __nv_bfloat16* __restrict__ wimg,
+                                                    const float* __restrict__ bias, int N, int nchunks, int TR,
+                                                    int stages, int ns, int ncols, __nv_bfloat16* __restrict__ y) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int plane = halo_plane_bytes(TR);
+  const int stage_a = 4 * plane;
+  const int stage_b = 9 * N * 64;
+  const int stage_bytes = stage_a + stage_b;
+  // bytes the copies of one stage deliver (a box counts in full, zero-filled
+  // parts included; the planes' tails past the box are padding)
+  const uint32_t tx_bytes = (uint32_t)(4 * (TR + 2) * HALO_W * 16 + stage_b);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + stages * stage_bytes);
+  uint64_t* empty = full + 2;
+  uint64_t* done = empty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int x0 = blockIdx.x * HALO_TW, y0 = blockIdx.y * TR, img = blockIdx.z;
+
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int q = 0; q < 2; q++) {
+      mbar_init(smem_u32(&full[q]), 1);
+      mbar_init(smem_u32(&empty[q]), 1);
+    }
+    mbar_init(smem_u32(done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  bool failed = false;
+
+  if (tid == 0) {
+    // ---- copies
+    int armed[2] = {0, 0};
+    for (int c = 0; c < nchunks; c++) {
+      const int s = stages == 2 ? (c & 1) : 0;
+      const int use = stages == 2 ? (c >> 1) : c;  // earlier uses of this stage
+      if (use > 0 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((use - 1) & 1))) {
+        failed = true;
+        break;
+      }
+      unsigned char* st = smem + s * stage_bytes;
+      const uint32_t fb = smem_u32(&full[s]);
+      mbar_expect_tx(fb, tx_bytes);
+#pragma unroll
+      for (int g = 0; g < 4; g++) tma_load_4d(smem_u32(st + g * plane), &xmap, c * 32 + 8 * g, x0 - 1, y0 - 1, img, fb);
+      bulk_load(smem_u32(st + stage_a), wimg + (long)c * 9 * 32 * N, (uint32_t)stage_b, fb);
+      armed[s]++;
+    }
+    // nothing issued may still be landing when the CTA ends
+    for (int s = 0; s < stages; s++)
+      if (armed[s] > 0 && !mbar_wait(smem_u32(&full[s]), (uint32_t)((armed[s] - 1) & 1))) failed = true;
+  } else if (tid == 32) {
+    // ---- MMAs
+    const uint32_t idesc = instr_desc(HALO_TW, N);
+    const uint32_t lbo_b = (uint32_t)N * 16;
+    for (int c = 0; c < nchunks; c++) {
+      const int s = stages == 2 ? (c & 1) : 0;
+      const int use = stages == 2 ? (c >> 1) : c;
+      if (!mbar_wait(smem_u32(&full[s]), (uint32_t)(use & 1))) {
+        failed = true;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(smem + s * stage_bytes), b0 = a0 + (uint32_t)stage_a;
+      for (int t = 0; t < 9; t++) {
+        const int ky = t / 3, kx = t % 3;
+        const uint32_t bt = b0 + (uint32_t)(t * N * 64);
+        for (int r = 0; r < TR; r++) {
+          const uint32_t at = a0 + 16u * (uint32_t)((r + ky) * HALO_W + kx);
+#pragma unroll
+          for (int kk = 0; kk < 2; kk++) {
+            const uint64_t ad = smem_desc(at + (uint32_t)(kk * 2 * plane), (uint32_t)plane, 128);
+            const uint64_t bd = smem_desc(bt + kk * 2 * lbo_b, lbo_b, 128);
+            mma_bf16(tmem + (uint32_t)(r * ns), ad, bd, idesc, (c > 0 || t > 0 || kk > 0) ? 1u : 0u);
+          }
+        }
+      }
+      mma_commit(smem_u32(&empty[s]));
+    }
+    // arrives when every MMA issued above has completed (also after a failed wait)
+    mma_commit(smem_u32(done));
+  }
+  __syncwarp();
+  if (!mbar_wait(smem_u32(done), 0u)) failed = true;
+  failed = __syncthreads_or(failed) != 0;
+  tc_fence_after();
+  if (failed) {
+    if (tid == 0) atomicExch(&g_tc_error, 1);
+  } else {
+    // TMEM lane = A row = output column x0 + tid; tcgen05.ld is warp-collective
+    const int x = x0 + tid;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int r = 0; r < TR; r++) {
+      const int yy = y0 + r;
+      const bool ok = x < W && yy < H;
+      __nv_bfloat16* out = y + (((long)img * H + (ok ? yy : 0)) * W + (ok ? x : 0)) * N;
+      for (int c = 0; c < N; c += 16) {
+        float v[16];
+        tmem_ld16(lane_base + (uint32_t)(r * ns + c), v);
+        if (ok) {
+          __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+          for (int k = 0; k < 16; k++) o[k] = __float2bfloat16_rn(fmaxf(v[k] + bias[c + k], 0.0f));
+          reinterpret_cast<uint4*>(out + c)[0] = reinterpret_cast<const uint4*>(o)[0];
+          reinterpret_cast<uint4*>(out + c)[1] = reinterpret_cast<const uint4*>(o)[1];
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 2) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+  }
+}
+
+// Weight image of one layer for the halo form: per 32-channel chunk c, per
+// tap t, per 8-channel group g, per output channel n, 8 channels:
+// img[(((c * 9 + t) * 4 + g) * N + n) * 8 + j] = w[(n * 9 + t) * Cin + 32c + 8g + j]
+// — the shared-memory B tiles of all 9 taps of a chunk, contiguous.
+__global__ void k_weight_image(const __nv_bfloat16* __restrict__ w, int Cin, int N, __nv_bfloat16* __restrict__ img) {
+  const long total = 9L * Cin * N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int j = (int)(i & 7);
+    long q = i >> 3;
+    const int n = (int)(q % N);
+    q /= N;
+    const int g = (int)(q & 3);
+    q >>= 2;
+    const int t = (int)(q % 9);
+    const int c = (int)(q / 9);
+    img[i] = w[((long)n * 9 + t) * Cin + 32 * c + 8 * g + j];
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+// The halo form's tile height and stages for a layer: the tallest tile
+// (fewer halo rows per output row) whose stages fit two CTAs per SM (shared
+// memory, and TMEM columns for two accumulator sets); failing that, one CTA
+// per SM. Returns false when nothing fits.
+bool halo_shape(int nchunks, int N, int* tr, int* stages, int* ns, int* ncols) {
+  int n_s = 32;
+  while (n_s < N) n_s <<= 1;
+  const int st = nchunks > 1 ? 2 : 1;
+  const int budgets[2] = {HALO_SMEM_MAX / 2, HALO_SMEM_MAX};
+  const int tmem_caps[2] = {256, 512};
+  for (int k = 0; k < 2; k++)
+    for (int t = 8; t >= 1; t >>= 1) {
+      if (t * n_s > tmem_caps[k]) continue;
+      if (st * halo_stage_bytes(t, N) + HALO_BAR_BYTES > budgets[k]) continue;
+      int cols = 32;
+      while (cols < t * n_s) cols <<= 1;
+      *tr = t;
+      *stages = st;
+      *ns = n_s;
+      *ncols = cols;
+      return true;
+    }
+  return false;
+}
+
 bool g_attr_set = false;
+bool g_halo_ok = false;
 
 }  // namespace
 
@@ -263,11 +489,54 @@ bool g_attr_set = false;
 // created (outside any stream capture).
 void unet_tc_setup() {
   g_attr_set = cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) == cudaSuccess;
+  g_halo_ok = cudaFuncSetAttribute(k_conv3_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, HALO_SMEM_MAX) ==
+              cudaSuccess;
+  if (!g_encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  g_halo_ok = g_halo_ok && g_encode != nullptr;
   cudaGetLastError();
 }
 
+void unet_tc_weight_image(cudaStream_t s, const __nv_bfloat16* w, int Cin, int Cout, __nv_bfloat16* img) {
+  const long total = 9L * Cin * Cout;
+  k_weight_image<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(w, Cin, Cout, img);
+}
+
 void unet_tc_enable(bool on) { g_tc_on = on; }
+void unet_tc_halo(bool on) { g_tc_halo = on; }
 bool unet_tc_enabled() { return g_tc_on; }
+
+namespace {
+
+bool launch_halo(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* wimg,
+                 const float* bias, int N, __nv_bfloat16* y) {
+  int tr, stages, ns, ncols;
+  const int nchunks = Cin / KC;
+  if (!halo_shape(nchunks, N, &tr, &stages, &ns, &ncols)) return false;
+  // x as a 4-D tensor (channels, columns, rows, images), boxes of 8 channels
+  // x 130 columns x (tr + 2) rows; outside the image the box reads zeros
+  CUtensorMap map;
+  const cuuint64_t dims[4] = {(cuuint64_t)Cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+  const cuuint64_t strides[3] = {(cuuint64_t)Cin * 2, (cuuint64_t)W * Cin * 2, (cuuint64_t)H * W * Cin * 2};
+  const cuuint32_t box[4] = {8, (cuuint32_t)HALO_W, (cuuint32_t)(tr + 2), 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  if (g_encode(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(x), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  const int smem = stages * halo_stage_bytes(tr, N) + HALO_BAR_BYTES;
+  dim3 grid((unsigned)((W + HALO_TW - 1) / HALO_TW), (unsigned)((H + tr - 1) / tr), (unsigned)B);
+  k_conv3_halo<<<grid, 128, smem, s>>>(map, H, W, wimg, bias, N, nchunks, tr, stages, ns, ncols, y);
+  return true;
+}
+
+}  // namespace
 
 int unet_tc_take_error() {
   int v = 0, z = 0;
@@ -277,12 +546,14 @@ int unet_tc_take_error() {
 }
 
 bool unet_tc_conv_fwd(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* w,
-                      const float* bias, int Cout, __nv_bfloat16* y) {
+                      const __nv_bfloat16* wimg, const float* bias, int Cout, __nv_bfloat16* y) {
   if (!g_tc_on) return false;
   if (Cin % KC != 0 || Cout % 16 != 0 || Cout < 16 || Cout > 128) return false;
   // 16-byte aligned rows of x, w and y
-  if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(w) | reinterpret_cast<uintptr_t>(y)) & 15)
+  if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(w) | reinterpret_cast<uintptr_t>(y) |
+       reinterpret_cast<uintptr_t>(wimg)) & 15)
     return false;
+  if (g_tc_halo && g_halo_ok && launch_halo(s, x, B, H, W, Cin, wimg, bias, Cout, y)) return true;
   if (!g_attr_set) return false;  // unet_tc_setup not called on this device
   int ncols = 32;
   while (ncols < Cout) ncols <<= 1;

@@ -293,9 +293,11 @@ int fl_unet_forward(fl_unet* u, int batch, int h, int w, const float* x, float* 
  * gradient. */
 int fl_unet_train_step(fl_unet* u, int batch, int h, int w, const float* x, const float* target, const float* mask,
                        double lr, int update, double* loss, float* grad);
-/* Process-wide switch between the tensor-core (tcgen05) and CUDA-core
- * forward convolutions (default: tensor cores where the shape allows). */
-int fl_unet_use_tensor_cores(int on);
+/* Process-wide choice of the forward 3x3 convolutions with 32 or more input
+ * channels: 0 CUDA cores; 1 tensor cores (tcgen05), halo tiles loaded once
+ * per 32 input channels by TMA and reused by all 9 taps (default); 2 tensor
+ * cores, each tap's input gathered per 32-channel chunk. */
+int fl_unet_use_tensor_cores(int mode);
 /* Attaches (or, with NULL, detaches) the network as the engine's warm start:
  * every multigrid step then runs it between the divergence and the solve.
  * The grid's sides must be multiples of 8 and fit the network's capacity;

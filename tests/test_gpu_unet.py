@@ -43,7 +43,7 @@ def net():
     n.close()
 
 
-@pytest.mark.parametrize("tc", [0, 1])
+@pytest.mark.parametrize("tc", [0, 1, 2])
 def test_forward_matches_oracle(net, tc):
     """bf16 activations: equal up to roundings that land on the other side
     of a bf16 step (relative L2 error < 1e-2)."""
@@ -52,6 +52,24 @@ def test_forward_matches_oracle(net, tc):
         th = random_params(1)
         net.set_params(th)
         x, _, _ = batch(2)
+        out = net.forward(x)
+        ref = U.Net(th, bf16=True).forward(x)
+        assert rel(out, ref) < 1e-2, rel(out, ref)
+    finally:
+        native.load().fl_unet_use_tensor_cores(1)
+
+
+@pytest.mark.parametrize("tc", [1, 2])
+def test_forward_tiles_and_edges(net, tc):
+    """A width of 264 (two full 128-column tiles and a partial one) and a
+    height of 40 (at the quarter-resolution level, 10 rows: a partial tile
+    of the 4-row halo tiles): the masked columns and rows of the edge tiles
+    and the zero fill beyond the image."""
+    native.load().fl_unet_use_tensor_cores(tc)
+    try:
+        th = random_params(11)
+        net.set_params(th)
+        x, _, _ = batch(12, B=1, H=40, W=264)
         out = net.forward(x)
         ref = U.Net(th, bf16=True).forward(x)
         assert rel(out, ref) < 1e-2, rel(out, ref)
