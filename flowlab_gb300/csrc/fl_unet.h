@@ -72,9 +72,9 @@ bool unet_tc_conv_fwd(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int 
 void unet_tc_weight_image(cudaStream_t s, const __nv_bfloat16* w, int Cin, int Cout, __nv_bfloat16* img);
 void unet_tc_setup();
 void unet_tc_enable(bool on);
-// true: the halo form (TMA halo tiles) where it applies; false: always the
+// 1: the halo form (TMA halo tiles) where it applies; 0: always the
 // chunked-gather form
-void unet_tc_halo(bool on);
+void unet_tc_form(int form);
 bool unet_tc_enabled();
 // Nonzero (and cleared) when a tensor-core launch gave up a bounded wait.
 int unet_tc_take_error();

@@ -197,7 +197,7 @@ int fl_unet_train_step(fl_unet* h, int B, int H, int W, const float* x, const fl
 int fl_unet_use_tensor_cores(int mode) {
   if (mode < 0 || mode > 2) return ufail(nullptr, FL_EINVAL, "tensor-core mode %d", mode);
   unet_tc_enable(mode != 0);
-  unet_tc_halo(mode == 1);
+  unet_tc_form(mode == 1 ? 1 : 0);
   return FL_OK;
 }
 

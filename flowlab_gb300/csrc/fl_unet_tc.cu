@@ -30,7 +30,8 @@ namespace fl {
 namespace {
 
 bool g_tc_on = true;
-bool g_tc_halo = true;  // the halo form where it applies; false: the chunked-gather form
+int g_tc_form = 1;  // 1: halo form where it applies, 0: always the chunked-gather form
+int g_num_sms = 0;
 
 constexpr int TM = 128;      // pixels per CTA (the MMA's M)
 constexpr int KC = 32;       // input channels per chunk
@@ -108,6 +109,18 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
+
+// 16 consecutive float32 columns of this thread's TMEM lane, without the
+// wait (tmem_wait_ld completes every load issued before it).
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, float* v) {
+  uint32_t* r = reinterpret_cast<uint32_t*>(v);
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // 16 consecutive float32 columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
@@ -261,33 +274,42 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
 
 // ---------------------------------------------------------------- halo form
 //
-// The main forward form. A CTA computes TR image rows x 128 columns of one
-// image (TR accumulators of 128 pixels x N channels in TMEM). Per chunk of
-// 32 input channels it loads, once, the (TR+2) x 130 pixel halo of the tile
-// with four TMA tensor loads (one per 8-channel group; zero fill outside
-// the image) into four "planes" [halo row][halo column][8 channels] of
-// 16-byte rows, and the chunk's weights for all 9 taps with one bulk copy
-// of a pre-arranged weight image. In a plane the pixels sit 16 bytes apart,
+// The main forward form. A tile is TR image rows x 128 columns of one image
+// (TR accumulators of 128 pixels x N channels in TMEM). Per chunk of 32
+// input channels the tile's (TR+2) x 130 pixel halo is loaded once, with
+// four TMA tensor loads (one per 8-channel group; zero fill outside the
+// image), into four "planes" [halo row][halo column][8 channels] of 16-byte
+// rows, and the chunk's weights for all 9 taps with one bulk copy of a
+// pre-arranged weight image. In a plane the pixels sit 16 bytes apart,
 // which is the no-swizzle K-major layout with its 8-row groups 128 bytes
-// apart; so the A operand of tap (ky, kx) for output row r is the same
-// halo with the descriptor's start moved by ((r + ky) * 130 + kx) * 16
-// bytes. No tap is re-gathered: per chunk the tensor core runs 9 x TR x 2
-// MMAs (128 x N x 16) from one copy of the halo.
+// apart; so the A operand of tap (ky, kx) for output row r is the same halo
+// with the descriptor's start moved by ((r + ky) * 130 + kx) * 16 bytes. No
+// tap is re-gathered: per chunk the tensor core runs 9 x TR x 2 MMAs
+// (128 x N x 16) from one copy of the halo.
 //
-// Roles: thread 0 issues the copies into a ring of 1 or 2 stages (waiting
-// on the stage's "empty" barrier, which the MMAs' commit arrives on), lane 0
-// of warp 1 issues the MMAs once a stage's "full" barrier (transaction
-// bytes) completes, warp 2 owns the TMEM allocation, and all four warps run
-// the epilogue (bias, ReLU, bf16 NHWC) after the last commit. Every wait is
-// bounded; before the CTA ends every copy it issued has landed and every
-// MMA has completed.
+// The kernel is persistent and warp-specialised: one CTA per SM walks the
+// tiles blockIdx.x, blockIdx.x + gridDim.x, ... Warp 0 (one lane) streams
+// every tile's chunks through a 2-stage ring (waiting on a stage's "empty"
+// barrier, which the MMAs' commit arrives on); warp 1 (one lane) issues the
+// MMAs once a stage's "full" barrier (transaction bytes) completes, into one
+// of two TMEM accumulator sets (tile i uses set i & 1), and commits
+// "accumulator full"; warps 2-9 run the epilogue (bias, ReLU, bf16 NHWC) of
+// tile i while the tensor core fills the other set with tile i+1, and
+// release the set ("accumulator empty", one arrive per warp). Epilogue warp
+// w reads TMEM lanes 32 (w % 4) .. +31, the lane quarter its rank in the
+// warpgroup may access; the two warps of a quarter take alternate rows.
+// Every wait is bounded; before the CTA ends every copy it issued has
+// landed and every MMA has completed.
 constexpr int HALO_TW = 128;            // output columns per tile (the MMA's M)
 constexpr int HALO_W = HALO_TW + 2;     // halo columns
 constexpr int HALO_SMEM_MAX = 227 * 1024;
 
 __host__ __device__ constexpr int halo_plane_bytes(int tr) { return ((tr + 2) * HALO_W * 16 + 127) / 128 * 128; }
 __host__ __device__ constexpr int halo_stage_bytes(int tr, int n) { return 4 * halo_plane_bytes(tr) + 9 * n * 64; }
-constexpr int HALO_BAR_BYTES = 64;  // 2 full + 2 empty + done barriers and the TMEM slot
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
 
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
@@ -308,35 +330,43 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
                : "memory");
 }
 
-__global__ void __launch_bounds__(128) k_conv3_halo(const __grid_constant__ CUtensorMap xmap, int H, int W,
-                                                    const __nv_bfloat16* __restrict__ wimg,
-                                                    const float* __restrict__ bias, int N, int nchunks, int TR,
-                                                    int stages, int ns, int ncols, __nv_bfloat16* __restrict__ y) {
+constexpr int WS_EPI_WARPS = 8;
+constexpr int WS_THREADS = 64 + 32 * WS_EPI_WARPS;
+
+__global__ void __launch_bounds__(WS_THREADS) k_conv3_halo_ws(const __grid_constant__ CUtensorMap xmap, int H,
+                                                              int W, int B, const __nv_bfloat16* __restrict__ wimg,
+                                                              const float* __restrict__ bias, int N, int nchunks,
+                                                              int TR, int ns, int ncols, int stacked,
+                                                              __nv_bfloat16* __restrict__ y) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int plane = halo_plane_bytes(TR);
   const int stage_a = 4 * plane;
   const int stage_b = 9 * N * 64;
   const int stage_bytes = stage_a + stage_b;
-  // bytes the copies of one stage deliver (a box counts in full, zero-filled
-  // parts included; the planes' tails past the box are padding)
   const uint32_t tx_bytes = (uint32_t)(4 * (TR + 2) * HALO_W * 16 + stage_b);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + stages * stage_bytes);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + 2 * stage_bytes);
   uint64_t* empty = full + 2;
-  uint64_t* done = empty + 2;
+  uint64_t* accf = empty + 2;
+  uint64_t* acce = accf + 2;
+  uint64_t* done = acce + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int x0 = blockIdx.x * HALO_TW, y0 = blockIdx.y * TR, img = blockIdx.z;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tiles_x = (W + HALO_TW - 1) / HALO_TW, tiles_y = (H + TR - 1) / TR;
+  const int ntiles = tiles_x * tiles_y * B;
+  const int acc_cols = TR * ns;  // one accumulator set
 
-  if (warp == 2) {
+  if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(ncols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  if (tid == 0) {
+  if (tid == 32) {
     for (int q = 0; q < 2; q++) {
       mbar_init(smem_u32(&full[q]), 1);
       mbar_init(smem_u32(&empty[q]), 1);
+      mbar_init(smem_u32(&accf[q]), 1);
+      mbar_init(smem_u32(&acce[q]), WS_EPI_WARPS);
     }
     mbar_init(smem_u32(done), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -347,88 +377,170 @@ __global__ void __launch_bounds__(128) k_conv3_halo(const __grid_constant__ CUte
   const uint32_t tmem = *tmem_slot;
   bool failed = false;
 
-  if (tid == 0) {
-    // ---- copies
-    int armed[2] = {0, 0};
-    for (int c = 0; c < nchunks; c++) {
-      const int s = stages == 2 ? (c & 1) : 0;
-      const int use = stages == 2 ? (c >> 1) : c;  // earlier uses of this stage
-      if (use > 0 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((use - 1) & 1))) {
-        failed = true;
-        break;
-      }
-      unsigned char* st = smem + s * stage_bytes;
-      const uint32_t fb = smem_u32(&full[s]);
-      mbar_expect_tx(fb, tx_bytes);
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- copies: chunk q (over all of this CTA's tiles) into stage q & 1
+      int q = 0;
+      for (int t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
+        const int bx = t % tiles_x, by = (t / tiles_x) % tiles_y, img = t / (tiles_x * tiles_y);
+        for (int c = 0; c < nchunks; c++, q++) {
+          const int s = q & 1, use = q >> 1;
+          if (use > 0 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((use - 1) & 1))) {
+            failed = true;
+            break;
+          }
+          unsigned char* st = smem + s * stage_bytes;
+          const uint32_t fb = smem_u32(&full[s]);
+          mbar_expect_tx(fb, tx_bytes);
 #pragma unroll
-      for (int g = 0; g < 4; g++) tma_load_4d(smem_u32(st + g * plane), &xmap, c * 32 + 8 * g, x0 - 1, y0 - 1, img, fb);
-      bulk_load(smem_u32(st + stage_a), wimg + (long)c * 9 * 32 * N, (uint32_t)stage_b, fb);
-      armed[s]++;
+          for (int g = 0; g < 4; g++)
+            tma_load_4d(smem_u32(st + g * plane), &xmap, c * 32 + 8 * g, bx * HALO_TW - 1, by * TR - 1, img, fb);
+          bulk_load(smem_u32(st + stage_a), wimg + (long)c * 9 * 32 * N, (uint32_t)stage_b, fb);
+        }
+      }
+      // nothing issued may still be landing when the CTA ends: the last
+      // arming of each stage (chunks q-1 and q-2) has completed
+      for (int k = 1; k <= 2 && k <= q; k++) {
+        const int qq = q - k;
+        if (!mbar_wait(smem_u32(&full[qq & 1]), (uint32_t)((qq >> 1) & 1))) failed = true;
+      }
     }
-    // nothing issued may still be landing when the CTA ends
-    for (int s = 0; s < stages; s++)
-      if (armed[s] > 0 && !mbar_wait(smem_u32(&full[s]), (uint32_t)((armed[s] - 1) & 1))) failed = true;
-  } else if (tid == 32) {
-    // ---- MMAs
-    const uint32_t idesc = instr_desc(HALO_TW, N);
-    const uint32_t lbo_b = (uint32_t)N * 16;
-    for (int c = 0; c < nchunks; c++) {
-      const int s = stages == 2 ? (c & 1) : 0;
-      const int use = stages == 2 ? (c >> 1) : c;
-      if (!mbar_wait(smem_u32(&full[s]), (uint32_t)(use & 1))) {
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMAs
+      const uint32_t idesc = instr_desc(HALO_TW, N);
+      const uint32_t lbo_b = (uint32_t)N * 16;
+      int q = 0, i = 0;
+      for (int t = blockIdx.x; t < ntiles && !failed; t += gridDim.x, i++) {
+        const int a = i & 1, ause = i >> 1;
+        if (ause > 0 && !mbar_wait(smem_u32(&acce[a]), (uint32_t)((ause - 1) & 1))) {
+          failed = true;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t dacc = tmem + (uint32_t)(a * acc_cols);
+        for (int c = 0; c < nchunks; c++, q++) {
+          const int s = q & 1, use = q >> 1;
+          if (!mbar_wait(smem_u32(&full[s]), (uint32_t)(use & 1))) {
+            failed = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(smem + s * stage_bytes), b0 = a0 + (uint32_t)stage_a;
+          if (stacked) {
+            // B holds, per kx, the three ky taps' weights stacked along N;
+            // halo row h (A shifted by kx) times it adds ky's part to output
+            // row h - ky, whose slot is N (TR - 1 - r) columns in: the parts
+            // of one MMA land in adjacent slots. Rows outside the tile are
+            // not computed (lo..hi). The first MMA into each slot (chunk 0,
+            // kx 0, the first k-step, ky 0) overwrites; the rest accumulate.
+            const uint32_t lbo_s = (uint32_t)(3 * N) * 16;
+            for (int h = 0; h < TR + 2; h++) {
+              const int lo = h - (TR - 1) > 0 ? h - (TR - 1) : 0;
+              const int hi = h < 2 ? h : 2;
+              const uint32_t d_lo = dacc + (uint32_t)(N * (TR - 1 - (h - lo)));
+              for (int kx = 0; kx < 3; kx++) {
+                const uint32_t at = a0 + 16u * (uint32_t)(h * HALO_W + kx);
+                const uint32_t bk = b0 + (uint32_t)(kx * 4 * 3 * N * 16);
+#pragma unroll
+                for (int kk = 0; kk < 2; kk++) {
+                  const uint64_t ad = smem_desc(at + (uint32_t)(kk * 2 * plane), (uint32_t)plane, 128);
+                  if (c == 0 && kx == 0 && kk == 0 && lo == 0) {
+                    mma_bf16(d_lo, ad, smem_desc(bk, lbo_s, 128), instr_desc(HALO_TW, N), 0u);
+                    if (hi >= 1)
+                      mma_bf16(d_lo + (uint32_t)N, ad, smem_desc(bk + (uint32_t)N * 16, lbo_s, 128),
+                               instr_desc(HALO_TW, hi * N), 1u);
+                  } else {
+                    const uint64_t bd = smem_desc(bk + kk * 2 * lbo_s + (uint32_t)(lo * N * 16), lbo_s, 128);
+                    mma_bf16(d_lo, ad, bd, instr_desc(HALO_TW, (hi - lo + 1) * N), 1u);
+                  }
+                }
+              }
+            }
+            mma_commit(smem_u32(&empty[s]));
+            continue;
+          }
+          // accumulator-major: the tensor core runs consecutive MMAs into
+          // one accumulator markedly faster than MMAs alternating between several
+          for (int r = 0; r < TR; r++) {
+            for (int tp = 0; tp < 9; tp++) {
+              const int ky = tp / 3, kx = tp % 3;
+              const uint32_t bt = b0 + (uint32_t)(tp * N * 64);
+              const uint32_t at = a0 + 16u * (uint32_t)((r + ky) * HALO_W + kx);
+#pragma unroll
+              for (int kk = 0; kk < 2; kk++) {
+                const uint64_t ad = smem_desc(at + (uint32_t)(kk * 2 * plane), (uint32_t)plane, 128);
+                const uint64_t bd = smem_desc(bt + kk * 2 * lbo_b, lbo_b, 128);
+                mma_bf16(dacc + (uint32_t)(r * ns), ad, bd, idesc, (c > 0 || tp > 0 || kk > 0) ? 1u : 0u);
+              }
+            }
+          }
+          mma_commit(smem_u32(&empty[s]));
+        }
+        if (failed) break;
+        mma_commit(smem_u32(&accf[a]));
+      }
+      // arrives when every MMA issued above has completed
+      mma_commit(smem_u32(done));
+    }
+  } else {
+    // ---- epilogue: warps 2..9; TMEM lane quarter warp % 4, rows
+    // (warp - 2) / 4, + 2, ...
+    const int quarter = warp & 3, row0 = (warp - 2) >> 2;
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    int i = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+      const int a = i & 1, ause = i >> 1;
+      if (!mbar_wait(smem_u32(&accf[a]), (uint32_t)(ause & 1))) {
         failed = true;
         break;
       }
       tc_fence_after();
-      const uint32_t a0 = smem_u32(smem + s * stage_bytes), b0 = a0 + (uint32_t)stage_a;
-      for (int t = 0; t < 9; t++) {
-        const int ky = t / 3, kx = t % 3;
-        const uint32_t bt = b0 + (uint32_t)(t * N * 64);
-        for (int r = 0; r < TR; r++) {
-          const uint32_t at = a0 + 16u * (uint32_t)((r + ky) * HALO_W + kx);
+      const int bx = t % tiles_x, by = (t / tiles_x) % tiles_y, img = t / (tiles_x * tiles_y);
+      const int x = bx * HALO_TW + quarter * 32 + lane;
+      for (int r = row0; r < TR; r += 2) {
+        const int yy = by * TR + r;
+        const bool ok = x < W && yy < H;
+        __nv_bfloat16* out = y + (((long)img * H + (ok ? yy : 0)) * W + (ok ? x : 0)) * N;
+        for (int c0 = 0; c0 < N; c0 += 64) {
+          // up to four 16-column loads in flight, one wait
+          float v[64];
+          const int nc = N - c0 < 64 ? (N - c0) / 16 : 4;
+          const int slot = stacked ? N * (TR - 1 - r) : r * ns;
+          const uint32_t ta = tmem + lane_base + (uint32_t)(a * acc_cols + slot + c0);
+          tmem_ld16_nowait(ta, v);
+          if (nc > 1) tmem_ld16_nowait(ta + 16, v + 16);
+          if (nc > 2) tmem_ld16_nowait(ta + 32, v + 32);
+          if (nc > 3) tmem_ld16_nowait(ta + 48, v + 48);
+          tmem_wait_ld();
+          if (ok) {
 #pragma unroll
-          for (int kk = 0; kk < 2; kk++) {
-            const uint64_t ad = smem_desc(at + (uint32_t)(kk * 2 * plane), (uint32_t)plane, 128);
-            const uint64_t bd = smem_desc(bt + kk * 2 * lbo_b, lbo_b, 128);
-            mma_bf16(tmem + (uint32_t)(r * ns), ad, bd, idesc, (c > 0 || t > 0 || kk > 0) ? 1u : 0u);
+            for (int q = 0; q < 4; q++) {
+              if (q < nc) {
+                __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+                for (int k = 0; k < 16; k++)
+                  o[k] = __float2bfloat16_rn(fmaxf(v[16 * q + k] + bias[c0 + 16 * q + k], 0.0f));
+                reinterpret_cast<uint4*>(out + c0 + 16 * q)[0] = reinterpret_cast<const uint4*>(o)[0];
+                reinterpret_cast<uint4*>(out + c0 + 16 * q)[1] = reinterpret_cast<const uint4*>(o)[1];
+              }
+            }
           }
         }
       }
-      mma_commit(smem_u32(&empty[s]));
+      // this warp's reads of the set are done (tcgen05.wait::ld above)
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&acce[a]));
     }
-    // arrives when every MMA issued above has completed (also after a failed wait)
-    mma_commit(smem_u32(done));
   }
   __syncwarp();
   if (!mbar_wait(smem_u32(done), 0u)) failed = true;
   failed = __syncthreads_or(failed) != 0;
-  tc_fence_after();
-  if (failed) {
-    if (tid == 0) atomicExch(&g_tc_error, 1);
-  } else {
-    // TMEM lane = A row = output column x0 + tid; tcgen05.ld is warp-collective
-    const int x = x0 + tid;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int r = 0; r < TR; r++) {
-      const int yy = y0 + r;
-      const bool ok = x < W && yy < H;
-      __nv_bfloat16* out = y + (((long)img * H + (ok ? yy : 0)) * W + (ok ? x : 0)) * N;
-      for (int c = 0; c < N; c += 16) {
-        float v[16];
-        tmem_ld16(lane_base + (uint32_t)(r * ns + c), v);
-        if (ok) {
-          __align__(16) __nv_bfloat16 o[16];
-#pragma unroll
-          for (int k = 0; k < 16; k++) o[k] = __float2bfloat16_rn(fmaxf(v[k] + bias[c + k], 0.0f));
-          reinterpret_cast<uint4*>(out + c)[0] = reinterpret_cast<const uint4*>(o)[0];
-          reinterpret_cast<uint4*>(out + c)[1] = reinterpret_cast<const uint4*>(o)[1];
-        }
-      }
-    }
-  }
+  if (failed && tid == 0) atomicExch(&g_tc_error, 1);
   tc_fence_before();
   __syncthreads();
-  if (warp == 2) {
+  if (warp == 0) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
   }
@@ -438,45 +550,60 @@ __global__ void __launch_bounds__(128) k_conv3_halo(const __grid_constant__ CUte
 // tap t, per 8-channel group g, per output channel n, 8 channels:
 // img[(((c * 9 + t) * 4 + g) * N + n) * 8 + j] = w[(n * 9 + t) * Cin + 32c + 8g + j]
 // — the shared-memory B tiles of all 9 taps of a chunk, contiguous.
-__global__ void k_weight_image(const __nv_bfloat16* __restrict__ w, int Cin, int N, __nv_bfloat16* __restrict__ img) {
+//
+// Stacked (3 N <= 256): per chunk c, per kx, per group g, the three ky taps'
+// rows stacked along N (row ky N + n), 8 channels:
+// img[((((c * 3 + kx) * 4 + g) * 3 + ky) * N + n) * 8 + j] = w[(n * 9 + 3 ky + kx) * Cin + 32c + 8g + j]
+__global__ void k_weight_image(const __nv_bfloat16* __restrict__ w, int Cin, int N, int stacked,
+                               __nv_bfloat16* __restrict__ img) {
   const long total = 9L * Cin * N;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
     const int j = (int)(i & 7);
     long q = i >> 3;
     const int n = (int)(q % N);
     q /= N;
-    const int g = (int)(q & 3);
-    q >>= 2;
-    const int t = (int)(q % 9);
-    const int c = (int)(q / 9);
+    int t, g, c;
+    if (stacked) {
+      const int ky = (int)(q % 3);
+      q /= 3;
+      g = (int)(q & 3);
+      q >>= 2;
+      const int kx = (int)(q % 3);
+      c = (int)(q / 3);
+      t = 3 * ky + kx;
+    } else {
+      g = (int)(q & 3);
+      q >>= 2;
+      t = (int)(q % 9);
+      c = (int)(q / 9);
+    }
     img[i] = w[((long)n * 9 + t) * Cin + 32 * c + 8 * g + j];
   }
 }
 
+// Layers whose three ky taps fit one MMA's N (<= 256) use the stacked form:
+// an M = 128 MMA costs about the same tensor-core time for every N up to 128.
+bool halo_stacked(int N) { return 3 * N <= 256; }
+
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
-// The halo form's tile height and stages for a layer: the tallest tile
-// (fewer halo rows per output row) whose stages fit two CTAs per SM (shared
-// memory, and TMEM columns for two accumulator sets); failing that, one CTA
-// per SM. Returns false when nothing fits.
-bool halo_shape(int nchunks, int N, int* tr, int* stages, int* ns, int* ncols) {
+constexpr int WS_BAR_BYTES = 128;  // 9 barriers and the TMEM slot
+
+// The persistent form's tile height: the tallest tile whose two stages fit
+// one CTA per SM and whose two accumulator sets fit TMEM.
+bool halo_ws_shape(int N, int* tr, int* ns, int* ncols) {
   int n_s = 32;
   while (n_s < N) n_s <<= 1;
-  const int st = nchunks > 1 ? 2 : 1;
-  const int budgets[2] = {HALO_SMEM_MAX / 2, HALO_SMEM_MAX};
-  const int tmem_caps[2] = {256, 512};
-  for (int k = 0; k < 2; k++)
-    for (int t = 8; t >= 1; t >>= 1) {
-      if (t * n_s > tmem_caps[k]) continue;
-      if (st * halo_stage_bytes(t, N) + HALO_BAR_BYTES > budgets[k]) continue;
-      int cols = 32;
-      while (cols < t * n_s) cols <<= 1;
-      *tr = t;
-      *stages = st;
-      *ns = n_s;
-      *ncols = cols;
-      return true;
-    }
+  for (int t = 8; t >= 1; t >>= 1) {
+    if (2 * t * n_s > 512) continue;
+    if (2 * halo_stage_bytes(t, N) + WS_BAR_BYTES > HALO_SMEM_MAX) continue;
+    int cols = 32;
+    while (cols < 2 * t * n_s) cols <<= 1;
+    *tr = t;
+    *ns = n_s;
+    *ncols = cols;
+    return true;
+  }
   return false;
 }
 
@@ -489,8 +616,13 @@ bool g_halo_ok = false;
 // created (outside any stream capture).
 void unet_tc_setup() {
   g_attr_set = cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) == cudaSuccess;
-  g_halo_ok = cudaFuncSetAttribute(k_conv3_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, HALO_SMEM_MAX) ==
+  g_halo_ok = cudaFuncSetAttribute(k_conv3_halo_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, HALO_SMEM_MAX) ==
               cudaSuccess;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    g_num_sms = 0;
+  g_halo_ok = g_halo_ok && g_num_sms > 0;
   if (!g_encode) {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
@@ -505,20 +637,20 @@ void unet_tc_setup() {
 
 void unet_tc_weight_image(cudaStream_t s, const __nv_bfloat16* w, int Cin, int Cout, __nv_bfloat16* img) {
   const long total = 9L * Cin * Cout;
-  k_weight_image<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(w, Cin, Cout, img);
+  k_weight_image<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(w, Cin, Cout, halo_stacked(Cout) ? 1 : 0, img);
 }
 
 void unet_tc_enable(bool on) { g_tc_on = on; }
-void unet_tc_halo(bool on) { g_tc_halo = on; }
+void unet_tc_form(int form) { g_tc_form = form; }
 bool unet_tc_enabled() { return g_tc_on; }
 
 namespace {
 
 bool launch_halo(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* wimg,
                  const float* bias, int N, __nv_bfloat16* y) {
-  int tr, stages, ns, ncols;
+  int tr, ns, ncols;
   const int nchunks = Cin / KC;
-  if (!halo_shape(nchunks, N, &tr, &stages, &ns, &ncols)) return false;
+  if (!halo_ws_shape(N, &tr, &ns, &ncols)) return false;
   // x as a 4-D tensor (channels, columns, rows, images), boxes of 8 channels
   // x 130 columns x (tr + 2) rows; outside the image the box reads zeros
   CUtensorMap map;
@@ -530,9 +662,13 @@ bool launch_halo(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int W, in
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return false;
-  const int smem = stages * halo_stage_bytes(tr, N) + HALO_BAR_BYTES;
-  dim3 grid((unsigned)((W + HALO_TW - 1) / HALO_TW), (unsigned)((H + tr - 1) / tr), (unsigned)B);
-  k_conv3_halo<<<grid, 128, smem, s>>>(map, H, W, wimg, bias, N, nchunks, tr, stages, ns, ncols, y);
+  const int tiles_x = (W + HALO_TW - 1) / HALO_TW, tiles_y = (H + tr - 1) / tr;
+  const long ntiles = (long)tiles_x * tiles_y * B;
+  if (ntiles >= (1L << 31)) return false;
+  const int grid = (int)(ntiles < g_num_sms ? ntiles : g_num_sms);
+  const int smem = 2 * halo_stage_bytes(tr, N) + WS_BAR_BYTES;
+  k_conv3_halo_ws<<<grid, WS_THREADS, smem, s>>>(map, H, W, B, wimg, bias, N, nchunks, tr, ns, ncols,
+                                                  halo_stacked(N) ? 1 : 0, y);
   return true;
 }
 
@@ -553,7 +689,7 @@ bool unet_tc_conv_fwd(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int 
   if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(w) | reinterpret_cast<uintptr_t>(y) |
        reinterpret_cast<uintptr_t>(wimg)) & 15)
     return false;
-  if (g_tc_halo && g_halo_ok && launch_halo(s, x, B, H, W, Cin, wimg, bias, Cout, y)) return true;
+  if (g_tc_form != 0 && g_halo_ok && launch_halo(s, x, B, H, W, Cin, wimg, bias, Cout, y)) return true;
   if (!g_attr_set) return false;  // unet_tc_setup not called on this device
   int ncols = 32;
   while (ncols < Cout) ncols <<= 1;
