@@ -13,10 +13,10 @@ advection with decay and inlet, CFL reduction.
   value   steps/s over K timed steps, fields resident in HBM, L2 flushed
           (a 320 MB write) before every timed step, CUDA events on the
           engine's stream; whole job = N ranks x K steps / max rank time.
-  e2e     the same steps through the C ABI with host buffers, as the
-          GpuStep seam runs them with invalidate() before every step: upload
-          u, v, p, label and dye from pinned host memory, step, read u and v
-          back (stepGpu.ts:521-522, 591-592: p and dye stay on the device).
+  e2e     the same steps through the C ABI with host buffers, the host
+          holding the whole state between steps: every step uploads u, v, p,
+          label and dye from pinned host memory (the GpuStep seam after
+          invalidate()), steps, and reads u, v, p and dye back.
   roofline  the phase with the most device time, algorithmic bytes / its
           event-timed duration, against MEASURED_PEAKS.json's HBM copy rate.
           Timed steps run as one CUDA graph each (the V-cycle loop is a
@@ -507,10 +507,12 @@ def run_ours(args, world, rank, local, pg):
         eng.call("fl_upload_fields", native.FL_F32, ptr(hu), ptr(hv), ptr(hp), ptr(hl), ptr(hd))
         eng.call("fl_step_auto", 1, ctypes.byref(iters))
         eng.call("fl_read_velocity", native.FL_F32, ptr(hu), ptr(hv))
+        eng.call("fl_read_pressure", native.FL_F32, ptr(hp))
+        eng.call("fl_read_dye", native.FL_F32, ptr(hd))
     e2e_s = max_over_ranks(pg, time.perf_counter() - te)
     e2e_value = world * args.e2e_steps / e2e_s
     h2d = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len) + eng.cells
-    d2h = 4 * (eng.ufaces + eng.vfaces)
+    d2h = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len)
 
     cnn = cnn_arm(args, local, stream, flush, state0=(f, patch)) if args.cnn_steps > 0 else None
 

@@ -574,12 +574,18 @@ int step_eager(Engine* e, bool device_dt) {
   return FL_OK;
 }
 
-void destroy_graphs(Engine* e) {
+void destroy_step_graphs(Engine* e) {
   for (auto& g : e->graph) {
     if (g) cudaGraphExecDestroy(g);
     g = nullptr;
   }
   e->graphs_valid = false;
+}
+
+void destroy_graphs(Engine* e) {
+  destroy_step_graphs(e);
+  if (e->upload_graph) cudaGraphExecDestroy(e->upload_graph);
+  e->upload_graph = nullptr;
 }
 
 // Enqueues one whole step for buffer parity `par` on e->stream while that
@@ -656,7 +662,7 @@ bool graph_eligible(const Engine* e) {
 
 int step_graph(Engine* e) {
   if (!e->graphs_valid) {
-    destroy_graphs(e);
+    destroy_step_graphs(e);
     for (int par = 0; par < 2; par++) TRY(build_graph(e, par, &e->graph[par]));
     e->graphs_valid = true;
   }
@@ -850,6 +856,20 @@ int fl_synchronize(fl_engine* h) {
   return sync(e, "synchronize");
 }
 
+// The device-side work of an upload once the fields have landed: p64 (the
+// float64 pressure of the defect-correction solve) from the float32 p
+// unless it came in float64, the second-order warm start's history, the
+// multigrid labels and stencil codes, the clock and the CFL scalars.
+void enqueue_after_upload(Engine* e, bool p64_from_p32) {
+  cudaStream_t s = e->stream;
+  if (p64_from_p32) launch_convert(s, e->levels[0].x[0], FL_F32, e->p64[0], FL_F64, e->cells());
+  cudaMemcpyAsync(e->pprev32, e->levels[0].x[0], e->cells() * 4, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(e->pprev64, e->p64[0], e->cells() * 8, cudaMemcpyDeviceToDevice, s);
+  mg_build_codes(*e);
+  cudaMemsetAsync(e->time_dev, 0, sizeof(double), s);
+  launch_max_speed(s, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);
+}
+
 int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
                      const void* dye) {
   ENTER(h);
@@ -862,22 +882,34 @@ int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, cons
     TRY(upload(e, e->levels[0].x[0], p, e->cells(), dtype, "upload p"));
   else
     TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].x[0], 0, e->cells() * 4, e->stream), "zero p"));
-  // the float64 pressure of the defect-correction solve starts from the same p
-  if (p && dtype == FL_F64)
+  const bool p64_direct = p && dtype == FL_F64;
+  if (p64_direct)
     TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, e->cells() * sizeof(double), cudaMemcpyHostToDevice, e->stream),
                     "upload p64"));
-  else
-    launch_convert(e->stream, e->levels[0].x[0], FL_F32, e->p64[0], FL_F64, e->cells());
   TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "upload label"));
   TRY(upload(e, e->dye[0], dye, 3 * e->dye_cells(), dtype, "upload dye"));
-  // the second-order warm start's history starts at the uploaded pressure
-  TRY(cuda_status(e, cudaMemcpyAsync(e->pprev32, e->levels[0].x[0], e->cells() * 4, cudaMemcpyDeviceToDevice,
-                                     e->stream), "previous pressure"));
-  TRY(cuda_status(e, cudaMemcpyAsync(e->pprev64, e->p64[0], e->cells() * 8, cudaMemcpyDeviceToDevice, e->stream),
-                  "previous pressure"));
-  mg_build_codes(*e);
-  TRY(cuda_status(e, cudaMemsetAsync(e->time_dev, 0, sizeof(double), e->stream), "clock"));
-  launch_max_speed(e->stream, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);
+  if (p64_direct || !e->use_graphs) {
+    enqueue_after_upload(e, !p64_direct);
+  } else {
+    // one graph launch instead of ~20 launches (captured once per parameter set)
+    if (!e->upload_graph) {
+      cudaGraph_t g = nullptr;
+      cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+      if (err == cudaSuccess) {
+        enqueue_after_upload(e, true);
+        err = cudaStreamEndCapture(e->stream, &g);
+      }
+      if (err == cudaSuccess) err = cudaGraphInstantiate(&e->upload_graph, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (err != cudaSuccess) {
+        cudaGetLastError();
+        e->upload_graph = nullptr;
+        return cuda_status(e, err, "upload graph");
+      }
+    }
+    TRY(cuda_status(e, cudaGraphLaunch(e->upload_graph, e->stream), "upload graph"));
+  }
+  TRY(check_launch(e, "upload"));
   TRY(sync(e, "upload"));
   e->uploaded = true;
   e->labels_dirty = false;

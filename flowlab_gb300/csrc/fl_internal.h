@@ -62,6 +62,8 @@ struct Engine {
   // whole-step CUDA graphs, one per velocity/dye buffer parity
   cudaStream_t stream2 = nullptr;  // capture stream of the cycle-loop body
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  // the device-side work of fl_upload_fields after its copies (float32 p)
+  cudaGraphExec_t upload_graph = nullptr;
   bool graphs_valid = false;
   bool use_graphs = true;
   bool stats_on_device = false;  // the last solve's statistics live in ctl
