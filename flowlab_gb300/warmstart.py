@@ -236,6 +236,26 @@ def save(path, params, meta):
     np.savez_compressed(path, params=np.asarray(params, np.float32), meta=json.dumps(meta))
 
 
+def time_forward(params, size, batch=1, repeat=3, seed=0):
+    """fl_unet_forward on a seeded standard-normal input of batch x size x
+    size x 3: wall-clock ms per call (host input and output copies
+    included), after one untimed call."""
+    x = np.random.default_rng(seed).standard_normal((batch, size, size, 3)).astype(np.float32)
+    net = native.Unet(batch * size * size)
+    try:
+        net.set_params(params)
+        net.forward(x)
+        t0 = time.perf_counter()
+        for _ in range(repeat):
+            out = net.forward(x)
+        ms = 1000.0 * (time.perf_counter() - t0) / max(1, repeat)
+    finally:
+        net.close()
+    flops, _ = forward_flops(size, size)
+    return {"size": size, "batch": batch, "ms_per_call": ms, "out_mean_abs": float(np.abs(out).mean()),
+            "forward_flops": flops * batch}
+
+
 def load(path):
     z = np.load(path)
     return z["params"], json.loads(str(z["meta"]))
@@ -256,6 +276,11 @@ def main(argv=None):
     e.add_argument("--weights", default=DEFAULT_WEIGHTS)
     e.add_argument("--size", type=int, default=1024)
     e.add_argument("--steps", type=int, default=30)
+    f = sub.add_parser("forward", help="time the forward pass on a seeded random input")
+    f.add_argument("--weights", default=DEFAULT_WEIGHTS)
+    f.add_argument("--size", type=int, default=1024)
+    f.add_argument("--batch", type=int, default=1)
+    f.add_argument("--repeat", type=int, default=3)
     a = ap.parse_args(argv)
     from . import build
 
@@ -272,6 +297,9 @@ def main(argv=None):
             meta["evaluation"] = evaluate(params, a.eval_size)
         save(a.out, params, meta)
         print(json.dumps(meta), flush=True)
+    elif a.cmd == "forward":
+        params, _ = load(a.weights)
+        print(json.dumps(time_forward(params, a.size, a.batch, a.repeat)), flush=True)
     else:
         params, meta = load(a.weights)
         print(json.dumps(evaluate(params, a.size, a.steps)), flush=True)
