@@ -66,6 +66,15 @@ LIMITERS = {
 }
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of a
+# phase's dominant kernel from one ncu capture of the 1024^2 plume's eager
+# profiled steps (profiles/): (bytes, kernel, summary file).
+TRAFFIC_PLUME_1024 = {
+    "defect64": (17.865216e6, "k_update_resid64<1>", "profiles/k_mg_coarse_resid64_plume_1024.md"),
+    "mg_coarse": (0.087552e6, "k_mg_coarse", "profiles/k_mg_coarse_resid64_plume_1024.md"),
+}
+
+
 def bf16_peak():
     try:
         with open(PEAKS_PATH) as fh:
@@ -537,6 +546,11 @@ def run_ours(args, world, rank, local, pg):
                 "algorithmic_bytes_per_launch": d["gbytes"] * 1e9 / d["launches"],
                 "avg_launch_us": 1000.0 * d["ms"] / d["launches"],
                 "limiter": LIMITERS.get(dom, "instruction issue (working set resident in L2)")}
+    if args.workload == "plume" and args.size == 1024 and dom in TRAFFIC_PLUME_1024:
+        tb, tk, tf = TRAFFIC_PLUME_1024[dom]
+        roofline["traffic"] = tb
+        roofline["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one %s launch (%s)" % (
+            tk, tf)
     # Launches in the timed region: the profiled steps give the launches per
     # V-cycle (smoothers, coarse tail, float64 update, cycle test) and per
     # step (the rest); the timed steps' own cycle counts scale them.
