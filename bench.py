@@ -41,6 +41,9 @@ import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# independent streams (the batched scenes' engines) get up to 32 hardware
+# queues instead of 8; read when CUDA initialises, so set before any CUDA use
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 sys.path.insert(0, ROOT)
 
 # The headline metric: steps/s of the 1024^2 plume solved to a 1e-6 relative
@@ -583,7 +586,8 @@ def run_ours(args, world, rank, local, pg):
 
 def run_batch(args, world, rank, local, pg):
     """The batched-scene workload: this rank's share of the scenes (dealt by
-    cost, no collective), all advanced by one graph launch per step."""
+    cost, no collective), every scene's step graph launched on its own
+    stream each step (fl_batch_step)."""
     import torch
 
     from flowlab_gb300 import batch, build, native
@@ -607,10 +611,6 @@ def run_batch(args, world, rank, local, pg):
         b.record(st_)
         b.synchronize()
         alone_ms += a.elapsed_time(b) / 2
-    # bring every engine to the same buffer parity
-    for e in engines:
-        if e.stats()["steps"] % 2:
-            e.call("fl_step_auto", 1, None)
     bt = native.Batch(engines)
     stream = torch.cuda.ExternalStream(bt.stream(), device=local)
     bt.step(args.warmup)
@@ -645,7 +645,8 @@ def run_batch(args, world, rank, local, pg):
         "data": "synthetic (seeded random closed-box scenes)",
         "config": {"workload": "%d closed-box scenes, sides 2^U{6..10} (%d cells), 0-12 discs, smoothed-noise "
                                "velocity, multigrid V(3,3) to 1e-6 (float32 fields and smoothing, float64 residual; "
-                               "cap 20 cycles), one graph launch per step" % (args.scenes, total_cells),
+                               "cap 40 cycles), each scene's step graph on its own stream (%s hardware queues)"
+                               % (args.scenes, total_cells, os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8")),
                    "scenes": args.scenes, "cells": total_cells, "l2": "working set far above L2 (no flush)",
                    "parallelism": "scenes dealt to ranks by cost" if world > 1 else "single GPU"},
         "cell_updates_per_s": value * total_cells,
@@ -654,6 +655,10 @@ def run_batch(args, world, rank, local, pg):
         "rank0_concurrency_gain": alone_ms / (ms / args.steps),
         "vcycles_per_step_mean": statistics.mean(s["cycles"] for s in stats),
         "rel_residual_max": max(s["rel_residual"] for s in stats),
+        # scenes whose last step reached the tolerance within the cycle cap
+        # (obstacle-rich scenes contract ~0.9 per V-cycle in this multigrid,
+        # the float64 oracle alike, and can end a step at the cap)
+        "scenes_converged_last_step": sum(1 for s in stats if 0 <= s["rel_residual"] <= 1e-6),
         "clocks": sampler.summary(t0, t1),
     }
     print(json.dumps(line), flush=True)

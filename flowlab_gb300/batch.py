@@ -5,10 +5,11 @@ log-uniformly from 64..1024 (powers of two), each a `configs.random_scene`
 (seeded discs, a divergence-free smoothed-noise velocity, a dye blob),
 multigrid to 1e-6: float32 fields and smoothing, with the float64 residual
 and correction (float32 alone stalls above 1e-6 on these scenes and runs
-to the cycle cap). All scenes on a GPU advance by one graph launch
-per step (`fl_batch_step`): every engine's whole step, with its own
-device-side V-cycle loop, is a branch of one CUDA graph, so small scenes run
-beside large ones instead of one after another.
+to the cycle cap). All scenes on a GPU advance together
+(`fl_batch_step`): every engine's whole step, with its own device-side
+V-cycle loop, is one graph launched on the engine's own stream, so small
+scenes run beside large ones instead of one after another (up to
+CUDA_DEVICE_MAX_CONNECTIONS hardware queues at once).
 
 Across GPUs the scenes shard with no collective: `shard()` deals scenes to
 ranks by their cost (cells), largest first, each to the least-loaded rank.
@@ -40,7 +41,7 @@ def shard(costs, world, rank):
     return [k for k in range(len(costs)) if owner[k] == rank]
 
 
-def make_engines(sides, seed=2024, device=0, params=None, tol=1e-6, max_cycles=20, mixed=1):
+def make_engines(sides, seed=2024, device=0, params=None, tol=1e-6, max_cycles=40, mixed=1):
     """One engine per side, fields uploaded; scene k uses seed + k."""
     engines = []
     for k, n in enumerate(sides):

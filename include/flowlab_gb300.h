@@ -311,22 +311,25 @@ int fl_read_rhs(fl_engine* e, int dtype, void* b);
 /* ------------------------------------------------------- batched scenes
  * No counterpart in the reference (one scene per Simulation). A batch
  * steps several engines (scenes of any sizes and parameters on one device)
- * with one CUDA-graph launch per step: the graph forks to every engine's
- * stream, runs each engine's whole step (its own device-side V-cycle loop)
- * and joins, so independent scenes run concurrently. The engines must have
- * uploaded fields, be eligible for graph steps (no profiling, pending stir
- * or label edit; multigrid, or red-black SOR with a fixed sweep count) and
- * sit at the same buffer parity (step them only through the batch, or all
- * by the same count). A batch is rebuilt (destroy + create) after any
- * engine's parameters change. Statistics and fields are read per engine. */
+ * together: each step launches every engine's own step graph (its whole
+ * step with its device-side V-cycle loop) on the engine's own stream,
+ * largest scenes first, so independent scenes run concurrently; how many at
+ * once is bounded by the process's hardware queues (the environment
+ * variable CUDA_DEVICE_MAX_CONNECTIONS, read when CUDA initialises; 8 by
+ * default, up to 32). The engines must have uploaded fields and be eligible
+ * for graph steps (no profiling, pending stir or label edit; multigrid, or
+ * red-black SOR with a fixed sweep count). Statistics and fields are read
+ * per engine. */
 typedef struct fl_batch fl_batch;
 int fl_batch_create(fl_engine* const* engines, int count, fl_batch** out);
 int fl_batch_destroy(fl_batch* b);
 const char* fl_batch_last_error(const fl_batch* b);
-/* The stream the batch launches on (cudaStream_t). */
+/* A stream (cudaStream_t) that completes after every engine's last step of
+ * the latest fl_batch_step. */
 void* fl_batch_stream(fl_batch* b);
-/* nsteps graph launches, asynchronous; ordered after each engine's earlier
- * work and before its later work. */
+/* nsteps steps of every engine, asynchronous; each engine's steps are
+ * ordered after its earlier work and before its later work (its stream),
+ * and after the batch stream's earlier work. */
 int fl_batch_step(fl_batch* b, int nsteps);
 
 #ifdef __cplusplus

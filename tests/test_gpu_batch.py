@@ -1,5 +1,6 @@
-"""Batched scenes (fl_batch_*): one graph launch steps every engine; each
-engine's result equals stepping it alone, bit for bit."""
+"""Batched scenes (fl_batch_*): every engine's step graph launched on its
+own stream per step; each engine's result equals stepping it alone, bit for
+bit."""
 import numpy as np
 import pytest
 
@@ -74,11 +75,30 @@ def test_batch_then_single_steps_stay_ordered():
         batch.close_all(a + c)
 
 
-def test_engines_at_different_parities_are_refused():
-    es = batch.make_engines([64, 64], seed=5)
+def test_engines_at_different_parities_step_together():
+    """An engine one step ahead of the other (the other buffer parity) steps
+    in the same batch; both equal the same steps taken alone."""
+    a = batch.make_engines([64, 128], seed=5)
+    c = batch.make_engines([64, 128], seed=5)
     try:
-        es[0].call("fl_step_auto", 1, None)
+        a[0].call("fl_step_auto", 4, None)
+        a[1].call("fl_step_auto", 3, None)
+        c[0].call("fl_step_auto", 1, None)
+        b = native.Batch(c)
+        b.step(3)
+        b.close()
+        for x, y in zip(a, c):
+            for fx, fy in zip(fields(x), fields(y)):
+                assert np.array_equal(fx, fy)
+            assert x.stats()["steps"] == y.stats()["steps"]
+    finally:
+        batch.close_all(a + c)
+
+
+def test_engine_listed_twice_is_refused():
+    es = batch.make_engines([64], seed=5)
+    try:
         with pytest.raises(native.FlowlabError):
-            native.Batch(es)
+            native.Batch([es[0], es[0]])
     finally:
         batch.close_all(es)
