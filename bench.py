@@ -14,9 +14,10 @@ advection with decay and inlet, CFL reduction.
           (a 320 MB write) before every timed step, CUDA events on the
           engine's stream; whole job = N ranks x K steps / max rank time.
   e2e     the same steps through the C ABI with host buffers, the host
-          holding the whole state between steps: every step uploads u, v, p,
-          label and dye from pinned host memory (the GpuStep seam after
-          invalidate()), steps, and reads u, v, p and dye back.
+          holding the whole state between steps: every step is one
+          fl_step_host call (the GpuStep.step seam after invalidate()) that
+          uploads u, v, p, label and dye from pinned host memory, steps, and
+          reads u, v, p and dye back.
   roofline  the phase with the most device time, algorithmic bytes / its
           event-timed duration, against MEASURED_PEAKS.json's HBM copy rate.
           Timed steps run as one CUDA graph each (the V-cycle loop is a
@@ -516,11 +517,9 @@ def run_ours(args, world, rank, local, pg):
     barrier(pg)
     te = time.perf_counter()
     for _ in range(args.e2e_steps):
-        eng.call("fl_upload_fields", native.FL_F32, ptr(hu), ptr(hv), ptr(hp), ptr(hl), ptr(hd))
-        eng.call("fl_step_auto", 1, ctypes.byref(iters))
-        eng.call("fl_read_velocity", native.FL_F32, ptr(hu), ptr(hv))
-        eng.call("fl_read_pressure", native.FL_F32, ptr(hp))
-        eng.call("fl_read_dye", native.FL_F32, ptr(hd))
+        # GpuStep.step with invalidate(): upload, step, readback in one call
+        eng.call("fl_step_host", ptr(hu), ptr(hv), ptr(hp), ptr(hl), ptr(hd), ptr(hu), ptr(hv), ptr(hp), ptr(hd),
+                 ctypes.byref(iters))
     e2e_s = max_over_ranks(pg, time.perf_counter() - te)
     e2e_value = world * args.e2e_steps / e2e_s
     h2d = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len) + eng.cells

@@ -191,6 +191,9 @@ void free_all(Engine* e) {
   for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
   if (e->acc_host) cudaFreeHost(e->acc_host);
   if (e->ctl_host) cudaFreeHost(e->ctl_host);
+  if (e->ev_dye) cudaEventDestroy(e->ev_dye);
+  if (e->ev_proj) cudaEventDestroy(e->ev_proj);
+  if (e->ev_prior) cudaEventDestroy(e->ev_prior);
   if (e->stream2) cudaStreamDestroy(e->stream2);
   if (e->stream) cudaStreamDestroy(e->stream);
 }
@@ -338,6 +341,18 @@ int read_ctl(Engine* e) {
   return sync(e, "read solve state");
 }
 
+// fl_step_host uploads the dye on the second stream while the step's first
+// kernels run: the first kernel that reads the dye waits here (an event wait
+// node when captured; the event is recorded before every graph launch).
+bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &st) == cudaSuccess && st == cudaStreamCaptureStatusActive;
+}
+
+void wait_dye(Engine* e, cudaStream_t s) {
+  cudaStreamWaitEvent(s, e->ev_dye, capturing(s) ? cudaEventWaitExternal : 0);
+}
+
 // advect u,v -> [stir] -> [confinement] -> body forces -> divergence
 void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
   Level& L0 = e->levels[0];
@@ -362,6 +377,7 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
     fbytes += (4 * F + 4 * N) + (4 * N + N + 8 * N);
     flaunch += 2;
   }
+  if (beta_on || alpha_on) wait_dye(e, s);
   if (beta_on || alpha_on || conf) {
     launch_forces(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, u, v, e->dye[par], L0.label, beta_on, alpha_on, conf,
                   e->fx, e->fy, e->sc);
@@ -465,6 +481,10 @@ void enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
   launch_subtract_outflow(s, e->nx, e->ny, L0.x[0], u, v, L0.label, e->sc, true, true, mixed ? e->p64[0] : nullptr,
                           mixed ? e->p64[1] : nullptr, e->ctl);
   prof_end(*e, tok, (mixed ? 8 : 4) * N + 4 * F + N + 4 * F, 1);
+  // velocity and pressure are final: fl_step_host reads them back from here
+  // on while the dye advection runs
+  cudaEventRecordWithFlags(e->ev_proj, s, capturing(s) ? cudaEventRecordExternal : 0);
+  wait_dye(e, s);
   tok = prof_begin(*e, FL_PH_ADVECT_DYE);
   launch_advect_dye(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, mac, u, v, e->dye[par], e->dye_hat, e->dye[1 - par],
                     L0.label, e->sc, true, e->patch, e->pi0, e->pj0, e->pnx, e->pny);
@@ -794,7 +814,10 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
     fail(e, FL_ENOMEM, "pinned accumulator");
     return bail(FL_ENOMEM);
   }
-  if (cudaStreamCreateWithFlags(&e->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&e->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->ev_dye, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->ev_proj, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->ev_prior, cudaEventDisableTiming) != cudaSuccess) {
     fail(e, FL_EDEVICE, "stream creation failed");
     return bail(FL_EDEVICE);
   }
@@ -870,11 +893,27 @@ void enqueue_after_upload(Engine* e, bool p64_from_p32) {
   launch_max_speed(s, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);
 }
 
-int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
-                     const void* dye) {
-  ENTER(h);
+}  // extern "C"
+
+namespace {
+
+// The body of fl_upload_fields. With `dye_async` the dye (float32) is copied
+// on the second stream, after the stream's earlier work, and ev_dye marks
+// its end; the step's first dye reader waits for it (wait_dye). Otherwise
+// ev_dye is recorded on the second stream with nothing in flight.
+int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
+                  const void* dye, bool dye_async) {
   e->cur = 0;
   e->stats_on_device = false;
+  if (dye_async) {
+    if (!dye) return fail(e, FL_EINVAL, "upload dye: null pointer");
+    // the dye buffer may still be read by the stream's earlier work
+    TRY(cuda_status(e, cudaEventRecord(e->ev_prior, e->stream), "upload dye"));
+    TRY(cuda_status(e, cudaStreamWaitEvent(e->stream2, e->ev_prior, 0), "upload dye"));
+    TRY(cuda_status(e, cudaMemcpyAsync(e->dye[0], dye, 3 * e->dye_cells() * sizeof(float), cudaMemcpyHostToDevice,
+                                       e->stream2), "upload dye"));
+  }
+  TRY(cuda_status(e, cudaEventRecord(e->ev_dye, e->stream2), "upload dye"));
   TRY(put_step_ctl(e, true));
   TRY(upload(e, e->u[0], u, e->ufaces(), dtype, "upload u"));
   TRY(upload(e, e->v[0], v, e->vfaces(), dtype, "upload v"));
@@ -887,7 +926,7 @@ int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, cons
     TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, e->cells() * sizeof(double), cudaMemcpyHostToDevice, e->stream),
                     "upload p64"));
   TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "upload label"));
-  TRY(upload(e, e->dye[0], dye, 3 * e->dye_cells(), dtype, "upload dye"));
+  if (!dye_async) TRY(upload(e, e->dye[0], dye, 3 * e->dye_cells(), dtype, "upload dye"));
   if (p64_direct || !e->use_graphs) {
     enqueue_after_upload(e, !p64_direct);
   } else {
@@ -910,11 +949,70 @@ int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, cons
     TRY(cuda_status(e, cudaGraphLaunch(e->upload_graph, e->stream), "upload graph"));
   }
   TRY(check_launch(e, "upload"));
-  TRY(sync(e, "upload"));
   e->uploaded = true;
   e->labels_dirty = false;
   e->steps = 0;
   e->time = 0;
+  return FL_OK;
+}
+
+int sync2(Engine* e, const char* what) { return cuda_status(e, cudaStreamSynchronize(e->stream2), what); }
+
+}  // namespace
+
+extern "C" {
+
+int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
+                     const void* dye) {
+  ENTER(h);
+  TRY(upload_fields(e, dtype, u, v, p, label, dye, false));
+  return sync(e, "upload");
+}
+
+int fl_step_host(fl_engine* h, const float* u, const float* v, const float* p, const uint8_t* label, const float* dye,
+                 float* u_out, float* v_out, float* p_out, float* dye_out, int* iters) {
+  ENTER(h);
+  const bool upload_in = u != nullptr;
+  if (upload_in && (!v || !label || !dye)) return fail(e, FL_EINVAL, "step_host: u without v, label or dye");
+  if (!upload_in && (v || p || label || dye)) return fail(e, FL_EINVAL, "step_host: inputs without u");
+  if (!upload_in && !e->uploaded) return fail(e, FL_ESTATE, "step before fl_upload_fields");
+  if (upload_in) {
+    TRY(upload_fields(e, FL_F32, u, v, p, label, dye, true));
+  } else {
+    TRY(cuda_status(e, cudaEventRecord(e->ev_dye, e->stream2), "step"));
+  }
+  TRY(graph_eligible(e) ? step_graph(e) : step_eager(e, true));
+  TRY(check_launch(e, "step"));
+  // velocity and pressure on the second stream once the projection is done
+  // (the step records ev_proj there), the dye after the whole step
+  TRY(cuda_status(e, cudaStreamWaitEvent(e->stream2, e->ev_proj, 0), "read back"));
+  if (u_out)
+    TRY(cuda_status(e, cudaMemcpyAsync(u_out, e->u[e->cur], e->ufaces() * sizeof(float), cudaMemcpyDeviceToHost,
+                                       e->stream2), "read u"));
+  if (v_out)
+    TRY(cuda_status(e, cudaMemcpyAsync(v_out, e->v[e->cur], e->vfaces() * sizeof(float), cudaMemcpyDeviceToHost,
+                                       e->stream2), "read v"));
+  if (p_out) {
+    const long n = e->cells();
+    if (step_mixed(e)) {
+      launch_select_p64(e->stream2, e->ctl, e->p64[0], e->p64[1], e->staging, false, n);
+      TRY(check_launch(e, "read p"));
+      TRY(cuda_status(e, cudaMemcpyAsync(p_out, e->staging, n * sizeof(float), cudaMemcpyDeviceToHost, e->stream2),
+                      "read p"));
+    } else {
+      TRY(cuda_status(e, cudaMemcpyAsync(p_out, e->levels[0].x[0], n * sizeof(float), cudaMemcpyDeviceToHost,
+                                         e->stream2), "read p"));
+    }
+  }
+  if (dye_out)
+    TRY(cuda_status(e, cudaMemcpyAsync(dye_out, e->dye[e->cur], 3 * e->dye_cells() * sizeof(float),
+                                       cudaMemcpyDeviceToHost, e->stream), "read dye"));
+  TRY(sync2(e, "read back"));
+  TRY(sync(e, "step"));
+  if (iters) {
+    TRY(solve_stats(e));
+    *iters = e->last_iters;
+  }
   return FL_OK;
 }
 

@@ -60,7 +60,11 @@ struct Engine {
   SolveCtl* ctl_host = nullptr;  // pinned mirror
 
   // whole-step CUDA graphs, one per velocity/dye buffer parity
-  cudaStream_t stream2 = nullptr;  // capture stream of the cycle-loop body
+  cudaStream_t stream2 = nullptr;  // capture stream of the cycle-loop body; copies of fl_step_host
+  // fl_step_host: the dye upload on stream2 (waited for by the step's first
+  // dye reader), the projection's end (velocity and pressure final), and
+  // the stream's earlier work (before stream2 overwrites an input)
+  cudaEvent_t ev_dye = nullptr, ev_proj = nullptr, ev_prior = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   // the device-side work of fl_upload_fields after its copies (float32 p)
   cudaGraphExec_t upload_graph = nullptr;

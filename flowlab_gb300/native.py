@@ -113,6 +113,7 @@ SIGNATURES = [
     ("fl_set_stir", _I, [_P, _P]),
     ("fl_step", _I, [_P, _D, _D, _D, _P, _P]),
     ("fl_step_auto", _I, [_P, _I, _P]),
+    ("fl_step_host", _I, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("fl_get_stats", _I, [_P, _P]),
     ("fl_read_velocity", _I, [_P, _I, _P, _P]),
     ("fl_read_dye", _I, [_P, _I, _P]),

@@ -178,6 +178,17 @@ int fl_step(fl_engine* e, double dt, double scale, double grad_scale, const doub
  * readback). No host synchronisation between steps unless tol > 0 requires
  * a residual readback. */
 int fl_step_auto(fl_engine* e, int nsteps, int* iters_last);
+/* One step the way GpuStep.step (simulation.ts:35-84, GpuStepper.step in
+ * stepGpu.ts:393-560) runs it, with host float32 buffers: when u is
+ * non-null the host fields (u, v, p, label, dye; p may be null: zero) are
+ * uploaded first, as after invalidate() (fl_upload_fields semantics); then
+ * one step with dt from the device (fl_step_auto); then the results are
+ * copied into the non-null outputs. The dye upload overlaps the step's
+ * first kernels, and the velocity and pressure readback overlaps the dye
+ * advection. Returns when every copy completed; results equal
+ * fl_upload_fields + fl_step_auto + fl_read_* bit for bit. */
+int fl_step_host(fl_engine* e, const float* u, const float* v, const float* p, const uint8_t* label,
+                 const float* dye, float* u_out, float* v_out, float* p_out, float* dye_out, int* iters);
 int fl_get_stats(fl_engine* e, fl_stats* out);
 /* Readbacks (drainReadback / readDye, stepGpu.ts:372-391, 578-604). */
 int fl_read_velocity(fl_engine* e, int dtype, void* u, void* v);

@@ -384,3 +384,52 @@ def test_extrapolated_warm_start_matches_float32_oracle(o32, mixed):
         assert mismatch(a, b) == 0, "%s: %d values differ from the float32 oracle" % (name, mismatch(a, b))
     if not mixed:
         assert mismatch(ep, p) == 0
+
+
+@pytest.mark.parametrize("case", ["plume_mixed", "plume_float32", "karman_rb"])
+def test_step_host_equals_upload_step_and_reads(case):
+    """fl_step_host (the GpuStep.step seam with host buffers: upload, step,
+    readback, copies overlapped with the step on a second stream) gives the
+    same fields and cycle counts as fl_upload_fields + fl_step_auto +
+    fl_read_*, step after step, with and without the upload."""
+    if case == "karman_rb":
+        g, f, patch = configs.karman(96, 64)
+        prm = configs.karman_params()
+    else:
+        g, f, patch = configs.plume(96)
+        prm = configs.plume_params(tol=1e-6 if case == "plume_mixed" else 1e-4, max_cycles=20,
+                                   mixed=int(case == "plume_mixed"))
+    engs = [native.Engine(g.nx, g.ny, g.h, params=prm) for _ in range(2)]
+    try:
+        for eng in engs:
+            if patch is not None:
+                eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+        a, b = engs
+        state = [f32(f.u).copy(), f32(f.v).copy(), f32(f.p).copy(), f32(f.dye).copy()]
+        label = np.ascontiguousarray(f.label)
+        out_b = [np.empty_like(x) for x in state]
+        for step in range(6):
+            upload = step % 3 != 2  # every third step continues on the device
+            if upload:
+                a.call("fl_upload_fields", native.FL_F32, ptr(state[0]), ptr(state[1]), ptr(state[2]), ptr(label),
+                       ptr(state[3]))
+            ia = ctypes.c_int()
+            a.call("fl_step_auto", 1, ctypes.byref(ia))
+            out_a = [np.empty_like(x) for x in state]
+            a.call("fl_read_velocity", native.FL_F32, ptr(out_a[0]), ptr(out_a[1]))
+            a.call("fl_read_pressure", native.FL_F32, ptr(out_a[2]))
+            a.call("fl_read_dye", native.FL_F32, ptr(out_a[3]))
+            ib = ctypes.c_int()
+            if upload:
+                b.call("fl_step_host", ptr(state[0]), ptr(state[1]), ptr(state[2]), ptr(label), ptr(state[3]),
+                       ptr(out_b[0]), ptr(out_b[1]), ptr(out_b[2]), ptr(out_b[3]), ctypes.byref(ib))
+            else:
+                b.call("fl_step_host", None, None, None, None, None, ptr(out_b[0]), ptr(out_b[1]), ptr(out_b[2]),
+                       ptr(out_b[3]), ctypes.byref(ib))
+            for name, x, y in zip(("u", "v", "p", "dye"), out_a, out_b):
+                assert mismatch(x, y) == 0, "step %d %s: %d values differ" % (step, name, mismatch(x, y))
+            assert ia.value == ib.value
+            state = [x.copy() for x in out_a]
+    finally:
+        for eng in engs:
+            eng.close()
