@@ -242,6 +242,17 @@ __global__ void __launch_bounds__(256) k_conv3_wgrad(const __nv_bfloat16* __rest
   }
 }
 
+// db[c] += sum over pixels of g[p][c]: thread t of a block handles channel
+// t % C over every (blockDim / C)-th pixel of the block's share.
+__global__ void __launch_bounds__(256) k_bias_grad(const float* __restrict__ g, long P, int C, float* __restrict__ db) {
+  const int per = blockDim.x / C;  // pixels in flight per block
+  if ((int)threadIdx.x >= per * C) return;
+  const int c = threadIdx.x % C, j = threadIdx.x / C;
+  float s = 0.0f;
+  for (long p = (long)blockIdx.x * per + j; p < P; p += (long)gridDim.x * per) s += g[p * C + c];
+  atomicAdd(&db[c], s);
+}
+
 // 2x2 average pooling, bf16 -> bf16 (the mean in float32). One thread per
 // coarse pixel and group of 8 channels (C is a multiple of 8).
 __global__ void k_pool(const __nv_bfloat16* __restrict__ x, int B, int H, int W, int C, __nv_bfloat16* __restrict__ y) {
@@ -442,7 +453,9 @@ int Unet::alloc(long max_pixels, std::string* err) {
   }
   bool ok = A((void**)&theta, nparam * 4, "weights") && A((void**)&m, nparam * 4, "adam m") &&
             A((void**)&v, nparam * 4, "adam v") && A((void**)&grad, nparam * 4, "gradient") &&
-            A((void**)&theta16, nparam * 2, "bf16 weights") && A((void**)&wimg, nparam * 2, "weight images") && A((void**)&wflip, 9L * 224 * 96 * 2, "flipped weights") &&
+            A((void**)&theta16, nparam * 2, "bf16 weights") && A((void**)&wimg, nparam * 2, "weight images") &&
+            A((void**)&wimg_flip, 9L * 224 * 96 * 2, "flipped weight image") &&
+            A((void**)&gbf, max_pixels * 32L * 2, "bf16 gradient") && A((void**)&wflip, 9L * 224 * 96 * 2, "flipped weights") &&
             A((void**)&loss_dev, sizeof(double), "loss");
   if (!ok) return FL_ENOMEM;
   const long P = max_pixels;
@@ -470,7 +483,7 @@ int Unet::alloc(long max_pixels, std::string* err) {
 }
 
 void Unet::release() {
-  void* ps[] = {theta, m, v, grad, theta16, wimg, wflip, loss_dev, gbuf[0], gbuf[1], gskip[0], gskip[1], gskip[2], gpool,
+  void* ps[] = {theta, m, v, grad, theta16, wimg, wimg_flip, gbf, wflip, loss_dev, gbuf[0], gbuf[1], gskip[0], gskip[1], gskip[2], gpool,
                 out, dout, target, mask, input, ws_acc};
   for (void* p : ps) cudaFree(p);
   for (auto* a : act) cudaFree(a);
@@ -495,11 +508,32 @@ void Unet::conv_fwd(cudaStream_t s, int l, const __nv_bfloat16* x, int B, int H,
 void Unet::conv_bwd(cudaStream_t s, int l, const __nv_bfloat16* x, const float* g, int B, int H, int W, float* gx,
                     const __nv_bfloat16* act_x) {
   const UnetLayer& L = kUnetLayers[l];
-  dim3 gw((unsigned)(((W + CT - 1) / CT) * ((H + CT - 1) / CT)), (unsigned)(B * ((L.cout + CO_T - 1) / CO_T)),
-          (unsigned)((L.cin + CK - 1) / CK));
-  k_conv3_wgrad<<<gw, 256, 0, s>>>(x, g, H, W, L.cin, L.cout, grad + woff[l], grad + boff[l]);
+  const long P = (long)B * H * W;
+  // tensor cores take the output gradient in bf16
+  const bool tc = unet_tc_enabled() && L.cout % 32 == 0;
+  if (tc) k_to_bf16<<<grid_for(P * L.cout), 256, 0, s>>>(g, P * L.cout, gbf);
+  if (tc && L.cin % 32 == 0 && unet_tc_conv_wgrad(s, x, gbf, B, H, W, L.cin, L.cout, grad + woff[l])) {
+    k_bias_grad<<<152, 256, 0, s>>>(g, P, L.cout, grad + boff[l]);
+  } else {
+    dim3 gw((unsigned)(((W + CT - 1) / CT) * ((H + CT - 1) / CT)), (unsigned)(B * ((L.cout + CO_T - 1) / CO_T)),
+            (unsigned)((L.cin + CK - 1) / CK));
+    k_conv3_wgrad<<<gw, 256, 0, s>>>(x, g, H, W, L.cin, L.cout, grad + woff[l], grad + boff[l]);
+  }
   if (gx == nullptr) return;
   k_flip_weights<<<grid_for(9L * L.cin * L.cout), 256, 0, s>>>(theta16 + woff[l], L.cin, L.cout, wflip);
+  if (tc) {
+    // the data gradient in tiles of at most 128 input channels (each tile's
+    // weight image built here)
+    const int tiles = (L.cin + 127) / 128, nt = L.cin / tiles;
+    bool ok = nt * tiles == L.cin && nt % 16 == 0;
+    for (int t = 0; ok && t < tiles; t++) {
+      const int n0 = t * nt;
+      unet_tc_weight_image(s, wflip + (long)n0 * 9 * L.cout, L.cout, nt, wimg_flip);
+      ok = unet_tc_conv_dgrad(s, gbf, B, H, W, L.cout, wimg_flip, nt, gx + n0, L.cin,
+                              act_x != nullptr ? act_x + n0 : nullptr);
+    }
+    if (ok) return;
+  }
   dim3 gd((unsigned)(((W + CT - 1) / CT) * ((H + CT - 1) / CT)), (unsigned)(B * ((L.cin + CO_T - 1) / CO_T)));
   k_conv3<float, EPI_GRAD><<<gd, CT * CT, 0, s>>>(g, H, W, L.cout, wflip, nullptr, L.cin, nullptr, gx, act_x);
 }

@@ -33,6 +33,8 @@ struct Unet {
   __nv_bfloat16* theta16 = nullptr;  // bf16 copies used by the kernels
   __nv_bfloat16* wflip = nullptr;    // flipped/transposed weights of one layer
   __nv_bfloat16* wimg = nullptr;     // tensor-core weight images (offsets woff)
+  __nv_bfloat16* wimg_flip = nullptr;  // image of one output-channel tile of the flipped weights
+  __nv_bfloat16* gbf = nullptr;        // bf16 copy of an output gradient (tensor-core data gradient)
   double* loss_dev = nullptr;
   __nv_bfloat16* act[ACT_COUNT] = {};
   long act_size[ACT_COUNT] = {};
@@ -70,6 +72,19 @@ struct Unet {
 bool unet_tc_conv_fwd(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* w,
                       const __nv_bfloat16* wimg, const float* bias, int Cout, __nv_bfloat16* y);
 void unet_tc_weight_image(cudaStream_t s, const __nv_bfloat16* w, int Cin, int Cout, __nv_bfloat16* img);
+// Tensor-core data gradient of a 3x3 convolution over the output-channel
+// tile of N channels: gx = conv(g, W') (g bf16 with Cin channels, wimg the
+// image of W' rows of the tile), zeroed where mask <= 0 (mask optional);
+// gx and mask rows are ldg elements apart. False (nothing launched) when the
+// shape is not covered or the tensor cores are off.
+// Tensor-core weight gradient of a 3x3 convolution: dw[n][tap][ci] +=
+// sum over pixels of g[p][n] x[p + off(tap)][ci] (x and g bf16 NHWC; dw
+// float, accumulated with atomics). Cin and Cout multiples of 32. False
+// (nothing launched) when not covered or the tensor cores are off.
+bool unet_tc_conv_wgrad(cudaStream_t s, const __nv_bfloat16* x, const __nv_bfloat16* g, int B, int H, int W, int Cin,
+                        int Cout, float* dw);
+bool unet_tc_conv_dgrad(cudaStream_t s, const __nv_bfloat16* g, int B, int H, int W, int Cin, const __nv_bfloat16* wimg,
+                        int N, float* gx, int ldg, const __nv_bfloat16* mask);
 void unet_tc_setup();
 void unet_tc_enable(bool on);
 // 1: the halo form (TMA halo tiles) where it applies; 0: always the

@@ -330,14 +330,25 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
                : "memory");
 }
 
+// Where the halo kernel's results go. Forward: y = bf16(relu(acc + bias)).
+// Data gradient (yf set): yf = acc, zeroed where mask <= 0 (the ReLU of the
+// layer's input; mask optional). Rows of y / yf / mask are ldy elements apart
+// (the caller offsets the pointers to an output-channel tile).
+struct HaloOut {
+  __nv_bfloat16* y;
+  float* yf;
+  const __nv_bfloat16* mask;
+  const float* bias;
+  int ldy;
+};
+
 constexpr int WS_EPI_WARPS = 8;
 constexpr int WS_THREADS = 64 + 32 * WS_EPI_WARPS;
 
 __global__ void __launch_bounds__(WS_THREADS) k_conv3_halo_ws(const __grid_constant__ CUtensorMap xmap, int H,
                                                               int W, int B, const __nv_bfloat16* __restrict__ wimg,
-                                                              const float* __restrict__ bias, int N, int nchunks,
-                                                              int TR, int ns, int ncols, int stacked,
-                                                              __nv_bfloat16* __restrict__ y) {
+                                                              int N, int nchunks, int TR, int ns, int ncols,
+                                                              int stacked, HaloOut out) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int plane = halo_plane_bytes(TR);
   const int stage_a = 4 * plane;
@@ -501,7 +512,7 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3_halo_ws(const __grid_const
       for (int r = row0; r < TR; r += 2) {
         const int yy = by * TR + r;
         const bool ok = x < W && yy < H;
-        __nv_bfloat16* out = y + (((long)img * H + (ok ? yy : 0)) * W + (ok ? x : 0)) * N;
+        const long pix = ((long)img * H + (ok ? yy : 0)) * W + (ok ? x : 0);
         for (int c0 = 0; c0 < N; c0 += 64) {
           // up to four 16-column loads in flight, one wait
           float v[64];
@@ -513,16 +524,34 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3_halo_ws(const __grid_const
           if (nc > 2) tmem_ld16_nowait(ta + 32, v + 32);
           if (nc > 3) tmem_ld16_nowait(ta + 48, v + 48);
           tmem_wait_ld();
-          if (ok) {
+          if (ok && out.yf == nullptr) {
+            __nv_bfloat16* dst = out.y + pix * out.ldy;
 #pragma unroll
             for (int q = 0; q < 4; q++) {
               if (q < nc) {
                 __align__(16) __nv_bfloat16 o[16];
 #pragma unroll
                 for (int k = 0; k < 16; k++)
-                  o[k] = __float2bfloat16_rn(fmaxf(v[16 * q + k] + bias[c0 + 16 * q + k], 0.0f));
-                reinterpret_cast<uint4*>(out + c0 + 16 * q)[0] = reinterpret_cast<const uint4*>(o)[0];
-                reinterpret_cast<uint4*>(out + c0 + 16 * q)[1] = reinterpret_cast<const uint4*>(o)[1];
+                  o[k] = __float2bfloat16_rn(fmaxf(v[16 * q + k] + out.bias[c0 + 16 * q + k], 0.0f));
+                reinterpret_cast<uint4*>(dst + c0 + 16 * q)[0] = reinterpret_cast<const uint4*>(o)[0];
+                reinterpret_cast<uint4*>(dst + c0 + 16 * q)[1] = reinterpret_cast<const uint4*>(o)[1];
+              }
+            }
+          } else if (ok) {
+            float* dst = out.yf + pix * out.ldy;
+            const __nv_bfloat16* m = out.mask != nullptr ? out.mask + pix * out.ldy : nullptr;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              if (q < nc) {
+                __align__(16) float o[16];
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                  const float g = v[16 * q + k];
+                  o[k] = (m != nullptr && !(__bfloat162float(m[c0 + 16 * q + k]) > 0.0f)) ? 0.0f : g;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                  reinterpret_cast<float4*>(dst + c0 + 16 * q)[k] = reinterpret_cast<const float4*>(o)[k];
               }
             }
           }
@@ -585,6 +614,154 @@ __global__ void k_weight_image(const __nv_bfloat16* __restrict__ w, int Cin, int
 // an M = 128 MMA costs about the same tensor-core time for every N up to 128.
 bool halo_stacked(int N) { return 3 * N <= 256; }
 
+// ---------------------------------------------------------- weight gradient
+//
+// dW[n][tap][ci] = sum over pixels p of g[p][n] * x[p + off(tap)][ci] on the
+// tensor cores: D[ci][n] += A[ci][p] B[n][p] with K = pixels. Both tensors
+// are NHWC (channels innermost), so both operands are MN-major: a plane of
+// 16-byte pixel rows per 8 channels, exactly the halo planes of the forward
+// kernel (MN-major no-swizzle descriptors: LBO = 128 bytes between groups of
+// 8 pixel rows, SBO = the plane stride between groups of 8 channels). A tile
+// is 128 pixels of one image row: its g planes (4 x 8 output channels) and
+// the x halo (3 rows x 130 pixels x up to 128 input channels) arrive by TMA;
+// tap (ky, kx) reads the halo from row ky, column kx on, so one copy serves
+// all 9 taps. A CTA owns 32 output channels x up to 128 input channels (M =
+// 128; rows past Cin are computed from unused shared memory and dropped) and
+// a range of tiles; its 9 tap accumulators (288 TMEM columns) are added to
+// dW with atomics at the end. Warp 0 issues the copies (2-stage ring), warp 1
+// the MMAs, warps 2-5 the epilogue; every wait is bounded.
+constexpr int WG_TW = 128;                                           // pixels per tile
+constexpr int WG_NB = 32;                                            // output channels per CTA (N)
+constexpr int WG_CB = 128;                                           // input channels per CTA (M)
+constexpr int WG_PL = ((3 * HALO_W * 16 + 127) / 128) * 128;         // x plane: 3 halo rows
+constexpr int WG_A = (WG_CB / 8) * WG_PL;
+constexpr int WG_GPL = WG_TW * 16;                                   // g plane
+constexpr int WG_B = (WG_NB / 8) * WG_GPL;
+constexpr int WG_STAGE = WG_A + WG_B;
+constexpr int WG_SMEM = 2 * WG_STAGE + 128;
+constexpr int WG_THREADS = 192;
+
+__global__ void __launch_bounds__(WG_THREADS) k_conv3_wgrad_tc(const __grid_constant__ CUtensorMap xmap,
+                                                               const __grid_constant__ CUtensorMap gmap, int H, int W,
+                                                               int B, int Cin, int tiles_per_cta,
+                                                               float* __restrict__ dw) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + 2 * WG_STAGE);
+  uint64_t* empty = full + 2;
+  uint64_t* done = empty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n0 = blockIdx.y * WG_NB, ci0 = blockIdx.z * WG_CB;
+  const int cb = Cin - ci0 < WG_CB ? Cin - ci0 : WG_CB;  // input channels of this CTA (multiple of 8)
+  const int tiles_x = (W + WG_TW - 1) / WG_TW;
+  const long ntiles = (long)tiles_x * H * B;
+  const long t0 = (long)blockIdx.x * tiles_per_cta;
+  const long t1 = t0 + tiles_per_cta < ntiles ? t0 + tiles_per_cta : ntiles;
+  const int mytiles = t1 > t0 ? (int)(t1 - t0) : 0;
+  constexpr uint32_t NCOLS = 512;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(NCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 32) {
+    for (int q = 0; q < 2; q++) {
+      mbar_init(smem_u32(&full[q]), 1);
+      mbar_init(smem_u32(&empty[q]), 1);
+    }
+    mbar_init(smem_u32(done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  bool failed = false;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      const uint32_t tx = (uint32_t)((cb / 8) * 3 * HALO_W * 16 + (WG_NB / 8) * WG_TW * 16);
+      int q = 0;
+      for (; q < mytiles; q++) {
+        const long t = t0 + q;
+        const int bx = (int)(t % tiles_x), y = (int)((t / tiles_x) % H), img = (int)(t / ((long)tiles_x * H));
+        const int s = q & 1, use = q >> 1;
+        if (use > 0 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((use - 1) & 1))) {
+          failed = true;
+          break;
+        }
+        unsigned char* st = smem + s * WG_STAGE;
+        const uint32_t fb = smem_u32(&full[s]);
+        mbar_expect_tx(fb, tx);
+        for (int g = 0; g < cb / 8; g++)
+          tma_load_4d(smem_u32(st + g * WG_PL), &xmap, ci0 + 8 * g, bx * WG_TW - 1, y - 1, img, fb);
+        for (int g = 0; g < WG_NB / 8; g++)
+          tma_load_4d(smem_u32(st + WG_A + g * WG_GPL), &gmap, n0 + 8 * g, bx * WG_TW, y, img, fb);
+      }
+      for (int k = 1; k <= 2 && k <= q; k++) {
+        const int qq = q - k;
+        if (!mbar_wait(smem_u32(&full[qq & 1]), (uint32_t)((qq >> 1) & 1))) failed = true;
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // M = 128, N = 32, both operands MN-major (bits 15 and 16)
+      const uint32_t idesc = instr_desc(WG_CB, WG_NB) | (1u << 15) | (1u << 16);
+      for (int q = 0; q < mytiles; q++) {
+        const int s = q & 1, use = q >> 1;
+        if (!mbar_wait(smem_u32(&full[s]), (uint32_t)(use & 1))) {
+          failed = true;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(smem + s * WG_STAGE), b0 = a0 + (uint32_t)WG_A;
+        for (int tp = 0; tp < 9; tp++) {
+          const int ky = tp / 3, kx = tp % 3;
+          const uint32_t dacc = tmem + (uint32_t)(tp * WG_NB);
+#pragma unroll
+          for (int k = 0; k < WG_TW / 16; k++) {
+            const uint64_t ad = smem_desc(a0 + 16u * (uint32_t)(ky * HALO_W + kx + 16 * k), 128, WG_PL);
+            const uint64_t bd = smem_desc(b0 + 16u * (uint32_t)(16 * k), 128, WG_GPL);
+            mma_bf16(dacc, ad, bd, idesc, (q > 0 || k > 0) ? 1u : 0u);
+          }
+        }
+        mma_commit(smem_u32(&empty[s]));
+      }
+      mma_commit(smem_u32(done));
+    }
+  }
+  __syncwarp();
+  if (!mbar_wait(smem_u32(done), 0u)) failed = true;
+  failed = __syncthreads_or(failed) != 0;
+  tc_fence_after();
+  if (failed) {
+    if (tid == 0) atomicExch(&g_tc_error, 1);
+  } else if (warp >= 2 && mytiles > 0) {
+    // TMEM lane = input channel ci0 + lane index; column = tap * 32 + output channel
+    const int quarter = warp & 3;
+    const int ci = ci0 + quarter * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+    for (int tp = 0; tp < 9; tp++) {
+      float v[32];
+      tmem_ld16_nowait(lane_base + (uint32_t)(tp * WG_NB), v);
+      tmem_ld16_nowait(lane_base + (uint32_t)(tp * WG_NB + 16), v + 16);
+      tmem_wait_ld();
+      if (quarter * 32 + lane < cb) {
+#pragma unroll
+        for (int j = 0; j < WG_NB; j++) atomicAdd(&dw[((long)(n0 + j) * 9 + tp) * Cin + ci], v[j]);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOLS) : "memory");
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
 constexpr int WS_BAR_BYTES = 128;  // 9 barriers and the TMEM slot
@@ -617,7 +794,9 @@ bool g_halo_ok = false;
 void unet_tc_setup() {
   g_attr_set = cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) == cudaSuccess;
   g_halo_ok = cudaFuncSetAttribute(k_conv3_halo_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, HALO_SMEM_MAX) ==
-              cudaSuccess;
+                  cudaSuccess &&
+              cudaFuncSetAttribute(k_conv3_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, WG_SMEM) ==
+                  cudaSuccess;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -647,7 +826,7 @@ bool unet_tc_enabled() { return g_tc_on; }
 namespace {
 
 bool launch_halo(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int W, int Cin, const __nv_bfloat16* wimg,
-                 const float* bias, int N, __nv_bfloat16* y) {
+                 int N, const HaloOut& out) {
   int tr, ns, ncols;
   const int nchunks = Cin / KC;
   if (!halo_ws_shape(N, &tr, &ns, &ncols)) return false;
@@ -667,12 +846,61 @@ bool launch_halo(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int W, in
   if (ntiles >= (1L << 31)) return false;
   const int grid = (int)(ntiles < g_num_sms ? ntiles : g_num_sms);
   const int smem = 2 * halo_stage_bytes(tr, N) + WS_BAR_BYTES;
-  k_conv3_halo_ws<<<grid, WS_THREADS, smem, s>>>(map, H, W, B, wimg, bias, N, nchunks, tr, ns, ncols,
-                                                  halo_stacked(N) ? 1 : 0, y);
+  if (smem > HALO_SMEM_MAX) return false;
+  k_conv3_halo_ws<<<grid, WS_THREADS, smem, s>>>(map, H, W, B, wimg, N, nchunks, tr, ns, ncols,
+                                                  halo_stacked(N) ? 1 : 0, out);
   return true;
 }
 
 }  // namespace
+
+bool unet_tc_conv_dgrad(cudaStream_t s, const __nv_bfloat16* g, int B, int H, int W, int Cin, const __nv_bfloat16* wimg,
+                        int N, float* gx, int ldg, const __nv_bfloat16* mask) {
+  if (!g_tc_on || g_tc_form == 0 || !g_halo_ok) return false;
+  if (Cin % KC != 0 || N % 16 != 0 || N < 16 || N > 128 || ldg % 4 != 0) return false;
+  if ((reinterpret_cast<uintptr_t>(g) | reinterpret_cast<uintptr_t>(wimg)) & 15) return false;
+  if (reinterpret_cast<uintptr_t>(gx) & 15) return false;
+  const HaloOut out{nullptr, gx, mask, nullptr, ldg};
+  return launch_halo(s, g, B, H, W, Cin, wimg, N, out);
+}
+
+bool unet_tc_conv_wgrad(cudaStream_t s, const __nv_bfloat16* x, const __nv_bfloat16* g, int B, int H, int W, int Cin,
+                        int Cout, float* dw) {
+  if (!g_tc_on || g_tc_form == 0 || !g_halo_ok) return false;
+  if (Cin % 32 != 0 || Cout % WG_NB != 0) return false;
+  if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(g)) & 15) return false;
+  CUtensorMap xmap, gmap;
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  {
+    const cuuint64_t dims[4] = {(cuuint64_t)Cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)Cin * 2, (cuuint64_t)W * Cin * 2, (cuuint64_t)H * W * Cin * 2};
+    const cuuint32_t box[4] = {8, (cuuint32_t)HALO_W, 3, 1};
+    if (g_encode(&xmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(x), dims, strides, box, estr,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  {
+    const cuuint64_t dims[4] = {(cuuint64_t)Cout, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)Cout * 2, (cuuint64_t)W * Cout * 2, (cuuint64_t)H * W * Cout * 2};
+    const cuuint32_t box[4] = {8, (cuuint32_t)WG_TW, 1, 1};
+    if (g_encode(&gmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(g), dims, strides, box, estr,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  const int nblk = Cout / WG_NB, cblk = (Cin + WG_CB - 1) / WG_CB;
+  const long ntiles = (long)((W + WG_TW - 1) / WG_TW) * H * B;
+  long ctas = (g_num_sms + nblk * cblk - 1) / (nblk * cblk);
+  if (ctas > ntiles) ctas = ntiles;
+  if (ctas < 1) ctas = 1;
+  const long per = (ntiles + ctas - 1) / ctas;
+  ctas = (ntiles + per - 1) / per;
+  if (per >= (1L << 30) || ctas >= 65535) return false;
+  dim3 grid((unsigned)ctas, (unsigned)nblk, (unsigned)cblk);
+  k_conv3_wgrad_tc<<<grid, WG_THREADS, WG_SMEM, s>>>(xmap, gmap, H, W, B, Cin, (int)per, dw);
+  return true;
+}
 
 int unet_tc_take_error() {
   int v = 0, z = 0;
@@ -689,7 +917,10 @@ bool unet_tc_conv_fwd(cudaStream_t s, const __nv_bfloat16* x, int B, int H, int 
   if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(w) | reinterpret_cast<uintptr_t>(y) |
        reinterpret_cast<uintptr_t>(wimg)) & 15)
     return false;
-  if (g_tc_form != 0 && g_halo_ok && launch_halo(s, x, B, H, W, Cin, wimg, bias, Cout, y)) return true;
+  if (g_tc_form != 0 && g_halo_ok) {
+    const HaloOut out{y, nullptr, nullptr, bias, Cout};
+    if (launch_halo(s, x, B, H, W, Cin, wimg, Cout, out)) return true;
+  }
   if (!g_attr_set) return false;  // unet_tc_setup not called on this device
   int ncols = 32;
   while (ncols < Cout) ncols <<= 1;

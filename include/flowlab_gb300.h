@@ -304,10 +304,12 @@ int fl_unet_forward(fl_unet* u, int batch, int h, int w, const float* x, float* 
  * gradient. */
 int fl_unet_train_step(fl_unet* u, int batch, int h, int w, const float* x, const float* target, const float* mask,
                        double lr, int update, double* loss, float* grad);
-/* Process-wide choice of the forward 3x3 convolutions with 32 or more input
- * channels: 0 CUDA cores; 1 tensor cores (tcgen05), halo tiles loaded once
+/* Process-wide choice for the 3x3 convolutions with 32 or more input
+ * channels: 0 CUDA cores; 1 tensor cores (tcgen05) for the forward pass and
+ * for the backward pass's data and weight gradients, halo tiles loaded once
  * per 32 input channels by TMA and reused by all 9 taps (default); 2 tensor
- * cores, each tap's input gathered per 32-channel chunk. */
+ * cores for the forward pass only, each tap's input gathered per 32-channel
+ * chunk (backward on CUDA cores). */
 int fl_unet_use_tensor_cores(int mode);
 /* Attaches (or, with NULL, detaches) the network as the engine's warm start:
  * every multigrid step then runs it between the divergence and the solve.

@@ -96,6 +96,26 @@ def test_gradient_matches_oracle(net):
         assert rel(g[bo:bo + cout], ref[bo:bo + cout]) < 5e-2, name
 
 
+def test_tensor_core_gradient_matches_cuda_cores(net):
+    """The data gradients on the tensor cores (bf16 output gradient, float32
+    accumulation) against the CUDA-core path (float32 output gradient): every
+    layer's weight gradient within 1e-2 (relative L2)."""
+    th = random_params(13)
+    net.set_params(th)
+    x, t, m = batch(14, B=1, H=40, W=264)
+    lib = native.load()
+    try:
+        lib.fl_unet_use_tensor_cores(0)
+        _, g0 = net.train_step(x, t, m, update=False, want_grad=True)
+        lib.fl_unet_use_tensor_cores(1)
+        _, g1 = net.train_step(x, t, m, update=False, want_grad=True)
+    finally:
+        lib.fl_unet_use_tensor_cores(1)
+    layout, _ = U.param_layout()
+    for name, wo, nw, bo, cout in layout:
+        assert rel(g1[wo:wo + nw], g0[wo:wo + nw]) < 1e-2, (name, rel(g1[wo:wo + nw], g0[wo:wo + nw]))
+
+
 def test_adam_step_matches_oracle(net):
     th = random_params(5)
     net.set_params(th)
