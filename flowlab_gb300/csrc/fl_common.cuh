@@ -279,6 +279,24 @@ __device__ __forceinline__ double scale_pow2(double x, int k) {
   return x * (double)(1 << k);
 }
 
+// Double -> float rounded to nearest even by integer operations when the
+// result is a normal float (a round-up that carries into the next binade,
+// or past the largest float to infinity, falls out of the addition); other
+// cases (results that are zero or subnormal, overflowing exponents, NaN)
+// take the conversion instruction. Equal to (float)d in every case.
+__device__ __forceinline__ float d2f_rn(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned ex = (unsigned)(b >> 52) & 0x7ffu;
+  if (ex >= 897u && ex <= 1150u) {  // float biased exponent 1..254
+    const unsigned long long m = b & 0xfffffffffffffull;
+    const unsigned long long rem = m & 0x1fffffffull;  // the 29 bits rounded away
+    unsigned long long f = ((unsigned long long)(ex - 896u) << 23) | (m >> 29);
+    f += (rem > 0x10000000ull || (rem == 0x10000000ull && (f & 1ull))) ? 1ull : 0ull;
+    return __uint_as_float((unsigned)(b >> 63) << 31 | (unsigned)f);
+  }
+  return (float)d;
+}
+
 // 0.0 + x: x itself except that -0.0 becomes +0.0.
 __device__ __forceinline__ double zero_plus(double x) {
   const long long bits = __double_as_longlong(x);

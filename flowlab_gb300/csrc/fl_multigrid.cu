@@ -656,8 +656,9 @@ __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
 // spends float64 instructions only where the result needs them: each p64' is
 // formed once and handed to its neighbours in registers (the rows above and
 // below, a rolling column) and by warp shuffles (left and right); the exact
-// float -> double widenings, the first addition to 0.0 and the products by 2
-// and 4 are done on the integer pipe with identical results. A warp owns 30
+// float -> double widenings, the first addition to 0.0, the products by 2
+// and 4 and the rounding of r to float are done on the integer pipe with
+// identical results. A warp owns 30
 // interior columns (lanes 1..30; lanes 0 and 31 are the halo) and UR_ROWS
 // rows; the halo rows and columns are formed redundantly. Eight rows keep the
 // kernel at 64 registers (32 warps per SM to hide the float64 latency):
@@ -741,7 +742,7 @@ __global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny
                           : cnt == 1 ? pn[t]
                                      : 3.0 * pn[t];
         const double rd = f2d_exact(bv[t - 1]) - (cp - sum);
-        r = (float)rd;
+        r = d2f_rn(rd);
         sq = fma(rd, rd, sq);
         n += 1;
       }
