@@ -243,14 +243,21 @@ __global__ void __launch_bounds__(256) k_conv3_wgrad(const __nv_bfloat16* __rest
 }
 
 // db[c] += sum over pixels of g[p][c]: thread t of a block handles channel
-// t % C over every (blockDim / C)-th pixel of the block's share.
+// t % C over every (blockDim / C)-th pixel of the block's share (coalesced
+// rows); the block's partials meet in shared memory, one atomic per channel.
 __global__ void __launch_bounds__(256) k_bias_grad(const float* __restrict__ g, long P, int C, float* __restrict__ db) {
+  __shared__ float sdb[256];
+  for (int c = threadIdx.x; c < C; c += blockDim.x) sdb[c] = 0.0f;
+  __syncthreads();
   const int per = blockDim.x / C;  // pixels in flight per block
-  if ((int)threadIdx.x >= per * C) return;
-  const int c = threadIdx.x % C, j = threadIdx.x / C;
-  float s = 0.0f;
-  for (long p = (long)blockIdx.x * per + j; p < P; p += (long)gridDim.x * per) s += g[p * C + c];
-  atomicAdd(&db[c], s);
+  if ((int)threadIdx.x < per * C) {
+    const int c = threadIdx.x % C, j = threadIdx.x / C;
+    float s = 0.0f;
+    for (long p = (long)blockIdx.x * per + j; p < P; p += (long)gridDim.x * per) s += g[p * C + c];
+    atomicAdd(&sdb[c], s);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&db[c], sdb[c]);
 }
 
 // 2x2 average pooling, bf16 -> bf16 (the mean in float32). One thread per
@@ -362,29 +369,48 @@ __global__ void __launch_bounds__(256) k_head_bwd(const __nv_bfloat16* __restric
                                                   const __nv_bfloat16* __restrict__ w, const float* __restrict__ dout,
                                                   float* __restrict__ g_d0, float* __restrict__ dw,
                                                   float* __restrict__ db) {
+  // one item = one pixel's group of 8 channels (C a multiple of 8, <= 64):
+  // 16-byte loads of d0, 32-byte stores of the gradient; a thread always
+  // meets the same group (the grid stride is a multiple of C / 8), so its
+  // weight-gradient partials are 8 registers, reduced in shared memory
   __shared__ float sw[64];
-  __shared__ float sdb[8];
-  float lw[32];
-  for (int c = 0; c < 32; c++) lw[c] = 0.0f;
+  __shared__ float sdb;
+  const int G = C / 8;
+  for (int c = threadIdx.x; c < C; c += blockDim.x) sw[c] = 0.0f;
+  if (threadIdx.x == 0) sdb = 0.0f;
+  __syncthreads();
+  const long gid = blockIdx.x * (long)blockDim.x + threadIdx.x, stride = (long)gridDim.x * blockDim.x;
+  const int q = (int)(gid % G);
+  float wq[8], acc[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    wq[k] = __bfloat162float(w[8 * q + k]);
+    acc[k] = 0.0f;
+  }
   float ldb = 0.0f;
-  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < P; p += (long)gridDim.x * blockDim.x) {
+  for (long e = gid; e < P * G; e += stride) {
+    const long p = e / G;
     const float d = dout[p];
-    ldb += d;
-    for (int c = 0; c < C && c < 32; c++) {
-      const float a = __bfloat162float(d0[p * C + c]);
-      lw[c] = __fmaf_rn(d, a, lw[c]);
-      g_d0[p * C + c] = a > 0.0f ? d * __bfloat162float(w[c]) : 0.0f;
+    if (q == 0) ldb += d;
+    const uint4 raw = *reinterpret_cast<const uint4*>(d0 + p * C + 8 * q);
+    const __nv_bfloat16* a8 = reinterpret_cast<const __nv_bfloat16*>(&raw);
+    __align__(16) float gout[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const float a = __bfloat162float(a8[k]);
+      acc[k] = __fmaf_rn(d, a, acc[k]);
+      gout[k] = a > 0.0f ? d * wq[k] : 0.0f;
     }
+    float4* dst = reinterpret_cast<float4*>(g_d0 + p * C + 8 * q);
+    dst[0] = reinterpret_cast<const float4*>(gout)[0];
+    dst[1] = reinterpret_cast<const float4*>(gout)[1];
   }
-  for (int c = 0; c < C && c < 32; c++) {
-    float v = lw[c];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&dw[c], v);
-  }
-  for (int o = 16; o > 0; o >>= 1) ldb += __shfl_down_sync(0xffffffffu, ldb, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(db, ldb);
-  (void)sw;
-  (void)sdb;
+#pragma unroll
+  for (int k = 0; k < 8; k++) atomicAdd(&sw[8 * q + k], acc[k]);
+  if (q == 0) atomicAdd(&sdb, ldb);
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&dw[c], sw[c]);
+  if (threadIdx.x == 0) atomicAdd(db, sdb);
 }
 
 // Masked mean squared error: dout = 2 (out - t) m / n, loss += (out - t)^2 m.
