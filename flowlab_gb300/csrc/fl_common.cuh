@@ -133,12 +133,15 @@ __device__ __forceinline__ float bilerp(float v00, float v10, float v01, float v
 
 __device__ __forceinline__ float ldg(const float* p) { return __ldg(p); }
 
+// The samplers index with 32-bit offsets: a sampled field holds fewer than
+// 2^31 values (the engine's grid and dye-grid limits guarantee it).
+
 // grid.ts:197-208 sampleU: u[i,j] at (i*h, (j+0.5)*h), (nx+1) x ny values.
 __device__ __forceinline__ float sample_u(const float* __restrict__ u, int nx, int ny, const Spacing& h, float x, float y) {
   AxisF a = clamped_axis(over(x, h), nx + 1);
   AxisF b = clamped_axis(over(y, h) - 0.5f, ny);
-  long s = nx + 1;
-  long k = a.i0 + (long)b.i0 * s;
+  const int s = nx + 1;
+  const int k = a.i0 + b.i0 * s;
   return bilerp(ldg(u + k), ldg(u + k + 1), ldg(u + k + s), ldg(u + k + s + 1), a.f, b.f);
 }
 
@@ -146,8 +149,8 @@ __device__ __forceinline__ float sample_u(const float* __restrict__ u, int nx, i
 __device__ __forceinline__ float sample_v(const float* __restrict__ v, int nx, int ny, const Spacing& h, float x, float y) {
   AxisF a = clamped_axis(over(x, h) - 0.5f, nx);
   AxisF b = clamped_axis(over(y, h), ny + 1);
-  long s = nx;
-  long k = a.i0 + (long)b.i0 * s;
+  const int s = nx;
+  const int k = a.i0 + b.i0 * s;
   return bilerp(ldg(v + k), ldg(v + k + 1), ldg(v + k + s), ldg(v + k + s + 1), a.f, b.f);
 }
 
@@ -155,8 +158,8 @@ __device__ __forceinline__ float sample_v(const float* __restrict__ v, int nx, i
 __device__ __forceinline__ float sample_p(const float* __restrict__ q, int nx, int ny, const Spacing& h, float x, float y) {
   AxisF a = clamped_axis(over(x, h) - 0.5f, nx);
   AxisF b = clamped_axis(over(y, h) - 0.5f, ny);
-  long s = nx;
-  long k = a.i0 + (long)b.i0 * s;
+  const int s = nx;
+  const int k = a.i0 + b.i0 * s;
   return bilerp(ldg(q + k), ldg(q + k + 1), ldg(q + k + s), ldg(q + k + s + 1), a.f, b.f);
 }
 
@@ -172,24 +175,24 @@ __device__ __forceinline__ float clamp_stencil_u(const float* __restrict__ u, in
                                                  float q) {
   int i0 = clamped_axis(over(x, h), nx + 1).i0;
   int j0 = clamped_axis(over(y, h) - 0.5f, ny).i0;
-  long s = nx + 1;
-  long k = i0 + (long)j0 * s;
+  const int s = nx + 1;
+  const int k = i0 + j0 * s;
   return clamp_to_range(q, ldg(u + k), ldg(u + k + 1), ldg(u + k + s), ldg(u + k + s + 1));
 }
 __device__ __forceinline__ float clamp_stencil_v(const float* __restrict__ v, int nx, int ny, const Spacing& h, float x, float y,
                                                  float q) {
   int i0 = clamped_axis(over(x, h) - 0.5f, nx).i0;
   int j0 = clamped_axis(over(y, h), ny + 1).i0;
-  long s = nx;
-  long k = i0 + (long)j0 * s;
+  const int s = nx;
+  const int k = i0 + j0 * s;
   return clamp_to_range(q, ldg(v + k), ldg(v + k + 1), ldg(v + k + s), ldg(v + k + s + 1));
 }
 __device__ __forceinline__ float clamp_stencil_p(const float* __restrict__ q, int nx, int ny, const Spacing& h, float x, float y,
                                                  float val) {
   int i0 = clamped_axis(over(x, h) - 0.5f, nx).i0;
   int j0 = clamped_axis(over(y, h) - 0.5f, ny).i0;
-  long s = nx;
-  long k = i0 + (long)j0 * s;
+  const int s = nx;
+  const int k = i0 + j0 * s;
   return clamp_to_range(val, ldg(q + k), ldg(q + k + 1), ldg(q + k + s), ldg(q + k + s + 1));
 }
 

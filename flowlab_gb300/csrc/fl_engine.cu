@@ -746,6 +746,10 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   if (nx < 2 || ny < 2 || nx > 32768 || ny > 32768) return fail(nullptr, FL_EINVAL, "grid %dx%d out of range", nx, ny);
   if (!(h > 0)) return fail(nullptr, FL_EINVAL, "cell size must be positive");
   if (dye_scale < 1 || dye_scale > 8) return fail(nullptr, FL_EINVAL, "dye_scale %d out of [1, 8]", dye_scale);
+  // the samplers address one field with 32-bit offsets
+  if ((long long)nx * dye_scale * ny * dye_scale >= (1LL << 31) || (long long)(nx + 1) * (ny + 1) >= (1LL << 31))
+    return fail(nullptr, FL_EINVAL, "dye grid %dx%d too large (at most 2^31 - 1 cells)", nx * dye_scale,
+                ny * dye_scale);
   int ndev = 0;
   cudaError_t err = cudaGetDeviceCount(&ndev);
   if (err != cudaSuccess || ndev == 0)
