@@ -39,7 +39,8 @@ __global__ void __launch_bounds__(256) k_advect_velocity(int nx, int ny, Spacing
                                                          const float* __restrict__ v_hat, float* __restrict__ u_out,
                                                          float* __restrict__ v_out,
                                                          const uint8_t* __restrict__ label,
-                                                         const StepScalars* __restrict__ sc) {
+                                                         const StepScalars* __restrict__ sc, float2* __restrict__ bt_u,
+                                                         float2* __restrict__ bt_v) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const float dt = sc->dt;
@@ -55,12 +56,19 @@ __global__ void __launch_bounds__(256) k_advect_velocity(int nx, int ny, Spacing
       float bx, by;
       if (MODE == 0) {
         backtrace(u_in, v_in, nx, ny, h, x, y, u0, v0, dt, bx, by);
+        if (bt_u != nullptr) bt_u[k] = make_float2(bx, by);
         u_out[k] = sample_u(u_in, nx, ny, h, bx, by);
       } else {
         backtrace(u_in, v_in, nx, ny, h, x, y, u0, v0, -dt, bx, by);
         const float ubar = sample_u(u_hat, nx, ny, h, bx, by);
         const float corrected = u_hat[k] + 0.5f * (u_in[k] - ubar);
-        backtrace(u_in, v_in, nx, ny, h, x, y, u0, v0, dt, bx, by);
+        if (bt_u != nullptr) {
+          const float2 b = bt_u[k];
+          bx = b.x;
+          by = b.y;
+        } else {
+          backtrace(u_in, v_in, nx, ny, h, x, y, u0, v0, dt, bx, by);
+        }
         u_out[k] = clamp_stencil_u(u_in, nx, ny, h, bx, by, corrected);
       }
     }
@@ -77,12 +85,19 @@ __global__ void __launch_bounds__(256) k_advect_velocity(int nx, int ny, Spacing
       float bx, by;
       if (MODE == 0) {
         backtrace(u_in, v_in, nx, ny, h, x, y, u0, v0, dt, bx, by);
+        if (bt_v != nullptr) bt_v[k] = make_float2(bx, by);
         v_out[k] = sample_v(v_in, nx, ny, h, bx, by);
       } else {
         backtrace(u_in, v_in, nx, ny, h, x, y, u0, v0, -dt, bx, by);
         const float vbar = sample_v(v_hat, nx, ny, h, bx, by);
         const float corrected = v_hat[k] + 0.5f * (v_in[k] - vbar);
-        backtrace(u_in, v_in, nx, ny, h, x, y, u0, v0, dt, bx, by);
+        if (bt_v != nullptr) {
+          const float2 b = bt_v[k];
+          bx = b.x;
+          by = b.y;
+        } else {
+          backtrace(u_in, v_in, nx, ny, h, x, y, u0, v0, dt, bx, by);
+        }
         v_out[k] = clamp_stencil_v(v_in, nx, ny, h, bx, by, corrected);
       }
     }
@@ -99,7 +114,7 @@ __global__ void __launch_bounds__(256) k_advect_dye(int nx, int ny, Spacing h, i
                                                     float* __restrict__ q_out, const uint8_t* __restrict__ label,
                                                     const StepScalars* __restrict__ sc,
                                                     const float* __restrict__ patch, int pi0, int pj0, int pnx,
-                                                    int pny) {
+                                                    int pny, float2* __restrict__ bt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= dnx || j >= dny) return;
@@ -121,12 +136,19 @@ __global__ void __launch_bounds__(256) k_advect_dye(int nx, int ny, Spacing h, i
     float bx, by;
     if (MODE == 0) {
       backtrace(u, v, nx, ny, h, x, y, u0, v0, dt, bx, by);
+      if (bt != nullptr) bt[k] = make_float2(bx, by);
 #pragma unroll
       for (int c = 0; c < DYE_CHANNELS; c++) q[c] = sample_p(q_in + c * cells, dnx, dny, dh, bx, by);
     } else {
       float rbx, rby;
       backtrace(u, v, nx, ny, h, x, y, u0, v0, -dt, rbx, rby);
-      backtrace(u, v, nx, ny, h, x, y, u0, v0, dt, bx, by);
+      if (bt != nullptr) {
+        const float2 b = bt[k];
+        bx = b.x;
+        by = b.y;
+      } else {
+        backtrace(u, v, nx, ny, h, x, y, u0, v0, dt, bx, by);
+      }
 #pragma unroll
       for (int c = 0; c < DYE_CHANNELS; c++) {
         const float qbar = sample_p(q_hat + c * cells, dnx, dny, dh, rbx, rby);
@@ -160,15 +182,20 @@ __global__ void __launch_bounds__(256) k_advect_dye(int nx, int ny, Spacing h, i
 
 void launch_advect_velocity(cudaStream_t s, int nx, int ny, float h, int mac, const float* u_in, const float* v_in,
                             float* u_hat, float* v_hat, float* u_out, float* v_out, const uint8_t* label,
-                            const StepScalars* sc) {
+                            const StepScalars* sc, float2* bt_u, float2* bt_v) {
   const Spacing hs = make_spacing(h);
   dim3 blk(32, 8);
   dim3 grd((nx + 1 + blk.x - 1) / blk.x, (ny + 1 + blk.y - 1) / blk.y);
   if (mac) {
-    k_advect_velocity<0><<<grd, blk, 0, s>>>(nx, ny, hs, u_in, v_in, nullptr, nullptr, u_hat, v_hat, label, sc);
-    k_advect_velocity<1><<<grd, blk, 0, s>>>(nx, ny, hs, u_in, v_in, u_hat, v_hat, u_out, v_out, label, sc);
+    // the correction reuses the forward pass's backtrace positions when
+    // there is room for them (bt_u, bt_v; identical to recomputing them)
+    k_advect_velocity<0><<<grd, blk, 0, s>>>(nx, ny, hs, u_in, v_in, nullptr, nullptr, u_hat, v_hat, label, sc, bt_u,
+                                             bt_v);
+    k_advect_velocity<1><<<grd, blk, 0, s>>>(nx, ny, hs, u_in, v_in, u_hat, v_hat, u_out, v_out, label, sc, bt_u,
+                                             bt_v);
   } else {
-    k_advect_velocity<0><<<grd, blk, 0, s>>>(nx, ny, hs, u_in, v_in, nullptr, nullptr, u_out, v_out, label, sc);
+    k_advect_velocity<0><<<grd, blk, 0, s>>>(nx, ny, hs, u_in, v_in, nullptr, nullptr, u_out, v_out, label, sc,
+                                             nullptr, nullptr);
   }
 }
 
@@ -181,26 +208,27 @@ cudaError_t preload_advect_kernels() {
 
 void launch_advect_dye(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, int mac, const float* u,
                        const float* v, const float* q_in, float* q_hat, float* q_out, const uint8_t* label,
-                       const StepScalars* sc, bool tail, const float* patch, int pi0, int pj0, int pnx, int pny) {
+                       const StepScalars* sc, bool tail, const float* patch, int pi0, int pj0, int pnx, int pny,
+                       float2* bt) {
   const Spacing hs = make_spacing(h), ds = make_spacing(dh);
   dim3 blk(32, 8);
   dim3 grd((dnx + blk.x - 1) / blk.x, (dny + blk.y - 1) / blk.y);
   if (mac) {
     k_advect_dye<0, false><<<grd, blk, 0, s>>>(nx, ny, hs, dnx, dny, ds, u, v, q_in, nullptr, q_hat, label, sc, nullptr,
-                                               0, 0, 0, 0);
+                                               0, 0, 0, 0, bt);
     if (tail)
       k_advect_dye<1, true><<<grd, blk, 0, s>>>(nx, ny, hs, dnx, dny, ds, u, v, q_in, q_hat, q_out, label, sc, patch,
-                                                pi0, pj0, pnx, pny);
+                                                pi0, pj0, pnx, pny, bt);
     else
       k_advect_dye<1, false><<<grd, blk, 0, s>>>(nx, ny, hs, dnx, dny, ds, u, v, q_in, q_hat, q_out, label, sc,
-                                                 nullptr, 0, 0, 0, 0);
+                                                 nullptr, 0, 0, 0, 0, bt);
   } else {
     if (tail)
       k_advect_dye<0, true><<<grd, blk, 0, s>>>(nx, ny, hs, dnx, dny, ds, u, v, q_in, nullptr, q_out, label, sc, patch,
-                                                pi0, pj0, pnx, pny);
+                                                pi0, pj0, pnx, pny, nullptr);
     else
       k_advect_dye<0, false><<<grd, blk, 0, s>>>(nx, ny, hs, dnx, dny, ds, u, v, q_in, nullptr, q_out, label, sc,
-                                                 nullptr, 0, 0, 0, 0);
+                                                 nullptr, 0, 0, 0, 0, nullptr);
   }
 }
 

@@ -179,6 +179,9 @@ void free_all(Engine* e) {
   cudaFree(e->r32);
   cudaFree(e->pprev32);
   cudaFree(e->pprev64);
+  cudaFree(e->bt_u);
+  cudaFree(e->bt_v);
+  cudaFree(e->bt_d);
   cudaFree(e->ctl);
   cudaFree(e->ws_scales);
   destroy_graphs(e);
@@ -360,9 +363,10 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
   const double N = (double)e->cells(), F = (double)(e->ufaces() + e->vfaces()), D = (double)e->dye_cells();
   int tok = prof_begin(*e, FL_PH_ADVECT_VELOCITY);
   launch_advect_velocity(s, e->nx, e->ny, e->h, mac, e->u[par], e->v[par], e->u_hat, e->v_hat, e->u[1 - par],
-                         e->v[1 - par], L0.label, e->sc);
-  // forward: carrier u,v + label in, faces out; correction: u,v + hat + label in, faces out
-  prof_end(*e, tok, mac ? (8 * F + N) + (12 * F + N) : 8 * F + N, mac ? 2 : 1);
+                         e->v[1 - par], L0.label, e->sc, e->bt_u, e->bt_v);
+  // forward: carrier u,v + label in, faces out (MacCormack: + backtrace positions out);
+  // correction: u,v + hat + positions + label in, faces out
+  prof_end(*e, tok, mac ? (16 * F + N) + (20 * F + N) : 8 * F + N, mac ? 2 : 1);
   float* u = e->u[1 - par];
   float* v = e->v[1 - par];
   if (stir) launch_stir(s, e->nx, e->ny, e->h, u, v, L0.label, e->stir);
@@ -487,9 +491,10 @@ void enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
   wait_dye(e, s);
   tok = prof_begin(*e, FL_PH_ADVECT_DYE);
   launch_advect_dye(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, mac, u, v, e->dye[par], e->dye_hat, e->dye[1 - par],
-                    L0.label, e->sc, true, e->patch, e->pi0, e->pj0, e->pnx, e->pny);
-  // forward: u,v + 3 planes + label in, 3 planes out; correction adds the hat planes
-  prof_end(*e, tok, mac ? (4 * F + 24 * D + N) + (4 * F + 36 * D + N) : 4 * F + 24 * D + N, mac ? 2 : 1);
+                    L0.label, e->sc, true, e->patch, e->pi0, e->pj0, e->pnx, e->pny, e->bt_d);
+  // forward: u,v + 3 planes + label in, 3 planes out (MacCormack: + backtrace
+  // positions out); correction adds the hat planes and the positions
+  prof_end(*e, tok, mac ? (4 * F + 32 * D + N) + (4 * F + 44 * D + N) : 4 * F + 24 * D + N, mac ? 2 : 1);
   tok = prof_begin(*e, FL_PH_CFL);
   launch_max_speed(s, e->nx, e->ny, u, v, e->acc, e->sc, e->time_dev, &e->prm, e->h, device_dt, device_dt);
   prof_end(*e, tok, 4 * F, 1);
@@ -810,6 +815,9 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   s = s ? s : dalloc(e, (void**)&e->r32, cf, "residual");
   s = s ? s : dalloc(e, (void**)&e->pprev32, cf, "previous pressure");
   s = s ? s : dalloc(e, (void**)&e->pprev64, (size_t)e->cells() * 8, "previous pressure");
+  s = s ? s : dalloc(e, (void**)&e->bt_u, (size_t)e->ufaces() * sizeof(float2), "backtrace positions");
+  s = s ? s : dalloc(e, (void**)&e->bt_v, (size_t)e->vfaces() * sizeof(float2), "backtrace positions");
+  s = s ? s : dalloc(e, (void**)&e->bt_d, (size_t)e->dye_cells() * sizeof(float2), "backtrace positions");
   s = s ? s : dalloc(e, (void**)&e->ctl, sizeof(SolveCtl), "solve control");
   s = s ? s : dalloc(e, (void**)&e->ws_scales, 4 * sizeof(float), "warm-start scales");
   if (s) return bail(s);

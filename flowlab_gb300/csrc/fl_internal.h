@@ -60,6 +60,9 @@ struct Engine {
   SolveCtl* ctl_host = nullptr;  // pinned mirror
 
   // whole-step CUDA graphs, one per velocity/dye buffer parity
+  float2* bt_u = nullptr;  // MacCormack backtrace positions (u faces, v faces, dye cells)
+  float2* bt_v = nullptr;
+  float2* bt_d = nullptr;
   cudaStream_t stream2 = nullptr;  // capture stream of the cycle-loop body; copies of fl_step_host
   // fl_step_host: the dye upload on stream2 (waited for by the step's first
   // dye reader), the projection's end (velocity and pressure final), and
@@ -139,12 +142,16 @@ void set_global_error(const char* fmt, ...);
 // ------------------------------------------------------------- launchers
 
 // fl_advect.cu
+// bt_u / bt_v / bt (optional): room for the MacCormack forward pass's
+// backtrace positions, which the correction then reads instead of
+// recomputing them (same values).
 void launch_advect_velocity(cudaStream_t s, int nx, int ny, float h, int mac, const float* u_in, const float* v_in,
                             float* u_hat, float* v_hat, float* u_out, float* v_out, const uint8_t* label,
-                            const StepScalars* sc);
+                            const StepScalars* sc, float2* bt_u = nullptr, float2* bt_v = nullptr);
 void launch_advect_dye(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, int mac, const float* u,
                        const float* v, const float* q_in, float* q_hat, float* q_out, const uint8_t* label,
-                       const StepScalars* sc, bool tail, const float* patch, int pi0, int pj0, int pnx, int pny);
+                       const StepScalars* sc, bool tail, const float* patch, int pi0, int pj0, int pnx, int pny,
+                       float2* bt = nullptr);
 // Loads the velocity-advection kernels (so that later launches need no module load).
 cudaError_t preload_advect_kernels();
 
