@@ -376,10 +376,9 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
   double fbytes = 0;
   int flaunch = 0;
   if (conf) {
-    launch_vorticity(s, e->nx, e->ny, e->h, u, v, e->w);
-    launch_confinement_force(s, e->nx, e->ny, e->h, e->w, L0.label, (float)e->prm.confinement, e->fx, e->fy);
-    fbytes += (4 * F + 4 * N) + (4 * N + N + 8 * N);
-    flaunch += 2;
+    launch_vort_confine(s, e->nx, e->ny, e->h, u, v, L0.label, (float)e->prm.confinement, e->fx, e->fy);
+    fbytes += 4 * F + N + 8 * N;
+    flaunch += 1;
   }
   if (beta_on || alpha_on) wait_dye(e, s);
   if (beta_on || alpha_on || conf) {

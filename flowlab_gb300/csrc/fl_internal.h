@@ -157,6 +157,9 @@ cudaError_t preload_advect_kernels();
 
 // fl_project.cu
 void launch_vorticity(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* w);
+// vorticity + confinement force in one pass (the same values as the two launches)
+void launch_vort_confine(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v,
+                         const uint8_t* label, float eps, float* fx, float* fy);
 void launch_confinement_force(cudaStream_t s, int nx, int ny, float h, const float* w, const uint8_t* label,
                               float eps, float* fx, float* fy);
 void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, float* u, float* v,

@@ -56,6 +56,53 @@ __global__ void k_confinement_force(int nx, int ny, Spacing h1, Spacing h2, cons
   fy[k] = epsh * (-(Nx * wk));
 }
 
+// k_vorticity and k_confinement_force in one pass: a 32 x 8 tile of cells
+// computes the vorticity of its cells and a one-cell ring into shared
+// memory (the same corner-curl formula and clamping), then the confinement
+// force of its own cells from it. u and v are only read here; the forces
+// are applied by k_forces afterwards.
+__global__ void __launch_bounds__(256) k_vort_confine(int nx, int ny, Spacing h, Spacing h1, Spacing h2,
+                                                      const float* __restrict__ u, const float* __restrict__ v,
+                                                      const uint8_t* __restrict__ label, float epsh,
+                                                      float* __restrict__ fx, float* __restrict__ fy) {
+  constexpr int TX = 32, TY = 8;
+  __shared__ float ws[TY + 2][TX + 2];
+  const int X0 = blockIdx.x * TX, Y0 = blockIdx.y * TY;
+  const int t = threadIdx.x + TX * threadIdx.y;
+  const int hiI = nx - 1, hiJ = ny - 1;
+  for (int e = t; e < (TX + 2) * (TY + 2); e += TX * TY) {
+    const int lx = e % (TX + 2), ly = e / (TX + 2);
+    const int i = X0 - 1 + lx, j = Y0 - 1 + ly;
+    float wv = 0.0f;
+    if (i >= 0 && j >= 0 && i < nx && j < ny) {
+      const int j0 = min(max(j, 1), hiJ), j1 = min(max(j + 1, 1), hiJ);
+      const int i0 = min(max(i, 1), hiI), i1 = min(max(i + 1, 1), hiI);
+      wv = 0.25f * (curl_at_corner(u, v, nx, h, i0, j0) + curl_at_corner(u, v, nx, h, i1, j0) +
+                    curl_at_corner(u, v, nx, h, i0, j1) + curl_at_corner(u, v, nx, h, i1, j1));
+    }
+    ws[ly][lx] = wv;
+  }
+  __syncthreads();
+  const int i = X0 + threadIdx.x, j = Y0 + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const long k = i + (long)j * nx;
+  if (label[k] == SOLID) {
+    fx[k] = 0.0f;
+    fy[k] = 0.0f;
+    return;
+  }
+  const int ie = min(i + 1, nx - 1), iw = max(i - 1, 0);
+  const int jn = min(j + 1, ny - 1), js = max(j - 1, 0);
+  const int lx = threadIdx.x + 1, ly = threadIdx.y + 1;
+  const float gx = over(fabsf(ws[ly][lx + (ie - i)]) - fabsf(ws[ly][lx - (i - iw)]), ie - iw == 2 ? h2 : h1);
+  const float gy = over(fabsf(ws[ly + (jn - j)][lx]) - fabsf(ws[ly - (j - js)][lx]), jn - js == 2 ? h2 : h1);
+  const float mag = sqrtf(gx * gx + gy * gy) + 1e-20f;
+  const float Nx = gx / mag, Ny = gy / mag;
+  const float wk = ws[ly][lx];
+  fx[k] = epsh * (Ny * wk);
+  fy[k] = epsh * (-(Nx * wk));
+}
+
 // Body forces on the faces they may write (buoyancy.ts:70-88 bounds for v,
 // stir.ts:49-83 bounds for u): v += (beta*dt)*T + (-alpha*dt)*s, then the
 // confinement face average. One thread per (u face, v face) pair, in place:
@@ -388,6 +435,13 @@ void launch_confinement_force(cudaStream_t s, int nx, int ny, float h, const flo
   dim3 b(32, 8);
   k_confinement_force<<<grid2(nx, ny, b), b, 0, s>>>(nx, ny, make_spacing(1.0f * h), make_spacing(2.0f * h), w,
                                                      label, eps * h, fx, fy);
+}
+
+void launch_vort_confine(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v,
+                         const uint8_t* label, float eps, float* fx, float* fy) {
+  dim3 b(32, 8);
+  k_vort_confine<<<grid2(nx, ny, b), b, 0, s>>>(nx, ny, make_spacing(h), make_spacing(1.0f * h),
+                                                make_spacing(2.0f * h), u, v, label, eps * h, fx, fy);
 }
 
 void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, float* u, float* v,
