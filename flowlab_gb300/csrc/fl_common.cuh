@@ -255,6 +255,28 @@ __device__ inline float block_max(float v, float* shm32) {
   return t;
 }
 
+// Bit casts opaque to the compiler's optimiser: through the plain
+// intrinsics it recognises sign-bit masks and flips on a double's bits as
+// fabs / fneg / compares and emits them as float64 instructions, the very
+// pipe these helpers exist to avoid.
+__device__ __forceinline__ unsigned long long dbits_opaque(double x) {
+  unsigned long long u;
+  asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+  return u;
+}
+__device__ __forceinline__ double dfrom_opaque(unsigned long long u) {
+  double x;
+  asm("mov.b64 %0, %1;" : "=d"(x) : "l"(u));
+  return x;
+}
+
+// The rare cases of the integer helpers below, out of line: inlined, the
+// compiler predicates these instructions into the common path, where they
+// would occupy GB300's slow float64 pipe on every call.
+static __device__ __noinline__ double f2d_slow(float f) { return (double)f; }
+static __device__ __noinline__ double dmul_slow(double x, double y) { return x * y; }
+static __device__ __noinline__ float d2f_slow(double d) { return (float)d; }
+
 // Exact float -> double by bit manipulation (integer pipe) for zero and
 // normal floats; subnormals, infinities and NaN take the conversion
 // instruction. The result equals (double)f in every case.
@@ -265,21 +287,21 @@ __device__ __forceinline__ double f2d_exact(float f) {
   if (ex != 0u && ex != 0xffu) {
     const unsigned long long bits =
         sign | ((unsigned long long)(ex + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)bits);
+    return dfrom_opaque(bits);
   }
-  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)sign);
-  return (double)f;
+  if ((u & 0x7fffffffu) == 0u) return dfrom_opaque(sign);
+  return f2d_slow(f);
 }
 
 // x * 2^k (k = 1, 2) by an exponent increment when x is normal and the
 // product stays normal; zero returns itself (as x * 2^k does); otherwise
 // the multiply. Equal to x * 2^k in every case.
 __device__ __forceinline__ double scale_pow2(double x, int k) {
-  const long long bits = __double_as_longlong(x);
+  const long long bits = (long long)dbits_opaque(x);
   const long long ex = (bits >> 52) & 0x7ff;
-  if (ex != 0 && ex < 0x7ff - k) return __longlong_as_double(bits + ((long long)k << 52));
+  if (ex != 0 && ex < 0x7ff - k) return dfrom_opaque((unsigned long long)(bits + ((long long)k << 52)));
   if ((bits & 0x7fffffffffffffffll) == 0) return x;
-  return x * (double)(1 << k);
+  return dmul_slow(x, (double)(1 << k));
 }
 
 // Double -> float rounded to nearest even by integer operations when the
@@ -288,7 +310,7 @@ __device__ __forceinline__ double scale_pow2(double x, int k) {
 // cases (results that are zero or subnormal, overflowing exponents, NaN)
 // take the conversion instruction. Equal to (float)d in every case.
 __device__ __forceinline__ float d2f_rn(double d) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned long long b = dbits_opaque(d);
   const unsigned ex = (unsigned)(b >> 52) & 0x7ffu;
   if (ex >= 897u && ex <= 1150u) {  // float biased exponent 1..254
     const unsigned long long m = b & 0xfffffffffffffull;
@@ -297,13 +319,13 @@ __device__ __forceinline__ float d2f_rn(double d) {
     f += (rem > 0x10000000ull || (rem == 0x10000000ull && (f & 1ull))) ? 1ull : 0ull;
     return __uint_as_float((unsigned)(b >> 63) << 31 | (unsigned)f);
   }
-  return (float)d;
+  return d2f_slow(d);
 }
 
 // 0.0 + x: x itself except that -0.0 becomes +0.0.
 __device__ __forceinline__ double zero_plus(double x) {
-  const long long bits = __double_as_longlong(x);
-  return bits == (long long)0x8000000000000000ull ? 0.0 : x;
+  const unsigned long long bits = dbits_opaque(x);
+  return bits == 0x8000000000000000ull ? 0.0 : x;
 }
 
 }  // namespace fl

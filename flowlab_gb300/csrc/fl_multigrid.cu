@@ -651,18 +651,20 @@ __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
 // The float64 defect-correction pass (iterative refinement, solveMixed):
 // p64' = p64 + e (when `update`), then r = b - (count*p64' - sum) in double
 // with the neighbour sum in the order +x, -x, +y, -y, r32 = float(r), and
-// the squared norm of r accumulated. GB300 issues few float64 operations per
-// clock, so this pass is bound by its float64 arithmetic, not by memory. It
-// spends float64 instructions only where the result needs them: each p64' is
-// formed once and handed to its neighbours in registers (the rows above and
-// below, a rolling column) and by warp shuffles (left and right); the exact
-// float -> double widenings, the first addition to 0.0, the products by 2
-// and 4 and the rounding of r to float are done on the integer pipe with
-// identical results. A warp owns 30
-// interior columns (lanes 1..30; lanes 0 and 31 are the halo) and UR_ROWS
-// rows; the halo rows and columns are formed redundantly. Eight rows keep the
-// kernel at 64 registers (32 warps per SM to hide the float64 latency):
-// faster than sixteen rows despite the larger halo share (measured).
+// the squared norm of r accumulated. GB300 issues float64 arithmetic at about
+// 1.6 lanes per clock per SM (measured; 32-bit integer adds: ~100), so this
+// pass is bound by its float64 instructions, not by memory, and spends them
+// only where the result needs them: each p64' is formed once and handed to
+// its neighbours in registers (the rows above and below) and by warp
+// shuffles (left and right); the exact float -> double widenings, the first
+// addition to 0.0, the products by 2 and 4 and the rounding of r to float
+// run on the integer pipe with identical results (fl_common.cuh), with their
+// rare cases out of line and their bit casts opaque, so that the compiler
+// neither predicates nor re-forms float64 instructions into every cell.
+// A warp owns 30 interior columns (lanes 1..30; lanes 0 and 31 are the halo
+// columns, formed redundantly) and walks UR_ROWS rows as a rolling window
+// (row above, row, row below), the raw values of the row two below loaded one
+// iteration ahead of their use.
 constexpr int UR_ROWS = 8;
 constexpr int UR_WARPS = 8;
 
@@ -685,42 +687,54 @@ __global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny
   const bool col = gx >= 0 && gx < nx;
   const bool own = col && lane != 0 && lane != 31;
 
-  double pn[UR_ROWS + 2];
-  float bv[UR_ROWS];
-  uint8_t cv[UR_ROWS];
-#pragma unroll
-  for (int t = 0; t < UR_ROWS + 2; t++) {
-    const int gy = y0 - 1 + t;
-    double v = 0.0;
-    if (col && gy >= 0 && gy < ny) {
-      const long k = gx + (long)gy * nx;
-      v = p_in[k];
-      if (UPDATE) v += f2d_exact(e[k]);
+  // raw p64 and e of row y (zero outside the grid), and p64' formed from them
+  auto raw = [&](int y, double& rp, float& re) {
+    rp = 0.0;
+    re = 0.0f;
+    if (col && y >= 0 && y < ny) {
+      const long k = gx + (long)y * nx;
+      rp = p_in[k];
+      if (UPDATE) re = e[k];
     }
-    pn[t] = v;
-    if (t >= 1 && t <= UR_ROWS) {
-      const bool in = own && gy < ny;
-      const long k = gx + (long)gy * nx;
-      bv[t - 1] = in ? b[k] : 0.0f;
-      cv[t - 1] = in ? code[k] : (uint8_t)CODE_OUTSIDE;
-    }
+  };
+  auto form = [](double rp, float re) { return UPDATE ? rp + f2d_exact(re) : rp; };
+  double rp, rp0;
+  float re, re0;
+  raw(y0 - 1, rp0, re0);
+  raw(y0, rp, re);
+  double pm = form(rp0, re0), pc = form(rp, re);
+  raw(y0 + 1, rp, re);
+  float bnext = 0.0f;
+  uint8_t cnext = (uint8_t)CODE_OUTSIDE;
+  if (own && y0 < ny) {
+    const long k = gx + (long)y0 * nx;
+    bnext = b[k];
+    cnext = code[k];
   }
 
   double sq = 0.0;
   unsigned long long n = 0;
-#pragma unroll
-  for (int t = 1; t <= UR_ROWS; t++) {
-    const double left = __shfl_up_sync(0xffffffffu, pn[t], 1);
-    const double right = __shfl_down_sync(0xffffffffu, pn[t], 1);
-    const int gy = y0 - 1 + t;
-    if (!own || gy >= ny) continue;
-    const long k = gx + (long)gy * nx;
-    if (UPDATE) p_out[k] = pn[t];
-    const uint8_t c = cv[t - 1];
-    float r = 0.0f;
-    if ((c & 3u) == FLUID) {
+#pragma unroll 1
+  for (int t = 0; t < UR_ROWS; t++) {
+    const int gy = y0 + t;
+    if (gy >= ny) break;  // the same for the whole warp
+    const double pp = form(rp, re);
+    raw(gy + 2, rp, re);
+    const float bv = bnext;
+    const uint8_t c = cnext;
+    if (own && gy + 1 < ny && t + 1 < UR_ROWS) {
+      const long k = gx + (long)(gy + 1) * nx;
+      bnext = b[k];
+      cnext = code[k];
+    }
+    const double left = __shfl_up_sync(0xffffffffu, pc, 1);
+    const double right = __shfl_down_sync(0xffffffffu, pc, 1);
+    if (own) {
+      const long k = gx + (long)gy * nx;
+      if (UPDATE) p_out[k] = pc;
+      float r = 0.0f;
       const int cnt = code_count(c);
-      if (cnt > 0) {
+      if ((c & 3u) == FLUID && cnt > 0) {
         // the first linked term enters as 0.0 + term
         double sum;
         bool first = true;
@@ -733,21 +747,23 @@ __global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny
           first = false;
         }
         if (c & LINK_YP) {
-          sum = first ? zero_plus(pn[t + 1]) : sum + pn[t + 1];
+          sum = first ? zero_plus(pp) : sum + pp;
           first = false;
         }
-        if (c & LINK_YM) sum = first ? zero_plus(pn[t - 1]) : sum + pn[t - 1];
-        const double cp = cnt == 4 ? scale_pow2(pn[t], 2)
-                          : cnt == 2 ? scale_pow2(pn[t], 1)
-                          : cnt == 1 ? pn[t]
-                                     : 3.0 * pn[t];
-        const double rd = f2d_exact(bv[t - 1]) - (cp - sum);
+        if (c & LINK_YM) sum = first ? zero_plus(pm) : sum + pm;
+        const double cp = cnt == 4 ? scale_pow2(pc, 2)
+                          : cnt == 2 ? scale_pow2(pc, 1)
+                          : cnt == 1 ? pc
+                                     : dmul_slow(pc, 3.0);
+        const double rd = f2d_exact(bv) - (cp - sum);
         r = d2f_rn(rd);
         sq = fma(rd, rd, sq);
         n += 1;
       }
+      r32[k] = r;
     }
-    r32[k] = r;
+    pm = pc;
+    pc = pp;
   }
   const double bs = block_sum(sq, red);
   const unsigned long long bn = block_sum_u64(n, redn);

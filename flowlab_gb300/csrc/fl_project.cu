@@ -182,9 +182,10 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
 // With nx == 2 both edges meet at face 1, handled left then right as the
 // reference's loop order does.
 // Pressure difference between two cells: float32, or with a float64
-// pressure the difference formed in double and rounded once.
+// pressure the difference formed in double and rounded once (the rounding
+// on the integer pipe: d2f_rn equals the conversion instruction).
 __device__ __forceinline__ float pdiff(const float* __restrict__ p, const double* __restrict__ p64, long a, long b) {
-  return p64 ? (float)(p64[a] - p64[b]) : p[a] - p[b];
+  return p64 ? d2f_rn(p64[a] - p64[b]) : p[a] - p[b];
 }
 
 __device__ __forceinline__ float projected_u(const float* __restrict__ p, const double* __restrict__ p64,
