@@ -63,7 +63,7 @@ def baseline_metric():
 # What bounds each phase's kernels at 1024^2 when it is not HBM (ncu summaries
 # under profiles/): the roofline line names it beside the HBM fraction.
 LIMITERS = {
-    "defect64": "float64 pipe (ncu: 71-74% of peak float64 issue), not memory",
+    "defect64": "float64 pipe (ncu: 73-74% of peak float64 issue), not memory",
     "mg_coarse": "latency: one CTA, a chain of dependent barrier phases",
     "mg_pre": "latency: small levels, few CTAs per launch",
     "mg_post": "latency: small levels, few CTAs per launch",
@@ -74,8 +74,8 @@ LIMITERS = {
 # phase's dominant kernel from one ncu capture of the 1024^2 plume's eager
 # profiled steps (profiles/): (bytes, kernel, summary file).
 TRAFFIC_PLUME_1024 = {
-    "defect64": (17.865216e6, "k_update_resid64<1>", "profiles/k_mg_coarse_resid64_plume_1024.md"),
-    "mg_coarse": (0.087552e6, "k_mg_coarse", "profiles/k_mg_coarse_resid64_plume_1024.md"),
+    "defect64": (17.8432e6, "k_update_resid64<1>", "profiles/k_mg_coarse_resid64_plume_1024.md"),
+    "mg_coarse": (0.089088e6, "k_mg_coarse", "profiles/k_mg_coarse_resid64_plume_1024.md"),
 }
 
 
