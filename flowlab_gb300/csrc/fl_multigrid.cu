@@ -196,7 +196,12 @@ __global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs
         bb[r][o] = 0.0f;
         xx[r][o] = 0.0f;
       }
-      xs[(li + lj) & 1][lj][tx] = xx[r][o];
+      // Solid cells (and cells outside the grid) are exactly the neighbours
+      // no link points to; they hold +0.0 in shared memory (their own value
+      // stays in xx), so that a sweep can add all four neighbours without a
+      // test: an unlinked one adds +0.0, which leaves the sum's bits
+      // unchanged (a sum that starts at +0.0 never becomes -0.0).
+      xs[(li + lj) & 1][lj][tx] = (cd[r][o] & 3u) == SOLID ? 0.0f : xx[r][o];
     }
   }
   __syncthreads();
@@ -212,7 +217,6 @@ __global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs
     int oc[2];
     oc[0] = (g + ty) & 1;
     oc[1] = 1 - oc[0];
-    uint8_t cc[2][2];
     bool act[2][2];
     float sb[2][2], rc[2][2], xc[2][2];
 #pragma unroll
@@ -223,7 +227,6 @@ __global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs
         const int lj = ty + RGN_T * r, li = 2 * tx + o;
         const uint8_t code = o ? cd[r][1] : cd[r][0];
         const int cnt = code_count(code);
-        cc[r][c] = code;
         act[r][c] = li != 0 && li != RGN - 1 && lj != 0 && lj != RGN - 1 && (code & 3u) == FLUID && cnt > 0;
         sb[r][c] = scale * (o ? bb[r][1] : bb[r][0]);
         rc[r][c] = cnt == 4 ? 0.25f : (cnt == 2 ? 0.5f : (cnt == 1 ? 1.0f : 0.0f));
@@ -239,12 +242,11 @@ __global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs
         if (!act[r][c]) continue;
         const int lj = ty + RGN_T * r;
         const int o = oc[c];
-        const uint8_t code = cc[r][c];
         float sum = 0.0f;
-        if (code & LINK_XP) sum += xo[lj][tx + o];
-        if (code & LINK_XM) sum += xo[lj][tx + o - 1];
-        if (code & LINK_YP) sum += xo[lj + 1][tx];
-        if (code & LINK_YM) sum += xo[lj - 1][tx];
+        sum += xo[lj][tx + o];
+        sum += xo[lj][tx + o - 1];
+        sum += xo[lj + 1][tx];
+        sum += xo[lj - 1][tx];
         const float d = sum - sb[r][c];
         const float third = div3(d);
         const float pgs = rc[r][c] != 0.0f ? d * rc[r][c] : third;
@@ -442,9 +444,9 @@ __device__ __forceinline__ float coarse_residual(const CoarseView& v, int i, int
 // levels most warps hold boundary cells, and a lane-divergent branch around
 // each neighbour load serialised the warp (measured: a one-warp half-sweep
 // took ~630 cycles that way, ~270 with unconditional loads). An unlinked
-// neighbour is read at the cell's own address and contributes +0.0, which
-// leaves the sum's bits unchanged: a running sum that starts at +0.0 never
-// becomes -0.0.
+// neighbour is read at the zero word that starts shared memory and adds
+// +0.0, which leaves the sum's bits unchanged: a running sum that starts at
+// +0.0 never becomes -0.0.
 __device__ __forceinline__ float lds_f32(uint32_t addr) {
   float v;
   asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
@@ -458,14 +460,14 @@ __device__ void tail_smooth(unsigned char* smem, const CoarseLevel& L, int l, in
                             int lane) {
   if (w >= L.nwarps) return;
   float* xs = reinterpret_cast<float*>(smem) + L.off_x;
-  const uint32_t xs_sh = static_cast<uint32_t>(__cvta_generic_to_shared(xs));
+  const uint32_t sm_sh = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
   const float* bs = reinterpret_cast<const float*>(smem) + L.off_b;
   const uint8_t* cs = smem + L.off_c;
   // row stride: the lanes per row (a power of two), so that the rows a warp
   // covers fall in distinct shared-memory banks
   const int rs = 1 << L.lsh;
   const int plane = L.ny * rs;
-  unsigned mask[2][2];  // bits 0-3: neighbour links; bit 4: the cell is updated
+  bool upd[2][2];  // the cell is updated
   int own[2][2], nb[2][2][4];
   float bq[2][2], xq[2][2], rc[2][2];
 #pragma unroll
@@ -478,27 +480,29 @@ __device__ void tail_smooth(unsigned char* smem, const CoarseLevel& L, int l, in
       const uint8_t code = ok ? cs[i + j * L.nx] : (uint8_t)CODE_OUTSIDE;
       const int cnt = code_count(code);
       const bool act = ok && (code & 3u) == FLUID && cnt > 0;
-      const int ow = ok ? c * plane + j * rs + (i >> 1) : 0;
-      const int o = (1 - c) * plane + j * rs + (i >> 1), d = i & 1;
+      // float indices from the start of shared memory; an unlinked
+      // neighbour (and every neighbour of a cell outside the level) is the
+      // zero word at index 0
+      const int ow = L.off_x + (ok ? c * plane + j * rs + (i >> 1) : 0);
+      const int o = L.off_x + (1 - c) * plane + j * rs + (i >> 1), d = i & 1;
       own[s][c] = ow;
-      nb[s][c][0] = (ok && (code & LINK_XP)) ? o + d : ow;
-      nb[s][c][1] = (ok && (code & LINK_XM)) ? o + d - 1 : ow;
-      nb[s][c][2] = (ok && (code & LINK_YP)) ? o + rs : ow;
-      nb[s][c][3] = (ok && (code & LINK_YM)) ? o - rs : ow;
-      mask[s][c] = (act ? 16u : 0u) | ((code & LINK_XP) ? 1u : 0u) | ((code & LINK_XM) ? 2u : 0u) |
-                   ((code & LINK_YP) ? 4u : 0u) | ((code & LINK_YM) ? 8u : 0u);
+      nb[s][c][0] = (ok && (code & LINK_XP)) ? o + d : 0;
+      nb[s][c][1] = (ok && (code & LINK_XM)) ? o + d - 1 : 0;
+      nb[s][c][2] = (ok && (code & LINK_YP)) ? o + rs : 0;
+      nb[s][c][3] = (ok && (code & LINK_YM)) ? o - rs : 0;
+      upd[s][c] = act;
       rc[s][c] = cnt == 4 ? 0.25f : (cnt == 2 ? 0.5f : (cnt == 1 ? 1.0f : 0.0f));
       bq[s][c] = ok ? bs[i + j * L.nx] : 0.0f;
-      xq[s][c] = ok ? xs[ow] : 0.0f;
+      xq[s][c] = ok ? xs[ow - L.off_x] : 0.0f;
     }
   // shared-space byte addresses (explicit ld/st.shared)
 #pragma unroll
   for (int s = 0; s < 2; s++)
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      own[s][c] = (int)(xs_sh + 4u * (uint32_t)own[s][c]);
+      own[s][c] = (int)(sm_sh + 4u * (uint32_t)own[s][c]);
 #pragma unroll
-      for (int k = 0; k < 4; k++) nb[s][c][k] = (int)(xs_sh + 4u * (uint32_t)nb[s][c][k]);
+      for (int k = 0; k < 4; k++) nb[s][c][k] = (int)(sm_sh + 4u * (uint32_t)nb[s][c][k]);
     }
   const bool two = L.slots == 2;
   const float keep = 1.0f - omega;
@@ -509,19 +513,18 @@ __device__ void tail_smooth(unsigned char* smem, const CoarseLevel& L, int l, in
 #pragma unroll
       for (int s = 0; s < 2; s++) {
         if (s == 1 && !two) continue;  // warp-uniform: the level has one row group per warp
-        const unsigned m = mask[s][c];
         const float v0 = lds_f32((uint32_t)nb[s][c][0]), v1 = lds_f32((uint32_t)nb[s][c][1]);
         const float v2 = lds_f32((uint32_t)nb[s][c][2]), v3 = lds_f32((uint32_t)nb[s][c][3]);
         float sum = 0.0f;
-        sum += (m & 1u) ? v0 : 0.0f;
-        sum += (m & 2u) ? v1 : 0.0f;
-        sum += (m & 4u) ? v2 : 0.0f;
-        sum += (m & 8u) ? v3 : 0.0f;
+        sum += v0;
+        sum += v1;
+        sum += v2;
+        sum += v3;
         const float dv = sum - (-1.0f) * bq[s][c];
         const float third = div3(dv);
         const float pgs = rc[s][c] != 0.0f ? dv * rc[s][c] : third;
         const float nv = keep * xq[s][c] + omega * pgs;
-        if (m & 16u) {
+        if (upd[s][c]) {
           xq[s][c] = nv;
           sts_f32((uint32_t)own[s][c], nv);
         }
@@ -536,6 +539,7 @@ __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x + 32 * threadIdx.y;
   const int lane = tid & 31, w = tid >> 5;
+  if (tid == 0) reinterpret_cast<float*>(smem)[0] = 0.0f;  // the zero word tail_smooth's unlinked neighbours read
   for (int l = 0; l < a.nlev; l++) {
     const CoarseLevel& L = a.lv[l];
     const int n = L.nx * L.ny;
@@ -1005,7 +1009,7 @@ static int tail_lsh(int nx) {
 }
 
 static size_t coarse_smem_bytes(const Engine& e, int from, int* off_x, int* off_b, int* off_c) {
-  size_t floats = 0;
+  size_t floats = 4;  // 16 bytes: the zero word
   for (int l = from; l < (int)e.levels.size(); l++) {
     const long n = (long)e.levels[l].nx * e.levels[l].ny;
     if (off_x) off_x[l - from] = (int)floats;
