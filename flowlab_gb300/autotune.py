@@ -6,7 +6,8 @@ What it chooses, per scene shape and solver:
                  and the coarsest level's sweep pairs: the fastest
                  combination (device time per step of the whole step, graph
                  path) among those that reach the tolerance on every
-                 measured step;
+                 measured step; then the first level of the single-CTA tail
+                 (mg_tail_side), whose results are identical, by time alone;
   red-black SOR  omega: the smallest relative residual after the fixed sweep
                  budget on the scene's own right-hand sides (the reference's
                  browser setting, a fixed budget, makes accuracy the
@@ -32,6 +33,7 @@ from .native import f32, ptr
 MG_SPACE = {"mg_coarsest": (4, 8, 16, 32), "mg_coarse_sweeps": (8, 16, 32)}
 RB_OMEGAS = (1.5, 1.6, 1.7, 1.8, 1.85, 1.9, 1.95, 1.98)
 RB_PAIRS = (1, 2, 3, 4)
+TAIL_SIDES = (16, 32, 64)
 
 
 def with_params(prm, **kw):
@@ -88,7 +90,7 @@ def pick_omega(results):
     return min(results, key=lambda r: (r[1], r[0]))[0]
 
 
-def tune_multigrid(scene, base, steps=8, warmup=3, space=MG_SPACE, device=0, log=None):
+def tune_multigrid(scene, base, steps=8, warmup=3, space=MG_SPACE, tail_sides=TAIL_SIDES, device=0, log=None):
     results = []
     keys = sorted(space)
     for values in itertools.product(*(space[k] for k in keys)):
@@ -98,7 +100,17 @@ def tune_multigrid(scene, base, steps=8, warmup=3, space=MG_SPACE, device=0, log
         if log:
             log("%s -> %.3f ms/step, %.2f cycles, rel %.2e" % (cand, m["ms"], m["cycles"], m["rel_max"]))
     best = pick_multigrid(results, base.tol)
-    return (best[0] if best else None), results
+    if best is None:
+        return None, results
+    chosen = dict(best[0])
+    timed = []
+    for side in tail_sides:
+        m = measure_steps(scene, with_params(base, mg_tail_side=side, **chosen), steps, warmup, device)
+        timed.append((m["ms"], side))
+        if log:
+            log("mg_tail_side %d -> %.3f ms/step" % (side, m["ms"]))
+    chosen["mg_tail_side"] = min(timed)[1]
+    return chosen, results
 
 
 def rb_residual(scene, base, omega, steps=3, device=0):
@@ -187,7 +199,8 @@ def main(argv=None):
         scene, base = configs.random_scene(a.size, 1), configs.random_scene_params(mixed=1)
     prm = tuned_params(scene, base, a.cache, log=lambda m: print(m, flush=True))
     print(json.dumps({"scene": a.scene, "size": a.size, "mg_coarsest": prm.mg_coarsest,
-                      "mg_coarse_sweeps": prm.mg_coarse_sweeps, "omega": prm.omega, "rb_pairs": prm.rb_pairs}))
+                      "mg_coarse_sweeps": prm.mg_coarse_sweeps, "mg_tail_side": prm.mg_tail_side,
+                      "omega": prm.omega, "rb_pairs": prm.rb_pairs}))
 
 
 if __name__ == "__main__":

@@ -211,6 +211,8 @@ int validate_params(Engine* e, const fl_params* p) {
   // the coarsest level is solved inside the single-CTA tail (sides <= 64)
   if (p->mg_coarsest < 1 || p->mg_coarsest > 64) return fail(e, FL_EINVAL, "mg_coarsest must be in [1, 64]");
   if (p->rb_pairs < 0 || p->rb_pairs > 4) return fail(e, FL_EINVAL, "rb_pairs must be in [0, 4]");
+  // the tail kernel's ownership map holds levels of at most 64 x 64 cells
+  if (p->mg_tail_side < 0 || p->mg_tail_side > 64) return fail(e, FL_EINVAL, "mg_tail_side must be in [0, 64]");
   if (!(p->cfl_target > 0) || !(p->dt_max > 0) || !(p->rho > 0))
     return fail(e, FL_EINVAL, "cfl_target, dt_max and rho must be positive");
   return FL_OK;
@@ -857,7 +859,7 @@ int fl_set_params(fl_engine* h, const fl_params* p) {
   ENTER(h);
   if (!p) return fail(e, FL_EINVAL, "null params");
   TRY(validate_params(e, p));
-  const bool reshape = p->mg_coarsest != e->prm.mg_coarsest;
+  const bool reshape = p->mg_coarsest != e->prm.mg_coarsest || p->mg_tail_side != e->prm.mg_tail_side;
   e->prm = *p;
   destroy_graphs(e);
   TRY(put_step_ctl(e, false));

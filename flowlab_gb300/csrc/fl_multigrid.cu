@@ -374,7 +374,11 @@ struct CoarseArgs {
   StepAccum* acc;
 };
 
-constexpr int COARSE_SIDE = 64;
+// Default first level of the single-CTA tail (fl_params.mg_tail_side = 0):
+// levels with both sides <= 32. Measured on the 1024^2 plume: 1641 steps/s
+// from 32, 1570 from 64, 1636 from 16, 1626 from 8 (below 32 the extra
+// launches cost more than the tail's shorter barrier chain saves).
+constexpr int TAIL_SIDE_DEFAULT = 32;
 
 struct CoarseView {
   float* xs;  // 2 * ny * rs floats
@@ -1075,10 +1079,12 @@ void mg_setup(Engine& e) {
     cudaMemsetAsync(L.x[1], 0, n * sizeof(float), e.stream);
     cudaMemsetAsync(L.b, 0, n * sizeof(float), e.stream);
   }
-  // the tail starts at the first level with both sides <= 64
+  // the tail starts at the first level with both sides <= mg_tail_side (the
+  // coarsest level at the latest)
+  const int side = e.prm.mg_tail_side > 0 ? e.prm.mg_tail_side : TAIL_SIDE_DEFAULT;
   int lc = (int)e.levels.size() - 1;
   for (int l = 0; l < (int)e.levels.size(); l++)
-    if (e.levels[l].nx <= COARSE_SIDE && e.levels[l].ny <= COARSE_SIDE) {
+    if (e.levels[l].nx <= side && e.levels[l].ny <= side) {
       lc = l;
       break;
     }

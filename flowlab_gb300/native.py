@@ -55,7 +55,8 @@ class Params(ctypes.Structure):
         ("mixed", ctypes.c_int),
         ("rb_pairs", ctypes.c_int),
         ("warm_extrapolate", ctypes.c_int),
-        ("reserved", ctypes.c_int * 5),
+        ("mg_tail_side", ctypes.c_int),
+        ("reserved", ctypes.c_int * 4),
     ]
 
 

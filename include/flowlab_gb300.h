@@ -90,7 +90,10 @@ typedef struct fl_params {
                             depth, i.e. the tile/halo shape; results do not depend on it */
   int warm_extrapolate;  /* 1: the multigrid starts from 2 p(n) - p(n-1) on Fluid cells instead of
                             p(n) (no reference counterpart; pressureSolver.ts:28-30 uses p(n)) */
-  int reserved[5];
+  int mg_tail_side;      /* the levels with both sides <= this (1..64; 0: 32) run inside one
+                            single-CTA kernel per V-cycle, the finer ones as their own launches;
+                            results do not depend on it */
+  int reserved[4];
 } fl_params;
 
 /* Per-step report (the reference's sim.iters / sim.dt plus the residual the

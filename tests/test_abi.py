@@ -42,6 +42,8 @@ def test_abi_version_and_defaults(lib):
     assert p.cfl_target == 2.0 and abs(p.dt_max - 1 / 30) < 1e-15 and p.tol == 5e-3
     assert (p.mg_pre, p.mg_post, p.mg_coarse_sweeps, p.mg_coarsest, p.mg_max_cycles) == (2, 2, 8, 4, 3)
     assert ctypes.sizeof(native.Params) == 160
+    assert p.mg_tail_side == 0  # the engine's default first tail level (32)
+    assert native.Params.mg_tail_side.offset == 140 and native.Params.reserved.offset == 144
 
 
 def test_create_fails_loudly_without_a_device(lib):

@@ -433,3 +433,21 @@ def test_step_host_equals_upload_step_and_reads(case):
     finally:
         for eng in engs:
             eng.close()
+
+
+@pytest.mark.parametrize("mixed", [0, 1])
+def test_tail_side_does_not_change_results(mixed):
+    """The levels inside the single-CTA tail (mg_tail_side) against their own
+    launches: identical fields and cycle counts for every split, on the
+    256^2 plume (levels 256..8) and on a 64^2 scene the tail solves whole."""
+    for n in (256, 64):
+        g, f, patch = configs.plume(n)
+        outs = []
+        for side in (8, 16, 32, 64):
+            prm = configs.plume_params(tol=1e-6 if mixed else 1e-4, max_cycles=20, mixed=mixed)
+            prm.mg_tail_side = side
+            outs.append(run_engine(g, f, patch, prm, 3))
+        for side, o in zip((16, 32, 64), outs[1:]):
+            for a, b, name in zip(outs[0][:4], o[:4], ("u", "v", "p", "dye")):
+                assert np.array_equal(a, b), (n, side, name, mismatch(a, b))
+            assert o[4]["cycles"] == outs[0][4]["cycles"]
