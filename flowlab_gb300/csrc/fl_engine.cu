@@ -208,7 +208,7 @@ int validate_params(Engine* e, const fl_params* p) {
     return fail(e, FL_EINVAL, "mg_pre/mg_post must be in [0, 4] (got %d, %d)", p->mg_pre, p->mg_post);
   if (p->mg_coarse_sweeps < 0 || p->mg_max_cycles < 0 || p->pressure_iters < 0)
     return fail(e, FL_EINVAL, "negative sweep or cycle count");
-  // the coarsest level is solved inside the single-CTA tail (sides <= 64)
+  // the coarsest level is solved inside the single-CTA tail (sides <= 64 at most)
   if (p->mg_coarsest < 1 || p->mg_coarsest > 64) return fail(e, FL_EINVAL, "mg_coarsest must be in [1, 64]");
   if (p->rb_pairs < 0 || p->rb_pairs > 4) return fail(e, FL_EINVAL, "rb_pairs must be in [0, 4]");
   // the tail kernel's ownership map holds levels of at most 64 x 64 cells

@@ -343,9 +343,10 @@ __global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs
 
 // ----------------------------------------------------- single-CTA coarse tail
 
-// Levels whose sides are both <= 64 run in ONE 1024-thread CTA, entirely in
-// shared memory: per level x split by parity, xs[(i+j)&1][j][i>>1] (row
-// stride 32), b and the stencil codes row-major. The CTA is bound by how
+// The coarsest levels (both sides <= fl_params.mg_tail_side, 32 by default,
+// at most 64) run in ONE 1024-thread CTA, entirely in shared memory (a zero
+// word first, then per level x split by parity, xs[(i+j)&1][j][i>>1] with a
+// power-of-two row stride, b and the stencil codes row-major). The CTA is bound by how
 // many instructions its warps issue, so each level is owned by as few warps
 // as hold its cells: a row of colour-c cells gets LPR = 2^lsh lanes (the
 // power of two >= ceil(nx/2)), a warp covers 32/LPR rows, and only the first
