@@ -184,6 +184,8 @@ void free_all(Engine* e) {
   cudaFree(e->bt_d);
   cudaFree(e->ctl);
   cudaFree(e->ws_scales);
+  cudaFree(e->label_in);
+  cudaFree(e->label_flag);
   destroy_graphs(e);
   if (!e->levels.empty()) cudaFree(e->levels[0].label);
   mg_free(*e);
@@ -263,6 +265,13 @@ int download(Engine* e, void* dst, const float* src, long n, int dtype, const ch
 int up32(Engine* e, void* dst, const void* src, size_t bytes, const char* what) {
   if (!src) return fail(e, FL_EINVAL, "%s: null pointer", what);
   return cuda_status(e, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, e->stream), what);
+}
+// Level-0 labels written by an entry point other than fl_upload_fields: the
+// multigrid labels and codes no longer follow them (the next upload rebuilds
+// them whatever it is given).
+int put_labels(Engine* e, const uint8_t* label, const char* what) {
+  e->codes_valid = false;
+  return up32(e, e->levels[0].label, label, (size_t)e->cells(), what);
 }
 int down32(Engine* e, void* dst, const void* src, size_t bytes, const char* what) {
   if (!dst) return fail(e, FL_EINVAL, "%s: null pointer", what);
@@ -821,7 +830,13 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   s = s ? s : dalloc(e, (void**)&e->bt_d, (size_t)e->dye_cells() * sizeof(float2), "backtrace positions");
   s = s ? s : dalloc(e, (void**)&e->ctl, sizeof(SolveCtl), "solve control");
   s = s ? s : dalloc(e, (void**)&e->ws_scales, 4 * sizeof(float), "warm-start scales");
+  s = s ? s : dalloc(e, (void**)&e->label_in, (size_t)e->cells(), "uploaded labels");
+  s = s ? s : dalloc(e, (void**)&e->label_flag, sizeof(int), "label flag");
   if (s) return bail(s);
+  if (cudaMemset(e->label_flag, 0, sizeof(int)) != cudaSuccess) {
+    fail(e, FL_EDEVICE, "label flag");
+    return bail(FL_EDEVICE);
+  }
   if (cudaMallocHost(&e->acc_host, sizeof(StepAccum)) != cudaSuccess ||
       cudaMallocHost(&e->ctl_host, sizeof(SolveCtl)) != cudaSuccess) {
     fail(e, FL_ENOMEM, "pinned accumulator");
@@ -896,14 +911,58 @@ int fl_synchronize(fl_engine* h) {
 // float64 pressure of the defect-correction solve) from the float32 p
 // unless it came in float64, the second-order warm start's history, the
 // multigrid labels and stencil codes, the clock and the CFL scalars.
-void enqueue_after_upload(Engine* e, bool p64_from_p32) {
+// The labels arrive in label_in; k_label_sync copies the cells that changed
+// into levels[0].label. Eagerly the multigrid labels and codes are rebuilt
+// every time; captured (`capture`), the rebuild is the body of an IF node
+// that runs only when some label changed (the caller forces it by filling
+// levels[0].label with a value no label has, when the codes are stale).
+cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture) {
   cudaStream_t s = e->stream;
+  cudaError_t err = cudaSuccess;
   if (p64_from_p32) launch_convert(s, e->levels[0].x[0], FL_F32, e->p64[0], FL_F64, e->cells());
   cudaMemcpyAsync(e->pprev32, e->levels[0].x[0], e->cells() * 4, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(e->pprev64, e->p64[0], e->cells() * 8, cudaMemcpyDeviceToDevice, s);
-  mg_build_codes(*e);
+  launch_label_sync(s, e->label_in, e->levels[0].label, e->cells(), e->label_flag);
+  if (!capture) {
+    cudaMemsetAsync(e->label_flag, 0, sizeof(int), s);
+    mg_build_codes(*e);
+  } else {
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t cap = nullptr;
+    err = cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap, nullptr, nullptr, nullptr);
+    cudaGraphConditionalHandle h = 0;
+    if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&h, cap, 0, cudaGraphCondAssignDefault);
+    if (err == cudaSuccess) {
+      launch_label_cond(s, e->label_flag, h);
+      const cudaGraphNode_t* deps = nullptr;
+      size_t ndeps = 0;
+      err = cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap, &deps, nullptr, &ndeps);
+      cudaGraphNodeParams cp{};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeIf;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node = nullptr;
+      if (err == cudaSuccess) err = cudaGraphAddNode(&node, cap, deps, nullptr, ndeps, &cp);
+      if (err == cudaSuccess) err = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+      if (err == cudaSuccess) {
+        // the body is captured from the second stream (mg_build_codes
+        // enqueues on e->stream, which points there meanwhile)
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        e->stream = e->stream2;
+        err = cudaStreamBeginCaptureToGraph(e->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (err == cudaSuccess) {
+          mg_build_codes(*e);
+          cudaGraph_t done = nullptr;
+          err = cudaStreamEndCapture(e->stream, &done);
+        }
+        e->stream = s;
+      }
+    }
+  }
   cudaMemsetAsync(e->time_dev, 0, sizeof(double), s);
   launch_max_speed(s, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);
+  return err;
 }
 
 }  // extern "C"
@@ -911,22 +970,15 @@ void enqueue_after_upload(Engine* e, bool p64_from_p32) {
 namespace {
 
 // The body of fl_upload_fields. With `dye_async` the dye (float32) is copied
-// on the second stream, after the stream's earlier work, and ev_dye marks
-// its end; the step's first dye reader waits for it (wait_dye). Otherwise
+// on the second stream, after the stream's earlier work and the other
+// fields' copies, and ev_dye marks its end; the step's first dye reader
+// waits for it (wait_dye). Otherwise
 // ev_dye is recorded on the second stream with nothing in flight.
 int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
                   const void* dye, bool dye_async) {
   e->cur = 0;
   e->stats_on_device = false;
-  if (dye_async) {
-    if (!dye) return fail(e, FL_EINVAL, "upload dye: null pointer");
-    // the dye buffer may still be read by the stream's earlier work
-    TRY(cuda_status(e, cudaEventRecord(e->ev_prior, e->stream), "upload dye"));
-    TRY(cuda_status(e, cudaStreamWaitEvent(e->stream2, e->ev_prior, 0), "upload dye"));
-    TRY(cuda_status(e, cudaMemcpyAsync(e->dye[0], dye, 3 * e->dye_cells() * sizeof(float), cudaMemcpyHostToDevice,
-                                       e->stream2), "upload dye"));
-  }
-  TRY(cuda_status(e, cudaEventRecord(e->ev_dye, e->stream2), "upload dye"));
+  if (dye_async && !dye) return fail(e, FL_EINVAL, "upload dye: null pointer");
   TRY(put_step_ctl(e, true));
   TRY(upload(e, e->u[0], u, e->ufaces(), dtype, "upload u"));
   TRY(upload(e, e->v[0], v, e->vfaces(), dtype, "upload v"));
@@ -938,18 +990,35 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
   if (p64_direct)
     TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, e->cells() * sizeof(double), cudaMemcpyHostToDevice, e->stream),
                     "upload p64"));
-  TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "upload label"));
-  if (!dye_async) TRY(upload(e, e->dye[0], dye, 3 * e->dye_cells(), dtype, "upload dye"));
-  if (p64_direct || !e->use_graphs) {
-    enqueue_after_upload(e, !p64_direct);
+  TRY(up32(e, e->label_in, label, (size_t)e->cells(), "upload label"));
+  if (dye_async) {
+    // after the copies the step starts with (which it would otherwise share
+    // the host link with) and the stream's earlier work (which may still read
+    // the dye buffer)
+    TRY(cuda_status(e, cudaEventRecord(e->ev_prior, e->stream), "upload dye"));
+    TRY(cuda_status(e, cudaStreamWaitEvent(e->stream2, e->ev_prior, 0), "upload dye"));
+    TRY(cuda_status(e, cudaMemcpyAsync(e->dye[0], dye, 3 * e->dye_cells() * sizeof(float), cudaMemcpyHostToDevice,
+                                       e->stream2), "upload dye"));
   } else {
-    // one graph launch instead of ~20 launches (captured once per parameter set)
+    TRY(upload(e, e->dye[0], dye, 3 * e->dye_cells(), dtype, "upload dye"));
+  }
+  TRY(cuda_status(e, cudaEventRecord(e->ev_dye, e->stream2), "upload dye"));
+  // stale codes (new levels, labels written by another entry point): make
+  // every cell differ so that the rebuild runs
+  if (!e->codes_valid || e->labels_dirty)
+    TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].label, 0xff, (size_t)e->cells(), e->stream), "upload label"));
+  if (p64_direct || !e->use_graphs) {
+    TRY(cuda_status(e, enqueue_after_upload(e, !p64_direct, false), "upload"));
+  } else {
+    // one graph launch instead of ~20 launches (captured once per parameter
+    // set); the label rebuild runs only when the labels changed
     if (!e->upload_graph) {
       cudaGraph_t g = nullptr;
       cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
       if (err == cudaSuccess) {
-        enqueue_after_upload(e, true);
-        err = cudaStreamEndCapture(e->stream, &g);
+        err = enqueue_after_upload(e, true, true);
+        cudaError_t end = cudaStreamEndCapture(e->stream, &g);
+        if (err == cudaSuccess) err = end;
       }
       if (err == cudaSuccess) err = cudaGraphInstantiate(&e->upload_graph, g, 0);
       if (g) cudaGraphDestroy(g);
@@ -962,6 +1031,7 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
     TRY(cuda_status(e, cudaGraphLaunch(e->upload_graph, e->stream), "upload graph"));
   }
   TRY(check_launch(e, "upload"));
+  e->codes_valid = true;
   e->uploaded = true;
   e->labels_dirty = false;
   e->steps = 0;
@@ -1031,7 +1101,7 @@ int fl_step_host(fl_engine* h, const float* u, const float* v, const float* p, c
 
 int fl_set_labels(fl_engine* h, const uint8_t* label) {
   ENTER(h);
-  TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "upload label"));
+  TRY(put_labels(e, label, "upload label"));
   e->labels_dirty = true;
   return sync(e, "set labels");
 }
@@ -1195,7 +1265,7 @@ int fl_advect_velocity(fl_engine* h, int scheme, const float* u_in, const float*
   e->uploaded = false;
   TRY(up32(e, e->u[0], u_in, e->ufaces() * 4, "u"));
   TRY(up32(e, e->v[0], v_in, e->vfaces() * 4, "v"));
-  TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "label"));
+  TRY(put_labels(e, label, "label"));
   TRY(put_scalars(e, host_scalars(e, dt, 0, 0, nullptr)));
   launch_advect_velocity(e->stream, e->nx, e->ny, e->h, scheme == FL_MACCORMACK, e->u[0], e->v[0], e->u_hat,
                          e->v_hat, e->u[1], e->v[1], e->levels[0].label, e->sc);
@@ -1212,7 +1282,7 @@ int fl_advect_dye(fl_engine* h, int scheme, const float* u, const float* v, cons
   TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
   TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
   TRY(up32(e, e->dye[0], q_in, 3 * e->dye_cells() * 4, "dye"));
-  TRY(up32(e, e->levels[0].label, label, (size_t)e->cells(), "label"));
+  TRY(put_labels(e, label, "label"));
   TRY(put_scalars(e, host_scalars(e, dt, 0, 0, nullptr)));
   launch_advect_dye(e->stream, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, scheme == FL_MACCORMACK, e->u[0], e->v[0],
                     e->dye[0], e->dye_hat, e->dye[1], e->levels[0].label, e->sc, false, nullptr, 0, 0, 0, 0);
@@ -1244,7 +1314,7 @@ int fl_rb_solve(fl_engine* h, float* p, const float* div, const uint8_t* label, 
   Level& L = e->levels[0];
   TRY(up32(e, L.x[0], p, n * 4, "p"));
   TRY(up32(e, L.b, div, n * 4, "div"));
-  TRY(up32(e, L.label, label, (size_t)n, "label"));
+  TRY(put_labels(e, label, "label"));
   launch_build_codes(e->stream, L.nx, L.ny, L.label, L.code);
   e->codes_valid = false;
   int u = 0;
@@ -1264,7 +1334,7 @@ int fl_mg_solve(fl_engine* h, float* p, const float* div, const uint8_t* label, 
   Level& L = e->levels[0];
   TRY(up32(e, L.x[0], p, n * 4, "p"));
   TRY(up32(e, e->u_hat, div, n * 4, "div"));  // u_hat is free scratch of >= n floats here
-  TRY(up32(e, L.label, label, (size_t)n, "label"));
+  TRY(put_labels(e, label, "label"));
   mg_build_codes(*e);
   TRY(zero_solve_accum(e));
   launch_scale_rhs(e->stream, n, e->u_hat, L.b, -scale, L.label, e->acc);
@@ -1289,7 +1359,7 @@ int fl_mg_solve_mixed(fl_engine* h, double* p, const float* div, const uint8_t* 
   e->stats_on_device = true;
   TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, n * sizeof(double), cudaMemcpyHostToDevice, e->stream), "p"));
   TRY(up32(e, e->u_hat, div, n * 4, "div"));
-  TRY(up32(e, L.label, label, (size_t)n, "label"));
+  TRY(put_labels(e, label, "label"));
   mg_build_codes(*e);
   TRY(zero_solve_accum(e));
   launch_scale_rhs(e->stream, n, e->u_hat, L.b, -scale, L.label, e->acc);
@@ -1324,7 +1394,7 @@ int fl_rb_sweep(fl_engine* h, float* p, const float* div, const uint8_t* label, 
   const long n = e->cells();
   TRY(up32(e, L.x[0], p, n * 4, "p"));
   TRY(up32(e, L.b, div, n * 4, "div"));
-  TRY(up32(e, L.label, label, (size_t)n, "label"));
+  TRY(put_labels(e, label, "label"));
   launch_build_codes(e->stream, L.nx, L.ny, L.label, L.code);
   e->codes_valid = false;
   launch_rb_halfsweep(e->stream, L.nx, L.ny, L.x[0], L.b, L.code, scale, omega, color);
@@ -1340,7 +1410,7 @@ int fl_subtract_gradient(fl_engine* h, const float* p, float* u, float* v, const
   TRY(up32(e, L.x[0], p, e->cells() * 4, "p"));
   TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
   TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
-  TRY(up32(e, L.label, label, (size_t)e->cells(), "label"));
+  TRY(put_labels(e, label, "label"));
   TRY(put_scalars(e, host_scalars(e, 1.0f, 1.0f, grad_scale, nullptr)));
   launch_subtract_outflow(e->stream, e->nx, e->ny, L.x[0], e->u[0], e->v[0], L.label, e->sc, true, false);
   TRY(check_launch(e, "subtract gradient"));
@@ -1355,7 +1425,7 @@ int fl_outflow(fl_engine* h, float* u, float* v, const uint8_t* label) {
   Level& L = e->levels[0];
   TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
   TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
-  TRY(up32(e, L.label, label, (size_t)e->cells(), "label"));
+  TRY(put_labels(e, label, "label"));
   launch_subtract_outflow(e->stream, e->nx, e->ny, L.x[0], e->u[0], e->v[0], L.label, e->sc, false, true);
   TRY(check_launch(e, "outflow"));
   TRY(down32(e, u, e->u[0], e->ufaces() * 4, "u"));
@@ -1371,7 +1441,7 @@ int fl_commit_labels(fl_engine* h, float* p, float* u, float* v, float* dye, con
   TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
   TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
   TRY(up32(e, e->dye[0], dye, 3 * e->dye_cells() * 4, "dye"));
-  TRY(up32(e, L.label, label, (size_t)e->cells(), "label"));
+  TRY(put_labels(e, label, "label"));
   launch_commit_labels(e->stream, e->nx, e->ny, L.label, L.x[0], e->u[0], e->v[0], e->dye[0], e->dye_cells());
   TRY(check_launch(e, "commit labels"));
   TRY(down32(e, p, L.x[0], e->cells() * 4, "p"));
@@ -1389,7 +1459,7 @@ int fl_body_forces(fl_engine* h, float* u, float* v, const float* dye, const uin
   TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
   TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
   TRY(up32(e, e->dye[0], dye, 3 * e->dye_cells() * 4, "dye"));
-  TRY(up32(e, L.label, label, (size_t)e->cells(), "label"));
+  TRY(put_labels(e, label, "label"));
   StepScalars s{};
   s.dt = dt;
   s.gain_beta = beta * dt;
@@ -1416,7 +1486,7 @@ int fl_stir(fl_engine* h, float* u, float* v, const uint8_t* label, float x, flo
   Level& L = e->levels[0];
   TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
   TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
-  TRY(up32(e, L.label, label, (size_t)e->cells(), "label"));
+  TRY(put_labels(e, label, "label"));
   const float st[5] = {x, y, r, dx, dy};
   launch_stir(e->stream, e->nx, e->ny, e->h, e->u[0], e->v[0], L.label, st);
   TRY(check_launch(e, "stir"));

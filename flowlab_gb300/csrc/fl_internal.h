@@ -71,6 +71,11 @@ struct Engine {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   // the device-side work of fl_upload_fields after its copies (float32 p)
   cudaGraphExec_t upload_graph = nullptr;
+  // fl_upload_fields copies the labels here; the upload compares them with
+  // levels[0].label and rebuilds the multigrid labels and codes only where
+  // they changed (label_flag: set when any cell differs)
+  uint8_t* label_in = nullptr;
+  int* label_flag = nullptr;
   bool graphs_valid = false;
   bool use_graphs = true;
   bool stats_on_device = false;  // the last solve's statistics live in ctl
@@ -208,6 +213,10 @@ void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* 
 void launch_rms_remaining(cudaStream_t s, int nx, int ny, const float* p, const float* div, const uint8_t* code,
                           float scale, StepAccum* acc);
 void launch_build_codes(cudaStream_t s, int nx, int ny, const uint8_t* label, uint8_t* code);
+// cur = in, raising *flag when any of the n labels changed
+void launch_label_sync(cudaStream_t s, const uint8_t* in, uint8_t* cur, long n, int* flag);
+// the conditional `h` = (*flag != 0), then *flag = 0
+void launch_label_cond(cudaStream_t s, int* flag, cudaGraphConditionalHandle h);
 void launch_rb_halfsweep(cudaStream_t s, int nx, int ny, float* p, const float* b, const uint8_t* code,
                          float scale, float omega, int color);
 

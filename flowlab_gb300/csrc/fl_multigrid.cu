@@ -46,6 +46,43 @@ __global__ void k_build_codes(int nx, int ny, const uint8_t* __restrict__ label,
   code[k] = c;
 }
 
+// The uploaded labels against the current ones: copies the cells that
+// differ and raises *flag if there were any (16 bytes per thread step; the
+// buffers come from cudaMalloc, so the 16-byte body is aligned).
+__global__ void __launch_bounds__(256) k_label_sync(const uint8_t* __restrict__ in, uint8_t* __restrict__ cur, long n,
+                                                    int* flag) {
+  bool changed = false;
+  const long stride = (long)gridDim.x * blockDim.x;
+  const long t0 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const uint4* in4 = reinterpret_cast<const uint4*>(in);
+  uint4* cur4 = reinterpret_cast<uint4*>(cur);
+  for (long k = t0; k < n / 16; k += stride) {
+    const uint4 a = in4[k], b = cur4[k];
+    if (a.x != b.x || a.y != b.y || a.z != b.z || a.w != b.w) {
+      cur4[k] = a;
+      changed = true;
+    }
+  }
+  for (long k = 16 * (n / 16) + t0; k < n; k += stride)
+    if (in[k] != cur[k]) {
+      cur[k] = in[k];
+      changed = true;
+    }
+  if (__syncthreads_or(changed) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+__global__ void k_label_cond(int* flag, cudaGraphConditionalHandle h) {
+  cudaGraphSetConditional(h, *flag != 0 ? 1u : 0u);
+  *flag = 0;
+}
+
+void launch_label_sync(cudaStream_t s, const uint8_t* in, uint8_t* cur, long n, int* flag) {
+  const long blocks = std::min(std::max(1L, (n / 16 + 255) / 256), 152L * 4);
+  k_label_sync<<<(unsigned)blocks, 256, 0, s>>>(in, cur, n, flag);
+}
+
+void launch_label_cond(cudaStream_t s, int* flag, cudaGraphConditionalHandle h) { k_label_cond<<<1, 1, 0, s>>>(flag, h); }
+
 // pressureMultigrid.ts:92-110 (multigrid.wgsl:259-286): Air > Fluid > Solid.
 __global__ void k_coarsen_labels(int fnx, int fny, const uint8_t* __restrict__ fine, int cnx, int cny,
                                  uint8_t* __restrict__ coarse) {

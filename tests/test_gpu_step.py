@@ -451,3 +451,42 @@ def test_tail_side_does_not_change_results(mixed):
             for a, b, name in zip(outs[0][:4], o[:4], ("u", "v", "p", "dye")):
                 assert np.array_equal(a, b), (n, side, name, mismatch(a, b))
             assert o[4]["cycles"] == outs[0][4]["cycles"]
+
+
+def test_upload_rebuilds_the_multigrid_only_for_changed_labels():
+    """fl_upload_fields rebuilds the multigrid labels and stencil codes (an IF
+    node of the upload graph) only when the uploaded labels differ from the
+    current ones: an engine re-uploaded with new labels (a solid block added)
+    steps exactly like a fresh engine given them, and re-uploading the same
+    labels again changes nothing."""
+    g, f, patch = configs.plume(128)
+    prm = configs.plume_params(tol=1e-6, max_cycles=30, mixed=1)
+    label2 = f.label.copy().reshape(g.ny, g.nx)
+    label2[60:70, 40:56] = 2
+    label2 = np.ascontiguousarray(label2.reshape(-1))
+
+    def upload(eng, label):
+        eng.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(label),
+                 ptr(f32(f.dye)))
+
+    def read(eng):
+        u = np.empty(eng.ufaces, np.float32)
+        v = np.empty(eng.vfaces, np.float32)
+        eng.call("fl_read_velocity", native.FL_F32, ptr(u), ptr(v))
+        return u, v, eng.stats()["cycles"]
+
+    outs = []
+    for first in (None, f.label, label2):
+        eng = native.Engine(g.nx, g.ny, g.h, params=prm)
+        try:
+            eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+            if first is not None:
+                upload(eng, first)
+                eng.call("fl_step_auto", 2, None)
+            upload(eng, label2)
+            eng.call("fl_step_auto", 3, None)
+            outs.append(read(eng))
+        finally:
+            eng.close()
+    for o in outs[1:]:
+        assert np.array_equal(o[0], outs[0][0]) and np.array_equal(o[1], outs[0][1]) and o[2] == outs[0][2]
