@@ -481,8 +481,10 @@ void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const floa
                       StepScalars* sc_next, double* time_dev, const fl_params* prm, float h, bool write_scalars,
                       bool add_time) {
   long nu = (long)(nx + 1) * ny, nv = (long)nx * (ny + 1);
-  long blocks = (nu + 255) / 256;
-  if (blocks > 152 * 8) blocks = 152 * 8;
+  // few blocks, several 16-byte loads per thread: every block ends in two
+  // atomics on the same words, which serialise
+  long blocks = (nu / 4 + 255) / 256;
+  if (blocks > 152 * 2) blocks = 152 * 2;
   if (blocks < 1) blocks = 1;
   k_max_speed<<<(unsigned)blocks, 256, 0, s>>>(nu, nv, u, v, acc, sc_next, time_dev, h, (float)prm->cfl_target,
                                               (float)prm->dt_max, (float)prm->rho, prm->dye_decay[0],
