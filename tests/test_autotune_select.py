@@ -23,3 +23,22 @@ def test_with_params_copies():
     assert p.mg_coarsest == 16 and base.mg_coarsest == 8 and p.tol == base.tol
     assert autotune.cache_key(p, 256, 128) == "mg:256x128:mixed"
     assert autotune.cache_key(configs.karman_params(), 128, 128) == "rb:128x128:f32"
+
+
+def test_tail_side_chosen_by_time_after_the_constants(monkeypatch):
+    """tune_multigrid: the fastest converged (mg_coarsest, mg_coarse_sweeps),
+    then the tail's first level by time alone, with those constants."""
+    seen = []
+
+    def fake_measure(scene, prm, steps, warmup, device):
+        seen.append((prm.mg_coarsest, prm.mg_coarse_sweeps, prm.mg_tail_side))
+        ms = 1.0 + 0.01 * prm.mg_coarsest + 0.001 * prm.mg_coarse_sweeps
+        if prm.mg_tail_side:
+            ms = {16: 0.95, 32: 0.90, 64: 0.97}[prm.mg_tail_side]
+        return {"ms": ms, "rel_max": 5e-7, "cycles": 4}
+
+    monkeypatch.setattr(autotune, "measure_steps", fake_measure)
+    best, results = autotune.tune_multigrid(None, configs.plume_params(tol=1e-6))
+    assert best == {"mg_coarsest": 4, "mg_coarse_sweeps": 8, "mg_tail_side": 32}
+    assert len(results) == 12
+    assert seen[-3:] == [(4, 8, 16), (4, 8, 32), (4, 8, 64)]
