@@ -74,7 +74,7 @@ LIMITERS = {
 # phase's dominant kernel from one ncu capture of the 1024^2 plume's eager
 # profiled steps (profiles/): (bytes, kernel, summary file).
 TRAFFIC_PLUME_1024 = {
-    "defect64": (17.842944e6, "k_update_resid64<1>", "profiles/k_mg_coarse_resid64_plume_1024.md"),
+    "defect64": (17.842688e6, "k_update_resid64<1>", "profiles/k_mg_coarse_resid64_plume_1024.md"),
     "mg_coarse": (0.07296e6, "k_mg_coarse", "profiles/k_mg_coarse_resid64_plume_1024.md"),
 }
 
