@@ -68,3 +68,27 @@ def test_profile_phases_match_the_header():
     assert [int(k) for _, k in names] == list(range(n))
     assert [nm.lower() for nm, _ in names] == native.PHASES
     assert ctypes.sizeof(native.Profile) == n * 24
+
+
+def test_plain_c_caller_links_and_fails_loudly_without_a_device(lib, tmp_path):
+    """tests/c_abi_step.c binds the ABI from plain C (gcc, the header and the
+    shared library, nothing else). Without a GPU it must stop at fl_create
+    with FL_EDEVICE and the CUDA message; with one, it takes a step."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("gcc not found")
+    here = os.path.dirname(os.path.abspath(__file__))
+    libdir = os.path.dirname(build.LIB)
+    exe = str(tmp_path / "c_abi_step")
+    subprocess.run([cc, "-std=c11", "-O1", "-Wall", "-Werror", "-I" + os.path.dirname(HEADER),
+                    os.path.join(here, "c_abi_step.c"), "-o", exe, "-L" + libdir, "-lflowlab_gb300",
+                    "-Wl,-rpath," + libdir, "-lm"], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    if r.returncode == 0:
+        assert "stepped:" in r.stdout
+    else:
+        assert r.returncode == 2, r.stdout + r.stderr
+        assert "no device" in r.stdout and "CUDA" in r.stdout
