@@ -334,7 +334,7 @@ def workload_config(args):
     n = args.size
     if args.workload == "plume":
         desc = ("thermal plume %dx%d, closed box, MacCormack, beta 1 / alpha 0.05 / confinement 0.3, "
-                "multigrid V(3,3) coarsest 8x8 in a float64 defect-correction loop, relative residual %.0e "
+                "multigrid V(3,3) coarsest 8x8 in a double-float defect-correction loop, relative residual %.0e "
                 "(cap %d cycles)" % (n, n, args.tol, args.max_cycles))
     else:
         desc = ("turbulence grid %dx%d, u = 1 inflow through a 16x16 lattice of solid squares, MacCormack, CFL 0.5, "
@@ -343,7 +343,10 @@ def workload_config(args):
     prm = workload_params(args)
     return {"workload": desc, "grid": [n, n],
             "solver": "multigrid V(3,3), %d coarse sweep pairs" % prm.mg_coarse_sweeps,
-            "tol": args.tol, "precision": "float32 fields and smoothing, float64 residual and correction",
+            "tol": args.tol,
+            "precision": ("float32 throughout: fields and smoothing in float32, the residual and correction in "
+                          "double-float pairs (float32 arithmetic)" if prm.mixed == 2 else
+                          "float32 fields and smoothing, float64 residual and correction"),
             "l2": "flushed (320 MB write) before every timed step",
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
 

@@ -322,6 +322,63 @@ __device__ __forceinline__ float d2f_rn(double d) {
   return d2f_slow(d);
 }
 
+// ------------------------------------------------------ double-float pairs
+//
+// The double-float pressure of the defect correction (fl_params.mixed = 2):
+// a value is the unevaluated sum hi + lo of two floats (float2 x = hi,
+// y = lo; ~48 significand bits) and lives in the same 8-byte-per-cell
+// buffers as the float64 pressure. The arithmetic is error-free float
+// transformations on the float32 pipe: TwoSum (Knuth, TAOCP vol. 2, 4.2.2),
+// FastTwoSum and Dekker's double-length addition (Numer. Math. 18, 1971),
+// and the product by 3 through one exact FMA. Each helper is a fixed
+// sequence of IEEE float operations (explicit _rn intrinsics: never
+// contracted or reordered), so results are reproducible bit for bit.
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return make_float2(s, e);
+}
+// exact when |a| >= |b| or a == 0
+__device__ __forceinline__ float2 df_fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float e = __fsub_rn(b, __fsub_rn(s, a));
+  return make_float2(s, e);
+}
+__device__ __forceinline__ float2 df_add(float2 x, float2 y) {
+  const float2 s = df_two_sum(x.x, y.x);
+  const float e = __fadd_rn(s.y, __fadd_rn(x.y, y.y));
+  return df_fast_two_sum(s.x, e);
+}
+__device__ __forceinline__ float2 df_neg(float2 x) { return make_float2(-x.x, -x.y); }
+__device__ __forceinline__ float2 df_add_f(float2 x, float f) {
+  const float2 s = df_two_sum(x.x, f);
+  const float e = __fadd_rn(s.y, x.y);
+  return df_fast_two_sum(s.x, e);
+}
+// count * x for a link count 1..4 (2 and 4 scale exactly)
+__device__ __forceinline__ float2 df_mul_count(float2 x, int count) {
+  if (count == 4) return make_float2(__fmul_rn(4.0f, x.x), __fmul_rn(4.0f, x.y));
+  if (count == 2) return make_float2(__fmul_rn(2.0f, x.x), __fmul_rn(2.0f, x.y));
+  if (count == 1) return x;
+  const float p = __fmul_rn(3.0f, x.x);
+  float e = __fmaf_rn(3.0f, x.x, -p);
+  e = __fmaf_rn(3.0f, x.y, e);
+  return df_fast_two_sum(p, e);
+}
+__device__ __forceinline__ float df_round(float2 x) { return __fadd_rn(x.x, x.y); }
+// a - b rounded to one float
+__device__ __forceinline__ float df_diff(float2 a, float2 b) {
+  const float2 s = df_two_sum(a.x, -b.x);
+  const float e = __fadd_rn(s.y, __fsub_rn(a.y, b.y));
+  return __fadd_rn(s.x, e);
+}
+__device__ __forceinline__ double df_to_double(float2 x) { return (double)x.x + (double)x.y; }
+__device__ __forceinline__ float2 df_from_double(double d) {
+  const float hi = (float)d;
+  return make_float2(hi, (float)(d - (double)hi));
+}
+
 // 0.0 + x: x itself except that -0.0 becomes +0.0.
 __device__ __forceinline__ double zero_plus(double x) {
   const unsigned long long bits = dbits_opaque(x);

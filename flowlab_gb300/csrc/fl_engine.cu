@@ -213,6 +213,7 @@ int validate_params(Engine* e, const fl_params* p) {
   // the coarsest level is solved inside the single-CTA tail (sides <= 64 at most)
   if (p->mg_coarsest < 1 || p->mg_coarsest > 64) return fail(e, FL_EINVAL, "mg_coarsest must be in [1, 64]");
   if (p->rb_pairs < 0 || p->rb_pairs > 4) return fail(e, FL_EINVAL, "rb_pairs must be in [0, 4]");
+  if (p->mixed < 0 || p->mixed > MIXED_DF) return fail(e, FL_EINVAL, "mixed must be 0, 1 or 2 (got %d)", p->mixed);
   // the tail kernel's ownership map holds levels of at most 64 x 64 cells
   if (p->mg_tail_side < 0 || p->mg_tail_side > 64) return fail(e, FL_EINVAL, "mg_tail_side must be in [0, 64]");
   if (!(p->cfl_target > 0) || !(p->dt_max > 0) || !(p->rho > 0))
@@ -341,6 +342,8 @@ int put_ctl(Engine* e, int mode, double tol, int max_cycles, bool reset_par) {
 }
 
 bool step_mixed(const Engine* e) { return e->prm.solver == FL_SOLVER_MG && e->prm.mixed; }
+// the refined pressure is double-float pairs (in the float64 buffers)
+bool refined_df(const Engine* e) { return e->prm.mixed == MIXED_DF; }
 
 // The step's solve settings from the engine parameters.
 int put_step_ctl(Engine* e, bool reset_par) {
@@ -406,7 +409,7 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
   if (e->prm.warm_extrapolate && e->prm.solver == FL_SOLVER_MG) {
     const bool mixed = e->prm.mixed != 0;
     launch_extrapolate(s, e->cells(), L0.label, L0.x[0], e->pprev32, mixed ? e->p64[0] : nullptr,
-                       mixed ? e->p64[1] : nullptr, e->pprev64, e->ctl);
+                       mixed ? e->p64[1] : nullptr, e->pprev64, e->ctl, refined_df(e));
   }
   if (e->warm != nullptr && e->prm.solver == FL_SOLVER_MG) {
     // p_prev -> p_guess in place: the float64 pressure of the defect
@@ -414,7 +417,8 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
     const bool mixed = e->prm.mixed != 0;
     tok = prof_begin(*e, FL_PH_WARM_START);
     unet_warm_start(*e->warm, s, e->nx, e->ny, L0.b, L0.label, e->acc, mixed ? nullptr : L0.x[0],
-                    mixed ? e->p64[0] : nullptr, mixed ? e->p64[1] : nullptr, &e->ctl->par, e->ws_scales);
+                    mixed ? e->p64[0] : nullptr, mixed ? e->p64[1] : nullptr, &e->ctl->par, e->ws_scales,
+                    refined_df(e));
     prof_end(*e, tok, 0, 0);
   }
 }
@@ -425,7 +429,7 @@ void enqueue_solve_prologue(Engine* e, cudaStream_t s, bool mixed, bool use_cond
   if (mixed) {
     const int tok = prof_begin(*e, FL_PH_DEFECT64);
     launch_update_resid64(s, e->nx, e->ny, e->p64[0], e->p64[1], e->ctl, nullptr, L0.b, L0.code, false, e->r32,
-                          e->acc);
+                          e->acc, refined_df(e));
     // p64, b, code in; r32 out
     prof_end(*e, tok, 17.0 * e->cells(), 1);
   }
@@ -443,7 +447,7 @@ void enqueue_solve_body(Engine* e, cudaStream_t s, bool mixed, bool use_cond, cu
     mg_vcycle_on(*e, e->r32, true, nullptr);
     const int tok = prof_begin(*e, FL_PH_DEFECT64);
     launch_update_resid64(s, e->nx, e->ny, e->p64[0], e->p64[1], e->ctl, L0.x[0], L0.b, L0.code, true, e->r32,
-                          e->acc);
+                          e->acc, refined_df(e));
     // p64, e, b, code in; p64 (other buffer), r32 out
     prof_end(*e, tok, 29.0 * e->cells(), 1);
   } else {
@@ -493,7 +497,7 @@ void enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
   float* v = e->v[1 - par];
   int tok = prof_begin(*e, FL_PH_PROJECT);
   launch_subtract_outflow(s, e->nx, e->ny, L0.x[0], u, v, L0.label, e->sc, true, true, mixed ? e->p64[0] : nullptr,
-                          mixed ? e->p64[1] : nullptr, e->ctl);
+                          mixed ? e->p64[1] : nullptr, e->ctl, refined_df(e));
   prof_end(*e, tok, (mixed ? 8 : 4) * N + 4 * F + N + 4 * F, 1);
   // velocity and pressure are final: fl_step_host reads them back from here
   // on while the dye advection runs
@@ -919,7 +923,7 @@ int fl_synchronize(fl_engine* h) {
 cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture) {
   cudaStream_t s = e->stream;
   cudaError_t err = cudaSuccess;
-  if (p64_from_p32) launch_convert(s, e->levels[0].x[0], FL_F32, e->p64[0], FL_F64, e->cells());
+  if (p64_from_p32) launch_convert(s, e->levels[0].x[0], FL_F32, e->p64[0], refined_df(e) ? DT_DF : FL_F64, e->cells());
   cudaMemcpyAsync(e->pprev32, e->levels[0].x[0], e->cells() * 4, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(e->pprev64, e->p64[0], e->cells() * 8, cudaMemcpyDeviceToDevice, s);
   launch_label_sync(s, e->label_in, e->levels[0].label, e->cells(), e->label_flag);
@@ -987,9 +991,15 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
   else
     TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].x[0], 0, e->cells() * 4, e->stream), "zero p"));
   const bool p64_direct = p && dtype == FL_F64;
-  if (p64_direct)
+  if (p64_direct && refined_df(e)) {
+    // the double-float pairs from the float64 pressure
+    TRY(cuda_status(e, cudaMemcpyAsync(e->staging, p, e->cells() * sizeof(double), cudaMemcpyHostToDevice, e->stream),
+                    "upload p64"));
+    launch_convert(e->stream, e->staging, FL_F64, e->p64[0], DT_DF, e->cells());
+  } else if (p64_direct) {
     TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, e->cells() * sizeof(double), cudaMemcpyHostToDevice, e->stream),
                     "upload p64"));
+  }
   TRY(up32(e, e->label_in, label, (size_t)e->cells(), "upload label"));
   if (dye_async) {
     // after the copies the step starts with (which it would otherwise share
@@ -1078,7 +1088,7 @@ int fl_step_host(fl_engine* h, const float* u, const float* v, const float* p, c
   if (p_out) {
     const long n = e->cells();
     if (step_mixed(e)) {
-      launch_select_p64(e->stream2, e->ctl, e->p64[0], e->p64[1], e->staging, false, n);
+      launch_select_p64(e->stream2, e->ctl, e->p64[0], e->p64[1], e->staging, false, n, refined_df(e));
       TRY(check_launch(e, "read p"));
       TRY(cuda_status(e, cudaMemcpyAsync(p_out, e->staging, n * sizeof(float), cudaMemcpyDeviceToHost, e->stream2),
                       "read p"));
@@ -1222,7 +1232,7 @@ int fl_read_pressure(fl_engine* h, int dtype, void* p) {
     if (dtype != FL_F32 && dtype != FL_F64) return fail(e, FL_EINVAL, "read p: dtype %d", dtype);
     const long n = e->cells();
     // the current float64 buffer is chosen on the device (no parity round trip)
-    launch_select_p64(e->stream, e->ctl, e->p64[0], e->p64[1], e->staging, dtype == FL_F64, n);
+    launch_select_p64(e->stream, e->ctl, e->p64[0], e->p64[1], e->staging, dtype == FL_F64, n, refined_df(e));
     TRY(check_launch(e, "read p"));
     TRY(cuda_status(e, cudaMemcpyAsync(p, e->staging, n * (dtype == FL_F64 ? sizeof(double) : sizeof(float)),
                                        cudaMemcpyDeviceToHost, e->stream),
@@ -1357,7 +1367,12 @@ int fl_mg_solve_mixed(fl_engine* h, double* p, const float* div, const uint8_t* 
   Level& L = e->levels[0];
   TRY(put_ctl(e, SOLVE_MIXED, tol, max_cycles, true));
   e->stats_on_device = true;
-  TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, n * sizeof(double), cudaMemcpyHostToDevice, e->stream), "p"));
+  if (refined_df(e)) {
+    TRY(cuda_status(e, cudaMemcpyAsync(e->staging, p, n * sizeof(double), cudaMemcpyHostToDevice, e->stream), "p"));
+    launch_convert(e->stream, e->staging, FL_F64, e->p64[0], DT_DF, n);
+  } else {
+    TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, n * sizeof(double), cudaMemcpyHostToDevice, e->stream), "p"));
+  }
   TRY(up32(e, e->u_hat, div, n * 4, "div"));
   TRY(put_labels(e, label, "label"));
   mg_build_codes(*e);
@@ -1368,8 +1383,14 @@ int fl_mg_solve_mixed(fl_engine* h, double* p, const float* div, const uint8_t* 
   TRY(read_ctl(e));
   if (cycles_used) *cycles_used = e->ctl_host->cycles;
   if (rel_residual) *rel_residual = e->ctl_host->rel;
-  TRY(cuda_status(e, cudaMemcpyAsync(p, e->p64[e->ctl_host->par], n * sizeof(double), cudaMemcpyDeviceToHost, e->stream),
-                  "p"));
+  if (refined_df(e)) {
+    launch_select_p64(e->stream, e->ctl, e->p64[0], e->p64[1], e->staging, true, n, true);
+    TRY(check_launch(e, "p"));
+    TRY(cuda_status(e, cudaMemcpyAsync(p, e->staging, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream), "p"));
+  } else {
+    TRY(cuda_status(e, cudaMemcpyAsync(p, e->p64[e->ctl_host->par], n * sizeof(double), cudaMemcpyDeviceToHost,
+                                       e->stream), "p"));
+  }
   return sync(e, "mg solve mixed");
 }
 

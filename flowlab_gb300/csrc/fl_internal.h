@@ -14,6 +14,11 @@
 
 namespace fl {
 
+// Conversion target of launch_convert: the double-float pressure pairs.
+constexpr int DT_DF = 2;
+// fl_params.mixed values
+constexpr int MIXED_F64 = 1, MIXED_DF = 2;
+
 // One multigrid level (pressureMultigrid.ts:211-217). x is double-buffered so
 // the temporally blocked smoother can read the pre-sweep values of its halo
 // while neighbouring tiles write their results.
@@ -172,10 +177,11 @@ void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, fl
                    const float* fx, const float* fy, const StepScalars* sc);
 void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
                        bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc);
+// p64a/p64b: the refined pressure (float64, or double-float pairs when df)
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
                              const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow,
                              const double* p64a = nullptr, const double* p64b = nullptr,
-                             const SolveCtl* ctl = nullptr);
+                             const SolveCtl* ctl = nullptr, bool df = false);
 void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const float* v, StepAccum* acc,
                       StepScalars* sc_next, double* time_dev, const fl_params* prm, float h, bool write_scalars,
                       bool add_time);
@@ -191,9 +197,10 @@ void launch_dye_patch(cudaStream_t s, int dnx, int dny, float* dye, const float*
                       int pny);
 void launch_hold(cudaStream_t s);
 void launch_select_p64(cudaStream_t s, const SolveCtl* ctl, const double* p64a, const double* p64b, void* out,
-                       bool as_f64, long n);
+                       bool as_f64, long n, bool df);
 void launch_extrapolate(cudaStream_t s, long n, const uint8_t* label, float* p32, float* pp32, double* p64a,
-                        double* p64b, double* pp64, const SolveCtl* ctl);
+                        double* p64b, double* pp64, const SolveCtl* ctl, bool df);
+// dtypes: FL_F32, FL_F64, and DT_DF (to the double-float pressure)
 void launch_convert(cudaStream_t s, const void* src, int src_dtype, void* dst, int dst_dtype, long n);
 
 // fl_multigrid.cu
@@ -202,9 +209,10 @@ void mg_free(Engine& e);
 void mg_build_codes(Engine& e);  // label chain + stencil codes from levels[0].label
 void mg_vcycle(Engine& e, StepAccum* acc_for_residual);
 void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc_for_residual);
+// the refined-pressure pass: float64, or double-float pairs in the same buffers when df
 void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, const SolveCtl* ctl,
                            const float* e, const float* b, const uint8_t* code, bool update, float* r32,
-                           StepAccum* acc);
+                           StepAccum* acc, bool df);
 void launch_solve_begin(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h);
 void launch_solve_check(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h);
 void launch_zero_if(cudaStream_t s, const SolveCtl* ctl, float* p32, double* p64a, double* p64b, long n);

@@ -822,6 +822,123 @@ __global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny
   }
 }
 
+// The same pass with the double-float pressure (fl_params.mixed = 2): p' =
+// p + e per cell (df_add_f), then r = b - (count*p' - sum) in double-float
+// arithmetic, the neighbour sum in the order +x, -x, +y, -y starting from
+// the first linked neighbour, r32 = the pair rounded to float. All of it is
+// float32 arithmetic (~80 operations per cell), so unlike the float64 pass
+// this one is bound by memory, not by a pipe: a warp owns 30 interior
+// columns (lanes 1..30; lanes 0 and 31 load the halo columns) of DF_ROWS
+// rows and issues every load of its rows (DF_ROWS + 2 rows of p and e,
+// DF_ROWS of b and codes) before any arithmetic, so each warp waits for
+// memory once. The residual norm sums r32^2: each square is an exact pair
+// (the product and its FMA error), accumulated per thread as a double-float
+// and widened to double once per thread for the block reduction.
+constexpr int DF_ROWS = 8;
+constexpr int DF_WARPS = 4;
+
+template <bool UPDATE>
+__global__ void __launch_bounds__(32 * DF_WARPS) k_update_resid_df(int nx, int ny, float2* __restrict__ p2a,
+                                                                   float2* __restrict__ p2b,
+                                                                   const SolveCtl* __restrict__ ctl,
+                                                                   const float* __restrict__ e,
+                                                                   const float* __restrict__ b,
+                                                                   const uint8_t* __restrict__ code,
+                                                                   float* __restrict__ r32, StepAccum* acc) {
+  __shared__ double red[32];
+  __shared__ unsigned long long redn[32];
+  const int par = ctl->par;
+  const float2* p_in = par ? p2b : p2a;
+  float2* p_out = par ? p2a : p2b;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gx = blockIdx.x * 30 - 1 + lane;
+  const int y0 = (blockIdx.y * DF_WARPS + w) * DF_ROWS;
+  const bool col = gx >= 0 && gx < nx;
+  const bool own = col && lane != 0 && lane != 31;
+
+  // rows y0-1 .. y0+DF_ROWS of p (and e), rows y0 .. y0+DF_ROWS-1 of b and
+  // the codes; zero / outside where the grid ends
+  float2 P[DF_ROWS + 2];
+  float E[DF_ROWS + 2];
+  float B[DF_ROWS];
+  uint8_t C[DF_ROWS];
+#pragma unroll
+  for (int r = 0; r < DF_ROWS + 2; r++) {
+    const int y = y0 - 1 + r;
+    P[r] = make_float2(0.0f, 0.0f);
+    E[r] = 0.0f;
+    if (col && y >= 0 && y < ny) {
+      const long k = gx + (long)y * nx;
+      P[r] = p_in[k];
+      if (UPDATE) E[r] = e[k];
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < DF_ROWS; r++) {
+    const int y = y0 + r;
+    B[r] = 0.0f;
+    C[r] = (uint8_t)CODE_OUTSIDE;
+    if (own && y < ny) {
+      const long k = gx + (long)y * nx;
+      B[r] = b[k];
+      C[r] = code[k];
+    }
+  }
+  if (UPDATE) {
+#pragma unroll
+    for (int r = 0; r < DF_ROWS + 2; r++) P[r] = df_add_f(P[r], E[r]);
+  }
+
+  float2 acc2 = make_float2(0.0f, 0.0f);
+  unsigned long long n = 0;
+#pragma unroll
+  for (int t = 0; t < DF_ROWS; t++) {
+    const int gy = y0 + t;
+    const float2 pc = P[t + 1];
+    const float2 left = make_float2(__shfl_up_sync(0xffffffffu, pc.x, 1), __shfl_up_sync(0xffffffffu, pc.y, 1));
+    const float2 right =
+        make_float2(__shfl_down_sync(0xffffffffu, pc.x, 1), __shfl_down_sync(0xffffffffu, pc.y, 1));
+    if (own && gy < ny) {
+      const long k = gx + (long)gy * nx;
+      if (UPDATE) p_out[k] = pc;
+      const uint8_t c = C[t];
+      float r = 0.0f;
+      const int cnt = code_count(c);
+      if ((c & 3u) == FLUID && cnt > 0) {
+        const float2 pp = P[t + 2], pm = P[t];
+        float2 sum = make_float2(0.0f, 0.0f);
+        bool first = true;
+        if (c & LINK_XP) {
+          sum = right;
+          first = false;
+        }
+        if (c & LINK_XM) {
+          sum = first ? left : df_add(sum, left);
+          first = false;
+        }
+        if (c & LINK_YP) {
+          sum = first ? pp : df_add(sum, pp);
+          first = false;
+        }
+        if (c & LINK_YM) sum = first ? pm : df_add(sum, pm);
+        const float2 d = df_add(df_mul_count(pc, cnt), df_neg(sum));
+        const float2 s = df_two_sum(B[t], -d.x);
+        r = __fadd_rn(s.x, __fsub_rn(s.y, d.y));
+        const float q = __fmul_rn(r, r);
+        acc2 = df_add(acc2, make_float2(q, __fmaf_rn(r, r, -q)));
+        n += 1;
+      }
+      r32[k] = r;
+    }
+  }
+  const double bs = block_sum(df_to_double(acc2), red);
+  const unsigned long long bn = block_sum_u64(n, redn);
+  if (threadIdx.x == 0) {
+    atomicAdd(&acc->res_sq, bs);
+    atomicAdd(&acc->n_res, bn);
+  }
+}
+
 __device__ __forceinline__ double acc_rms(double sq, unsigned long long n) { return n ? sqrt(sq / (double)n) : 0.0; }
 
 // Before the cycle loop (pressureMultigrid.ts:294-300, solveMixed): the rhs
@@ -1013,7 +1130,17 @@ void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* 
 
 void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, const SolveCtl* ctl,
                            const float* e, const float* b, const uint8_t* code, bool update, float* r32,
-                           StepAccum* acc) {
+                           StepAccum* acc, bool df) {
+  if (df) {
+    float2* a = reinterpret_cast<float2*>(p64a);
+    float2* bb = reinterpret_cast<float2*>(p64b);
+    dim3 g((nx + 29) / 30, (ny + DF_WARPS * DF_ROWS - 1) / (DF_WARPS * DF_ROWS));
+    if (update)
+      k_update_resid_df<true><<<g, 32 * DF_WARPS, 0, s>>>(nx, ny, a, bb, ctl, e, b, code, r32, acc);
+    else
+      k_update_resid_df<false><<<g, 32 * DF_WARPS, 0, s>>>(nx, ny, a, bb, ctl, e, b, code, r32, acc);
+    return;
+  }
   dim3 g((nx + 29) / 30, (ny + UR_WARPS * UR_ROWS - 1) / (UR_WARPS * UR_ROWS));
   if (update)
     k_update_resid64<true><<<g, 32 * UR_WARPS, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, code, r32, acc);

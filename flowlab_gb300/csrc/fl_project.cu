@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
   __shared__ double red[32];
   __shared__ unsigned long long redn[32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double sq = 0.0;
+  float2 sq = make_float2(0.0f, 0.0f);
   unsigned long long n = 0;
   const float coef = 1.0f / h;
   const float ns = as_rhs ? sc->neg_scale : 0.0f;
@@ -159,14 +159,15 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
     const float o = as_rhs ? ns * d : d;
     out[k] = o;
     if (label != nullptr && label[k] == FLUID) {
-      // one float64 operation per cell (the widening is exact on the integer pipe)
-      const double od = f2d_exact(o);
-      sq = fma(od, od, sq);
+      // the square as an exact pair (product + FMA error) added to a
+      // double-float sum: float32 work per cell, one widening per thread
+      const float q = __fmul_rn(o, o);
+      sq = df_add(sq, make_float2(q, __fmaf_rn(o, o, -q)));
       n += 1;
     }
   }
   if (acc == nullptr) return;
-  double bs = block_sum(sq, red);
+  double bs = block_sum(df_to_double(sq), red);
   unsigned long long bn = block_sum_u64(n, redn);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     atomicAdd(&acc->b_sq, bs);
@@ -183,28 +184,34 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
 // reference's loop order does.
 // Pressure difference between two cells: float32, or with a float64
 // pressure the difference formed in double and rounded once (the rounding
-// on the integer pipe: d2f_rn equals the conversion instruction).
-__device__ __forceinline__ float pdiff(const float* __restrict__ p, const double* __restrict__ p64, long a, long b) {
+// on the integer pipe: d2f_rn equals the conversion instruction), or with
+// the double-float pressure (`df`) the pairs' difference rounded once.
+__device__ __forceinline__ float pdiff(const float* __restrict__ p, const double* __restrict__ p64, bool df, long a,
+                                       long b) {
+  if (p64 && df) {
+    const float2* q = reinterpret_cast<const float2*>(p64);
+    return df_diff(q[a], q[b]);
+  }
   return p64 ? d2f_rn(p64[a] - p64[b]) : p[a] - p[b];
 }
 
-__device__ __forceinline__ float projected_u(const float* __restrict__ p, const double* __restrict__ p64,
+__device__ __forceinline__ float projected_u(const float* __restrict__ p, const double* __restrict__ p64, bool df,
                                              const float* __restrict__ u, const uint8_t* __restrict__ label, int nx,
                                              int ny, int i, int j, float gs, bool subtract) {
   float val = u[i + (long)j * (nx + 1)];
   if (subtract && i >= 1 && i < nx) {
     if (!(solid_or_outside(label, nx, ny, i - 1, j) || solid_or_outside(label, nx, ny, i, j)))
-      val -= gs * pdiff(p, p64, i + (long)j * nx, (i - 1) + (long)j * nx);
+      val -= gs * pdiff(p, p64, df, i + (long)j * nx, (i - 1) + (long)j * nx);
   }
   return val;
 }
-__device__ __forceinline__ float projected_v(const float* __restrict__ p, const double* __restrict__ p64,
+__device__ __forceinline__ float projected_v(const float* __restrict__ p, const double* __restrict__ p64, bool df,
                                              const float* __restrict__ v, const uint8_t* __restrict__ label, int nx,
                                              int ny, int i, int j, float gs, bool subtract) {
   float val = v[i + (long)j * nx];
   if (subtract && j >= 1 && j < ny) {
     if (!(solid_or_outside(label, nx, ny, i, j - 1) || solid_or_outside(label, nx, ny, i, j)))
-      val -= gs * pdiff(p, p64, i + (long)j * nx, i + (long)(j - 1) * nx);
+      val -= gs * pdiff(p, p64, df, i + (long)j * nx, i + (long)(j - 1) * nx);
   }
   return val;
 }
@@ -215,7 +222,7 @@ __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const 
                                                           const SolveCtl* __restrict__ ctl, float* __restrict__ u,
                                                           float* __restrict__ v, const uint8_t* __restrict__ label,
                                                           const StepScalars* __restrict__ sc, int subtract,
-                                                          int outflow) {
+                                                          int outflow, int df) {
   // the float64 pressure, when there is one, is the buffer ctl->par names
   const double* p64 = p64a ? (ctl->par ? p64b : p64a) : nullptr;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -223,7 +230,7 @@ __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const 
   const float gs = subtract ? sc->grad_scale : 0.0f;
   // u faces: threads 1..nx-1 write; faces 0 and nx are written only by outflow.
   if (j < ny && i >= 1 && i < nx) {
-    float val = projected_u(p, p64, u, label, nx, ny, i, j, gs, subtract);
+    float val = projected_u(p, p64, df, u, label, nx, ny, i, j, gs, subtract);
     if (outflow) {
       if (i == 1 && label[0 + (long)j * nx] == AIR) {
         val = smin(val, 0.0f);
@@ -237,7 +244,7 @@ __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const 
     u[i + (long)j * (nx + 1)] = val;
   }
   if (i < nx && j >= 1 && j < ny) {
-    float val = projected_v(p, p64, v, label, nx, ny, i, j, gs, subtract);
+    float val = projected_v(p, p64, df, v, label, nx, ny, i, j, gs, subtract);
     if (outflow) {
       if (j == 1 && label[i] == AIR) {
         val = smin(val, 0.0f);
@@ -321,17 +328,18 @@ __global__ void __launch_bounds__(256) k_scale_rhs(long n, const float* __restri
                                                    StepAccum* acc) {
   __shared__ double red[32];
   __shared__ unsigned long long redn[32];
-  double sq = 0.0;
+  float2 sq = make_float2(0.0f, 0.0f);
   unsigned long long cnt = 0;
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
     const float o = b ? neg_scale * div[k] : div[k];
     if (b) b[k] = o;
     if (label[k] == FLUID) {
-      sq = fma(f2d_exact(o), f2d_exact(o), sq);
+      const float q = __fmul_rn(o, o);
+      sq = df_add(sq, make_float2(q, __fmaf_rn(o, o, -q)));
       cnt += 1;
     }
   }
-  const double bs = block_sum(sq, red);
+  const double bs = block_sum(df_to_double(sq), red);
   const unsigned long long bn = block_sum_u64(cnt, redn);
   if (threadIdx.x == 0) {
     atomicAdd(&acc->b_sq, bs);
@@ -421,6 +429,16 @@ __global__ void k_convert_f32_f64(const float* __restrict__ a, double* __restric
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
     b[k] = (double)a[k];
 }
+// to the double-float pressure: (p, 0) from float32, the rounded double and
+// its remainder from float64
+__global__ void k_convert_f32_df(const float* __restrict__ a, float2* __restrict__ b, long n) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+    b[k] = make_float2(a[k], 0.0f);
+}
+__global__ void k_convert_f64_df(const double* __restrict__ a, float2* __restrict__ b, long n) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+    b[k] = df_from_double(a[k]);
+}
 
 // ------------------------------------------------------------- launchers
 
@@ -463,10 +481,10 @@ void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, 
 
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
                              const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow,
-                             const double* p64a, const double* p64b, const SolveCtl* ctl) {
+                             const double* p64a, const double* p64b, const SolveCtl* ctl, bool df) {
   dim3 b(32, 8);
   k_subtract_outflow<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, p, p64a, p64b, ctl, u, v, label, sc, subtract,
-                                                            outflow);
+                                                            outflow, df);
 }
 
 void launch_scale_rhs(cudaStream_t s, long n, const float* div, float* b, float neg_scale, const uint8_t* label,
@@ -519,6 +537,10 @@ void launch_convert(cudaStream_t s, const void* src, int src_dtype, void* dst, i
     k_convert_f64_f32<<<(unsigned)blocks, 256, 0, s>>>((const double*)src, (float*)dst, n);
   else if (src_dtype == FL_F32 && dst_dtype == FL_F64)
     k_convert_f32_f64<<<(unsigned)blocks, 256, 0, s>>>((const float*)src, (double*)dst, n);
+  else if (src_dtype == FL_F32 && dst_dtype == DT_DF)
+    k_convert_f32_df<<<(unsigned)blocks, 256, 0, s>>>((const float*)src, (float2*)dst, n);
+  else if (src_dtype == FL_F64 && dst_dtype == DT_DF)
+    k_convert_f64_df<<<(unsigned)blocks, 256, 0, s>>>((const double*)src, (float2*)dst, n);
 }
 
 // A fixed-duration single-thread kernel (about 40 us, bounded by its loop
@@ -532,15 +554,21 @@ void launch_hold(cudaStream_t s) { k_hold<<<1, 1, 0, s>>>(); }
 
 // Second-order warm start (no reference counterpart): on fluid cells
 // p = p + (p - p_prev) and p_prev = the old p, in float (the plain
-// multigrid's pressure) or float64 (the defect correction's current buffer,
-// chosen by the device parity).
+// multigrid's pressure), float64 or double-float (`df`; the defect
+// correction's current buffer, chosen by the device parity).
 __global__ void k_extrapolate(long n, const uint8_t* __restrict__ label, float* __restrict__ p32,
                               float* __restrict__ pp32, double* __restrict__ p64a, double* __restrict__ p64b,
-                              double* __restrict__ pp64, const SolveCtl* __restrict__ ctl) {
+                              double* __restrict__ pp64, const SolveCtl* __restrict__ ctl, int df) {
   double* p64 = p64a ? (ctl->par ? p64b : p64a) : nullptr;
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
     if (label[k] != FLUID) continue;
-    if (p64) {
+    if (p64 && df) {
+      float2* q = reinterpret_cast<float2*>(p64);
+      float2* qq = reinterpret_cast<float2*>(pp64);
+      const float2 t = q[k];
+      q[k] = df_add(t, df_add(t, df_neg(qq[k])));
+      qq[k] = t;
+    } else if (p64) {
       const double t = p64[k];
       p64[k] = t + (t - pp64[k]);
       pp64[k] = t;
@@ -553,17 +581,23 @@ __global__ void k_extrapolate(long n, const uint8_t* __restrict__ label, float* 
 }
 
 void launch_extrapolate(cudaStream_t s, long n, const uint8_t* label, float* p32, float* pp32, double* p64a,
-                        double* p64b, double* pp64, const SolveCtl* ctl) {
+                        double* p64b, double* pp64, const SolveCtl* ctl, bool df) {
   long blocks = std::min((n + 255) / 256, 152L * 8);
-  k_extrapolate<<<(unsigned)std::max(1L, blocks), 256, 0, s>>>(n, label, p32, pp32, p64a, p64b, pp64, ctl);
+  k_extrapolate<<<(unsigned)std::max(1L, blocks), 256, 0, s>>>(n, label, p32, pp32, p64a, p64b, pp64, ctl, df);
 }
 
-// out = p64[ctl->par] as float64 or rounded to float32.
+// out = p64[ctl->par] as float64 or rounded to float32 (the double-float
+// pressure: hi + lo in double, or the pair rounded to float).
 __global__ void k_select_p64(const SolveCtl* __restrict__ ctl, const double* __restrict__ p64a,
-                             const double* __restrict__ p64b, void* __restrict__ out, int as_f64, long n) {
+                             const double* __restrict__ p64b, void* __restrict__ out, int as_f64, long n, int df) {
   const double* src = ctl->par ? p64b : p64a;
+  const float2* src2 = reinterpret_cast<const float2*>(src);
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
-    if (as_f64)
+    if (df && as_f64)
+      static_cast<double*>(out)[k] = df_to_double(src2[k]);
+    else if (df)
+      static_cast<float*>(out)[k] = df_round(src2[k]);
+    else if (as_f64)
       static_cast<double*>(out)[k] = src[k];
     else
       static_cast<float*>(out)[k] = (float)src[k];
@@ -571,9 +605,9 @@ __global__ void k_select_p64(const SolveCtl* __restrict__ ctl, const double* __r
 }
 
 void launch_select_p64(cudaStream_t s, const SolveCtl* ctl, const double* p64a, const double* p64b, void* out,
-                       bool as_f64, long n) {
+                       bool as_f64, long n, bool df) {
   long blocks = std::min((n + 255) / 256, 152L * 8);
-  k_select_p64<<<(unsigned)std::max(1L, blocks), 256, 0, s>>>(ctl, p64a, p64b, out, as_f64, n);
+  k_select_p64<<<(unsigned)std::max(1L, blocks), 256, 0, s>>>(ctl, p64a, p64b, out, as_f64, n, df);
 }
 
 }  // namespace fl

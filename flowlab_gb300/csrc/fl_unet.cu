@@ -658,19 +658,22 @@ void Unet::refresh_weight_images(cudaStream_t s) {
 
 namespace {
 
-__device__ __forceinline__ double p_prev_at(const float* p32, const double* p64, long k) {
+// p_prev from the float pressure, the float64 one, or the double-float pairs
+// stored in the float64 buffers (df)
+__device__ __forceinline__ double p_prev_at(const float* p32, const double* p64, int df, long k) {
+  if (p64 && df) return df_to_double(reinterpret_cast<const float2*>(p64)[k]);
   return p64 ? p64[k] : (double)p32[k];
 }
 
 __global__ void __launch_bounds__(256) k_ws_psq(long n, const uint8_t* __restrict__ label, const float* __restrict__ p32,
                                                 const double* __restrict__ p64a, const double* __restrict__ p64b,
-                                                const int* __restrict__ par, double* __restrict__ sums) {
+                                                const int* __restrict__ par, int df, double* __restrict__ sums) {
   __shared__ double red[32];
   const double* p64 = p64a ? (*par ? p64b : p64a) : nullptr;
   double s = 0.0, c = 0.0;
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
     if (label[k] != FLUID) continue;
-    const double p = p_prev_at(p32, p64, k);
+    const double p = p_prev_at(p32, p64, df, k);
     s += p * p;
     c += 1.0;
   }
@@ -696,7 +699,7 @@ __global__ void k_ws_scales(const StepAccum* __restrict__ acc, const double* __r
 
 __global__ void k_ws_input(long n, const float* __restrict__ b, const uint8_t* __restrict__ label,
                            const float* __restrict__ p32, const double* __restrict__ p64a,
-                           const double* __restrict__ p64b, const int* __restrict__ par,
+                           const double* __restrict__ p64b, const int* __restrict__ par, int df,
                            const float* __restrict__ scales, float* __restrict__ x) {
   const double* p64 = p64a ? (*par ? p64b : p64a) : nullptr;
   const float ib = scales[2], ip = scales[3];
@@ -704,20 +707,22 @@ __global__ void k_ws_input(long n, const float* __restrict__ b, const uint8_t* _
     const bool fl = label[k] == FLUID;
     x[3 * k + 0] = fl ? b[k] * ib : 0.0f;
     x[3 * k + 1] = fl ? 1.0f : 0.0f;
-    x[3 * k + 2] = fl ? (float)p_prev_at(p32, p64, k) * ip : 0.0f;
+    x[3 * k + 2] = fl ? (float)p_prev_at(p32, p64, df, k) * ip : 0.0f;
   }
 }
 
 __global__ void k_ws_apply(long n, const float* __restrict__ out, const uint8_t* __restrict__ label,
                            const float* __restrict__ scales, float* __restrict__ p32, double* __restrict__ p64a,
-                           double* __restrict__ p64b, const int* __restrict__ par) {
+                           double* __restrict__ p64b, const int* __restrict__ par, int df) {
   if (!(scales[0] > 0.0f)) return;
   double* p64 = p64a ? (*par ? p64b : p64a) : nullptr;
   const float sp = scales[1];
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
     if (label[k] != FLUID) continue;
     const float d = sp * out[k];
-    if (p64)
+    if (p64 && df)
+      reinterpret_cast<float2*>(p64)[k] = df_add_f(reinterpret_cast<float2*>(p64)[k], d);
+    else if (p64)
       p64[k] += (double)d;
     else
       p32[k] += d;
@@ -728,14 +733,14 @@ __global__ void k_ws_apply(long n, const float* __restrict__ out, const uint8_t*
 
 void unet_warm_start(Unet& u, cudaStream_t s, int nx, int ny, const float* b, const uint8_t* label,
                      const StepAccum* acc, float* p32, double* p64a, double* p64b, const int* par,
-                     float* scales_dev) {
+                     float* scales_dev, bool df) {
   const long n = (long)nx * ny;
   cudaMemsetAsync(u.ws_acc, 0, 2 * sizeof(double), s);
-  k_ws_psq<<<grid_for(n), 256, 0, s>>>(n, label, p32, p64a, p64b, par, u.ws_acc);
+  k_ws_psq<<<grid_for(n), 256, 0, s>>>(n, label, p32, p64a, p64b, par, df, u.ws_acc);
   k_ws_scales<<<1, 1, 0, s>>>(acc, u.ws_acc, scales_dev);
-  k_ws_input<<<grid_for(n), 256, 0, s>>>(n, b, label, p32, p64a, p64b, par, scales_dev, u.input);
+  k_ws_input<<<grid_for(n), 256, 0, s>>>(n, b, label, p32, p64a, p64b, par, df, scales_dev, u.input);
   u.forward(s, 1, ny, nx);
-  k_ws_apply<<<grid_for(n), 256, 0, s>>>(n, u.out, label, scales_dev, p32, p64a, p64b, par);
+  k_ws_apply<<<grid_for(n), 256, 0, s>>>(n, u.out, label, scales_dev, p32, p64a, p64b, par, df);
 }
 
 }  // namespace fl

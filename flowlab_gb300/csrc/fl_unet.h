@@ -96,10 +96,11 @@ int unet_tc_take_error();
 
 // Warm start inside the engine's step: input from (b, labels, p_prev), the
 // forward pass, p = p_prev + s_p * out on fluid cells. p_prev is float
-// (p32) or one of two float64 buffers chosen by a device parity word.
+// (p32) or one of two float64 buffers chosen by a device parity word
+// (holding double-float pairs when df).
 struct StepAccum;
 void unet_warm_start(Unet& u, cudaStream_t s, int nx, int ny, const float* b, const uint8_t* label,
                      const StepAccum* acc, float* p32, double* p64a, double* p64b, const int* par,
-                     float* scales_dev);
+                     float* scales_dev, bool df);
 
 }  // namespace fl

@@ -27,7 +27,8 @@
  *     same engine is running returns FL_EBUSY (the reference throws
  *     "... is not re-entrant", stepGpu.ts:402, multigridGpu.ts:318).
  *   - Compute is float32 (the reference's WGSL precision), optionally with a
- *     float64 fine-level pressure for iterative refinement (fl_params.mixed).
+ *     refined fine-level pressure for iterative refinement (fl_params.mixed):
+ *     float64, or a double-float pair of floats computed on the float32 pipe.
  */
 #ifndef FLOWLAB_GB300_H
 #define FLOWLAB_GB300_H
@@ -85,7 +86,9 @@ typedef struct fl_params {
   int mg_coarse_sweeps;  /* sweep pairs on the coarsest level (reference 8) */
   int mg_coarsest;       /* stop coarsening at <= this many cells a side (reference 4; at most 64) */
   double mg_omega;       /* smoother relaxation (reference 1.0) */
-  int mixed;             /* 1: float64 fine pressure + float64 residual (defect correction) */
+  int mixed;             /* defect correction around the multigrid: 0 off; 1 float64 fine pressure and
+                            residual; 2 the same with a double-float pressure (hi + lo, two floats,
+                            ~48 significand bits) and residual, all float32 arithmetic */
   int rb_pairs;          /* red-black sweep pairs per launch, 1..4 (0: 4): the temporal-blocking
                             depth, i.e. the tile/halo shape; results do not depend on it */
   int warm_extrapolate;  /* 1: the multigrid starts from 2 p(n) - p(n-1) on Fluid cells instead of
@@ -223,11 +226,14 @@ int fl_rb_solve(fl_engine* e, float* p, const float* div, const uint8_t* label, 
 int fl_mg_solve(fl_engine* e, float* p, const float* div, const uint8_t* label, float scale, int max_cycles,
                 double tol, int* cycles_used, double* rel_residual);
 
-/* The same multigrid wrapped in float64 defect correction (NEW, no reference
+/* The same multigrid wrapped in defect correction (NEW, no reference
  * counterpart): p is a float64 in/out warm start; each pass forms
- * r = b - A p in float64, runs one float32 V-cycle on A e = r from e = 0 and
- * adds e back in float64, until the relative residual <= tol or max_cycles.
- * This is what reaches relative residuals below float32's ~1e-5 floor. */
+ * r = b - A p in extended precision, runs one float32 V-cycle on A e = r from
+ * e = 0 and adds e back, until the relative residual <= tol or max_cycles.
+ * The extended precision is the engine's fl_params.mixed: float64 (1), or
+ * double-float pairs (2; p is converted to pairs on the way in and back to
+ * float64 as hi + lo on the way out). This is what reaches relative
+ * residuals below float32's ~1e-5 floor. */
 int fl_mg_solve_mixed(fl_engine* e, double* p, const float* div, const uint8_t* label, float scale, int max_cycles,
                       double tol, int* cycles_used, double* rel_residual);
 

@@ -99,6 +99,8 @@ def lib():
             for name in ("orc_rms_remaining_", "orc_fluid_div_rms_", "orc_relres_b_"):
                 getattr(_LIB, name + suf).restype = ctypes.c_double
             getattr(_LIB, "orc_sim_create_" + suf).restype = ctypes.c_void_p
+        _LIB.orc_mg_solve_df_f32.restype = ctypes.c_int
+        _LIB.orc_residual_df_f32.restype = ctypes.c_double
     return _LIB
 
 
@@ -192,6 +194,24 @@ class Oracle:
                                          ctypes.c_double(tol), int(pre), int(post), int(coarse), int(coarsest),
                                          ctypes.c_double(omega), ctypes.byref(rr))
         return p64, used, rr.value
+
+    def mg_solve_df(self, nx, ny, p64, div, label, scale, cycles, tol, pre=2, post=2, coarse=8, coarsest=4,
+                    omega=1.0):
+        """solveMixedDF (float32 only): the defect correction with a double-float
+        pressure. p64 in (float64, split into pairs as the engine does) and out
+        (hi + lo in float64)."""
+        assert self.suf == "f32"
+        p64 = np.ascontiguousarray(p64, dtype=np.float64)
+        hi = p64.astype(np.float32)
+        pairs = np.empty(2 * p64.size, np.float32)
+        pairs[0::2] = hi
+        pairs[1::2] = (p64 - hi.astype(np.float64)).astype(np.float32)
+        div, label = self._arr(div), self._lab(label)
+        rr = ctypes.c_double(-1)
+        used = self.L.orc_mg_solve_df_f32(nx, ny, _p(pairs), _p(div), _p(label), ctypes.c_float(scale), int(cycles),
+                                          ctypes.c_double(tol), int(pre), int(post), int(coarse), int(coarsest),
+                                          ctypes.c_double(omega), ctypes.byref(rr))
+        return pairs[0::2].astype(np.float64) + pairs[1::2].astype(np.float64), used, rr.value
 
     def residual(self, nx, ny, x, b, label):
         x, b, label = self._arr(x), self._arr(b), self._lab(label)

@@ -721,6 +721,152 @@ int solveMixed(Multigrid<T>& mg, const Grid<T>& g, double* p, const T* div, cons
   return c;
 }
 
+// NEW — double-float defect correction (mixed = 2): the outer loop of
+// solveMixed with the pressure kept as an unevaluated sum hi + lo of two
+// floats (about 48 significand bits) instead of a double, and the residual
+// formed with error-free float transformations: TwoSum (Knuth, TAOCP vol. 2,
+// 4.2.2), FastTwoSum and the double-length sum of Dekker ("A floating-point
+// technique for extending the available precision", 1971), and an FMA-based
+// exact product for the count 3. Every operation is one IEEE float32
+// operation (or a fused multiply-add where written), so the CUDA kernels
+// reproduce the results bit for bit. The pressure lives in pairs
+// (p[2k] = hi, p[2k+1] = lo).
+namespace df {
+struct F2 {
+  float hi, lo;
+};
+// s + e = a + b exactly.
+inline F2 twoSum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  const float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+// s + e = a + b exactly when |a| >= |b| (or a == 0).
+inline F2 fastTwoSum(float a, float b) {
+  const float s = a + b;
+  const float e = b - (s - a);
+  return {s, e};
+}
+// (x.hi + x.lo) + (y.hi + y.lo), renormalised.
+inline F2 add(F2 x, F2 y) {
+  const F2 s = twoSum(x.hi, y.hi);
+  const float e = s.lo + (x.lo + y.lo);
+  return fastTwoSum(s.hi, e);
+}
+inline F2 neg(F2 x) { return {-x.hi, -x.lo}; }
+// (x.hi + x.lo) + f, renormalised.
+inline F2 addF(F2 x, float f) {
+  const F2 s = twoSum(x.hi, f);
+  const float e = s.lo + x.lo;
+  return fastTwoSum(s.hi, e);
+}
+// count * x for a link count 1..4 (2 and 4 scale exactly; 3 through the
+// exact product 3*hi = p + fma(3, hi, -p)).
+inline F2 mulCount(F2 x, int count) {
+  if (count == 4) return {4.0f * x.hi, 4.0f * x.lo};
+  if (count == 2) return {2.0f * x.hi, 2.0f * x.lo};
+  if (count == 1) return x;
+  const float p = 3.0f * x.hi;
+  float e = std::fma(3.0f, x.hi, -p);
+  e = std::fma(3.0f, x.lo, e);
+  return fastTwoSum(p, e);
+}
+// The pair rounded to one float.
+inline float round(F2 x) { return x.hi + x.lo; }
+// a - b of two pairs, rounded to one float (the projection's pressure
+// difference).
+inline float diff(F2 a, F2 b) {
+  const F2 s = twoSum(a.hi, -b.hi);
+  const float e = s.lo + (a.lo - b.lo);
+  return s.hi + e;
+}
+inline double toDouble(F2 x) { return (double)x.hi + (double)x.lo; }
+inline F2 fromDouble(double d) {
+  const float hi = (float)d;
+  return {hi, (float)(d - (double)hi)};
+}
+inline F2 at(const float* p, long k) { return {p[2 * k], p[2 * k + 1]}; }
+inline void put(float* p, long k, F2 x) {
+  p[2 * k] = x.hi;
+  p[2 * k + 1] = x.lo;
+}
+}  // namespace df
+
+// r = b - (count*p - sum) in double-float arithmetic, the neighbour sum in
+// the order +x, -x, +y, -y starting from the first linked neighbour; r32 is
+// the result rounded to float (0 off-fluid and on cells without links). The
+// norm is the sum of r32^2 (squares exact in double) over fluid cells with
+// links; bSq/nb are the rhs sums over fluid cells, as residual64.
+inline double residualDF(const Grid<float>& g, const float* p, const float* b, const uint8_t* label, float* r32,
+                         double& bSq, long& nb) {
+  double sumSq = 0;
+  long n = 0;
+  bSq = 0;
+  nb = 0;
+  for (int j = 0; j < g.ny; j++)
+    for (int i = 0; i < g.nx; i++) {
+      const long k = idxP(g.nx, i, j);
+      r32[k] = 0;
+      if (label[k] != FLUID) continue;
+      bSq += (double)b[k] * (double)b[k];
+      nb += 1;
+      const bool links[4] = {!solidOrOutside(g, label, i + 1, j), !solidOrOutside(g, label, i - 1, j),
+                             !solidOrOutside(g, label, i, j + 1), !solidOrOutside(g, label, i, j - 1)};
+      const long nbk[4] = {k + 1, k - 1, k + g.nx, k - g.nx};
+      int count = 0;
+      df::F2 sum{0.0f, 0.0f};
+      for (int q = 0; q < 4; q++) {
+        if (!links[q]) continue;
+        sum = count == 0 ? df::at(p, nbk[q]) : df::add(sum, df::at(p, nbk[q]));
+        count += 1;
+      }
+      if (count == 0) continue;
+      const df::F2 d = df::add(df::mulCount(df::at(p, k), count), df::neg(sum));
+      const df::F2 s = df::twoSum(b[k], -d.hi);
+      const float e = s.lo - d.lo;
+      const float r = s.hi + e;
+      r32[k] = r;
+      sumSq += (double)r * (double)r;
+      n += 1;
+    }
+  return n > 0 ? std::sqrt(sumSq / (double)n) : 0.0;
+}
+
+// solveMixed with the double-float pressure `p` (2n floats): the same loop,
+// tests and cycle count rule; each pass adds the V-cycle's e to every
+// cell's pair (p = p + e, renormalised).
+inline int solveMixedDF(Multigrid<float>& mg, const Grid<float>& g, float* p, const float* div, const uint8_t* label,
+                        float scale, int cycles, double tol, double* relRes) {
+  const long n = (long)g.nx * g.ny;
+  mg.prepare(g, div, label, scale);
+  std::vector<float> b(mg.levels[0].b);
+  std::vector<float> e(n);
+  double bSq;
+  long nb;
+  double rr = residualDF(g, p, b.data(), label, mg.levels[0].b.data(), bSq, nb);
+  const double bRms = nb > 0 ? std::sqrt(bSq / (double)nb) : 0.0;
+  if (relRes) *relRes = -1;
+  if (bRms == 0) {
+    std::fill(p, p + 2 * n, 0.0f);
+    if (relRes) *relRes = 0;
+    return 0;
+  }
+  double rel = rr / bRms;
+  if (relRes) *relRes = rel;
+  int c = 0;
+  while (c < cycles && !(rel <= tol)) {
+    std::fill(e.begin(), e.end(), 0.0f);
+    mg.vcycle(0, e.data());
+    for (long k = 0; k < n; k++) df::put(p, k, df::addF(df::at(p, k), e[k]));
+    rr = residualDF(g, p, b.data(), label, mg.levels[0].b.data(), bSq, nb);
+    rel = rr / bRms;
+    if (relRes) *relRes = rel;
+    c++;
+  }
+  return c;
+}
+
 // ------------------------------------------------------------- projection
 
 // subtractGradient.ts:40-61
@@ -751,6 +897,22 @@ void subtractGradient64(const Grid<T>& g, const double* p, T* u, T* v, const uin
     for (int i = 0; i < g.nx; i++) {
       if (solidOrOutside(g, label, i, j - 1) || solidOrOutside(g, label, i, j)) continue;
       v[idxV(g.nx, i, j)] -= gradScale * (T)(p[idxP(g.nx, i, j)] - p[idxP(g.nx, i, j - 1)]);
+    }
+}
+
+// subtractGradient with the double-float pressure (pairs): the difference
+// of two pairs rounded once (df::diff) before the float update.
+inline void subtractGradientDF(const Grid<float>& g, const float* p, float* u, float* v, const uint8_t* label,
+                               float gradScale) {
+  for (int j = 0; j < g.ny; j++)
+    for (int i = 1; i < g.nx; i++) {
+      if (solidOrOutside(g, label, i - 1, j) || solidOrOutside(g, label, i, j)) continue;
+      u[idxU(g.nx, i, j)] -= gradScale * df::diff(df::at(p, idxP(g.nx, i, j)), df::at(p, idxP(g.nx, i - 1, j)));
+    }
+  for (int j = 1; j < g.ny; j++)
+    for (int i = 0; i < g.nx; i++) {
+      if (solidOrOutside(g, label, i, j - 1) || solidOrOutside(g, label, i, j)) continue;
+      v[idxV(g.nx, i, j)] -= gradScale * df::diff(df::at(p, idxP(g.nx, i, j)), df::at(p, idxP(g.nx, i, j - 1)));
     }
 }
 
@@ -961,7 +1123,7 @@ struct StepParams {
   double beta = 0, alpha = 0, confinement = 0;
   MgShape mg;
   int mgMaxCycles = 3;
-  int mixed = 0;  // NEW: float64 pressure + defect correction around the multigrid
+  int mixed = 0;  // NEW: defect correction around the multigrid, 1: float64 pressure, 2: double-float (float32 only)
   int warmExtrapolate = 0;  // NEW: the multigrid starts from 2 p(n) - p(n-1) on fluid cells
 };
 
@@ -973,6 +1135,7 @@ struct Simulation {
   std::vector<double> p64;  // the pressure when prm.mixed
   std::vector<double> pPrev64;  // the previous step's pressure (warmExtrapolate, mixed)
   std::vector<T> pPrev;         // the previous step's pressure (warmExtrapolate)
+  std::vector<float> pdf, pPrevDF;  // the double-float pressure and its previous value (mixed = 2, float32)
   std::vector<uint8_t> label;
   std::vector<T> dye[DYE_CHANNELS], dyeNext[DYE_CHANNELS];
   std::vector<float> patch;
@@ -998,8 +1161,26 @@ struct Simulation {
     p64.assign(n, 0.0);
     pPrev64.assign(n, 0.0);
     pPrev.assign(n, 0);
+    pdf.assign(2 * n, 0.0f);
+    pPrevDF.assign(2 * n, 0.0f);
     for (int c = 0; c < DYE_CHANNELS; c++) { dye[c].assign(nd, 0); dyeNext[c].assign(nd, 0); }
     mg.shape = prm.mg;
+  }
+
+  // mixed = 2 keeps the pressure as float pairs; the float64 instantiation
+  // (the precision oracle) runs every mixed mode as float64.
+  bool useDF() const { return prm.mixed == 2 && std::is_same<T, float>::value; }
+
+  // The refined pressure (p64 / pdf) from the float pressure p, as an upload
+  // of p sets it.
+  void seedRefined() {
+    for (size_t k = 0; k < p.size(); k++) {
+      p64[k] = (double)p[k];
+      pdf[2 * k] = (float)p[k];
+      pdf[2 * k + 1] = 0.0f;
+    }
+    pPrev64 = p64;
+    pPrevDF = pdf;
   }
 
   // simulation.ts:451-459
@@ -1045,7 +1226,13 @@ struct Simulation {
       const long n = (long)g.nx * g.ny;
       for (long k = 0; k < n; k++) {
         if (label[k] != FLUID) continue;
-        if (prm.mixed) {
+        if (useDF()) {
+          if constexpr (std::is_same<T, float>::value) {
+            const df::F2 t = df::at(pdf.data(), k);
+            df::put(pdf.data(), k, df::add(t, df::add(t, df::neg(df::at(pPrevDF.data(), k)))));
+            df::put(pPrevDF.data(), k, t);
+          }
+        } else if (prm.mixed) {
           const double t = p64[k];
           p64[k] = t + (t - pPrev64[k]);
           pPrev64[k] = t;
@@ -1056,7 +1243,13 @@ struct Simulation {
         }
       }
     }
-    if (prm.solver == 1 && prm.mixed) {
+    if (prm.solver == 1 && useDF()) {
+      if constexpr (std::is_same<T, float>::value) {
+        iters = solveMixedDF(mg, g, pdf.data(), div.data(), label.data(), scale, prm.mgMaxCycles, prm.tol,
+                             &lastRelRes);
+        for (size_t k = 0; k < p.size(); k++) p[k] = df::round(df::at(pdf.data(), (long)k));
+      }
+    } else if (prm.solver == 1 && prm.mixed) {
       iters = solveMixed(mg, g, p64.data(), div.data(), label.data(), scale, prm.mgMaxCycles, prm.tol, &lastRelRes);
       for (size_t k = 0; k < p.size(); k++) p[k] = (T)p64[k];
     } else if (prm.solver == 1) {
@@ -1066,7 +1259,10 @@ struct Simulation {
     } else {
       iters = solvePressure(g, p.data(), div.data(), label.data(), scale, prm.pressureIters, T(prm.omega), prm.tol);
     }
-    if (prm.solver == 1 && prm.mixed)
+    if (prm.solver == 1 && useDF()) {
+      if constexpr (std::is_same<T, float>::value)
+        subtractGradientDF(g, pdf.data(), u.data(), v.data(), label.data(), gradScale);
+    } else if (prm.solver == 1 && prm.mixed)
       subtractGradient64(g, p64.data(), u.data(), v.data(), label.data(), gradScale);
     else
       subtractGradient(g, p.data(), u.data(), v.data(), label.data(), gradScale);

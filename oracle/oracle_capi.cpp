@@ -128,7 +128,10 @@ static StepParams toParams(const orc_params* c) {
   }                                                                                                     \
   void orc_sim_get_p64_##SUF(void* sp, double* p) {                                                     \
     Simulation<T>* s = (Simulation<T>*)sp;                                                              \
-    std::copy(s->p64.begin(), s->p64.end(), p);                                                         \
+    if (s->useDF())                                                                                     \
+      for (size_t k = 0; k < s->p.size(); k++) p[k] = df::toDouble(df::at(s->pdf.data(), (long)k));     \
+    else                                                                                                \
+      std::copy(s->p64.begin(), s->p64.end(), p);                                                       \
   }                                                                                                     \
   void orc_residual_##SUF(int nx, int ny, const T* x, const T* b, const uint8_t* label, T* r) {         \
     computeResidual(Grid<T>{nx, ny, T(1)}, x, b, label, r);                                             \
@@ -201,7 +204,7 @@ static StepParams toParams(const orc_params* c) {
     std::copy(p, p + s->p.size(), s->p.begin());                                                       \
     std::copy(label, label + s->label.size(), s->label.begin());                                       \
     std::copy(p, p + s->p.size(), s->pPrev.begin());                                                   \
-    std::copy(s->p64.begin(), s->p64.end(), s->pPrev64.begin());                                       \
+    s->seedRefined();                                                                                   \
     long cells = (long)s->dye[0].size();                                                                \
     for (int c = 0; c < DYE_CHANNELS; c++)                                                              \
       std::copy(dye + c * cells, dye + (c + 1) * cells, s->dye[c].begin());                             \
@@ -238,3 +241,27 @@ static StepParams toParams(const orc_params* c) {
 
 ORC_DEFINE(double, f64)
 ORC_DEFINE(float, f32)
+
+// Double-float defect correction (mixed = 2), float32 only: p is 2n floats
+// (hi, lo per cell), in/out.
+extern "C" int orc_mg_solve_df_f32(int nx, int ny, float* p, const float* div, const uint8_t* label, float scale,
+                                   int cycles, double tol, int pre, int post, int coarseSweeps, int coarsest,
+                                   double omega, double* relRes) {
+  Multigrid<float> mg;
+  mg.shape.pre = pre;
+  mg.shape.post = post;
+  mg.shape.coarseSweeps = coarseSweeps;
+  mg.shape.coarsest = coarsest;
+  mg.shape.omega = omega;
+  return solveMixedDF(mg, Grid<float>{nx, ny, 1.0f}, p, div, label, scale, cycles, tol, relRes);
+}
+
+// One double-float residual pass: r32 and the norm ratio rms(r) / rms(b).
+extern "C" double orc_residual_df_f32(int nx, int ny, const float* p, const float* b, const uint8_t* label,
+                                      float* r32) {
+  double bSq;
+  long nb;
+  const double rr = residualDF(Grid<float>{nx, ny, 1.0f}, p, b, label, r32, bSq, nb);
+  const double bRms = nb > 0 ? std::sqrt(bSq / (double)nb) : 0.0;
+  return bRms > 0 ? rr / bRms : 0.0;
+}

@@ -127,15 +127,17 @@ def test_dye_decay_exponential_in_time():
     assert d[300] == 0
 
 
-def test_plume_mixed_steps_match_float32_oracle(o32):
-    """The plume with the float64 defect-correction solve to 1e-6, identical to
-    the oracle's float32-fields / float64-pressure step."""
+@pytest.mark.parametrize("mixed", [1, 2])
+def test_plume_mixed_steps_match_float32_oracle(o32, mixed):
+    """The plume with the defect-correction solve to 1e-6 (float64 or
+    double-float pressure), identical to the oracle's float32-fields step with
+    the same refined pressure."""
     g, f, patch = configs.plume(64)
-    prm = configs.plume_params(tol=1e-6, max_cycles=30, mixed=1)
+    prm = configs.plume_params(tol=1e-6, max_cycles=30, mixed=mixed)
     steps = 8
     u, v, p, d, st = run_engine(g, f, patch, prm, steps)
     eu, ev, ep, ed, info = run_oracle(o32, g, f, patch, prm, steps)
-    for name, a, b in (("u", eu, u), ("v", ev, v), ("dye", ed, d)):
+    for name, a, b in (("u", eu, u), ("v", ev, v), ("p", ep, p), ("dye", ed, d)):
         assert mismatch(a, b) == 0, "%s: %d values differ from the float32 oracle" % (name, mismatch(a, b))
     assert 0 <= st["rel_residual"] <= 1e-6 and abs(st["rel_residual"] - info["rel_res"]) <= 1e-9 * info["rel_res"] + 1e-15
 
