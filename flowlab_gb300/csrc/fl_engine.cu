@@ -177,6 +177,7 @@ void free_all(Engine* e) {
   cudaFree(e->p64[0]);
   cudaFree(e->p64[1]);
   cudaFree(e->r32);
+  cudaFree(e->b_lo);
   cudaFree(e->pprev32);
   cudaFree(e->pprev64);
   cudaFree(e->bt_u);
@@ -404,7 +405,8 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
   prof_end(*e, tok, fbytes, flaunch);
   cudaMemsetAsync(e->acc, 0, 4 * sizeof(double), s);
   tok = prof_begin(*e, FL_PH_DIVERGENCE);
-  launch_divergence(s, e->nx, e->ny, e->h, u, v, L0.b, e->prm.solver == FL_SOLVER_MG, L0.label, e->sc, e->acc);
+  launch_divergence(s, e->nx, e->ny, e->h, u, v, L0.b, e->prm.solver == FL_SOLVER_MG, L0.label, e->sc, e->acc,
+                    step_mixed(e) ? e->b_lo : nullptr);
   prof_end(*e, tok, 4 * F + N + 4 * N, 1);
   if (e->prm.warm_extrapolate && e->prm.solver == FL_SOLVER_MG) {
     const bool mixed = e->prm.mixed != 0;
@@ -428,8 +430,8 @@ void enqueue_solve_prologue(Engine* e, cudaStream_t s, bool mixed, bool use_cond
   Level& L0 = e->levels[0];
   if (mixed) {
     const int tok = prof_begin(*e, FL_PH_DEFECT64);
-    launch_update_resid64(s, e->nx, e->ny, e->p64[0], e->p64[1], e->ctl, nullptr, L0.b, L0.code, false, e->r32,
-                          e->acc, refined_df(e));
+    launch_update_resid64(s, e->nx, e->ny, e->p64[0], e->p64[1], e->ctl, nullptr, L0.b, e->b_lo, L0.code, false,
+                          e->r32, e->acc, refined_df(e));
     // p64, b, code in; r32 out
     prof_end(*e, tok, 17.0 * e->cells(), 1);
   }
@@ -446,8 +448,8 @@ void enqueue_solve_body(Engine* e, cudaStream_t s, bool mixed, bool use_cond, cu
   if (mixed) {
     mg_vcycle_on(*e, e->r32, true, nullptr);
     const int tok = prof_begin(*e, FL_PH_DEFECT64);
-    launch_update_resid64(s, e->nx, e->ny, e->p64[0], e->p64[1], e->ctl, L0.x[0], L0.b, L0.code, true, e->r32,
-                          e->acc, refined_df(e));
+    launch_update_resid64(s, e->nx, e->ny, e->p64[0], e->p64[1], e->ctl, L0.x[0], L0.b, e->b_lo, L0.code, true,
+                          e->r32, e->acc, refined_df(e));
     // p64, e, b, code in; p64 (other buffer), r32 out
     prof_end(*e, tok, 29.0 * e->cells(), 1);
   } else {
@@ -727,6 +729,8 @@ int solve_stats(Engine* e) {
     e->last_relres = c.rel;
   }
   if (c.nonfinite) return fail(e, FL_ENONFINITE, "non-finite %s", c.cycles ? "residual" : "divergence");
+  if (e->warm != nullptr && unet_tc_take_error())
+    return fail(e, FL_ETIMEOUT, "the warm start's tensor-core convolution gave up a bounded wait");
   return FL_OK;
 }
 
@@ -827,6 +831,7 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   s = s ? s : dalloc(e, (void**)&e->p64[0], (size_t)e->cells() * 8, "p64");
   s = s ? s : dalloc(e, (void**)&e->p64[1], (size_t)e->cells() * 8, "p64");
   s = s ? s : dalloc(e, (void**)&e->r32, cf, "residual");
+  s = s ? s : dalloc(e, (void**)&e->b_lo, cf, "rhs rounding error");
   s = s ? s : dalloc(e, (void**)&e->pprev32, cf, "previous pressure");
   s = s ? s : dalloc(e, (void**)&e->pprev64, (size_t)e->cells() * 8, "previous pressure");
   s = s ? s : dalloc(e, (void**)&e->bt_u, (size_t)e->ufaces() * sizeof(float2), "backtrace positions");
@@ -906,9 +911,13 @@ int fl_set_params(fl_engine* h, const fl_params* p) {
 
 void* fl_stream(fl_engine* h) { return h ? (void*)h->e.stream : nullptr; }
 
+// Also reports what the last steps left for a synchronising call: a
+// non-finite solve (FL_ENONFINITE) or a timed-out tensor-core wait of the
+// warm start (FL_ETIMEOUT).
 int fl_synchronize(fl_engine* h) {
   ENTER(h);
-  return sync(e, "synchronize");
+  TRY(sync(e, "synchronize"));
+  return solve_stats(e);
 }
 
 // The device-side work of an upload once the fields have landed: p64 (the
@@ -1102,10 +1111,8 @@ int fl_step_host(fl_engine* h, const float* u, const float* v, const float* p, c
                                        cudaMemcpyDeviceToHost, e->stream), "read dye"));
   TRY(sync2(e, "read back"));
   TRY(sync(e, "step"));
-  if (iters) {
-    TRY(solve_stats(e));
-    *iters = e->last_iters;
-  }
+  TRY(solve_stats(e));
+  if (iters) *iters = e->last_iters;
   return FL_OK;
 }
 
@@ -1347,7 +1354,7 @@ int fl_mg_solve(fl_engine* h, float* p, const float* div, const uint8_t* label, 
   TRY(put_labels(e, label, "label"));
   mg_build_codes(*e);
   TRY(zero_solve_accum(e));
-  launch_scale_rhs(e->stream, n, e->u_hat, L.b, -scale, L.label, e->acc);
+  launch_scale_rhs(e->stream, n, e->u_hat, L.b, -scale, L.label, e->acc, e->b_lo);
   TRY(check_launch(e, "rhs"));
   TRY(put_ctl(e, SOLVE_MG, tol, max_cycles, true));
   e->stats_on_device = true;
@@ -1377,7 +1384,7 @@ int fl_mg_solve_mixed(fl_engine* h, double* p, const float* div, const uint8_t* 
   TRY(put_labels(e, label, "label"));
   mg_build_codes(*e);
   TRY(zero_solve_accum(e));
-  launch_scale_rhs(e->stream, n, e->u_hat, L.b, -scale, L.label, e->acc);
+  launch_scale_rhs(e->stream, n, e->u_hat, L.b, -scale, L.label, e->acc, e->b_lo);
   TRY(check_launch(e, "rhs"));
   TRY(solve_mg_eager(e, true, max_cycles));
   TRY(read_ctl(e));

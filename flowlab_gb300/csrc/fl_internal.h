@@ -58,6 +58,10 @@ struct Engine {
   // p64[ctl->par] is the pressure, r32 the float residual fed to each V-cycle.
   double* p64[2] = {nullptr, nullptr};
   float* r32 = nullptr;
+  // the rounding error of the fine rhs b = (-scale) * div (b + b_lo is the
+  // exact product): the defect correction's residual is formed against it,
+  // so its tolerance test is on the unrounded rhs
+  float* b_lo = nullptr;
   // the previous step's pressure of the second-order warm start
   float* pprev32 = nullptr;
   double* pprev64 = nullptr;
@@ -175,8 +179,10 @@ void launch_confinement_force(cudaStream_t s, int nx, int ny, float h, const flo
 void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, float dh, float* u, float* v,
                    const float* dye, const uint8_t* label, bool beta_on, bool alpha_on, bool conf_on,
                    const float* fx, const float* fy, const StepScalars* sc);
+// out_lo (optional): the exact rounding error of each b = (-scale) * div (b + out_lo is the product)
 void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
-                       bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc);
+                       bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc,
+                       float* out_lo = nullptr);
 // p64a/p64b: the refined pressure (float64, or double-float pairs when df)
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
                              const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow,
@@ -187,7 +193,7 @@ void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const floa
                       bool add_time);
 // b = (-scale)*div (b may be null: only accumulate div^2) with fluid sums.
 void launch_scale_rhs(cudaStream_t s, long n, const float* div, float* b, float neg_scale, const uint8_t* label,
-                      StepAccum* acc);
+                      StepAccum* acc, float* b_lo = nullptr);
 void launch_commit_labels(cudaStream_t s, int nx, int ny, const uint8_t* label, float* p, float* u, float* v,
                           float* dye, long dye_cells, double* p64a = nullptr, double* p64b = nullptr,
                           const SolveCtl* ctl = nullptr);
@@ -211,8 +217,8 @@ void mg_vcycle(Engine& e, StepAccum* acc_for_residual);
 void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc_for_residual);
 // the refined-pressure pass: float64, or double-float pairs in the same buffers when df
 void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, const SolveCtl* ctl,
-                           const float* e, const float* b, const uint8_t* code, bool update, float* r32,
-                           StepAccum* acc, bool df);
+                           const float* e, const float* b, const float* b_lo, const uint8_t* code, bool update,
+                           float* r32, StepAccum* acc, bool df);
 void launch_solve_begin(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h);
 void launch_solve_check(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h);
 void launch_zero_if(cudaStream_t s, const SolveCtl* ctl, float* p32, double* p64a, double* p64b, long n);

@@ -723,6 +723,7 @@ __global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny
                                                                 const SolveCtl* __restrict__ ctl,
                                                                 const float* __restrict__ e,
                                                                 const float* __restrict__ b,
+                                                                const float* __restrict__ b_lo,
                                                                 const uint8_t* __restrict__ code,
                                                                 float* __restrict__ r32, StepAccum* acc) {
   __shared__ double red[32];
@@ -753,11 +754,12 @@ __global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny
   raw(y0, rp, re);
   double pm = form(rp0, re0), pc = form(rp, re);
   raw(y0 + 1, rp, re);
-  float bnext = 0.0f;
+  float bnext = 0.0f, blnext = 0.0f;
   uint8_t cnext = (uint8_t)CODE_OUTSIDE;
   if (own && y0 < ny) {
     const long k = gx + (long)y0 * nx;
     bnext = b[k];
+    blnext = b_lo[k];
     cnext = code[k];
   }
 
@@ -769,11 +771,12 @@ __global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny
     if (gy >= ny) break;  // the same for the whole warp
     const double pp = form(rp, re);
     raw(gy + 2, rp, re);
-    const float bv = bnext;
+    const float bv = bnext, blv = blnext;
     const uint8_t c = cnext;
     if (own && gy + 1 < ny && t + 1 < UR_ROWS) {
       const long k = gx + (long)(gy + 1) * nx;
       bnext = b[k];
+      blnext = b_lo[k];
       cnext = code[k];
     }
     const double left = __shfl_up_sync(0xffffffffu, pc, 1);
@@ -804,7 +807,8 @@ __global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny
                           : cnt == 2 ? scale_pow2(pc, 1)
                           : cnt == 1 ? pc
                                      : dmul_slow(pc, 3.0);
-        const double rd = f2d_exact(bv) - (cp - sum);
+        // b + b_lo is exact in double (at most 49 significant bits)
+        const double rd = (f2d_exact(bv) + f2d_exact(blv)) - (cp - sum);
         r = d2f_rn(rd);
         sq = fma(rd, rd, sq);
         n += 1;
@@ -834,15 +838,18 @@ __global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny
 // memory once. The residual norm sums r32^2: each square is an exact pair
 // (the product and its FMA error), accumulated per thread as a double-float
 // and widened to double once per thread for the block reduction.
+// At 64 registers 8 blocks fit an SM, so a 1024^2 grid's 1120 blocks run
+// in one wave (at 72 registers, 7 per SM, the last 56 blocks made a second).
 constexpr int DF_ROWS = 8;
 constexpr int DF_WARPS = 4;
 
 template <bool UPDATE>
-__global__ void __launch_bounds__(32 * DF_WARPS) k_update_resid_df(int nx, int ny, float2* __restrict__ p2a,
+__global__ void __launch_bounds__(32 * DF_WARPS, 8) k_update_resid_df(int nx, int ny, float2* __restrict__ p2a,
                                                                    float2* __restrict__ p2b,
                                                                    const SolveCtl* __restrict__ ctl,
                                                                    const float* __restrict__ e,
                                                                    const float* __restrict__ b,
+                                                                   const float* __restrict__ b_lo,
                                                                    const uint8_t* __restrict__ code,
                                                                    float* __restrict__ r32, StepAccum* acc) {
   __shared__ double red[32];
@@ -860,7 +867,7 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_update_resid_df(int nx, int n
   // the codes; zero / outside where the grid ends
   float2 P[DF_ROWS + 2];
   float E[DF_ROWS + 2];
-  float B[DF_ROWS];
+  float B[DF_ROWS], BL[DF_ROWS];
   uint8_t C[DF_ROWS];
 #pragma unroll
   for (int r = 0; r < DF_ROWS + 2; r++) {
@@ -877,10 +884,12 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_update_resid_df(int nx, int n
   for (int r = 0; r < DF_ROWS; r++) {
     const int y = y0 + r;
     B[r] = 0.0f;
+    BL[r] = 0.0f;
     C[r] = (uint8_t)CODE_OUTSIDE;
     if (own && y < ny) {
       const long k = gx + (long)y * nx;
       B[r] = b[k];
+      BL[r] = b_lo[k];
       C[r] = code[k];
     }
   }
@@ -922,8 +931,9 @@ __global__ void __launch_bounds__(32 * DF_WARPS) k_update_resid_df(int nx, int n
         }
         if (c & LINK_YM) sum = first ? pm : df_add(sum, pm);
         const float2 d = df_add(df_mul_count(pc, cnt), df_neg(sum));
+        // (b + b_lo) - d: b_lo (the rhs's rounding error) joins the low parts
         const float2 s = df_two_sum(B[t], -d.x);
-        r = __fadd_rn(s.x, __fsub_rn(s.y, d.y));
+        r = __fadd_rn(s.x, __fadd_rn(s.y, __fsub_rn(BL[t], d.y)));
         const float q = __fmul_rn(r, r);
         acc2 = df_add(acc2, make_float2(q, __fmaf_rn(r, r, -q)));
         n += 1;
@@ -1129,23 +1139,23 @@ void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* 
 }
 
 void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, const SolveCtl* ctl,
-                           const float* e, const float* b, const uint8_t* code, bool update, float* r32,
-                           StepAccum* acc, bool df) {
+                           const float* e, const float* b, const float* b_lo, const uint8_t* code, bool update,
+                           float* r32, StepAccum* acc, bool df) {
   if (df) {
     float2* a = reinterpret_cast<float2*>(p64a);
     float2* bb = reinterpret_cast<float2*>(p64b);
     dim3 g((nx + 29) / 30, (ny + DF_WARPS * DF_ROWS - 1) / (DF_WARPS * DF_ROWS));
     if (update)
-      k_update_resid_df<true><<<g, 32 * DF_WARPS, 0, s>>>(nx, ny, a, bb, ctl, e, b, code, r32, acc);
+      k_update_resid_df<true><<<g, 32 * DF_WARPS, 0, s>>>(nx, ny, a, bb, ctl, e, b, b_lo, code, r32, acc);
     else
-      k_update_resid_df<false><<<g, 32 * DF_WARPS, 0, s>>>(nx, ny, a, bb, ctl, e, b, code, r32, acc);
+      k_update_resid_df<false><<<g, 32 * DF_WARPS, 0, s>>>(nx, ny, a, bb, ctl, e, b, b_lo, code, r32, acc);
     return;
   }
   dim3 g((nx + 29) / 30, (ny + UR_WARPS * UR_ROWS - 1) / (UR_WARPS * UR_ROWS));
   if (update)
-    k_update_resid64<true><<<g, 32 * UR_WARPS, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, code, r32, acc);
+    k_update_resid64<true><<<g, 32 * UR_WARPS, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, b_lo, code, r32, acc);
   else
-    k_update_resid64<false><<<g, 32 * UR_WARPS, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, code, r32, acc);
+    k_update_resid64<false><<<g, 32 * UR_WARPS, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, b_lo, code, r32, acc);
 }
 
 void launch_solve_begin(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h) {

@@ -142,7 +142,8 @@ __global__ void __launch_bounds__(256) k_forces(int nx, int ny, float h, int dnx
 __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, const float* __restrict__ u,
                                                     const float* __restrict__ v, float* __restrict__ out, int as_rhs,
                                                     const uint8_t* __restrict__ label,
-                                                    const StepScalars* __restrict__ sc, StepAccum* acc) {
+                                                    const StepScalars* __restrict__ sc, StepAccum* acc,
+                                                    float* __restrict__ out_lo) {
   __shared__ double red[32];
   __shared__ unsigned long long redn[32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -158,6 +159,9 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
                             v[i + (long)j * nx]);
     const float o = as_rhs ? ns * d : d;
     out[k] = o;
+    // the rounding error of b = (-scale) * div, exactly (an FMA of the
+    // product against its rounded value): b + b_lo is the exact product
+    if (out_lo) out_lo[k] = as_rhs ? __fmaf_rn(ns, d, -o) : 0.0f;
     if (label != nullptr && label[k] == FLUID) {
       // the square as an exact pair (product + FMA error) added to a
       // double-float sum: float32 work per cell, one widening per thread
@@ -325,7 +329,7 @@ __global__ void __launch_bounds__(256) k_max_speed(long nu, long nv, const float
 // pressure.ts:177-186), for solves handed a divergence field.
 __global__ void __launch_bounds__(256) k_scale_rhs(long n, const float* __restrict__ div, float* __restrict__ b,
                                                    float neg_scale, const uint8_t* __restrict__ label,
-                                                   StepAccum* acc) {
+                                                   StepAccum* acc, float* __restrict__ b_lo) {
   __shared__ double red[32];
   __shared__ unsigned long long redn[32];
   float2 sq = make_float2(0.0f, 0.0f);
@@ -333,6 +337,7 @@ __global__ void __launch_bounds__(256) k_scale_rhs(long n, const float* __restri
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
     const float o = b ? neg_scale * div[k] : div[k];
     if (b) b[k] = o;
+    if (b && b_lo) b_lo[k] = __fmaf_rn(neg_scale, div[k], -o);
     if (label[k] == FLUID) {
       const float q = __fmul_rn(o, o);
       sq = df_add(sq, make_float2(q, __fmaf_rn(o, o, -q)));
@@ -472,11 +477,11 @@ void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, fl
 }
 
 void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
-                       bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc) {
+                       bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc, float* out_lo) {
   dim3 b(32, 8);
   dim3 g = grid2(nx, ny, b);
   g.y = std::min(g.y, std::max(1u, 1024u / g.x));
-  k_divergence<<<g, b, 0, s>>>(nx, ny, h, u, v, out, as_rhs, label, sc, acc);
+  k_divergence<<<g, b, 0, s>>>(nx, ny, h, u, v, out, as_rhs, label, sc, acc, out_lo);
 }
 
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
@@ -488,11 +493,11 @@ void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, flo
 }
 
 void launch_scale_rhs(cudaStream_t s, long n, const float* div, float* b, float neg_scale, const uint8_t* label,
-                      StepAccum* acc) {
+                      StepAccum* acc, float* b_lo) {
   long blocks = (n + 255) / 256;
   if (blocks > 152 * 8) blocks = 152 * 8;
   if (blocks < 1) blocks = 1;
-  k_scale_rhs<<<(unsigned)blocks, 256, 0, s>>>(n, div, b, neg_scale, label, acc);
+  k_scale_rhs<<<(unsigned)blocks, 256, 0, s>>>(n, div, b, neg_scale, label, acc, b_lo);
 }
 
 void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const float* v, StepAccum* acc,

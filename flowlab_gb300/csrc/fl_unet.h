@@ -93,6 +93,8 @@ void unet_tc_form(int form);
 bool unet_tc_enabled();
 // Nonzero (and cleared) when a tensor-core launch gave up a bounded wait.
 int unet_tc_take_error();
+// The tensor-core kernels' progress-wait bound in polls (<= 0: default).
+int unet_tc_set_wait_limit(long long polls);
 
 // Warm start inside the engine's step: input from (b, labels, p_prev), the
 // forward pass, p = p_prev + s_p * out on fluid cells. p_prev is float

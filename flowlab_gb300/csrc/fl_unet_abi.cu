@@ -194,6 +194,11 @@ int fl_unet_train_step(fl_unet* h, int B, int H, int W, const float* x, const fl
   return FL_OK;
 }
 
+int fl_unet_set_wait_limit(long long polls) {
+  if (unet_tc_set_wait_limit(polls) != 0) return ufail(nullptr, FL_EDEVICE, "setting the wait limit failed");
+  return FL_OK;
+}
+
 int fl_unet_use_tensor_cores(int mode) {
   if (mode < 0 || mode > 2) return ufail(nullptr, FL_EINVAL, "tensor-core mode %d", mode);
   unet_tc_enable(mode != 0);

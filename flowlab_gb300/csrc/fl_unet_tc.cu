@@ -16,7 +16,13 @@
 //
 // Every wait is bounded: on timeout the kernel records the failure in a
 // device word (read by unet_tc_take_error), stops issuing, waits (bounded)
-// for what it issued, frees its TMEM and returns.
+// for what it issued, frees its TMEM and returns. Two bounds: the waits that
+// gate progress (a ring slot freed, a tile's data landed, an accumulator
+// ready) give up after g_tc_wait_limit polls, a runtime value
+// (fl_unet_set_wait_limit); the waits that drain what the CTA itself issued
+// (its last copies, its MMAs' final commit) always allow WAIT_LIMIT polls,
+// so that however early the progress waits give up, no copy or MMA is in
+// flight when the TMEM is freed and the CTA ends.
 #include <cstdint>
 
 #include <cuda.h>  // CUtensorMap and its enums; the encoder is fetched through the runtime
@@ -45,6 +51,7 @@ constexpr int SMEM_BYTES = SMEM_TILES + SLACK + 64;
 constexpr long WAIT_LIMIT = 1L << 22;
 
 __device__ int g_tc_error = 0;
+__device__ long long g_tc_wait_limit = WAIT_LIMIT;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -86,11 +93,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Bounded wait; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (long k = 0; k < WAIT_LIMIT; k++)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit) {
+  for (long long k = 0; k < limit; k++)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+// The drain bound (see the top of this file).
+__device__ __forceinline__ bool mbar_drain(uint32_t bar, uint32_t parity) { return mbar_wait(bar, parity, WAIT_LIMIT); }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -180,6 +189,7 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
   const uint32_t lbo_a = (TM / 8) * 128, lbo_b = (uint32_t)(N / 8) * 128;
   bool failed = false;
   int issued = 0;  // chunks committed
+  const long long lim = g_tc_wait_limit;
 
   // chunk loads go through registers one chunk ahead: the global (L2)
   // latency of chunk it+1 overlaps the barrier and MMA issue of chunk it
@@ -207,7 +217,7 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
     unsigned char* B = tiles + 2 * STAGE_A + buf * STAGE_B_MAX;
     if (it >= 2) {
       // the MMAs of chunk it-2 read this buffer
-      if (!mbar_wait(smem_u32(&bars[buf]), (uint32_t)(((it - 2) >> 1) & 1))) failed = true;
+      if (!mbar_wait(smem_u32(&bars[buf]), (uint32_t)(((it - 2) >> 1) & 1), lim)) failed = true;
     }
     if (__syncthreads_or(failed)) {
       failed = true;
@@ -242,7 +252,7 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const __nv_bfloat16* __restric
   // also on failure, so that nothing is in flight when TMEM is freed
   if (issued > 0) {
     const int last = issued - 1;
-    if (!mbar_wait(smem_u32(&bars[last & 1]), (uint32_t)((last >> 1) & 1))) failed = true;
+    if (!mbar_drain(smem_u32(&bars[last & 1]), (uint32_t)((last >> 1) & 1))) failed = true;
   }
   failed = __syncthreads_or(failed) != 0;
   tc_fence_after();
@@ -387,6 +397,7 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3_halo_ws(const __grid_const
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   bool failed = false;
+  const long long lim = g_tc_wait_limit;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -396,7 +407,7 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3_halo_ws(const __grid_const
         const int bx = t % tiles_x, by = (t / tiles_x) % tiles_y, img = t / (tiles_x * tiles_y);
         for (int c = 0; c < nchunks; c++, q++) {
           const int s = q & 1, use = q >> 1;
-          if (use > 0 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((use - 1) & 1))) {
+          if (use > 0 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((use - 1) & 1), lim)) {
             failed = true;
             break;
           }
@@ -413,7 +424,7 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3_halo_ws(const __grid_const
       // arming of each stage (chunks q-1 and q-2) has completed
       for (int k = 1; k <= 2 && k <= q; k++) {
         const int qq = q - k;
-        if (!mbar_wait(smem_u32(&full[qq & 1]), (uint32_t)((qq >> 1) & 1))) failed = true;
+        if (!mbar_drain(smem_u32(&full[qq & 1]), (uint32_t)((qq >> 1) & 1))) failed = true;
       }
     }
   } else if (warp == 1) {
@@ -424,7 +435,7 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3_halo_ws(const __grid_const
       int q = 0, i = 0;
       for (int t = blockIdx.x; t < ntiles && !failed; t += gridDim.x, i++) {
         const int a = i & 1, ause = i >> 1;
-        if (ause > 0 && !mbar_wait(smem_u32(&acce[a]), (uint32_t)((ause - 1) & 1))) {
+        if (ause > 0 && !mbar_wait(smem_u32(&acce[a]), (uint32_t)((ause - 1) & 1), lim)) {
           failed = true;
           break;
         }
@@ -432,7 +443,7 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3_halo_ws(const __grid_const
         const uint32_t dacc = tmem + (uint32_t)(a * acc_cols);
         for (int c = 0; c < nchunks; c++, q++) {
           const int s = q & 1, use = q >> 1;
-          if (!mbar_wait(smem_u32(&full[s]), (uint32_t)(use & 1))) {
+          if (!mbar_wait(smem_u32(&full[s]), (uint32_t)(use & 1), lim)) {
             failed = true;
             break;
           }
@@ -502,7 +513,7 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3_halo_ws(const __grid_const
     int i = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
       const int a = i & 1, ause = i >> 1;
-      if (!mbar_wait(smem_u32(&accf[a]), (uint32_t)(ause & 1))) {
+      if (!mbar_wait(smem_u32(&accf[a]), (uint32_t)(ause & 1), lim)) {
         failed = true;
         break;
       }
@@ -564,7 +575,7 @@ __global__ void __launch_bounds__(WS_THREADS) k_conv3_halo_ws(const __grid_const
     }
   }
   __syncwarp();
-  if (!mbar_wait(smem_u32(done), 0u)) failed = true;
+  if (!mbar_drain(smem_u32(done), 0u)) failed = true;
   failed = __syncthreads_or(failed) != 0;
   if (failed && tid == 0) atomicExch(&g_tc_error, 1);
   tc_fence_before();
@@ -679,6 +690,7 @@ __global__ void __launch_bounds__(WG_THREADS) k_conv3_wgrad_tc(const __grid_cons
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   bool failed = false;
+  const long long lim = g_tc_wait_limit;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -688,7 +700,7 @@ __global__ void __launch_bounds__(WG_THREADS) k_conv3_wgrad_tc(const __grid_cons
         const long t = t0 + q;
         const int bx = (int)(t % tiles_x), y = (int)((t / tiles_x) % H), img = (int)(t / ((long)tiles_x * H));
         const int s = q & 1, use = q >> 1;
-        if (use > 0 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((use - 1) & 1))) {
+        if (use > 0 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((use - 1) & 1), lim)) {
           failed = true;
           break;
         }
@@ -702,7 +714,7 @@ __global__ void __launch_bounds__(WG_THREADS) k_conv3_wgrad_tc(const __grid_cons
       }
       for (int k = 1; k <= 2 && k <= q; k++) {
         const int qq = q - k;
-        if (!mbar_wait(smem_u32(&full[qq & 1]), (uint32_t)((qq >> 1) & 1))) failed = true;
+        if (!mbar_drain(smem_u32(&full[qq & 1]), (uint32_t)((qq >> 1) & 1))) failed = true;
       }
     }
   } else if (warp == 1) {
@@ -711,7 +723,7 @@ __global__ void __launch_bounds__(WG_THREADS) k_conv3_wgrad_tc(const __grid_cons
       const uint32_t idesc = instr_desc(WG_CB, WG_NB) | (1u << 15) | (1u << 16);
       for (int q = 0; q < mytiles; q++) {
         const int s = q & 1, use = q >> 1;
-        if (!mbar_wait(smem_u32(&full[s]), (uint32_t)(use & 1))) {
+        if (!mbar_wait(smem_u32(&full[s]), (uint32_t)(use & 1), lim)) {
           failed = true;
           break;
         }
@@ -733,7 +745,7 @@ __global__ void __launch_bounds__(WG_THREADS) k_conv3_wgrad_tc(const __grid_cons
     }
   }
   __syncwarp();
-  if (!mbar_wait(smem_u32(done), 0u)) failed = true;
+  if (!mbar_drain(smem_u32(done), 0u)) failed = true;
   failed = __syncthreads_or(failed) != 0;
   tc_fence_after();
   if (failed) {
@@ -900,6 +912,13 @@ bool unet_tc_conv_wgrad(cudaStream_t s, const __nv_bfloat16* x, const __nv_bfloa
   dim3 grid((unsigned)ctas, (unsigned)nblk, (unsigned)cblk);
   k_conv3_wgrad_tc<<<grid, WG_THREADS, WG_SMEM, s>>>(xmap, gmap, H, W, B, Cin, (int)per, dw);
   return true;
+}
+
+// Polls a progress wait allows before it gives up (<= 0: the default,
+// WAIT_LIMIT); on the current device.
+int unet_tc_set_wait_limit(long long polls) {
+  const long long v = polls > 0 ? polls : WAIT_LIMIT;
+  return cudaMemcpyToSymbol(g_tc_wait_limit, &v, sizeof v) == cudaSuccess ? 0 : -1;
 }
 
 int unet_tc_take_error() {

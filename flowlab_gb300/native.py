@@ -144,6 +144,7 @@ SIGNATURES = [
     ("fl_unet_forward", _I, [_P, _I, _I, _I, _P, _P]),
     ("fl_unet_train_step", _I, [_P, _I, _I, _I, _P, _P, _P, _D, _I, _P, _P]),
     ("fl_unet_use_tensor_cores", _I, [_I]),
+    ("fl_unet_set_wait_limit", _I, [ctypes.c_longlong]),
     ("fl_set_warm_start", _I, [_P, _P]),
     ("fl_read_rhs", _I, [_P, _I, _P]),
     ("fl_batch_create", _I, [_P, _I, ctypes.POINTER(_P)]),

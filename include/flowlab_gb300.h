@@ -262,18 +262,20 @@ int fl_dye_patch(fl_engine* e, float* dye, int i0, int j0, int pnx, int pny, con
  * Velocity advection (semi-Lagrangian or MacCormack, as fl_advect_velocity)
  * on the caller's own DEVICE buffers, allocating nothing. This entry point has
  * no counterpart in the reference. It is for callers that cannot call
- * cudaMalloc where they advect: code recorded into a CUDA graph by stream
- * capture, real-time or callback threads that must not block in an
- * allocator, and hosts whose device memory comes from an arena they do not
- * own. The MacCormack scratch lives in one fixed array of the library's
- * device memory (about 8.8 MB on every GPU that loads the library, held until
- * exit), so the grid may have at most 2,200,000 faces, (nx+1)*ny + nx*(ny+1)
- * (1024x1024 fits); larger grids return FL_EINVAL. The first call on each
- * device looks the array up and loads the kernels, so make it before any
- * stream capture. Calls on one device share the array: calls whose work
- * overlaps on the GPU race, so order them on one stream. Work is queued on
- * `stream` (a cudaStream_t, NULL for the default stream) and not waited for.
- * Errors are reported by fl_last_error(NULL).
+ * cudaMalloc where they advect: real-time threads that must not block
+ * (cudaMalloc can synchronise the device), hosts whose device memory all
+ * comes from an arena or caching allocator they do not own, and processes
+ * that reserve their whole device-memory budget up front. The MacCormack
+ * scratch lives in one fixed array of the library's device memory (about
+ * 8.8 MB on every GPU that loads the library, held until exit), so the grid
+ * may have at most 2,200,000 faces, (nx+1)*ny + nx*(ny+1) (1024x1024 fits);
+ * larger grids return FL_EINVAL. The outputs must not overlap each other or
+ * the inputs (FL_EINVAL). The first call on each device looks the array up
+ * and loads the kernels, so make it before any stream capture; calls after
+ * cudaDeviceReset are not supported. Calls on one device share the array:
+ * calls whose work overlaps on the GPU race, so order them on one stream.
+ * Work is queued on `stream` (a cudaStream_t, NULL for the default stream)
+ * and not waited for. Errors are reported by fl_last_error(NULL).
  */
 int fl_advect_velocity_noalloc(int scheme, int nx, int ny, float h, float dt, const float* u_in, const float* v_in,
                                float* u_out, float* v_out, const uint8_t* label, void* stream);
@@ -320,6 +322,15 @@ int fl_unet_train_step(fl_unet* u, int batch, int h, int w, const float* x, cons
  * cores for the forward pass only, each tap's input gathered per 32-channel
  * chunk (backward on CUDA cores). */
 int fl_unet_use_tensor_cores(int mode);
+/* The tensor-core kernels wait on their own copies and MMAs with bounded
+ * mbarrier polls. A wait that gates progress gives up after `polls` polls
+ * (<= 0 restores the default, about 4 million) and the call then returns
+ * FL_ETIMEOUT; the waits that drain a CTA's own in-flight copies and MMAs
+ * before it frees its tensor memory keep the default bound. For tests of
+ * the timeout path (a limit of 1 makes the waits run out) and for callers
+ * that need a call to fail fast. Applies to the current device. No
+ * counterpart in the reference. */
+int fl_unet_set_wait_limit(long long polls);
 /* Attaches (or, with NULL, detaches) the network as the engine's warm start:
  * every multigrid step then runs it between the divergence and the solve.
  * The grid's sides must be multiples of 8 and fit the network's capacity;

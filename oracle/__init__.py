@@ -351,6 +351,18 @@ class OracleSimulation:
     def step(self):
         return self.o._f("sim_step")(self.handle)
 
+    def get_div(self):
+        """The last step's divergence (the pressure solve's input)."""
+        d = np.zeros(self.nx * self.ny, self.o.dtype)
+        self.o._f("sim_get_div")(self.handle, _p(d))
+        return d
+
+    def scale(self):
+        """The last step's scale rho*h^2/dt."""
+        f = self.o._f("sim_scale")
+        f.restype = ctypes.c_double
+        return f(self.handle)
+
     def info(self):
         dt, t, rr = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         self.o._f("sim_info")(self.handle, ctypes.byref(dt), ctypes.byref(t), ctypes.byref(rr))

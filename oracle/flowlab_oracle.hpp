@@ -657,13 +657,19 @@ struct Multigrid {
 
 // NEW — float64 defect correction (iterative refinement) around the float32
 // multigrid: the pressure is kept in double; each outer pass
-// forms the residual r = b - A p in double (b = float32 rhs, neighbour sum
-// in the order +x, -x, +y, -y), runs ONE float32 V-cycle on A e = float(r)
-// from e = 0, and adds e back in double. The relative residual is
-// rms(r over fluid cells with links) / rms(b over fluid cells), tested
-// before each pass, so an already converged warm start costs no cycle.
+// forms the residual r = b - A p in double (neighbour sum in the order +x,
+// -x, +y, -y), runs ONE float32 V-cycle on A e = float(r) from e = 0, and
+// adds e back in double. The rhs of the residual is the unrounded product
+// -scale * div: the float b plus its rounding error bLo = fma(-scale, div,
+// -b) (exact), so the tolerance is met by the reference's own quantity
+// (rmsRemainingDivergence / fluidDivRms, pressure.ts:102-186) and not only
+// by the rounded rhs, whose rounding alone leaves ~3e-8 of it. The relative
+// residual is rms(r over fluid cells with links) / rms(b over fluid cells),
+// tested before each pass, so an already converged warm start costs no
+// cycle.
 template <class T>
-double residual64(const Grid<T>& g, const double* p, const T* b, const uint8_t* label, T* r32, double& bSq, long& nb) {
+double residual64(const Grid<T>& g, const double* p, const T* b, const T* bLo, const uint8_t* label, T* r32,
+                  double& bSq, long& nb) {
   double sumSq = 0;
   long n = 0;
   bSq = 0;
@@ -681,7 +687,8 @@ double residual64(const Grid<T>& g, const double* p, const T* b, const uint8_t* 
       if (!solidOrOutside(g, label, i, j + 1)) { count += 1.0; sum += p[k + g.nx]; }
       if (!solidOrOutside(g, label, i, j - 1)) { count += 1.0; sum += p[k - g.nx]; }
       if (count == 0) continue;
-      double r = (double)b[k] - (count * p[k] - sum);
+      // b + bLo: the rhs with its rounding error restored (exact in double)
+      double r = ((double)b[k] + (double)bLo[k]) - (count * p[k] - sum);
       r32[k] = (T)r;
       sumSq += r * r;
       n += 1;
@@ -694,11 +701,12 @@ int solveMixed(Multigrid<T>& mg, const Grid<T>& g, double* p, const T* div, cons
                int cycles, double tol, double* relRes) {
   const long n = (long)g.nx * g.ny;
   mg.prepare(g, div, label, scale);  // labels + levels[0].b = -scale*div
-  std::vector<T> b(mg.levels[0].b);
+  std::vector<T> b(mg.levels[0].b), bLo(n);
+  for (long k = 0; k < n; k++) bLo[k] = std::fma(-scale, div[k], -b[k]);
   std::vector<T> e(n);
   double bSq;
   long nb;
-  double rr = residual64(g, p, b.data(), label, mg.levels[0].b.data(), bSq, nb);
+  double rr = residual64(g, p, b.data(), bLo.data(), label, mg.levels[0].b.data(), bSq, nb);
   const double bRms = nb > 0 ? std::sqrt(bSq / (double)nb) : 0.0;
   if (relRes) *relRes = -1;
   if (bRms == 0) {
@@ -713,7 +721,7 @@ int solveMixed(Multigrid<T>& mg, const Grid<T>& g, double* p, const T* div, cons
     std::fill(e.begin(), e.end(), T(0));
     mg.vcycle(0, e.data());  // levels[0].b holds float(r)
     for (long k = 0; k < n; k++) p[k] += (double)e[k];
-    rr = residual64(g, p, b.data(), label, mg.levels[0].b.data(), bSq, nb);
+    rr = residual64(g, p, b.data(), bLo.data(), label, mg.levels[0].b.data(), bSq, nb);
     rel = rr / bRms;
     if (relRes) *relRes = rel;
     c++;
@@ -793,13 +801,14 @@ inline void put(float* p, long k, F2 x) {
 }
 }  // namespace df
 
-// r = b - (count*p - sum) in double-float arithmetic, the neighbour sum in
+// r = (b + bLo) - (count*p - sum) in double-float arithmetic (bLo: the
+// rhs's rounding error, as in solveMixed), the neighbour sum in
 // the order +x, -x, +y, -y starting from the first linked neighbour; r32 is
 // the result rounded to float (0 off-fluid and on cells without links). The
 // norm is the sum of r32^2 (squares exact in double) over fluid cells with
 // links; bSq/nb are the rhs sums over fluid cells, as residual64.
-inline double residualDF(const Grid<float>& g, const float* p, const float* b, const uint8_t* label, float* r32,
-                         double& bSq, long& nb) {
+inline double residualDF(const Grid<float>& g, const float* p, const float* b, const float* bLo,
+                         const uint8_t* label, float* r32, double& bSq, long& nb) {
   double sumSq = 0;
   long n = 0;
   bSq = 0;
@@ -824,7 +833,7 @@ inline double residualDF(const Grid<float>& g, const float* p, const float* b, c
       if (count == 0) continue;
       const df::F2 d = df::add(df::mulCount(df::at(p, k), count), df::neg(sum));
       const df::F2 s = df::twoSum(b[k], -d.hi);
-      const float e = s.lo - d.lo;
+      const float e = s.lo + (bLo[k] - d.lo);
       const float r = s.hi + e;
       r32[k] = r;
       sumSq += (double)r * (double)r;
@@ -840,11 +849,12 @@ inline int solveMixedDF(Multigrid<float>& mg, const Grid<float>& g, float* p, co
                         float scale, int cycles, double tol, double* relRes) {
   const long n = (long)g.nx * g.ny;
   mg.prepare(g, div, label, scale);
-  std::vector<float> b(mg.levels[0].b);
+  std::vector<float> b(mg.levels[0].b), bLo(n);
+  for (long k = 0; k < n; k++) bLo[k] = std::fma(-scale, div[k], -b[k]);
   std::vector<float> e(n);
   double bSq;
   long nb;
-  double rr = residualDF(g, p, b.data(), label, mg.levels[0].b.data(), bSq, nb);
+  double rr = residualDF(g, p, b.data(), bLo.data(), label, mg.levels[0].b.data(), bSq, nb);
   const double bRms = nb > 0 ? std::sqrt(bSq / (double)nb) : 0.0;
   if (relRes) *relRes = -1;
   if (bRms == 0) {
@@ -859,7 +869,7 @@ inline int solveMixedDF(Multigrid<float>& mg, const Grid<float>& g, float* p, co
     std::fill(e.begin(), e.end(), 0.0f);
     mg.vcycle(0, e.data());
     for (long k = 0; k < n; k++) df::put(p, k, df::addF(df::at(p, k), e[k]));
-    rr = residualDF(g, p, b.data(), label, mg.levels[0].b.data(), bSq, nb);
+    rr = residualDF(g, p, b.data(), bLo.data(), label, mg.levels[0].b.data(), bSq, nb);
     rel = rr / bRms;
     if (relRes) *relRes = rel;
     c++;

@@ -231,6 +231,16 @@ static StepParams toParams(const orc_params* c) {
     for (int k = 0; k < 5; k++) s->stir[k] = st ? (T)st[k] : T(0);                                      \
   }                                                                                                     \
   int orc_sim_step_##SUF(void* sp) { return ((Simulation<T>*)sp)->step(); }                             \
+  /* the last step's divergence (the pressure solve's input) */                                         \
+  void orc_sim_get_div_##SUF(void* sp, T* div) {                                                        \
+    Simulation<T>* s = (Simulation<T>*)sp;                                                              \
+    std::copy(s->div.begin(), s->div.end(), div);                                                       \
+  }                                                                                                     \
+  /* the last step's scale rho*h^2/dt */                                                                \
+  double orc_sim_scale_##SUF(void* sp) {                                                                \
+    Simulation<T>* s = (Simulation<T>*)sp;                                                              \
+    return (double)((T(s->prm.rho) * s->g.h * s->g.h) / s->dt);                                         \
+  }                                                                                                     \
   void orc_sim_info_##SUF(void* sp, double* dt, double* time, double* relRes) {                         \
     Simulation<T>* s = (Simulation<T>*)sp;                                                              \
     *dt = (double)s->dt;                                                                                \
@@ -261,7 +271,8 @@ extern "C" double orc_residual_df_f32(int nx, int ny, const float* p, const floa
                                       float* r32) {
   double bSq;
   long nb;
-  const double rr = residualDF(Grid<float>{nx, ny, 1.0f}, p, b, label, r32, bSq, nb);
+  std::vector<float> bLo((size_t)nx * ny, 0.0f);
+  const double rr = residualDF(Grid<float>{nx, ny, 1.0f}, p, b, bLo.data(), label, r32, bSq, nb);
   const double bRms = nb > 0 ? std::sqrt(bSq / (double)nb) : 0.0;
   return bRms > 0 ? rr / bRms : 0.0;
 }

@@ -10,6 +10,7 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a engine)")
+    config.addinivalue_line("markers", "slow: minutes of oracle time (still part of the -m gpu run)")
 
 
 @pytest.fixture(scope="session")
