@@ -2,14 +2,15 @@
 // allocation by the library.
 //
 // Who needs this: callers that cannot call cudaMalloc at the point where they
-// advect — code being recorded into a CUDA graph by stream capture (an
-// allocation cannot be captured), real-time or callback threads that must not
-// block in the allocator, and hosts whose device memory all comes from an
-// arena that something else owns. They already hold device buffers for the
-// fields they pass in and get back; what the MacCormack scheme needs beyond
-// those is a scratch copy of the forward-advected faces (advect.ts:161 uHat /
-// vHat) and the step's scalars. Here that scratch is one fixed array in the
-// library's own device memory, sized for grids up to NOALLOC_MAX_FACES faces.
+// advect — real-time threads that must not block (cudaMalloc can synchronise
+// the device and wait on other work), hosts whose device memory all comes
+// from an arena or caching allocator that something else owns, and processes
+// that reserve their whole device-memory budget up front and may not grow
+// it. They already hold device buffers for the fields they pass in and get
+// back; what the MacCormack scheme needs beyond those is a scratch copy of
+// the forward-advected faces (advect.ts:161 uHat / vHat) and the step's
+// scalars. Here that scratch is one fixed array in the library's own device
+// memory, sized for grids up to NOALLOC_MAX_FACES faces.
 //
 // The array is a file-scope __device__ variable: every GPU that loads the
 // library holds it (about 8.8 MB) until the process exits. In host code its
@@ -21,7 +22,9 @@
 // (for example on two streams) race on it, so order them on one stream.
 // Nothing in the scratch has to start at zero: the forward pass writes every
 // face of it before the correction reads any, and the scalars are rewritten
-// by every call.
+// by every call. The looked-up address belongs to the device's current
+// context: after cudaDeviceReset the library may be loaded at another
+// address, so calls after a reset are not supported.
 #include <mutex>
 
 #include "fl_internal.h"
@@ -108,6 +111,23 @@ extern "C" int fl_advect_velocity_noalloc(int scheme, int nx, int ny, float h, f
   if (!u_in || !v_in || !u_out || !v_out || !label || !(h > 0)) {
     set_global_error("null device pointer or non-positive cell size");
     return FL_EINVAL;
+  }
+  // The advection reads its inputs' neighbours while it writes the outputs:
+  // an output that overlaps an input (an in-place call) would read faces
+  // already overwritten. Reject it rather than return wrong velocities.
+  {
+    const uintptr_t nu = (uintptr_t)(nx + 1) * ny * sizeof(float), nv = (uintptr_t)nx * (ny + 1) * sizeof(float);
+    const uintptr_t nl = (uintptr_t)nx * ny;
+    auto overlap = [](const void* a, uintptr_t na, const void* b, uintptr_t nb) {
+      const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b;
+      return x < y + nb && y < x + na;
+    };
+    if (overlap(u_out, nu, u_in, nu) || overlap(u_out, nu, v_in, nv) || overlap(u_out, nu, label, nl) ||
+        overlap(v_out, nv, u_in, nu) || overlap(v_out, nv, v_in, nv) || overlap(v_out, nv, label, nl) ||
+        overlap(u_out, nu, v_out, nv)) {
+      set_global_error("the output velocity buffers must not overlap each other or the inputs");
+      return FL_EINVAL;
+    }
   }
   float* scratch = nullptr;
   int st = noalloc_setup(&scratch);

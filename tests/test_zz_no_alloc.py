@@ -2,14 +2,16 @@
 allocating per-pass entry point (fl_advect_velocity), through the C ABI.
 
 fl_advect_velocity_noalloc serves callers that cannot allocate device memory
-where they advect (stream capture, allocator-free real-time threads, memory
-from someone else's arena): it takes their device buffers and keeps its
-MacCormack scratch in a fixed array of the library's own device memory. The
-test holds its device buffers in torch tensors (the test may allocate; the
-entry point must not), runs two calls in a row on different inputs, and
-requires the same output as the existing entry point — bit for bit, the
-tolerance every other advection test here uses. This file is named to run
-last, so a failure here cannot hide another test's result.
+where they advect (real-time threads that must not block in cudaMalloc,
+memory owned by someone else's arena, a device-memory budget fixed up front):
+it takes their device buffers and keeps its MacCormack scratch in a fixed
+array of the library's own device memory. The test holds its device buffers
+in torch tensors (the test may allocate; the entry point must not), runs two
+calls in a row on different inputs, and requires the same output as the
+existing entry point — bit for bit, the tolerance every other advection test
+here uses — and the device's free memory unchanged across a call made after
+the first. This file is named to run last, so a failure here cannot hide
+another test's result.
 """
 import ctypes
 
@@ -42,11 +44,13 @@ def noalloc_advect(lib, torch, nx, ny, h, scheme, u, v, label, dt, stream):
     uo = torch.full_like(du, float("nan"))
     vo = torch.full_like(dv, float("nan"))
     torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(dev)[0]
     st = lib.fl_advect_velocity_noalloc(scheme, nx, ny, float(h), float(np.float32(dt)), du.data_ptr(), dv.data_ptr(),
                                         uo.data_ptr(), vo.data_ptr(), dl.data_ptr(), ctypes.c_void_p(stream))
     assert st == native.FL_OK, lib.fl_last_error(None).decode()
     torch.cuda.synchronize()
-    return uo.cpu().numpy(), vo.cpu().numpy()
+    free1 = torch.cuda.mem_get_info(dev)[0]
+    return uo.cpu().numpy(), vo.cpu().numpy(), free0, free1
 
 
 @pytest.mark.parametrize("scheme", [native.FL_SEMI_LAGRANGIAN, native.FL_MACCORMACK])
@@ -61,12 +65,29 @@ def test_noalloc_matches_allocating_entry_point_twice(scheme):
     h2, dt2, u2, v2, label2, _, _, _, _ = fx.advect_fixture(1, nx, ny)
     label2 = fx.scaled_block_labels(nx, ny)
     cases.append((nx, ny, h2, -0.7 * u2, 1.3 * v2, label2, 0.8 * dt2))
-    for nx, ny, h, u, v, label, dt in cases:  # two calls in a row, different inputs and sizes
+    for k, (nx, ny, h, u, v, label, dt) in enumerate(cases):  # two calls in a row, different inputs and sizes
         eu, ev = engine_advect(nx, ny, h, scheme, u, v, label, dt)
-        gu, gv = noalloc_advect(lib, torch, nx, ny, h, scheme, u, v, label, dt, stream)
+        gu, gv, free0, free1 = noalloc_advect(lib, torch, nx, ny, h, scheme, u, v, label, dt, stream)
+        if k > 0:
+            # the set-up (address look-up, kernel loading) is done: no device memory taken
+            assert free1 == free0, "device free memory changed by %d bytes" % (free0 - free1)
         assert np.isfinite(gu).all() and np.isfinite(gv).all()
         assert np.array_equal(eu, gu), "u differs in %d faces" % int((eu != gu).sum())
         assert np.array_equal(ev, gv), "v differs in %d faces" % int((ev != gv).sum())
+
+
+def test_noalloc_rejects_overlapping_outputs():
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    nx, ny = 40, 32
+    u = torch.zeros((nx + 1) * ny, device="cuda")
+    v = torch.zeros(nx * (ny + 1), device="cuda")
+    lab = torch.zeros(nx * ny, dtype=torch.uint8, device="cuda")
+    vo = torch.zeros_like(v)
+    st = lib.fl_advect_velocity_noalloc(native.FL_MACCORMACK, nx, ny, 1.0 / ny, 0.01, u.data_ptr(), v.data_ptr(),
+                                        u.data_ptr(), vo.data_ptr(), lab.data_ptr(), None)
+    assert st == native.FL_EINVAL
+    assert b"overlap" in lib.fl_last_error(None)
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch():
