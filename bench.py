@@ -521,8 +521,8 @@ def run_ours(args, world, rank, local, pg):
     te = time.perf_counter()
     for _ in range(args.e2e_steps):
         # GpuStep.step with invalidate(): upload, step, readback in one call
-        eng.call("fl_step_host", ptr(hu), ptr(hv), ptr(hp), ptr(hl), ptr(hd), ptr(hu), ptr(hv), ptr(hp), ptr(hd),
-                 ctypes.byref(iters))
+        eng.call("fl_step_host", native.FL_F32, ptr(hu), ptr(hv), ptr(hp), ptr(hl), ptr(hd), ptr(hu), ptr(hv), ptr(hp),
+                 ptr(hd), ctypes.byref(iters))
     e2e_s = max_over_ranks(pg, time.perf_counter() - te)
     e2e_value = world * args.e2e_steps / e2e_s
     h2d = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len) + eng.cells

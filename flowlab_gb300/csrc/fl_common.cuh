@@ -59,6 +59,19 @@ struct StepAccum {
   unsigned int nonfinite;
 };
 
+// The residual diagnostic (simulation.ts:539-540, SimulationParams.
+// residualEvery): the post-step divergence of the projected velocity,
+// recomputed on steps whose index is a multiple of residual_every, and its
+// FLUID-cell statistics (viz/fieldView.ts:44-60).
+struct DiagAccum {
+  double div_sq;               // sum div^2 over fluid cells
+  unsigned long long n_fluid;
+  unsigned long long counter;  // steps begun since the engine was created
+  long long last_step;         // index of the step that computed it (-1: none)
+  unsigned int div_max_bits;   // max |div| over fluid cells as float bits
+  int on;                      // the current step computes it
+};
+
 // Device-side state of one pressure solve, so that the cycle loop can run
 // without the host: the begin/check kernels decide whether another cycle
 // runs (a CUDA-graph WHILE condition, or a flag the host reads), count

@@ -187,6 +187,8 @@ void free_all(Engine* e) {
   cudaFree(e->ws_scales);
   cudaFree(e->label_in);
   cudaFree(e->label_flag);
+  cudaFree(e->div_post);
+  cudaFree(e->diag);
   destroy_graphs(e);
   if (!e->levels.empty()) cudaFree(e->levels[0].label);
   mg_free(*e);
@@ -197,6 +199,7 @@ void free_all(Engine* e) {
   for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
   if (e->acc_host) cudaFreeHost(e->acc_host);
   if (e->ctl_host) cudaFreeHost(e->ctl_host);
+  if (e->diag_host) cudaFreeHost(e->diag_host);
   if (e->ev_dye) cudaEventDestroy(e->ev_dye);
   if (e->ev_proj) cudaEventDestroy(e->ev_proj);
   if (e->ev_prior) cudaEventDestroy(e->ev_prior);
@@ -217,6 +220,7 @@ int validate_params(Engine* e, const fl_params* p) {
   if (p->mixed < 0 || p->mixed > MIXED_DF) return fail(e, FL_EINVAL, "mixed must be 0, 1 or 2 (got %d)", p->mixed);
   // the tail kernel's ownership map holds levels of at most 64 x 64 cells
   if (p->mg_tail_side < 0 || p->mg_tail_side > 64) return fail(e, FL_EINVAL, "mg_tail_side must be in [0, 64]");
+  if (p->residual_every < 0) return fail(e, FL_EINVAL, "residual_every must be >= 0");
   if (!(p->cfl_target > 0) || !(p->dt_max > 0) || !(p->rho > 0))
     return fail(e, FL_EINVAL, "cfl_target, dt_max and rho must be positive");
   return FL_OK;
@@ -489,8 +493,50 @@ void enqueue_rb_fixed(Engine* e, cudaStream_t s) {
   launch_zero_if(s, e->ctl, L.x[0], nullptr, nullptr, e->cells());
 }
 
+// The residual diagnostic after the projection (simulation.ts:539-540): the
+// step's decision and, when on, the post-step divergence. Captured, the
+// divergence kernel is the body of an IF node that only the deciding
+// kernel opens; eagerly it runs and returns at once on steps left off.
+cudaError_t enqueue_diag(Engine* e, cudaStream_t s, const float* u, const float* v) {
+  if (e->prm.residual_every <= 0) return cudaSuccess;
+  const bool cap = capturing(s);
+  cudaGraphConditionalHandle h = 0;
+  cudaGraph_t graph = nullptr;
+  cudaStreamCaptureStatus cst;
+  bool cond = false;
+  if (cap && cudaStreamGetCaptureInfo(s, &cst, nullptr, &graph, nullptr, nullptr, nullptr) == cudaSuccess &&
+      cudaGraphConditionalHandleCreate(&h, graph, 0, cudaGraphCondAssignDefault) == cudaSuccess)
+    cond = true;
+  launch_diag_begin(s, e->diag, e->prm.residual_every, cond, h);
+  if (!cond) {
+    launch_post_divergence(s, e->nx, e->ny, e->h, u, v, e->div_post, e->levels[0].label, e->diag);
+    return cudaSuccess;
+  }
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  cudaError_t err = cudaStreamGetCaptureInfo(s, &cst, nullptr, &graph, &deps, nullptr, &ndeps);
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  if (err == cudaSuccess) err = cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &cp);
+  if (err == cudaSuccess) err = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  // the body is captured from the second stream
+  if (err == cudaSuccess)
+    err = cudaStreamBeginCaptureToGraph(e->stream2, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal);
+  if (err == cudaSuccess) {
+    launch_post_divergence(e->stream2, e->nx, e->ny, e->h, u, v, e->div_post, e->levels[0].label, e->diag);
+    cudaGraph_t done = nullptr;
+    err = cudaStreamEndCapture(e->stream2, &done);
+  }
+  return err;
+}
+
 // subtract gradient + outflow -> dye (advect, decay, inlet) -> CFL
-void enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
+cudaError_t enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
   Level& L0 = e->levels[0];
   const int mac = e->prm.scheme == FL_MACCORMACK;
   const double N = (double)e->cells(), F = (double)(e->ufaces() + e->vfaces()), D = (double)e->dye_cells();
@@ -504,6 +550,10 @@ void enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
   // velocity and pressure are final: fl_step_host reads them back from here
   // on while the dye advection runs
   cudaEventRecordWithFlags(e->ev_proj, s, capturing(s) ? cudaEventRecordExternal : 0);
+  tok = prof_begin(*e, FL_PH_RESIDUAL);
+  const cudaError_t err = enqueue_diag(e, s, u, v);
+  // u, v, label in; div out
+  prof_end(*e, tok, e->prm.residual_every > 0 ? 4 * F + N + 4 * N : 0, e->prm.residual_every > 0 ? 2 : 0);
   wait_dye(e, s);
   tok = prof_begin(*e, FL_PH_ADVECT_DYE);
   launch_advect_dye(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, mac, u, v, e->dye[par], e->dye_hat, e->dye[1 - par],
@@ -514,6 +564,7 @@ void enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
   tok = prof_begin(*e, FL_PH_CFL);
   launch_max_speed(s, e->nx, e->ny, u, v, e->acc, e->sc, e->time_dev, &e->prm, e->h, device_dt, device_dt);
   prof_end(*e, tok, 4 * F, 1);
+  return err;
 }
 
 // Red-black SOR to a tolerance (pressureRedBlack.ts:88-113): checked every
@@ -609,7 +660,7 @@ int step_eager(Engine* e, bool device_dt) {
       TRY(rb_solve_device(e, hs.scale, e->prm.pressure_iters, (float)e->prm.omega, e->prm.tol, div_rms, &iters));
     e->last_iters = iters;
   }
-  enqueue_post(e, s, par, device_dt);
+  TRY(cuda_status(e, enqueue_post(e, s, par, device_dt), "project / dye / CFL"));
   TRY(check_launch(e, "project / dye / CFL"));
   e->cur = 1 - par;
   e->steps++;
@@ -674,7 +725,7 @@ cudaError_t capture_step(Engine* e, int par) {
   } else {
     enqueue_rb_fixed(e, s);
   }
-  if (err == cudaSuccess) enqueue_post(e, s, par, true);
+  if (err == cudaSuccess) err = enqueue_post(e, s, par, true);
   return err;
 }
 
@@ -757,6 +808,7 @@ void fl_default_params(fl_params* p) {
   p->mg_coarse_sweeps = 8;
   p->mg_coarsest = 4;
   p->mg_omega = 1.0;
+  p->residual_every = 1;  // simulation.ts:233
 }
 
 int fl_abi_version(void) { return FL_ABI_VERSION; }
@@ -841,13 +893,21 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   s = s ? s : dalloc(e, (void**)&e->ws_scales, 4 * sizeof(float), "warm-start scales");
   s = s ? s : dalloc(e, (void**)&e->label_in, (size_t)e->cells(), "uploaded labels");
   s = s ? s : dalloc(e, (void**)&e->label_flag, sizeof(int), "label flag");
+  s = s ? s : dalloc(e, (void**)&e->div_post, cf, "post-step divergence");
+  s = s ? s : dalloc(e, (void**)&e->diag, sizeof(DiagAccum), "residual diagnostic");
   if (s) return bail(s);
-  if (cudaMemset(e->label_flag, 0, sizeof(int)) != cudaSuccess) {
-    fail(e, FL_EDEVICE, "label flag");
-    return bail(FL_EDEVICE);
+  {
+    DiagAccum d0{};
+    d0.last_step = -1;
+    if (cudaMemset(e->label_flag, 0, sizeof(int)) != cudaSuccess || cudaMemset(e->div_post, 0, cf) != cudaSuccess ||
+        cudaMemcpy(e->diag, &d0, sizeof d0, cudaMemcpyHostToDevice) != cudaSuccess) {
+      fail(e, FL_EDEVICE, "label flag / diagnostic");
+      return bail(FL_EDEVICE);
+    }
   }
   if (cudaMallocHost(&e->acc_host, sizeof(StepAccum)) != cudaSuccess ||
-      cudaMallocHost(&e->ctl_host, sizeof(SolveCtl)) != cudaSuccess) {
+      cudaMallocHost(&e->ctl_host, sizeof(SolveCtl)) != cudaSuccess ||
+      cudaMallocHost(&e->diag_host, sizeof(DiagAccum)) != cudaSuccess) {
     fail(e, FL_ENOMEM, "pinned accumulator");
     return bail(FL_ENOMEM);
   }
@@ -1060,6 +1120,24 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
 
 int sync2(Engine* e, const char* what) { return cuda_status(e, cudaStreamSynchronize(e->stream2), what); }
 
+// fl_read_pressure's body: the refined pressure when there is one.
+int read_pressure(Engine* e, int dtype, void* p) {
+  if (step_mixed(e) && e->uploaded) {
+    if (!p) return fail(e, FL_EINVAL, "read p: null pointer");
+    if (dtype != FL_F32 && dtype != FL_F64) return fail(e, FL_EINVAL, "read p: dtype %d", dtype);
+    const long n = e->cells();
+    // the current float64 buffer is chosen on the device (no parity round trip)
+    launch_select_p64(e->stream, e->ctl, e->p64[0], e->p64[1], e->staging, dtype == FL_F64, n, refined_df(e));
+    TRY(check_launch(e, "read p"));
+    TRY(cuda_status(e, cudaMemcpyAsync(p, e->staging, n * (dtype == FL_F64 ? sizeof(double) : sizeof(float)),
+                                       cudaMemcpyDeviceToHost, e->stream),
+                    "read p"));
+    return sync(e, "read pressure");
+  }
+  TRY(download(e, p, e->levels[0].x[0], e->cells(), dtype, "read p"));
+  return sync(e, "read pressure");
+}
+
 }  // namespace
 
 extern "C" {
@@ -1071,13 +1149,28 @@ int fl_upload_fields(fl_engine* h, int dtype, const void* u, const void* v, cons
   return sync(e, "upload");
 }
 
-int fl_step_host(fl_engine* h, const float* u, const float* v, const float* p, const uint8_t* label, const float* dye,
-                 float* u_out, float* v_out, float* p_out, float* dye_out, int* iters) {
+int fl_step_host(fl_engine* h, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
+                 const void* dye, void* u_out, void* v_out, void* p_out, void* dye_out, int* iters) {
   ENTER(h);
   const bool upload_in = u != nullptr;
+  if (dtype != FL_F32 && dtype != FL_F64) return fail(e, FL_EINVAL, "step_host: dtype %d", dtype);
   if (upload_in && (!v || !label || !dye)) return fail(e, FL_EINVAL, "step_host: u without v, label or dye");
   if (!upload_in && (v || p || label || dye)) return fail(e, FL_EINVAL, "step_host: inputs without u");
   if (!upload_in && !e->uploaded) return fail(e, FL_ESTATE, "step before fl_upload_fields");
+  if (dtype == FL_F64) {
+    // Float64Array fields: converted on the device around synchronous copies
+    if (upload_in) TRY(upload_fields(e, FL_F64, u, v, p, label, dye, false));
+    TRY(graph_eligible(e) ? step_graph(e) : step_eager(e, true));
+    TRY(check_launch(e, "step"));
+    if (u_out) TRY(download(e, u_out, e->u[e->cur], e->ufaces(), FL_F64, "read u"));
+    if (v_out) TRY(download(e, v_out, e->v[e->cur], e->vfaces(), FL_F64, "read v"));
+    if (p_out) TRY(read_pressure(e, FL_F64, p_out));
+    if (dye_out) TRY(download(e, dye_out, e->dye[e->cur], 3 * e->dye_cells(), FL_F64, "read dye"));
+    TRY(sync(e, "step"));
+    TRY(solve_stats(e));
+    if (iters) *iters = e->last_iters;
+    return FL_OK;
+  }
   if (upload_in) {
     TRY(upload_fields(e, FL_F32, u, v, p, label, dye, true));
   } else {
@@ -1167,10 +1260,16 @@ int fl_set_stir(fl_engine* h, const double* st) {
   return FL_OK;
 }
 
-int fl_step(fl_engine* h, double dt, double scale, double grad_scale, const double keep[3], int* iters) {
+int fl_step(fl_engine* h, int scheme, double dt, double scale, double grad_scale, const double keep[3], int* iters) {
   ENTER(h);
   if (!e->uploaded) return fail(e, FL_ESTATE, "step before fl_upload_fields");
+  if (scheme != FL_SEMI_LAGRANGIAN && scheme != FL_MACCORMACK) return fail(e, FL_EINVAL, "scheme %d", scheme);
   if (!(dt > 0)) return fail(e, FL_EINVAL, "dt must be positive");
+  if (scheme != e->prm.scheme) {
+    // the seam passes the scheme per step; the captured step graphs hold the old one
+    e->prm.scheme = scheme;
+    destroy_step_graphs(e);
+  }
   TRY(put_scalars(e, host_scalars(e, (float)dt, (float)scale, (float)grad_scale, keep)));
   TRY(step_eager(e, false));
   e->time += dt;
@@ -1216,7 +1315,21 @@ int fl_get_stats(fl_engine* h, fl_stats* out) {
   float m;
   std::memcpy(&m, &bits, 4);
   out->max_face_speed = m;
+  TRY(cuda_status(e, cudaMemcpyAsync(e->diag_host, e->diag, sizeof(DiagAccum), cudaMemcpyDeviceToHost, e->stream),
+                  "stats"));
+  TRY(sync(e, "stats"));
+  const DiagAccum& d = *e->diag_host;
+  out->post_div_step = d.last_step;
+  out->post_div_rms = d.last_step >= 0 ? rms(d.div_sq, d.n_fluid) : 0.0;
+  std::memcpy(&m, &d.div_max_bits, 4);
+  out->post_div_max = d.last_step >= 0 ? m : 0.0;
   return FL_OK;
+}
+
+int fl_read_divergence(fl_engine* h, int dtype, void* div) {
+  ENTER(h);
+  TRY(download(e, div, e->div_post, e->cells(), dtype, "read divergence"));
+  return sync(e, "read divergence");
 }
 
 int fl_read_velocity(fl_engine* h, int dtype, void* u, void* v) {
@@ -1234,20 +1347,7 @@ int fl_read_dye(fl_engine* h, int dtype, void* dye) {
 
 int fl_read_pressure(fl_engine* h, int dtype, void* p) {
   ENTER(h);
-  if (step_mixed(e) && e->uploaded) {
-    if (!p) return fail(e, FL_EINVAL, "read p: null pointer");
-    if (dtype != FL_F32 && dtype != FL_F64) return fail(e, FL_EINVAL, "read p: dtype %d", dtype);
-    const long n = e->cells();
-    // the current float64 buffer is chosen on the device (no parity round trip)
-    launch_select_p64(e->stream, e->ctl, e->p64[0], e->p64[1], e->staging, dtype == FL_F64, n, refined_df(e));
-    TRY(check_launch(e, "read p"));
-    TRY(cuda_status(e, cudaMemcpyAsync(p, e->staging, n * (dtype == FL_F64 ? sizeof(double) : sizeof(float)),
-                                       cudaMemcpyDeviceToHost, e->stream),
-                    "read p"));
-    return sync(e, "read pressure");
-  }
-  TRY(download(e, p, e->levels[0].x[0], e->cells(), dtype, "read p"));
-  return sync(e, "read pressure");
+  return read_pressure(e, dtype, p);
 }
 
 int fl_profile_enable(fl_engine* h, int on) {
@@ -1292,19 +1392,21 @@ int fl_advect_velocity(fl_engine* h, int scheme, const float* u_in, const float*
   return sync(e, "advect velocity");
 }
 
-int fl_advect_dye(fl_engine* h, int scheme, const float* u, const float* v, const float* q_in, float* q_out,
-                  const uint8_t* label, float dt) {
+int fl_advect_dye(fl_engine* h, int scheme, const float* u, const float* v, const float* const* q_in,
+                  float* const* q_out, const uint8_t* label, float dt) {
   ENTER(h);
+  if (!q_in || !q_out) return fail(e, FL_EINVAL, "advect dye: null plane array");
   e->uploaded = false;
   TRY(up32(e, e->u[0], u, e->ufaces() * 4, "u"));
   TRY(up32(e, e->v[0], v, e->vfaces() * 4, "v"));
-  TRY(up32(e, e->dye[0], q_in, 3 * e->dye_cells() * 4, "dye"));
+  // the planes land end to end, the layout the kernels read
+  for (int c = 0; c < 3; c++) TRY(up32(e, e->dye[0] + (size_t)c * e->dye_cells(), q_in[c], e->dye_cells() * 4, "dye"));
   TRY(put_labels(e, label, "label"));
   TRY(put_scalars(e, host_scalars(e, dt, 0, 0, nullptr)));
   launch_advect_dye(e->stream, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, scheme == FL_MACCORMACK, e->u[0], e->v[0],
                     e->dye[0], e->dye_hat, e->dye[1], e->levels[0].label, e->sc, false, nullptr, 0, 0, 0, 0);
   TRY(check_launch(e, "advect dye"));
-  TRY(down32(e, q_out, e->dye[1], 3 * e->dye_cells() * 4, "dye"));
+  for (int c = 0; c < 3; c++) TRY(down32(e, q_out[c], e->dye[1] + (size_t)c * e->dye_cells(), e->dye_cells() * 4, "dye"));
   return sync(e, "advect dye");
 }
 

@@ -102,6 +102,12 @@ struct Engine {
   bool stir_pending = false;
   float stir[5] = {0, 0, 0, 0, 0};
 
+  // the residual diagnostic (fl_params.residual_every): the post-step
+  // divergence field and its statistics
+  float* div_post = nullptr;
+  DiagAccum* diag = nullptr;       // device
+  DiagAccum* diag_host = nullptr;  // pinned mirror
+
   StepScalars* sc = nullptr;   // device
   StepAccum* acc = nullptr;    // device
   StepAccum* acc_host = nullptr;  // pinned mirror
@@ -183,6 +189,11 @@ void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, fl
 void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
                        bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc,
                        float* out_lo = nullptr);
+// The residual diagnostic: the step's decision (and counter; with a graph
+// handle, the IF node's condition), then the post-step divergence when on.
+void launch_diag_begin(cudaStream_t s, DiagAccum* d, int every, bool use_cond, cudaGraphConditionalHandle h);
+void launch_post_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
+                            const uint8_t* label, DiagAccum* d);
 // p64a/p64b: the refined pressure (float64, or double-float pairs when df)
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
                              const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow,

@@ -476,6 +476,78 @@ void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, fl
                                                   conf_on, fx, fy, sc);
 }
 
+// ------------------------------------------------- residual diagnostic
+
+// Decides whether this step recomputes the post-step divergence
+// (simulation.ts:539: residualEvery > 0 && steps % residualEvery === 0,
+// `steps` counting every step ever taken) and counts the step; with a
+// graph handle it also opens or closes the IF node around the kernel below.
+__global__ void k_diag_begin(DiagAccum* d, int every, int use_cond, cudaGraphConditionalHandle h) {
+  const unsigned long long c = d->counter;
+  const int on = every > 0 && c % (unsigned long long)every == 0;
+  d->counter = c + 1;
+  d->on = on;
+  if (on) {
+    d->div_sq = 0;
+    d->n_fluid = 0;
+    d->div_max_bits = 0;
+    d->last_step = (long long)c;
+  }
+  if (use_cond) cudaGraphSetConditional(h, on ? 1u : 0u);
+}
+
+// computeDivergence (divergence.ts:17-25) of the projected velocity into
+// `out` (every cell), with the sum of squares and the max of |div| over
+// FLUID cells (divergenceStats, viz/fieldView.ts:44-60). A no-op on steps
+// k_diag_begin left off.
+__global__ void __launch_bounds__(256) k_post_divergence(int nx, int ny, float h, const float* __restrict__ u,
+                                                         const float* __restrict__ v, float* __restrict__ out,
+                                                         const uint8_t* __restrict__ label, DiagAccum* d) {
+  __shared__ double red[32];
+  __shared__ unsigned long long redn[32];
+  __shared__ float redm[32];
+  if (!d->on) return;  // the same for every thread
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float2 sq = make_float2(0.0f, 0.0f);
+  unsigned long long n = 0;
+  float mx = 0.0f;
+  const float coef = 1.0f / h;
+  for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
+    if (i >= nx) break;
+    const long k = i + (long)j * nx;
+    const float dv = coef * (u[(i + 1) + (long)j * (nx + 1)] - u[i + (long)j * (nx + 1)] + v[i + (long)(j + 1) * nx] -
+                             v[i + (long)j * nx]);
+    out[k] = dv;
+    if (label[k] == FLUID) {
+      const float q = __fmul_rn(dv, dv);
+      sq = df_add(sq, make_float2(q, __fmaf_rn(dv, dv, -q)));
+      mx = fmaxf(mx, fabsf(dv));
+      n += 1;
+    }
+  }
+  const double bs = block_sum(df_to_double(sq), red);
+  const unsigned long long bn = block_sum_u64(n, redn);
+  const float bm = block_max(mx, redm);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    atomicAdd(&d->div_sq, bs);
+    atomicAdd(&d->n_fluid, bn);
+    // non-negative floats order as their bits
+    atomicMax(&d->div_max_bits, __float_as_uint(bm));
+  }
+}
+
+void launch_diag_begin(cudaStream_t s, DiagAccum* d, int every, bool use_cond, cudaGraphConditionalHandle h) {
+  k_diag_begin<<<1, 1, 0, s>>>(d, every, use_cond, h);
+}
+
+void launch_post_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
+                            const uint8_t* label, DiagAccum* d) {
+  dim3 b(32, 8);
+  dim3 g = grid2(nx, ny, b);
+  g.y = std::min(g.y, std::max(1u, 1024u / g.x));
+  k_post_divergence<<<g, b, 0, s>>>(nx, ny, h, u, v, out, label, d);
+}
+
 void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
                        bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc, float* out_lo) {
   dim3 b(32, 8);

@@ -51,21 +51,27 @@ def _check_ctx(ctx):
 
 
 def _planes(q, cells):
-    """Accept a list of 3 planes or one flat 3-plane array; return flat f32."""
+    """The reference's qIn: FieldArray[] (advector.ts:52-62), or one flat
+    3-plane array: three contiguous float32 planes of `cells` each."""
     if isinstance(q, (list, tuple)):
-        return f32(np.concatenate([np.asarray(c).ravel() for c in q]))
-    a = np.asarray(q).ravel()
-    assert a.size == DYE_CHANNELS * cells
-    return f32(a)
-
-
-def _store(dst, src):
-    if isinstance(dst, (list, tuple)):
-        n = src.size // len(dst)
-        for c, d in enumerate(dst):
-            d[:] = src[c * n:(c + 1) * n]
+        planes = [f32(np.asarray(c).ravel()) for c in q]
     else:
-        dst[:] = src
+        a = np.asarray(q).ravel()
+        planes = [f32(a[c * cells:(c + 1) * cells]) for c in range(DYE_CHANNELS)]
+    assert len(planes) == DYE_CHANNELS and all(pl.size == cells for pl in planes)
+    return planes
+
+
+def _plane_ptrs(planes):
+    return (ctypes.c_void_p * len(planes))(*[pl.ctypes.data for pl in planes])
+
+
+def _store(dst, planes):
+    if isinstance(dst, (list, tuple)):
+        for d, pl in zip(dst, planes):
+            d[:] = pl
+    else:
+        dst[:] = np.concatenate(planes)
 
 
 class GpuAdvector:
@@ -99,9 +105,10 @@ class GpuAdvector:
         self._guard("dye")
         n = self.eng.dnx * self.eng.dny
         q = _planes(q_in, n)
-        qo = np.empty_like(q)
+        qo = [np.empty(n, np.float32) for _ in range(DYE_CHANNELS)]
         a, b, lab = f32(u), f32(v), np.ascontiguousarray(label, np.uint8)
-        self.eng.call("fl_advect_dye", SCHEMES[scheme], ptr(a), ptr(b), ptr(q), ptr(qo), ptr(lab), float(dt))
+        self.eng.call("fl_advect_dye", SCHEMES[scheme], ptr(a), ptr(b), _plane_ptrs(q), _plane_ptrs(qo), ptr(lab),
+                      float(dt))
         _store(q_out, qo)
 
     def destroy(self):
@@ -233,15 +240,14 @@ class GpuStepper:
         _check_ctx(self.ctx)
         self.busy = True
         try:
-            want = SCHEMES[scheme]
-            if self.params.scheme != want:
-                self.params.scheme = want
-                self.eng.set_params(self.params)
             if self.dirty:
                 self.upload(f)
             keep = (ctypes.c_double * 3)(*dye_keep)
             iters = ctypes.c_int(0)
-            self.eng.call("fl_step", float(dt), float(scale), float(grad_scale), keep, ctypes.byref(iters))
+            # the scheme is per step, as in the seam (simulation.ts:36-38)
+            self.eng.call("fl_step", SCHEMES[scheme], float(dt), float(scale), float(grad_scale), keep,
+                          ctypes.byref(iters))
+            self.params.scheme = SCHEMES[scheme]
             self.read_velocity(f)
             return iters.value
         finally:
@@ -270,6 +276,11 @@ class GpuStepper:
     def read_pressure(self, p):
         dtype = native.FL_F64 if p.dtype == np.float64 else native.FL_F32
         self.eng.call("fl_read_pressure", dtype, ptr(p))
+
+    def read_divergence(self, div):
+        """The post-step divergence of the last step that computed it."""
+        dtype = native.FL_F64 if div.dtype == np.float64 else native.FL_F32
+        self.eng.call("fl_read_divergence", dtype, ptr(div))
 
     def stats(self):
         return self.eng.stats()
@@ -318,8 +329,14 @@ class Simulation:
         if self.ctx is None:
             raise RuntimeError("no CUDA device: the flowlab_gb300 engine has no CPU path")
         prm = engine_params if engine_params is not None else native.default_params()
+        # the residual diagnostic runs on the device, on the same cadence
+        prm.residual_every = int(self.params["residualEvery"])
         self.stepper = GpuStepper(self.ctx, self.g, self.dye_g, prm)
         self._u_max = None
+        # simulation.ts:324-326, 369: steps taken (never reset) and the
+        # post-step divergence, refreshed every residualEvery steps
+        self.steps = 0
+        self.div = np.zeros(nx * ny, dtype)
 
     def reset(self, scene):
         """simulation.ts:388-416 — seeds in order, commitLabels, then the
@@ -368,9 +385,20 @@ class Simulation:
         self.stepper.set_stir(stir)
         keep = dye_keep_for(p["dyeDecay"], dt)
         self.iters = self.stepper.step(self.f, p["scheme"], dt, scale, grad_scale, keep)
+        # simulation.ts:495-496: the residual on this step's cadence, computed
+        # on the device from the projected velocity and read back
+        if p["residualEvery"] > 0 and self.steps % p["residualEvery"] == 0:
+            self.stepper.read_divergence(self.div)
         self._u_max = None
         self.dt = dt
         self.time += dt
+        self.steps += 1
+
+    def divergence_stats(self, max_speed):
+        """viz/fieldView.ts:44-60 divergenceStats on the device's figures:
+        (divMax, divRms as a fraction of maxSpeed/h) over FLUID cells."""
+        st = self.stepper.stats()
+        return st["post_div_max"], st["post_div_rms"] / ((max_speed or 1) / self.g.h)
 
     @property
     def cfl(self):

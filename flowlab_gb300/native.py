@@ -56,7 +56,8 @@ class Params(ctypes.Structure):
         ("rb_pairs", ctypes.c_int),
         ("warm_extrapolate", ctypes.c_int),
         ("mg_tail_side", ctypes.c_int),
-        ("reserved", ctypes.c_int * 4),
+        ("residual_every", ctypes.c_int),
+        ("reserved", ctypes.c_int * 3),
     ]
 
 
@@ -73,13 +74,17 @@ class Stats(ctypes.Structure):
         ("rel_residual", ctypes.c_double),
         ("div_rms", ctypes.c_double),
         ("max_face_speed", ctypes.c_double),
+        ("post_div_rms", ctypes.c_double),
+        ("post_div_max", ctypes.c_double),
+        ("post_div_step", ctypes.c_longlong),
     ]
 
 
-ABI_VERSION = 2  # FL_ABI_VERSION
+ABI_VERSION = 3  # FL_ABI_VERSION
 
 PHASES = ["advect_velocity", "body_forces", "divergence", "mg_pre_fine", "mg_pre", "mg_coarse", "mg_post",
-          "mg_post_fine", "defect64", "rb_sweeps", "project", "advect_dye", "cfl", "control", "warm_start"]
+          "mg_post_fine", "defect64", "rb_sweeps", "project", "advect_dye", "cfl", "control", "warm_start",
+          "residual"]
 
 
 class Profile(ctypes.Structure):
@@ -112,13 +117,14 @@ SIGNATURES = [
     ("fl_set_buoyancy", _I, [_P, _D, _D]),
     ("fl_set_confinement", _I, [_P, _D]),
     ("fl_set_stir", _I, [_P, _P]),
-    ("fl_step", _I, [_P, _D, _D, _D, _P, _P]),
+    ("fl_step", _I, [_P, _I, _D, _D, _D, _P, _P]),
     ("fl_step_auto", _I, [_P, _I, _P]),
-    ("fl_step_host", _I, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("fl_step_host", _I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("fl_get_stats", _I, [_P, _P]),
     ("fl_read_velocity", _I, [_P, _I, _P, _P]),
     ("fl_read_dye", _I, [_P, _I, _P]),
     ("fl_read_pressure", _I, [_P, _I, _P]),
+    ("fl_read_divergence", _I, [_P, _I, _P]),
     ("fl_profile_enable", _I, [_P, _I]),
     ("fl_profile_read", _I, [_P, _P]),
     ("fl_advect_velocity", _I, [_P, _I, _P, _P, _P, _P, _P, _F]),
@@ -176,9 +182,23 @@ def load():
     return lib
 
 
+# fl_default_params' values (simulation.ts:223-234, pressureMultigrid.ts:47-67),
+# held here so that building parameters needs neither the library nor a GPU;
+# a CPU test checks them against the library's own.
+DEFAULTS = dict(cfl_target=2.0, dt_max=1.0 / 30.0, rho=1.0, scheme=FL_SEMI_LAGRANGIAN, solver=FL_SOLVER_MG,
+                pressure_iters=100, mg_max_cycles=3, omega=1.9, tol=5e-3, dye_decay=(0.0, 0.0, 0.0), beta=0.0,
+                alpha=0.0, confinement=0.0, mg_pre=2, mg_post=2, mg_coarse_sweeps=8, mg_coarsest=4, mg_omega=1.0,
+                mixed=0, rb_pairs=0, warm_extrapolate=0, mg_tail_side=0, residual_every=1)
+
+
 def default_params(**overrides):
+    """fl_params with the reference defaults and the given fields replaced."""
     p = Params()
-    load().fl_default_params(ctypes.byref(p))
+    for k, v in DEFAULTS.items():
+        if k == "dye_decay":
+            p.dye_decay[:] = list(v)
+        else:
+            setattr(p, k, v)
     for k, v in overrides.items():
         if k == "dye_decay":
             p.dye_decay[:] = list(v)

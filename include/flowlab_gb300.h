@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define FL_ABI_VERSION 2
+#define FL_ABI_VERSION 3
 
 typedef struct fl_engine fl_engine;
 
@@ -96,7 +96,11 @@ typedef struct fl_params {
   int mg_tail_side;      /* the levels with both sides <= this (1..64; 0: 32) run inside one
                             single-CTA kernel per V-cycle, the finer ones as their own launches;
                             results do not depend on it */
-  int reserved[4];
+  int residual_every;    /* simulation.ts:193-206 residualEvery: recompute the post-step divergence
+                            (the residual diagnostic, simulation.ts:539-540) on the steps whose
+                            index, counted from the engine's creation, is a multiple of this;
+                            0 never (the reference's default is 1). Nothing in the step reads it. */
+  int reserved[3];
 } fl_params;
 
 /* Per-step report (the reference's sim.iters / sim.dt plus the residual the
@@ -109,6 +113,14 @@ typedef struct fl_stats {
   double rel_residual;   /* RMS remaining divergence / RMS fluid divergence, last solve; -1 if unchecked */
   double div_rms;        /* RMS of b = -scale*div over fluid cells, last solve */
   double max_face_speed; /* max |u|,|v| after the last step (CFL input of the next one) */
+  /* The residual diagnostic of the last step that computed it
+   * (fl_params.residual_every): RMS and max of |div| over FLUID cells of the
+   * projected velocity, the inputs of viz/fieldView.ts:44-60 divergenceStats
+   * before its normalisation by maxSpeed/h; post_div_step is that step's
+   * index counted from the engine's creation (-1: never computed). */
+  double post_div_rms;
+  double post_div_max;
+  long long post_div_step;
 } fl_stats;
 
 /* Per-phase device timing of fused steps, from CUDA events recorded on the
@@ -120,15 +132,17 @@ typedef struct fl_stats {
  * engine attributes to the phase: each array a kernel must read or write,
  * counted once per launch. No counterpart in the reference (its profiler is
  * host-side phase timing, src/core/profiler.ts:39-113). */
-#define FL_PHASES 15
+#define FL_PHASES 16
 /* phase indices: the multigrid phases separate the finest level's smoother
  * launches from the coarser levels'; CONTROL is the one-thread solve-control
  * kernels (tolerance test, cycle decision) and the p = 0 fill; WARM_START
- * is the learned warm start (input, network, correction) when attached. */
+ * is the learned warm start (input, network, correction) when attached;
+ * RESIDUAL is the post-step divergence diagnostic (residual_every). */
 enum fl_phase {
   FL_PH_ADVECT_VELOCITY = 0, FL_PH_BODY_FORCES = 1, FL_PH_DIVERGENCE = 2, FL_PH_MG_PRE_FINE = 3, FL_PH_MG_PRE = 4,
   FL_PH_MG_COARSE = 5, FL_PH_MG_POST = 6, FL_PH_MG_POST_FINE = 7, FL_PH_DEFECT64 = 8, FL_PH_RB_SWEEPS = 9,
-  FL_PH_PROJECT = 10, FL_PH_ADVECT_DYE = 11, FL_PH_CFL = 12, FL_PH_CONTROL = 13, FL_PH_WARM_START = 14
+  FL_PH_PROJECT = 10, FL_PH_ADVECT_DYE = 11, FL_PH_CFL = 12, FL_PH_CONTROL = 13, FL_PH_WARM_START = 14,
+  FL_PH_RESIDUAL = 15
 };
 typedef struct fl_profile {
   double ms[FL_PHASES];
@@ -176,30 +190,40 @@ int fl_set_confinement(fl_engine* e, double eps);
 /* setStir (stepGpu.ts:319-321): x, y, r, dx, dy in world units; consumed by
  * the next step. NULL clears. */
 int fl_set_stir(fl_engine* e, const double* stir5);
-/* step (stepGpu.ts:393-559) with the caller's dt, scale, gradScale and
- * per-channel keep factors. Returns the pressure iterations in *iters. */
-int fl_step(fl_engine* e, double dt, double scale, double grad_scale, const double keep[3], int* iters);
+/* step(f, scheme, dt, scale, gradScale, dyeKeep) (simulation.ts:36-38,
+ * stepGpu.ts:393-559) with the caller's advection scheme, dt, scale,
+ * gradScale and per-channel keep factors. The scheme is per call, as in the
+ * seam; it also becomes the engine's fl_params.scheme for later
+ * fl_step_auto calls. Returns the pressure iterations in *iters. */
+int fl_step(fl_engine* e, int scheme, double dt, double scale, double grad_scale, const double keep[3], int* iters);
 /* `nsteps` steps with dt from the CURRENT velocity on the device
  * (simulation.ts:474-479 without the host scan or the one-step-stale
  * readback). No host synchronisation between steps unless tol > 0 requires
  * a residual readback. */
 int fl_step_auto(fl_engine* e, int nsteps, int* iters_last);
 /* One step the way GpuStep.step (simulation.ts:35-84, GpuStepper.step in
- * stepGpu.ts:393-560) runs it, with host float32 buffers: when u is
- * non-null the host fields (u, v, p, label, dye; p may be null: zero) are
- * uploaded first, as after invalidate() (fl_upload_fields semantics); then
- * one step with dt from the device (fl_step_auto); then the results are
- * copied into the non-null outputs. The dye upload overlaps the step's
- * first kernels, and the velocity and pressure readback overlaps the dye
- * advection. Returns when every copy completed; results equal
- * fl_upload_fields + fl_step_auto + fl_read_* bit for bit. */
-int fl_step_host(fl_engine* e, const float* u, const float* v, const float* p, const uint8_t* label,
-                 const float* dye, float* u_out, float* v_out, float* p_out, float* dye_out, int* iters);
+ * stepGpu.ts:393-560) runs it, with host buffers of `dtype` (FL_F32 or
+ * FL_F64: the reference's FieldArray is Float32Array or Float64Array,
+ * grid.ts:53-54) for every float field in and out: when u is non-null the
+ * host fields (u, v, p, label, dye; p may be null: zero) are uploaded first,
+ * as after invalidate() (fl_upload_fields semantics); then one step with dt
+ * from the device (fl_step_auto); then the results are copied into the
+ * non-null outputs. With FL_F32 the dye upload overlaps the step's first
+ * kernels and the velocity and pressure readback overlaps the dye
+ * advection; FL_F64 converts on the device around synchronous copies.
+ * Returns when every copy completed; results equal fl_upload_fields +
+ * fl_step_auto + fl_read_* bit for bit. */
+int fl_step_host(fl_engine* e, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
+                 const void* dye, void* u_out, void* v_out, void* p_out, void* dye_out, int* iters);
 int fl_get_stats(fl_engine* e, fl_stats* out);
 /* Readbacks (drainReadback / readDye, stepGpu.ts:372-391, 578-604). */
 int fl_read_velocity(fl_engine* e, int dtype, void* u, void* v);
 int fl_read_dye(fl_engine* e, int dtype, void* dye);
 int fl_read_pressure(fl_engine* e, int dtype, void* p);
+/* The post-step divergence field (Simulation.div after a step that
+ * recomputed it, simulation.ts:539-540; nx*ny cells, every label) of the
+ * last step that computed it (fl_stats.post_div_step); zeros before any. */
+int fl_read_divergence(fl_engine* e, int dtype, void* div);
 
 /* Enables (1) or disables (0) phase timing and clears the counters. */
 int fl_profile_enable(fl_engine* e, int on);
@@ -211,9 +235,12 @@ int fl_profile_read(fl_engine* e, fl_profile* out);
 /* advectVelocity / advectVelocityMacCormack (advect.ts:126-211). */
 int fl_advect_velocity(fl_engine* e, int scheme, const float* u_in, const float* v_in, float* u_out, float* v_out,
                        const uint8_t* label, float dt);
-/* advectScalar / advectScalarMacCormack over all 3 channels (advect.ts:241-312). */
-int fl_advect_dye(fl_engine* e, int scheme, const float* u, const float* v, const float* q_in, float* q_out,
-                  const uint8_t* label, float dt);
+/* dye(g, scheme, u, v, qIn[], qOut[], label, dt, dg) (advector.ts:52-62):
+ * advectScalar / advectScalarMacCormack (advect.ts:241-312) of the three
+ * channels on one backtrace; q_in and q_out are arrays of three plane
+ * pointers of dnx*dny floats each (dnx = nx*dye_scale). */
+int fl_advect_dye(fl_engine* e, int scheme, const float* u, const float* v, const float* const* q_in,
+                  float* const* q_out, const uint8_t* label, float dt);
 
 /* ---------------------------- PressureSolver (pressureSolver.ts:21-41), float32 host arrays */
 

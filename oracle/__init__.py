@@ -45,6 +45,7 @@ class Params(ctypes.Structure):
         ("mgOmega", ctypes.c_double),
         ("mixed", ctypes.c_int),
         ("warmExtrapolate", ctypes.c_int),
+        ("residualEvery", ctypes.c_int),
     ]
 
 
@@ -71,6 +72,7 @@ def make_params(**kw):
     p.mgPre, p.mgPost, p.mgCoarseSweeps, p.mgCoarsest = 2, 2, 8, 4
     p.mgOmega = 1.0
     p.mixed = 0
+    p.residualEvery = 1
     for k, v in kw.items():
         if k == "dyeDecay":
             p.dyeDecay[:] = list(v)
@@ -86,7 +88,7 @@ def params_from_engine(p):
                 mgMaxCycles=p.mg_max_cycles, omega=p.omega, tol=p.tol, dyeDecay=tuple(p.dye_decay), beta=p.beta,
                 alpha=p.alpha, confinement=p.confinement, mgPre=p.mg_pre, mgPost=p.mg_post,
                 mgCoarseSweeps=p.mg_coarse_sweeps, mgCoarsest=p.mg_coarsest, mgOmega=p.mg_omega, mixed=p.mixed,
-                warmExtrapolate=p.warm_extrapolate)
+                warmExtrapolate=p.warm_extrapolate, residualEvery=p.residual_every)
 
 
 def lib():
@@ -356,6 +358,14 @@ class OracleSimulation:
         d = np.zeros(self.nx * self.ny, self.o.dtype)
         self.o._f("sim_get_div")(self.handle, _p(d))
         return d
+
+    def get_div_post(self):
+        """(post-step divergence, index of the step that computed it or -1)."""
+        d = np.zeros(self.nx * self.ny, self.o.dtype)
+        f = self.o._f("sim_get_div_post")
+        f.restype = ctypes.c_longlong
+        step = f(self.handle, _p(d))
+        return d, int(step)
 
     def scale(self):
         """The last step's scale rho*h^2/dt."""

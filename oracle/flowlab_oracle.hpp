@@ -1135,6 +1135,7 @@ struct StepParams {
   int mgMaxCycles = 3;
   int mixed = 0;  // NEW: defect correction around the multigrid, 1: float64 pressure, 2: double-float (float32 only)
   int warmExtrapolate = 0;  // NEW: the multigrid starts from 2 p(n) - p(n-1) on fluid cells
+  int residualEvery = 1;    // simulation.ts:193-206, 233
 };
 
 template <class T>
@@ -1142,6 +1143,11 @@ struct Simulation {
   Grid<T> g, dg;
   StepParams prm;
   std::vector<T> u, v, p, div, uNext, vNext, uHat, vHat, qHat, fx, fy;
+  // the post-step divergence (simulation.ts:539-540), kept apart from `div`
+  // (the solve's input, which the reference reuses for it) so both can be
+  // read; divPostStep is the index of the step that last computed it
+  std::vector<T> divPost;
+  long long steps = 0, divPostStep = -1;
   std::vector<double> p64;  // the pressure when prm.mixed
   std::vector<double> pPrev64;  // the previous step's pressure (warmExtrapolate, mixed)
   std::vector<T> pPrev;         // the previous step's pressure (warmExtrapolate)
@@ -1164,7 +1170,7 @@ struct Simulation {
     int s = std::max(1, dyeScale);
     dg = s == 1 ? g : Grid<T>{nx * s, ny * s, T(1.0 / (double)(ny * s))};
     long n = (long)nx * ny, nu = (long)(nx + 1) * ny, nv = (long)nx * (ny + 1), nd = (long)dg.nx * dg.ny;
-    u.assign(nu, 0); v.assign(nv, 0); p.assign(n, 0); div.assign(n, 0);
+    u.assign(nu, 0); v.assign(nv, 0); p.assign(n, 0); div.assign(n, 0); divPost.assign(n, 0);
     uNext.assign(nu, 0); vNext.assign(nv, 0); uHat.assign(nu, 0); vHat.assign(nv, 0);
     qHat.assign(nd, 0); fx.assign(n, 0); fy.assign(n, 0);
     label.assign(n, FLUID);
@@ -1277,6 +1283,12 @@ struct Simulation {
     else
       subtractGradient(g, p.data(), u.data(), v.data(), label.data(), gradScale);
     applyOutflow(g, u.data(), v.data(), label.data());
+    // simulation.ts:539-540 — the residual diagnostic; `steps` counts every
+    // step taken (simulation.ts:324-326, 586)
+    if (prm.residualEvery > 0 && steps % prm.residualEvery == 0) {
+      computeDivergence(g, u.data(), v.data(), divPost.data());
+      divPostStep = steps;
+    }
 
     for (int c = 0; c < DYE_CHANNELS; c++) {
       if (prm.macCormack)
@@ -1296,6 +1308,7 @@ struct Simulation {
       applyDyePatch(dg, planes, pi0, pj0, pnx, pny, patch.data());
     }
     time += (double)dt;
+    steps++;
     return iters;
   }
 };

@@ -20,6 +20,7 @@ struct orc_params {
   double mgOmega;
   int mixed;
   int warmExtrapolate;
+  int residualEvery;
 };
 
 int orc_abi_version(void) { return 1; }
@@ -48,6 +49,7 @@ static StepParams toParams(const orc_params* c) {
   p.mg.omega = c->mgOmega;
   p.mixed = c->mixed;
   p.warmExtrapolate = c->warmExtrapolate;
+  p.residualEvery = c->residualEvery;
   return p;
 }
 
@@ -235,6 +237,12 @@ static StepParams toParams(const orc_params* c) {
   void orc_sim_get_div_##SUF(void* sp, T* div) {                                                        \
     Simulation<T>* s = (Simulation<T>*)sp;                                                              \
     std::copy(s->div.begin(), s->div.end(), div);                                                       \
+  }                                                                                                     \
+  /* the post-step divergence and the index of the step that computed it */                               \
+  long long orc_sim_get_div_post_##SUF(void* sp, T* div) {                                              \
+    Simulation<T>* s = (Simulation<T>*)sp;                                                              \
+    std::copy(s->divPost.begin(), s->divPost.end(), div);                                                 \
+    return s->divPostStep;                                                                              \
   }                                                                                                     \
   /* the last step's scale rho*h^2/dt */                                                                \
   double orc_sim_scale_##SUF(void* sp) {                                                                \

@@ -38,7 +38,7 @@ int main(void) {
       dye[i + (long)j * nx] = (float)exp(-(x * x + y * y) / 0.01); /* channel 0: temperature */
     }
   int cycles = 0;
-  st = fl_step_host(e, u, v, p, label, dye, u, v, p, dye, &cycles);
+  st = fl_step_host(e, FL_F32, u, v, p, label, dye, u, v, p, dye, &cycles);
   if (st != FL_OK) {
     printf("step failed (%d): %s\n", st, fl_last_error(e));
     fl_destroy(e);

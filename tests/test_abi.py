@@ -36,14 +36,27 @@ def test_bindings_cover_the_header():
 
 
 def test_abi_version_and_defaults(lib):
-    assert lib.fl_abi_version() == native.ABI_VERSION == 2
+    assert lib.fl_abi_version() == native.ABI_VERSION == 3
     p = native.default_params()
     # simulation.ts:223-234 and pressureMultigrid.ts:47-67
     assert p.cfl_target == 2.0 and abs(p.dt_max - 1 / 30) < 1e-15 and p.tol == 5e-3
     assert (p.mg_pre, p.mg_post, p.mg_coarse_sweeps, p.mg_coarsest, p.mg_max_cycles) == (2, 2, 8, 4, 3)
+    assert p.residual_every == 1  # simulation.ts:233
     assert ctypes.sizeof(native.Params) == 160
     assert p.mg_tail_side == 0  # the engine's default first tail level (32)
-    assert native.Params.mg_tail_side.offset == 140 and native.Params.reserved.offset == 144
+    assert native.Params.mg_tail_side.offset == 140 and native.Params.residual_every.offset == 144
+    assert native.Params.reserved.offset == 148
+    assert ctypes.sizeof(native.Stats) == 88 and native.Stats.post_div_step.offset == 80
+
+
+def test_python_defaults_equal_the_library_defaults(lib):
+    # default_params() builds fl_params without the library (the CPU
+    # reference arm of the bench must not load it); the library's own
+    # fl_default_params (host code only) is the authority
+    ours = native.default_params()
+    theirs = native.Params()
+    lib.fl_default_params(ctypes.byref(theirs))
+    assert bytes(ours) == bytes(theirs)
 
 
 def test_create_fails_loudly_without_a_device(lib):

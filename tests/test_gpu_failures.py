@@ -58,8 +58,8 @@ def test_nan_velocity_is_reported_and_the_engine_recovers():
 
         n = (eng.ufaces, eng.vfaces, eng.cells, eng.dye_len)
         outs = [np.empty(k, np.float32) for k in n]
-        st = status(lambda: eng.call("fl_step_host", ptr(bad), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
-                                     ptr(f32(f.dye)), *[ptr(o) for o in outs], ctypes.byref(iters)))
+        st = status(lambda: eng.call("fl_step_host", native.FL_F32, ptr(bad), ptr(f32(f.v)), ptr(f32(f.p)),
+                                     ptr(f.label), ptr(f32(f.dye)), *[ptr(o) for o in outs], ctypes.byref(iters)))
         assert st == native.FL_ENONFINITE
 
         # recovery: clean fields step normally and match a fresh engine

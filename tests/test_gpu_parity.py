@@ -10,6 +10,8 @@ reference's own tolerances — 1e-5 x peak for p/u/v/dye
 (redBlack.gputest.ts:158, advect.gputest.ts:272) and 1e-6 absolute for the
 projection passes on O(1) data (project.gputest.ts:288).
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -219,8 +221,14 @@ def test_advection(o32, o64, mac, dye_scale):
         vo = np.empty_like(f32(v))
         scheme = native.FL_MACCORMACK if mac else native.FL_SEMI_LAGRANGIAN
         eng.call("fl_advect_velocity", scheme, ptr(f32(u)), ptr(f32(v)), ptr(uo), ptr(vo), ptr(label), np.float32(dt))
-        qo = np.empty_like(f32(dye))
-        eng.call("fl_advect_dye", scheme, ptr(f32(u)), ptr(f32(v)), ptr(f32(dye)), ptr(qo), ptr(label), np.float32(dt))
+        # the seam's qIn[] / qOut[]: three plane pointers each (advector.ts:52-62)
+        nd = dnx * dny
+        qi = [f32(dye)[c * nd:(c + 1) * nd].copy() for c in range(3)]
+        qp = [np.empty(nd, np.float32) for _ in range(3)]
+        planes = lambda ps: (ctypes.c_void_p * 3)(*[a.ctypes.data for a in ps])
+        eng.call("fl_advect_dye", scheme, ptr(f32(u)), ptr(f32(v)), planes(qi), planes(qp), ptr(label),
+                 np.float32(dt))
+        qo = np.concatenate(qp)
     finally:
         eng.close()
     hf, dtf, dhf = float(np.float32(h)), float(np.float32(dt)), float(np.float32(dh))
@@ -308,7 +316,7 @@ def test_stir(eng40, o64):
 
 def test_errors_are_status_codes(eng40):
     with pytest.raises(native.FlowlabError) as ei:
-        eng40.call("fl_step", 0.01, 1.0, 1.0, None, None)
+        eng40.call("fl_step", native.FL_SEMI_LAGRANGIAN, 0.01, 1.0, 1.0, None, None)
     assert ei.value.status == native.FL_ESTATE
     bad = native.default_params(mg_pre=9)
     with pytest.raises(native.FlowlabError) as ei:

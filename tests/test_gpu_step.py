@@ -96,7 +96,7 @@ def test_host_dt_step_matches_device_dt_step():
         s0 = eng.stats()
         keep = (ctypes.c_double * 3)(*[np.exp(-d * np.float64(np.float32(s0["dt"]))) if d > 0 else 1.0
                                        for d in prm.dye_decay])
-        eng.call("fl_step", s0["dt"], s0["scale"], s0["grad_scale"], keep, None)
+        eng.call("fl_step", prm.scheme, s0["dt"], s0["scale"], s0["grad_scale"], keep, None)
         u = np.empty(eng.ufaces, np.float32)
         v = np.empty(eng.vfaces, np.float32)
         eng.call("fl_read_velocity", native.FL_F32, ptr(u), ptr(v))
@@ -423,11 +423,11 @@ def test_step_host_equals_upload_step_and_reads(case):
             a.call("fl_read_dye", native.FL_F32, ptr(out_a[3]))
             ib = ctypes.c_int()
             if upload:
-                b.call("fl_step_host", ptr(state[0]), ptr(state[1]), ptr(state[2]), ptr(label), ptr(state[3]),
-                       ptr(out_b[0]), ptr(out_b[1]), ptr(out_b[2]), ptr(out_b[3]), ctypes.byref(ib))
+                b.call("fl_step_host", native.FL_F32, ptr(state[0]), ptr(state[1]), ptr(state[2]), ptr(label),
+                       ptr(state[3]), ptr(out_b[0]), ptr(out_b[1]), ptr(out_b[2]), ptr(out_b[3]), ctypes.byref(ib))
             else:
-                b.call("fl_step_host", None, None, None, None, None, ptr(out_b[0]), ptr(out_b[1]), ptr(out_b[2]),
-                       ptr(out_b[3]), ctypes.byref(ib))
+                b.call("fl_step_host", native.FL_F32, None, None, None, None, None, ptr(out_b[0]), ptr(out_b[1]),
+                       ptr(out_b[2]), ptr(out_b[3]), ctypes.byref(ib))
             for name, x, y in zip(("u", "v", "p", "dye"), out_a, out_b):
                 assert mismatch(x, y) == 0, "step %d %s: %d values differ" % (step, name, mismatch(x, y))
             assert ia.value == ib.value
