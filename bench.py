@@ -51,8 +51,7 @@ sys.path.insert(0, ROOT)
 # residual, plain multigrid against the U-Net warm start, with HBM GB/s.
 METRIC = "steps/s at 1024\u00b2 to 1e-6 residual: plain MG vs CNN warm-start MG; HBM GB/s"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
-REF_WARMUP = 2       # the CPU reference arm's warm-up steps at most
-REF_BUDGET_S = 60.0  # and its timed seconds (about)
+REF_BUDGET_S = 60.0  # the CPU reference arm's timed seconds (about; its warm-up is the requested one)
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -60,23 +59,52 @@ def baseline_metric():
     return METRIC
 
 
-# What bounds each phase's kernels at 1024^2 when it is not HBM (ncu summaries
-# under profiles/): the roofline line names it beside the HBM fraction.
+# What bounds each phase's kernels at 1024^2 when it is not HBM: the
+# roofline line names it beside the HBM fraction.
 LIMITERS = {
-    "defect64": "float64 pipe (ncu: 73-74% of peak float64 issue), not memory",
+    "defect64": "float32 issue (double-float pairs) / float64 pipe (the float64 pass)",
     "mg_coarse": "latency: one CTA, a chain of dependent barrier phases",
     "mg_pre": "latency: small levels, few CTAs per launch",
     "mg_post": "latency: small levels, few CTAs per launch",
+    "mg_fine": "instruction issue: temporally blocked sweeps with halo recompute, working set in L2",
 }
 
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of a
-# phase's dominant kernel from one ncu capture of the 1024^2 plume's eager
-# profiled steps (profiles/): (bytes, kernel, summary file).
-TRAFFIC_PLUME_1024 = {
-    "defect64": (17.842688e6, "k_update_resid64<1>", "profiles/k_mg_coarse_resid64_plume_1024.md"),
-    "mg_coarse": (0.07296e6, "k_mg_coarse", "profiles/k_mg_coarse_resid64_plume_1024.md"),
-}
+def phase_bytes_per_cell(prm, size, tail_side=32):
+    """Algorithmic bytes per fine cell per LAUNCH of each phase's kernels:
+    every array a pass must read or write counted once, float32 4 B, labels
+    1 B. A red-black half-sweep reads p (4), the rhs of its colour (2) and
+    the labels (1) and writes its colour (2): 9 B, 18 per sweep pair. A
+    V(3,3) finest level is then 3 x 18 + 11 (residual and restriction) on
+    the way down and 10 (prolongation) + 3 x 18 on the way up. MacCormack
+    velocity: forward 13 + 13 (u, v faces), correction 17 + 17; MacCormack
+    dye: forward 33, correction 45; divergence 12 (u, v in, div out);
+    subtract + outflow 21; the CFL scan 8; the residual-diagnostic
+    divergence 13 (with the labels); the defect correction's residual
+    x 8 + b 4 + label 1 + r 8 = 21; buoyancy (alpha, beta) 17 and
+    confinement 25 per step. The coarser smoother levels (levels above the
+    single-CTA tail) are summed over their sizes, per launch averaged."""
+    pre, post = prm.mg_pre, prm.mg_post
+    down, up = pre * 18 + 11, 10 + post * 18
+    levels, n = [], size // 2
+    while n > tail_side:
+        levels.append((n / size) ** 2)
+        n //= 2
+    mid = sum(levels)
+    out = {
+        "advect_velocity": 60 / 2 if prm.scheme == 1 else 26,
+        "body_forces": (17 + 25) / 2,
+        "divergence": 12,
+        "mg_fine": (down + up) / 2,
+        "mg_pre": down * mid / max(1, len(levels)),
+        "mg_post": up * mid / max(1, len(levels)),
+        "defect64": 21,
+        "project": 21,
+        "advect_dye": 78 / 2 if prm.scheme == 1 else 33,
+        "cfl": 8,
+        "residual": 13 / 2,
+    }
+    return out
 
 
 def bf16_peak():
@@ -111,6 +139,8 @@ def parse():
     ap.add_argument("--tol", type=float, default=None)
     ap.add_argument("--max-cycles", type=int, default=None)
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU-baseline sample")
+    ap.add_argument("--parity-steps", type=int, default=2,
+                    help="steps from the warmed-up state diffed against the float32 and float64 oracles (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--profile-steps", type=int, default=8, help="eager steps with phase events, after the timed ones")
     ap.add_argument("--cnn-steps", type=int, default=30,
@@ -299,7 +329,8 @@ def run_reference_batch(args):
             "n_gpus": args.gpus, "steps": n, "warmup": 0, "ms_per_step": 1000.0 * step_s, "higher_is_better": True,
             "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": "%d closed-box scenes, sides 2^U{6..10}" % len(sides), "scenes": len(sides)},
-            "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": 1, "host_cores": os.cpu_count(),
+                             "kind": "port", "sample": sample},
             "e2e": {"value": sps, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -310,9 +341,9 @@ def run_reference(args, world, rank, pg):
         return
     if args.workload == "batch":
         return run_reference_batch(args)
-    # bounded: at most REF_WARMUP warm-up steps and REF_BUDGET_S seconds of
-    # timed steps, whatever --steps / --warmup ask for
-    warm = min(args.warmup, REF_WARMUP)
+    # the requested warm-up, then at most REF_BUDGET_S seconds of the
+    # requested timed steps
+    warm = args.warmup
     sps, secs, done = cpu_port_steps(args, args.steps, warm, budget_s=REF_BUDGET_S)
     sample = "%d of %d requested steps (%.1f s, after %d warm-up steps from the reset scene) of the %d^2 %s, " \
              "float64 CPU port of the reference's Simulation.step, one thread" % (
@@ -321,7 +352,8 @@ def run_reference(args, world, rank, pg):
             "warmup": warm, "ms_per_step": 1000.0 / sps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(args), "impl": "reference",
-            "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": 1, "host_cores": os.cpu_count(),
+                             "kind": "port", "sample": sample},
             "e2e": {"value": sps, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -352,6 +384,78 @@ def workload_config(args):
 
 
 # ------------------------------------------------------------ our engine
+
+def parity_check(args, state, device):
+    """`args.parity_steps` steps of the workload from the warmed-up state
+    (host copies of u, v, p, dye) on a fresh engine (graph path), the float32
+    oracle and the float64 oracle side by side (two threads; the oracle's
+    calls release the interpreter lock). Reports the float32 oracle
+    mismatches per field (the bar: none), the drift from the float64 oracle
+    per field as max |gpu - f64| / max |f64| (p: the refined pressure), and
+    the last step's relative residual by the engine's own definition and by
+    the reference's (rmsRemainingDivergence / fluidDivRms, pressure.ts:
+    102-186, in float64 on the engine's pressure and the step's float32
+    divergence and scale)."""
+    import numpy as np
+
+    from flowlab_gb300 import native
+    from flowlab_gb300.native import f32, ptr
+    from oracle import Oracle, params_from_engine as oracle_params
+
+    g, f, patch, prm = workload(args)
+    k = args.parity_steps
+    u0, v0, p0, d0 = (np.asarray(x, np.float32) for x in state)
+    eng = native.Engine(g.nx, g.ny, g.h, params=prm, device=device)
+    try:
+        if patch is not None:
+            eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+        eng.call("fl_upload_fields", native.FL_F32, ptr(u0), ptr(v0), ptr(p0), ptr(f.label), ptr(d0))
+        eng.call("fl_step_auto", k, None)
+        gpu = {"u": np.empty(eng.ufaces, np.float32), "v": np.empty(eng.vfaces, np.float32),
+               "p": np.empty(eng.cells, np.float32), "dye": np.empty(eng.dye_len, np.float32)}
+        eng.call("fl_read_velocity", native.FL_F32, ptr(gpu["u"]), ptr(gpu["v"]))
+        eng.call("fl_read_pressure", native.FL_F32, ptr(gpu["p"]))
+        eng.call("fl_read_dye", native.FL_F32, ptr(gpu["dye"]))
+        p64 = np.empty(eng.cells, np.float64)
+        eng.call("fl_read_pressure", native.FL_F64, ptr(p64))
+        st = eng.stats()
+    finally:
+        eng.close()
+    out = {}
+
+    def run(tag):
+        o = Oracle(tag)
+        sim = o.simulation(g.nx, g.ny, 1, **oracle_params(prm))
+        sim.set_fields(u0, v0, p0, f.label, d0)
+        if patch is not None:
+            sim.set_patch(patch.i0, patch.j0, patch.nx, patch.ny, patch.data)
+        for _ in range(k):
+            sim.step()
+        u, v, p, d = sim.get_fields()
+        out[tag] = dict(u=u, v=v, p=p, dye=d, p64=sim.get_p64(), div=sim.get_div(), scale=sim.scale())
+
+    t0 = time.perf_counter()
+    ts = [threading.Thread(target=run, args=(t,)) for t in ("f32", "f64")]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    r32, r64 = out["f32"], out["f64"]
+    mism = {n: int((np.asarray(r32[n], np.float32) != gpu[n]).sum()) for n in ("u", "v", "p", "dye")}
+    drift = {}
+    for n in ("u", "v", "p", "dye"):
+        a = np.asarray(r64["p64"] if n == "p" else r64[n], np.float64)
+        b = p64 if n == "p" else gpu[n].astype(np.float64)
+        drift[n] = float(np.abs(a - b).max() / max(1e-30, np.abs(a).max()))
+    o64 = Oracle("f64")
+    div = np.asarray(r32["div"], np.float64)
+    scale = float(np.float32(r32["scale"]))
+    rr_ref = o64.rms_remaining(g.nx, g.ny, p64, div, f.label, scale) / o64.fluid_div_rms(div, f.label)
+    return {"steps": k, "from": "the warmed-up state after the warm-up steps",
+            "mismatches_vs_f32_oracle": mism, "drift_vs_f64_oracle": drift,
+            "rel_residual_engine": st["rel_residual"], "rel_residual_reference_definition": rr_ref,
+            "post_div_rms": st["post_div_rms"], "oracle_seconds": time.perf_counter() - t0}
+
 
 def cnn_arm(args, local, stream_unused, flush, state0):
     """The same workload from the same reset scene, stepped with the trained
@@ -456,7 +560,7 @@ def run_ours(args, world, rank, local, pg):
 
     # Host copy of the warmed-up state: the CPU baseline continues from it.
     state = None
-    if rank == 0 and args.cpu_steps > 0:
+    if rank == 0 and (args.cpu_steps > 0 or args.parity_steps > 0):
         su = np.empty(eng.ufaces, np.float32)
         sv = np.empty(eng.vfaces, np.float32)
         sp = np.empty(eng.cells, np.float32)
@@ -529,11 +633,12 @@ def run_ours(args, world, rank, local, pg):
     d2h = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len)
 
     cnn = cnn_arm(args, local, stream, flush, state0=(f, patch)) if args.cnn_steps > 0 else None
+    parity = parity_check(args, state, local) if state is not None and args.parity_steps > 0 else None
 
     cpu = None
     if rank == 0 and args.cpu_steps > 0:
         sps, secs, _ = cpu_port_steps(args, args.cpu_steps, 0, state)
-        cpu = {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
+        cpu = {"value": sps, "unit": "steps/s", "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
                "sample": "%d steps of the %d^2 %s continuing from the GPU's warmed-up state, float64 CPU "
                          "port of the reference's Simulation.step, one thread (%.1f s)"
                          % (args.cpu_steps, args.size, workload_name(args), secs)}
@@ -542,23 +647,42 @@ def run_ours(args, world, rank, local, pg):
         return
 
     peak, peak_kind = hbm_peak()
+    nsteps_prof = max(1, len(prof_cycles))
     phases = {n: {"ms": ms, "launches": int(l), "gbytes": b / 1e9} for n, (ms, l, b) in prof.items() if l > 0}
-    # the dominant kernel: the phase with the most device time per step among
-    # those that launch one kernel (mg_pre / mg_post hold every coarser
-    # level's smoother, a different launch shape per level)
-    dom = max((n for n in phases if n not in ("mg_pre", "mg_post")), key=lambda n: phases[n]["ms"])
-    d = phases[dom]
-    achieved = (d["gbytes"] / d["launches"]) / ((d["ms"] / d["launches"]) / 1000.0)
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
-                "algorithmic_bytes_per_launch": d["gbytes"] * 1e9 / d["launches"],
-                "avg_launch_us": 1000.0 * d["ms"] / d["launches"],
+    # the finest level's smoother is one kernel (k_smooth on level 0) in its
+    # PRE and POST forms: one row
+    fine = {n: phases[n] for n in ("mg_pre_fine", "mg_post_fine") if n in phases}
+    rows = {n: dict(p) for n, p in phases.items() if n not in fine}
+    if fine:
+        rows["mg_fine"] = {k: sum(p[k] for p in fine.values()) for k in ("ms", "launches", "gbytes")}
+    per_cell = phase_bytes_per_cell(prm, args.size)
+    cells = args.size * args.size
+    table = {}
+    for n, r in rows.items():
+        if r["launches"] == 0 or r["ms"] <= 0:
+            continue
+        us = 1000.0 * r["ms"] / r["launches"]
+        t = {"ms_per_step": r["ms"] / nsteps_prof, "launches_per_step": r["launches"] / nsteps_prof,
+             "avg_launch_us": us, "engine_bytes_per_launch": r["gbytes"] * 1e9 / r["launches"]}
+        if n in per_cell:
+            b = per_cell[n] * cells
+            t["algorithmic_bytes_per_launch"] = b
+            t["achieved_gbs"] = b / (us * 1e-6) / 1e9
+            t["frac"] = t["achieved_gbs"] / peak
+        table[n] = t
+    # the dominant kernel: the most device time per step among the phases
+    # that run one kernel shape (mg_pre / mg_post hold every coarser
+    # level's smoother, a different launch shape per level; control is the
+    # one-thread solve-control kernels)
+    cand = [n for n in table if n not in ("mg_pre", "mg_post", "control") and "frac" in table[n]]
+    dom = max(cand, key=lambda n: table[n]["ms_per_step"])
+    d = table[dom]
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": d["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                "frac": d["frac"], "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": d["algorithmic_bytes_per_launch"],
+                "avg_launch_us": d["avg_launch_us"],
+                "engine_bytes_per_launch": d["engine_bytes_per_launch"],
                 "limiter": LIMITERS.get(dom, "instruction issue (working set resident in L2)")}
-    if args.workload == "plume" and args.size == 1024 and dom in TRAFFIC_PLUME_1024:
-        tb, tk, tf = TRAFFIC_PLUME_1024[dom]
-        roofline["traffic"] = tb
-        roofline["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one %s launch (%s)" % (
-            tk, tf)
     # Launches in the timed region: the profiled steps give the launches per
     # V-cycle (smoothers, coarse tail, float64 update, cycle test) and per
     # step (the rest); the timed steps' own cycle counts scale them.
@@ -584,6 +708,8 @@ def run_ours(args, world, rank, local, pg):
         "cnn_warm_start": cnn,
         "clocks": sampler.summary(t0, t1),
         "phases_ms_per_step": {n: p["ms"] / len(prof_cycles) for n, p in phases.items()},
+        "kernels": table,
+        "parity": parity,
         "phase_sample": "%d eager profiled steps after the timed region" % len(prof_cycles),
     }
     print(json.dumps(line), flush=True)
