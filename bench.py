@@ -496,7 +496,7 @@ def cnn_arm(args, local, stream_unused, flush, state0):
                     eng.call("fl_step_auto", 1, None)
                 eng.call("fl_synchronize")
                 st_ = torch.cuda.ExternalStream(eng.stream(), device=local)
-                ms, cyc, rr = [], [], []
+                ms, cyc, rr, r0 = [], [], [], []
                 for _ in range(args.cnn_steps):
                     with torch.cuda.stream(st_):
                         flush.zero_()
@@ -508,9 +508,10 @@ def cnn_arm(args, local, stream_unused, flush, state0):
                     st = eng.stats()
                     cyc.append(st["cycles"])
                     rr.append(st["rel_residual"])
+                    r0.append(st["initial_rel_residual"])
                     ms.append(a.elapsed_time(b))
                 out[arm] = {"steps_per_s": 1000.0 * len(ms) / sum(ms), "vcycles_per_step": statistics.mean(cyc),
-                            "rel_residual_max": max(rr)}
+                            "rel_residual_max": max(rr), "initial_rel_residual_mean": statistics.mean(r0)}
                 if arm == "cnn":
                     # the network's own device time, from phase events on a few eager steps
                     eng.profile(True)
@@ -533,8 +534,19 @@ def cnn_arm(args, local, stream_unused, flush, state0):
     out["vcycles_saved_per_step"] = out["plain"]["vcycles_per_step"] - out["cnn"]["vcycles_per_step"]
     out["extrapolated_vcycles_saved_per_step"] = (out["plain"]["vcycles_per_step"]
                                                   - out["extrapolated"]["vcycles_per_step"])
+    # the autotuner's rule: the network stays attached only if the
+    # warm-started step is faster and still reaches the tolerance
+    from flowlab_gb300 import autotune
+
+    def meas(a):
+        return {"ms": 1000.0 / out[a]["steps_per_s"], "cycles": out[a]["vcycles_per_step"],
+                "rel_max": out[a]["rel_residual_max"]}
+
+    attach, reason = autotune.warm_start_pays(meas("plain"), meas("cnn"), prm.tol)
+    out["gate"] = {"attach": attach, "reason": reason}
     out["steps"] = args.cnn_steps
-    out["training"] = {k: meta[k] for k in ("pairs", "size", "batch", "lr", "train_seconds") if k in meta}
+    out["training"] = {k: meta[k] for k in ("pairs", "sizes", "pixels_per_step", "size", "batch", "lr", "train_seconds")
+                       if k in meta}
     return out
 
 

@@ -13,7 +13,11 @@ What it chooses, per scene shape and solver:
                  browser setting, a fixed budget, makes accuracy the
                  objective); then the sweep pairs per launch (rb_pairs: the
                  temporal-blocking depth, i.e. the tile/halo shape), whose
-                 results are identical, by time alone.
+                 results are identical, by time alone;
+  warm start     whether the learned warm start stays attached: only when
+                 the warm-started step is measured faster than the plain
+                 one on the scene itself (the network's forward pass must
+                 cost less than the V-cycles it saves).
 
 Results are cached in a JSON file keyed by solver, grid shape and precision.
 
@@ -44,10 +48,12 @@ def with_params(prm, **kw):
     return out
 
 
-def measure_steps(scene, prm, steps=8, warmup=3, device=0):
-    """Graph-path steps of a fresh engine on `scene` = (grid, fields, patch):
+def measure_steps(scene, prm, steps=8, warmup=3, device=0, net=None):
+    """Graph-path steps of a fresh engine on `scene` = (grid, fields, patch),
+    with the learned warm start `net` (a native.Unet) attached when given:
     mean device ms per step (CUDA events on the engine's stream), V-cycles per
-    step and the largest relative residual."""
+    step, the largest relative residual and the mean initial relative
+    residual (the warm start's, before any cycle)."""
     import torch
 
     g, f, patch = scene
@@ -57,9 +63,11 @@ def measure_steps(scene, prm, steps=8, warmup=3, device=0):
             eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
         eng.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
                  ptr(f32(f.dye)))
+        if net is not None:
+            eng.call("fl_set_warm_start", net.h)
         eng.call("fl_step_auto", warmup, None)
         stream = torch.cuda.ExternalStream(eng.stream(), device=device)
-        ms, cyc, rr = [], [], []
+        ms, cyc, rr, r0 = [], [], [], []
         for _ in range(steps):
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
@@ -70,7 +78,9 @@ def measure_steps(scene, prm, steps=8, warmup=3, device=0):
             ms.append(a.elapsed_time(b))
             cyc.append(st["cycles"])
             rr.append(st["rel_residual"])
-        return {"ms": float(np.mean(ms)), "cycles": float(np.mean(cyc)), "rel_max": float(max(rr))}
+            r0.append(st["initial_rel_residual"])
+        return {"ms": float(np.mean(ms)), "cycles": float(np.mean(cyc)), "rel_max": float(max(rr)),
+                "rel0_mean": float(np.mean(r0))}
     finally:
         eng.close()
 
@@ -82,6 +92,28 @@ def pick_multigrid(results, tol):
     if not ok:
         return None
     return min(ok, key=lambda cm: (cm[1]["ms"], sorted(cm[0].items())))
+
+
+def warm_start_pays(plain, warm, tol):
+    """Keep the learned warm start attached only if every warm-started step
+    reached `tol` and the warm-started step is faster; plain / warm are
+    measure_steps results. Returns (attach, reason)."""
+    if not (0 <= warm["rel_max"] <= tol):
+        return False, "the warm-started solve missed the tolerance"
+    saved = plain["cycles"] - warm["cycles"]
+    if warm["ms"] >= plain["ms"]:
+        return False, ("slower: %.3f against %.3f ms per step (%.2f V-cycles saved per step)"
+                       % (warm["ms"], plain["ms"], saved))
+    return True, "faster: %.3f against %.3f ms per step (%.2f V-cycles saved)" % (warm["ms"], plain["ms"], saved)
+
+
+def tune_warm_start(scene, prm, net, steps=8, warmup=3, device=0):
+    """Measures the scene with and without the network; the decision of
+    warm_start_pays with both measurements."""
+    plain = measure_steps(scene, prm, steps, warmup, device)
+    warm = measure_steps(scene, prm, steps, warmup, device, net=net)
+    attach, reason = warm_start_pays(plain, warm, prm.tol)
+    return {"attach": attach, "reason": reason, "plain": plain, "warm": warm}
 
 
 def pick_omega(results):

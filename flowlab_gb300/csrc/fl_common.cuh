@@ -88,6 +88,7 @@ struct SolveCtl {
   int nonfinite;     // a NaN/Inf showed up in the rhs or the residual
   int par;           // which float64 pressure buffer holds p
   int pad;
+  double rel0;       // the relative residual of the warm start, before any cycle (-1: not evaluated)
 };
 constexpr int SOLVE_MG = 0, SOLVE_MIXED = 1, SOLVE_RB = 2;
 

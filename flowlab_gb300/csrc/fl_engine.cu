@@ -779,6 +779,7 @@ int solve_stats(Engine* e) {
     e->last_iters = c.cycles;
     e->last_relres = c.rel;
   }
+  e->last_relres0 = c.mode == SOLVE_MIXED ? c.rel0 : -1;
   if (c.nonfinite) return fail(e, FL_ENONFINITE, "non-finite %s", c.cycles ? "residual" : "divergence");
   if (e->warm != nullptr && unet_tc_take_error())
     return fail(e, FL_ETIMEOUT, "the warm start's tensor-core convolution gave up a bounded wait");
@@ -1320,6 +1321,7 @@ int fl_get_stats(fl_engine* h, fl_stats* out) {
   TRY(sync(e, "stats"));
   const DiagAccum& d = *e->diag_host;
   out->post_div_step = d.last_step;
+  out->initial_rel_residual = e->last_relres0;
   out->post_div_rms = d.last_step >= 0 ? rms(d.div_sq, d.n_fluid) : 0.0;
   std::memcpy(&m, &d.div_max_bits, 4);
   out->post_div_max = d.last_step >= 0 ? m : 0.0;

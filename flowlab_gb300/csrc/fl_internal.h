@@ -140,6 +140,7 @@ struct Engine {
   int steps = 0;
   int last_iters = 0;
   double last_relres = -1;
+  double last_relres0 = -1;
   double last_div_rms = 0;
   double last_dt = 0, last_scale = 0, last_grad_scale = 0;
 

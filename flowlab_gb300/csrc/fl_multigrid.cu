@@ -973,6 +973,7 @@ __global__ void k_solve_begin(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaG
     ctl->rel = -1.0;
     cont = ctl->max_cycles > 0;
   }
+  ctl->rel0 = ctl->rel;
   acc->res_sq = 0.0;
   acc->n_res = 0ull;
   ctl->cont = cont;

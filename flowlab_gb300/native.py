@@ -77,6 +77,7 @@ class Stats(ctypes.Structure):
         ("post_div_rms", ctypes.c_double),
         ("post_div_max", ctypes.c_double),
         ("post_div_step", ctypes.c_longlong),
+        ("initial_rel_residual", ctypes.c_double),
     ]
 
 

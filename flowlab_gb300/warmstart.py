@@ -6,8 +6,11 @@ Training pairs come from the engine itself: each step of a running scene
 gives the step's right-hand side b, the warm start p_prev it started from
 and the converged pressure p_conv the multigrid reached, and the target is
 (p_conv - p_prev) / s_p on fluid cells. Scenes: the thermal plume, the
-turbulence grid and seeded batched-scene members at one training size,
-each restarted (new seed) after a fixed number of steps.
+turbulence grid and seeded batched-scene members at every training size
+(256^2, 512^2 and 1024^2 by default), each restarted (new seed) after a
+fixed number of steps; a training step takes one size, as many pairs as
+fill its pixel budget (16 at 256^2, 4 at 512^2, 1 at 1024^2), the sizes
+in turn.
 
   python -m flowlab_gb300.warmstart train --pairs 20000 --out weights.npz
   python -m flowlab_gb300.warmstart evaluate --weights weights.npz
@@ -146,31 +149,44 @@ def he_init(seed=0):
     return np.concatenate(chunks)
 
 
-def train(pairs=20000, size=256, batch=4, lr=1e-3, seed=0, log=None, params=None):
+def train(pairs=20000, sizes=(256, 512, 1024), pixels=1 << 20, lr=1e-3, seed=0, log=None, params=None):
     """Trains a fresh network (or `params`) on `pairs` pairs generated while
-    training, each used once, in batches; returns (network, per-step losses)."""
-    net = native.Unet(batch * size * size)
+    training, each used once. Training steps take the sizes in turn, each
+    with a batch of pixels // size^2 pairs of that size (at least one), the
+    pairs drawn in turn from that size's plume, turbulence-grid and two
+    batched-scene sources. Returns (network, per-step losses)."""
+    net = native.Unet(max(pixels, max(sizes) ** 2))
     net.set_params(he_init(seed) if params is None else params)
     kinds = ["plume", "turbulence", "random", "random"]
-    sources = [PairSource(k, size, seed + 17 * i) for i, k in enumerate(kinds)]
+    sources = {n: [PairSource(k, n, seed + 17 * i + 1000003 * j) for i, k in enumerate(kinds)]
+               for j, n in enumerate(sizes)}
+    turn = {n: 0 for n in sizes}
     losses = []
     t0 = time.time()
+    done = s = 0
     try:
-        steps = pairs // batch
-        for s in range(steps):
+        while done < pairs:
+            n = sizes[s % len(sizes)]
+            batch = min(max(1, pixels // (n * n)), pairs - done)
             xs, ts, ms = [], [], []
-            for k in range(batch):
-                x, t, m = sources[(s * batch + k) % len(sources)].pair()
+            for _ in range(batch):
+                src = sources[n][turn[n] % len(kinds)]
+                turn[n] += 1
+                x, t, m = src.pair()
                 xs.append(x)
                 ts.append(t)
                 ms.append(m)
             loss = net.train_step(np.stack(xs), np.stack(ts), np.stack(ms), lr=lr)
             losses.append(loss)
-            if log and (s % 100 == 0 or s == steps - 1):
-                log("step %d/%d loss %.4g (%.0f s)" % (s + 1, steps, float(np.mean(losses[-100:])), time.time() - t0))
+            done += batch
+            s += 1
+            if log and s % 100 == 0:
+                log("step %d, %d/%d pairs, loss %.4g (%.0f s)" % (s, done, pairs, float(np.mean(losses[-100:])),
+                                                                   time.time() - t0))
     finally:
-        for src in sources:
-            src.close()
+        for srcs in sources.values():
+            for src in srcs:
+                src.close()
     return net, losses
 
 
@@ -266,8 +282,8 @@ def main(argv=None):
     sub = ap.add_subparsers(dest="cmd", required=True)
     t = sub.add_parser("train")
     t.add_argument("--pairs", type=int, default=20000)
-    t.add_argument("--size", type=int, default=256)
-    t.add_argument("--batch", type=int, default=4)
+    t.add_argument("--sizes", default="256,512,1024", help="training grid sides, taken in turn")
+    t.add_argument("--pixels", type=int, default=1 << 20, help="pixels per training step (batch = pixels // side^2)")
     t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--seed", type=int, default=0)
     t.add_argument("--out", default=DEFAULT_WEIGHTS)
@@ -287,10 +303,11 @@ def main(argv=None):
     build.build()
     if a.cmd == "train":
         t0 = time.time()
-        net, losses = train(a.pairs, a.size, a.batch, a.lr, a.seed, log=lambda m: print(m, flush=True))
+        sizes = tuple(int(x) for x in a.sizes.split(","))
+        net, losses = train(a.pairs, sizes, a.pixels, a.lr, a.seed, log=lambda m: print(m, flush=True))
         params = net.get_params()
         net.close()
-        meta = {"pairs": a.pairs, "size": a.size, "batch": a.batch, "lr": a.lr, "seed": a.seed,
+        meta = {"pairs": a.pairs, "sizes": list(sizes), "pixels_per_step": a.pixels, "lr": a.lr, "seed": a.seed,
                 "train_seconds": time.time() - t0, "loss_first100": float(np.mean(losses[:100])),
                 "loss_last100": float(np.mean(losses[-100:]))}
         if a.eval_size:

@@ -121,6 +121,10 @@ typedef struct fl_stats {
   double post_div_rms;
   double post_div_max;
   long long post_div_step;
+  /* The relative residual of the last solve's starting pressure (the warm
+   * start), before any cycle: evaluated by the defect-correction solve
+   * (fl_params.mixed), -1 otherwise. What a better warm start lowers. */
+  double initial_rel_residual;
 } fl_stats;
 
 /* Per-phase device timing of fused steps, from CUDA events recorded on the

@@ -46,7 +46,7 @@ def test_abi_version_and_defaults(lib):
     assert p.mg_tail_side == 0  # the engine's default first tail level (32)
     assert native.Params.mg_tail_side.offset == 140 and native.Params.residual_every.offset == 144
     assert native.Params.reserved.offset == 148
-    assert ctypes.sizeof(native.Stats) == 88 and native.Stats.post_div_step.offset == 80
+    assert ctypes.sizeof(native.Stats) == 96 and native.Stats.initial_rel_residual.offset == 88
 
 
 def test_python_defaults_equal_the_library_defaults(lib):

@@ -42,3 +42,15 @@ def test_tail_side_chosen_by_time_after_the_constants(monkeypatch):
     assert best == {"mg_coarsest": 4, "mg_coarse_sweeps": 8, "mg_tail_side": 32}
     assert len(results) == 12
     assert seen[-3:] == [(4, 8, 16), (4, 8, 32), (4, 8, 64)]
+
+
+def test_warm_start_gate():
+    """The learned warm start stays attached only when it makes the step
+    faster and still reaches the tolerance."""
+    plain = {"ms": 0.58, "cycles": 4.2, "rel_max": 9e-7, "rel0_mean": 6e-3}
+    slow = {"ms": 1.33, "cycles": 4.2, "rel_max": 9e-7, "rel0_mean": 4e-3}
+    fast = {"ms": 0.50, "cycles": 3.0, "rel_max": 9e-7, "rel0_mean": 4e-4}
+    missed = {"ms": 0.40, "cycles": 3.0, "rel_max": 2e-6, "rel0_mean": 4e-4}
+    assert autotune.warm_start_pays(plain, slow, 1e-6)[0] is False
+    assert autotune.warm_start_pays(plain, fast, 1e-6)[0] is True
+    assert autotune.warm_start_pays(plain, missed, 1e-6)[0] is False
