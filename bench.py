@@ -79,8 +79,9 @@ def phase_bytes_per_cell(prm, size, tail_side=32):
     the way down and 10 (prolongation) + 3 x 18 on the way up. MacCormack
     velocity: forward 13 + 13 (u, v faces), correction 17 + 17; MacCormack
     dye: forward 33, correction 45; divergence 12 (u, v in, div out);
-    subtract + outflow 21; the CFL scan 8; the residual-diagnostic
-    divergence 13 (with the labels); the defect correction's residual
+    subtract + outflow 21; the CFL scan 8, plus 13 (the labels in, the
+    divergence out) on the residual diagnostic's steps; the defect
+    correction's residual
     x 8 + b 4 + label 1 + r 8 = 21; buoyancy (alpha, beta) 17 and
     confinement 25 per step. The coarser smoother levels (levels above the
     single-CTA tail) are summed over their sizes, per launch averaged."""
@@ -101,8 +102,9 @@ def phase_bytes_per_cell(prm, size, tail_side=32):
         "defect64": 21,
         "project": 21,
         "advect_dye": 78 / 2 if prm.scheme == 1 else 33,
-        "cfl": 8,
-        "residual": 13 / 2,
+        # the CFL scan, with the residual diagnostic's divergence (13) on
+        # the steps it runs
+        "cfl": 8 + (13.0 / prm.residual_every if prm.residual_every > 0 else 0),
     }
     return out
 

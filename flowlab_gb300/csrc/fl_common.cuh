@@ -64,12 +64,18 @@ struct StepAccum {
 // recomputed on steps whose index is a multiple of residual_every, and its
 // FLUID-cell statistics (viz/fieldView.ts:44-60).
 struct DiagAccum {
+  // sums of the step in progress (zeroed again once a step's are final)
   double div_sq;               // sum div^2 over fluid cells
   unsigned long long n_fluid;
-  unsigned long long counter;  // steps begun since the engine was created
-  long long last_step;         // index of the step that computed it (-1: none)
   unsigned int div_max_bits;   // max |div| over fluid cells as float bits
-  int on;                      // the current step computes it
+  unsigned int blocks_done;    // last-block detection
+  unsigned long long counter;  // steps finished since the engine was created
+  // the last step that computed it
+  double last_sq;
+  unsigned long long last_n;
+  long long last_step;         // its index (-1: none)
+  unsigned int last_max_bits;
+  int pad;
 };
 
 // Device-side state of one pressure solve, so that the cycle loop can run

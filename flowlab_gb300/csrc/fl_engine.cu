@@ -493,48 +493,6 @@ void enqueue_rb_fixed(Engine* e, cudaStream_t s) {
   launch_zero_if(s, e->ctl, L.x[0], nullptr, nullptr, e->cells());
 }
 
-// The residual diagnostic after the projection (simulation.ts:539-540): the
-// step's decision and, when on, the post-step divergence. Captured, the
-// divergence kernel is the body of an IF node that only the deciding
-// kernel opens; eagerly it runs and returns at once on steps left off.
-cudaError_t enqueue_diag(Engine* e, cudaStream_t s, const float* u, const float* v) {
-  if (e->prm.residual_every <= 0) return cudaSuccess;
-  const bool cap = capturing(s);
-  cudaGraphConditionalHandle h = 0;
-  cudaGraph_t graph = nullptr;
-  cudaStreamCaptureStatus cst;
-  bool cond = false;
-  if (cap && cudaStreamGetCaptureInfo(s, &cst, nullptr, &graph, nullptr, nullptr, nullptr) == cudaSuccess &&
-      cudaGraphConditionalHandleCreate(&h, graph, 0, cudaGraphCondAssignDefault) == cudaSuccess)
-    cond = true;
-  launch_diag_begin(s, e->diag, e->prm.residual_every, cond, h);
-  if (!cond) {
-    launch_post_divergence(s, e->nx, e->ny, e->h, u, v, e->div_post, e->levels[0].label, e->diag);
-    return cudaSuccess;
-  }
-  const cudaGraphNode_t* deps = nullptr;
-  size_t ndeps = 0;
-  cudaError_t err = cudaStreamGetCaptureInfo(s, &cst, nullptr, &graph, &deps, nullptr, &ndeps);
-  cudaGraphNodeParams cp{};
-  cp.type = cudaGraphNodeTypeConditional;
-  cp.conditional.handle = h;
-  cp.conditional.type = cudaGraphCondTypeIf;
-  cp.conditional.size = 1;
-  cudaGraphNode_t node = nullptr;
-  if (err == cudaSuccess) err = cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &cp);
-  if (err == cudaSuccess) err = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
-  // the body is captured from the second stream
-  if (err == cudaSuccess)
-    err = cudaStreamBeginCaptureToGraph(e->stream2, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                        cudaStreamCaptureModeThreadLocal);
-  if (err == cudaSuccess) {
-    launch_post_divergence(e->stream2, e->nx, e->ny, e->h, u, v, e->div_post, e->levels[0].label, e->diag);
-    cudaGraph_t done = nullptr;
-    err = cudaStreamEndCapture(e->stream2, &done);
-  }
-  return err;
-}
-
 // subtract gradient + outflow -> dye (advect, decay, inlet) -> CFL
 cudaError_t enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
   Level& L0 = e->levels[0];
@@ -550,10 +508,6 @@ cudaError_t enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
   // velocity and pressure are final: fl_step_host reads them back from here
   // on while the dye advection runs
   cudaEventRecordWithFlags(e->ev_proj, s, capturing(s) ? cudaEventRecordExternal : 0);
-  tok = prof_begin(*e, FL_PH_RESIDUAL);
-  const cudaError_t err = enqueue_diag(e, s, u, v);
-  // u, v, label in; div out
-  prof_end(*e, tok, e->prm.residual_every > 0 ? 4 * F + N + 4 * N : 0, e->prm.residual_every > 0 ? 2 : 0);
   wait_dye(e, s);
   tok = prof_begin(*e, FL_PH_ADVECT_DYE);
   launch_advect_dye(s, e->nx, e->ny, e->h, e->dnx, e->dny, e->dh, mac, u, v, e->dye[par], e->dye_hat, e->dye[1 - par],
@@ -562,9 +516,17 @@ cudaError_t enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
   // positions out); correction adds the hat planes and the positions
   prof_end(*e, tok, mac ? (4 * F + 32 * D + N) + (4 * F + 44 * D + N) : 4 * F + 24 * D + N, mac ? 2 : 1);
   tok = prof_begin(*e, FL_PH_CFL);
-  launch_max_speed(s, e->nx, e->ny, u, v, e->acc, e->sc, e->time_dev, &e->prm, e->h, device_dt, device_dt);
-  prof_end(*e, tok, 4 * F, 1);
-  return err;
+  if (e->prm.residual_every > 0) {
+    // with the residual diagnostic (simulation.ts:539-540) on its cadence
+    launch_cfl_residual(s, e->nx, e->ny, e->h, u, v, e->div_post, L0.label, e->prm.residual_every, e->diag, e->acc,
+                        e->sc, e->time_dev, &e->prm, device_dt, device_dt);
+    // u, v in; on diagnostic steps labels in and the divergence out
+    prof_end(*e, tok, 4 * F + N + 4 * N, 1);
+  } else {
+    launch_max_speed(s, e->nx, e->ny, u, v, e->acc, e->sc, e->time_dev, &e->prm, e->h, device_dt, device_dt);
+    prof_end(*e, tok, 4 * F, 1);
+  }
+  return cudaSuccess;
 }
 
 // Red-black SOR to a tolerance (pressureRedBlack.ts:88-113): checked every
@@ -1322,8 +1284,8 @@ int fl_get_stats(fl_engine* h, fl_stats* out) {
   const DiagAccum& d = *e->diag_host;
   out->post_div_step = d.last_step;
   out->initial_rel_residual = e->last_relres0;
-  out->post_div_rms = d.last_step >= 0 ? rms(d.div_sq, d.n_fluid) : 0.0;
-  std::memcpy(&m, &d.div_max_bits, 4);
+  out->post_div_rms = d.last_step >= 0 ? rms(d.last_sq, d.last_n) : 0.0;
+  std::memcpy(&m, &d.last_max_bits, 4);
   out->post_div_max = d.last_step >= 0 ? m : 0.0;
   return FL_OK;
 }

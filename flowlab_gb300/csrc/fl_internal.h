@@ -190,11 +190,12 @@ void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, fl
 void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
                        bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc,
                        float* out_lo = nullptr);
-// The residual diagnostic: the step's decision (and counter; with a graph
-// handle, the IF node's condition), then the post-step divergence when on.
-void launch_diag_begin(cudaStream_t s, DiagAccum* d, int every, bool use_cond, cudaGraphConditionalHandle h);
-void launch_post_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
-                            const uint8_t* label, DiagAccum* d);
+// The end-of-step CFL scan with the residual diagnostic folded in (every
+// residual_every steps: the post-step divergence and its statistics); the
+// step's dt joins the clock and the next step's scalars are written.
+void launch_cfl_residual(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* div_out,
+                         const uint8_t* label, int every, DiagAccum* d, StepAccum* acc, StepScalars* sc_next,
+                         double* time_dev, const fl_params* prm, bool write_scalars, bool add_time);
 // p64a/p64b: the refined pressure (float64, or double-float pairs when df)
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
                              const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow,

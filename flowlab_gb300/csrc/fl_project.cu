@@ -266,6 +266,28 @@ __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const 
 // max |u|, |v| over every face (simulation.ts:451-459). The last block to
 // finish turns it into the next step's scalars (simulation.ts:474-479,
 // 243-247) and adds this step's dt to the device clock — no host round trip.
+// The next step's scalars from the max face speed: simulation.ts:477-479,
+// evaluated in float32 in the reference's order, and the per-channel keep
+// factors of the dye decay (simulation.ts:243-247).
+__device__ StepScalars cfl_scalars(float umax, float h, float cfl, float dt_max, float rho, double d0, double d1,
+                                   double d2, float beta, float alpha) {
+  const float dt = umax > 1e-9f ? smin(dt_max, (cfl * h) / umax) : dt_max;
+  StepScalars s;
+  s.dt = dt;
+  s.scale = (rho * h * h) / dt;
+  s.grad_scale = dt / (rho * h);
+  const double dd = (double)dt;
+  s.keep[0] = d0 > 0 ? (float)exp(-d0 * dd) : 1.0f;
+  s.keep[1] = d1 > 0 ? (float)exp(-d1 * dd) : 1.0f;
+  s.keep[2] = d2 > 0 ? (float)exp(-d2 * dd) : 1.0f;
+  s.gain_beta = beta * dt;
+  s.gain_alpha = -alpha * dt;
+  s.half_dt = 0.5f * dt;
+  s.neg_scale = -s.scale;
+  for (int q = 0; q < 6; q++) s.pad[q] = 0;
+  return s;
+}
+
 __global__ void __launch_bounds__(256) k_max_speed(long nu, long nv, const float* __restrict__ u,
                                                    const float* __restrict__ v, StepAccum* acc,
                                                    StepScalars* sc_next, double* time_dev, float h, float cfl,
@@ -307,22 +329,7 @@ __global__ void __launch_bounds__(256) k_max_speed(long nu, long nv, const float
   // the clock before the scalars are replaced (simulation.ts:585).
   if (add_time && time_dev) *time_dev += (double)sc_next->dt;
   if (!write_scalars) return;
-  // simulation.ts:477-479, evaluated in float32 in the reference's order.
-  const float dt = umax > 1e-9f ? smin(dt_max, (cfl * h) / umax) : dt_max;
-  StepScalars s;
-  s.dt = dt;
-  s.scale = (rho * h * h) / dt;
-  s.grad_scale = dt / (rho * h);
-  const double dd = (double)dt;
-  s.keep[0] = d0 > 0 ? (float)exp(-d0 * dd) : 1.0f;
-  s.keep[1] = d1 > 0 ? (float)exp(-d1 * dd) : 1.0f;
-  s.keep[2] = d2 > 0 ? (float)exp(-d2 * dd) : 1.0f;
-  s.gain_beta = beta * dt;
-  s.gain_alpha = -alpha * dt;
-  s.half_dt = 0.5f * dt;
-  s.neg_scale = -s.scale;
-  for (int q = 0; q < 6; q++) s.pad[q] = 0;
-  *sc_next = s;
+  *sc_next = cfl_scalars(umax, h, cfl, dt_max, rho, d0, d1, d2, beta, alpha);
 }
 
 // b = (-scale) * div with the fluid sum of squares (pressureMultigrid.ts:311,
@@ -476,78 +483,6 @@ void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, fl
                                                   conf_on, fx, fy, sc);
 }
 
-// ------------------------------------------------- residual diagnostic
-
-// Decides whether this step recomputes the post-step divergence
-// (simulation.ts:539: residualEvery > 0 && steps % residualEvery === 0,
-// `steps` counting every step ever taken) and counts the step; with a
-// graph handle it also opens or closes the IF node around the kernel below.
-__global__ void k_diag_begin(DiagAccum* d, int every, int use_cond, cudaGraphConditionalHandle h) {
-  const unsigned long long c = d->counter;
-  const int on = every > 0 && c % (unsigned long long)every == 0;
-  d->counter = c + 1;
-  d->on = on;
-  if (on) {
-    d->div_sq = 0;
-    d->n_fluid = 0;
-    d->div_max_bits = 0;
-    d->last_step = (long long)c;
-  }
-  if (use_cond) cudaGraphSetConditional(h, on ? 1u : 0u);
-}
-
-// computeDivergence (divergence.ts:17-25) of the projected velocity into
-// `out` (every cell), with the sum of squares and the max of |div| over
-// FLUID cells (divergenceStats, viz/fieldView.ts:44-60). A no-op on steps
-// k_diag_begin left off.
-__global__ void __launch_bounds__(256) k_post_divergence(int nx, int ny, float h, const float* __restrict__ u,
-                                                         const float* __restrict__ v, float* __restrict__ out,
-                                                         const uint8_t* __restrict__ label, DiagAccum* d) {
-  __shared__ double red[32];
-  __shared__ unsigned long long redn[32];
-  __shared__ float redm[32];
-  if (!d->on) return;  // the same for every thread
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  float2 sq = make_float2(0.0f, 0.0f);
-  unsigned long long n = 0;
-  float mx = 0.0f;
-  const float coef = 1.0f / h;
-  for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
-    if (i >= nx) break;
-    const long k = i + (long)j * nx;
-    const float dv = coef * (u[(i + 1) + (long)j * (nx + 1)] - u[i + (long)j * (nx + 1)] + v[i + (long)(j + 1) * nx] -
-                             v[i + (long)j * nx]);
-    out[k] = dv;
-    if (label[k] == FLUID) {
-      const float q = __fmul_rn(dv, dv);
-      sq = df_add(sq, make_float2(q, __fmaf_rn(dv, dv, -q)));
-      mx = fmaxf(mx, fabsf(dv));
-      n += 1;
-    }
-  }
-  const double bs = block_sum(df_to_double(sq), red);
-  const unsigned long long bn = block_sum_u64(n, redn);
-  const float bm = block_max(mx, redm);
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    atomicAdd(&d->div_sq, bs);
-    atomicAdd(&d->n_fluid, bn);
-    // non-negative floats order as their bits
-    atomicMax(&d->div_max_bits, __float_as_uint(bm));
-  }
-}
-
-void launch_diag_begin(cudaStream_t s, DiagAccum* d, int every, bool use_cond, cudaGraphConditionalHandle h) {
-  k_diag_begin<<<1, 1, 0, s>>>(d, every, use_cond, h);
-}
-
-void launch_post_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
-                            const uint8_t* label, DiagAccum* d) {
-  dim3 b(32, 8);
-  dim3 g = grid2(nx, ny, b);
-  g.y = std::min(g.y, std::max(1u, 1024u / g.x));
-  k_post_divergence<<<g, b, 0, s>>>(nx, ny, h, u, v, out, label, d);
-}
-
 void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
                        bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc, float* out_lo) {
   dim3 b(32, 8);
@@ -570,6 +505,107 @@ void launch_scale_rhs(cudaStream_t s, long n, const float* div, float* b, float 
   if (blocks > 152 * 8) blocks = 152 * 8;
   if (blocks < 1) blocks = 1;
   k_scale_rhs<<<(unsigned)blocks, 256, 0, s>>>(n, div, b, neg_scale, label, acc, b_lo);
+}
+
+// The end-of-step scan with the residual diagnostic folded in: each thread
+// owns a cell and reads its four faces once, which covers every face, for
+// the max face speed of the next step's CFL dt (as k_max_speed); on the
+// steps the diagnostic runs (simulation.ts:539: residualEvery > 0 &&
+// steps % residualEvery === 0, `steps` counting every step taken) it also
+// writes the post-step divergence (divergence.ts:17-25) of every cell and
+// sums its square and max over FLUID cells (viz/fieldView.ts:44-60). The
+// last block finishes the CFL scalars, publishes the diagnostic's sums and
+// counts the step.
+__global__ void __launch_bounds__(256) k_cfl_residual(int nx, int ny, float h, const float* __restrict__ u,
+                                                      const float* __restrict__ v, float* __restrict__ div_out,
+                                                      const uint8_t* __restrict__ label, int every, DiagAccum* d,
+                                                      StepAccum* acc, StepScalars* sc_next, double* time_dev,
+                                                      float cfl, float dt_max, float rho, double d0, double d1,
+                                                      double d2, float beta, float alpha, int write_scalars,
+                                                      int add_time) {
+  __shared__ double red[32];
+  __shared__ unsigned long long redn[32];
+  __shared__ float redm[32];
+  __shared__ bool last;
+  const unsigned long long step = d->counter;  // advanced only by the last block, after every block read it
+  const bool on = every > 0 && step % (unsigned long long)every == 0;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float m = 0.0f, mx = 0.0f;
+  float2 sq = make_float2(0.0f, 0.0f);
+  unsigned long long n = 0;
+  const float coef = 1.0f / h;
+  for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
+    if (i >= nx) break;
+    const long ku = i + (long)j * (nx + 1), kv = i + (long)j * nx;
+    const float u0 = u[ku], u1 = u[ku + 1], v0 = v[kv], v1 = v[kv + nx];
+    m = smax(m, smax(smax(fabsf(u0), fabsf(u1)), smax(fabsf(v0), fabsf(v1))));
+    if (on) {
+      const float dv = coef * (u1 - u0 + v1 - v0);
+      div_out[kv] = dv;
+      if (label[kv] == FLUID) {
+        const float q = __fmul_rn(dv, dv);
+        sq = df_add(sq, make_float2(q, __fmaf_rn(dv, dv, -q)));
+        mx = fmaxf(mx, fabsf(dv));
+        n += 1;
+      }
+    }
+  }
+  const float bm = block_max(m, redm);
+  double bs = 0.0;
+  unsigned long long bn = 0;
+  float bx = 0.0f;
+  if (on) {  // the same for the whole block
+    bs = block_sum(df_to_double(sq), red);
+    bn = block_sum_u64(n, redn);
+    __syncthreads();
+    bx = block_max(mx, redm);
+  }
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  const unsigned nblocks = gridDim.x * gridDim.y;
+  if (tid == 0) {
+    atomicMax(&acc->max_speed_bits, __float_as_uint(bm));
+    if (on) {
+      atomicAdd(&d->div_sq, bs);
+      atomicAdd(&d->n_fluid, bn);
+      // non-negative floats order as their bits
+      atomicMax(&d->div_max_bits, __float_as_uint(bx));
+    }
+    __threadfence();
+    const unsigned done = atomicAdd(&acc->blocks_done, 1u);
+    last = done == nblocks - 1;
+  }
+  __syncthreads();
+  if (!last || tid != 0) return;
+  __threadfence();
+  if (on) {
+    d->last_sq = d->div_sq;
+    d->last_n = d->n_fluid;
+    d->last_max_bits = d->div_max_bits;
+    d->last_step = (long long)step;
+    d->div_sq = 0.0;
+    d->n_fluid = 0ull;
+    d->div_max_bits = 0u;
+  }
+  d->counter = step + 1;
+  const float umax = __uint_as_float(atomicExch(&acc->max_speed_bits, 0u));
+  acc->blocks_done = 0u;
+  acc->last_max_bits = __float_as_uint(umax);
+  // the step that just finished ran with the current scalars: its dt joins
+  // the clock before the scalars are replaced (simulation.ts:585)
+  if (add_time && time_dev) *time_dev += (double)sc_next->dt;
+  if (write_scalars) sc_next[0] = cfl_scalars(umax, h, cfl, dt_max, rho, d0, d1, d2, beta, alpha);
+}
+
+void launch_cfl_residual(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* div_out,
+                         const uint8_t* label, int every, DiagAccum* d, StepAccum* acc, StepScalars* sc_next,
+                         double* time_dev, const fl_params* prm, bool write_scalars, bool add_time) {
+  dim3 b(32, 8);
+  dim3 g = grid2(nx, ny, b);
+  g.y = std::min(g.y, std::max(1u, 1024u / g.x));
+  k_cfl_residual<<<g, b, 0, s>>>(nx, ny, h, u, v, div_out, label, every, d, acc, sc_next, time_dev,
+                                 (float)prm->cfl_target, (float)prm->dt_max, (float)prm->rho, prm->dye_decay[0],
+                                 prm->dye_decay[1], prm->dye_decay[2], (float)prm->beta, (float)prm->alpha,
+                                 write_scalars, add_time);
 }
 
 void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const float* v, StepAccum* acc,

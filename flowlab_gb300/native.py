@@ -84,8 +84,7 @@ class Stats(ctypes.Structure):
 ABI_VERSION = 3  # FL_ABI_VERSION
 
 PHASES = ["advect_velocity", "body_forces", "divergence", "mg_pre_fine", "mg_pre", "mg_coarse", "mg_post",
-          "mg_post_fine", "defect64", "rb_sweeps", "project", "advect_dye", "cfl", "control", "warm_start",
-          "residual"]
+          "mg_post_fine", "defect64", "rb_sweeps", "project", "advect_dye", "cfl", "control", "warm_start"]
 
 
 class Profile(ctypes.Structure):

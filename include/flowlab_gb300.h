@@ -136,17 +136,17 @@ typedef struct fl_stats {
  * engine attributes to the phase: each array a kernel must read or write,
  * counted once per launch. No counterpart in the reference (its profiler is
  * host-side phase timing, src/core/profiler.ts:39-113). */
-#define FL_PHASES 16
+#define FL_PHASES 15
 /* phase indices: the multigrid phases separate the finest level's smoother
  * launches from the coarser levels'; CONTROL is the one-thread solve-control
  * kernels (tolerance test, cycle decision) and the p = 0 fill; WARM_START
  * is the learned warm start (input, network, correction) when attached;
- * RESIDUAL is the post-step divergence diagnostic (residual_every). */
+ * CFL is the end-of-step scan, which also runs the post-step divergence
+ * diagnostic (residual_every). */
 enum fl_phase {
   FL_PH_ADVECT_VELOCITY = 0, FL_PH_BODY_FORCES = 1, FL_PH_DIVERGENCE = 2, FL_PH_MG_PRE_FINE = 3, FL_PH_MG_PRE = 4,
   FL_PH_MG_COARSE = 5, FL_PH_MG_POST = 6, FL_PH_MG_POST_FINE = 7, FL_PH_DEFECT64 = 8, FL_PH_RB_SWEEPS = 9,
-  FL_PH_PROJECT = 10, FL_PH_ADVECT_DYE = 11, FL_PH_CFL = 12, FL_PH_CONTROL = 13, FL_PH_WARM_START = 14,
-  FL_PH_RESIDUAL = 15
+  FL_PH_PROJECT = 10, FL_PH_ADVECT_DYE = 11, FL_PH_CFL = 12, FL_PH_CONTROL = 13, FL_PH_WARM_START = 14
 };
 typedef struct fl_profile {
   double ms[FL_PHASES];

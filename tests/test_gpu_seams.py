@@ -264,17 +264,20 @@ def test_solver_ladder(o32, o64, karman_problem):
     p0 = np.zeros(n)
     peak = lambda a: float(np.abs(a).max())
     ctx = engine.init_gpu()
-    # converged references in float64: lexicographic (cpu-sor), red-black
-    # (cpu-rbsor), multigrid (cpu-mg)
+    # converged references in float64: red-black (cpu-rbsor) and multigrid
+    # (cpu-mg) to 1e-12; lexicographic SOR with its four sweep directions
+    # (cpu-sor) converges slowest on this channel (at the optimal omega it
+    # stalls near 2e-6; at 1.9 it reaches ~3e-8 in 20000 sweeps)
+    rel = lambda p: o64.rms_remaining(nx, ny, p, div, label, scale) / o64.fluid_div_rms(div, label)
     w = engine.optimal_omega(nx, ny)
-    p_sor, _ = o64.sor_solve(nx, ny, p0, div, label, scale, 20000, w, 1e-12)
     p_rb, _ = o64.rb_solve(nx, ny, p0, div, label, scale, 20000, w, 1e-12)
     p_mg, _, rr = o64.mg_solve(nx, ny, p0, div, label, scale, 60, 1e-12)
-    assert rr <= 1e-12
+    p_sor, _ = o64.sor_solve(nx, ny, p0, div, label, scale, 20000, 1.9, 1e-12)
+    assert rr <= 1e-12 and rel(p_rb) <= 1e-12 and rel(p_sor) <= 1e-7
     # ordering: lexicographic and red-black converge to the same pressure
-    assert np.abs(p_sor - p_rb).max() <= 1e-8 * peak(p_rb)
+    assert np.abs(p_sor - p_rb).max() <= 1e-6 * peak(p_rb)
     # algorithm: multigrid and red-black converge to the same pressure
-    assert np.abs(p_mg - p_rb).max() <= 1e-8 * peak(p_rb)
+    assert np.abs(p_mg - p_rb).max() <= 1e-10 * peak(p_rb)
 
     # red-black on a fixed budget (the reference's GPU use): float64 ->
     # float32 (precision), float32 oracle -> gpu-rbsor (plumbing: identical)
