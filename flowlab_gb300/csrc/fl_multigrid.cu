@@ -189,8 +189,24 @@ struct Tile {
   static constexpr int T = R - 2 * H;  // tile side, even
 };
 
-template <int P, int MODE, int R>
-__global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs a) {
+// Loads of data an earlier phase of the same launch may have written (the
+// persistent solve): through L2 only, so that no stale L1 line is read.
+// Otherwise plain loads, and the read-only path for the coarse correction.
+template <bool COH>
+__device__ __forceinline__ float ld_coherent(const float* p) {
+  if constexpr (COH) return __ldcg(p);
+  return *p;
+}
+template <bool COH>
+__device__ __forceinline__ float ld_ro(const float* p) {
+  if constexpr (COH) return __ldcg(p);
+  return __ldg(p);
+}
+
+// One region of the temporally blocked smoother, region (bx, by) of the
+// level; called by one whole block (every thread, in step).
+template <int P, int MODE, int R, bool COH>
+__device__ __forceinline__ void smooth_tile(const SmoothArgs& a, int bx, int by) {
   constexpr int RGN = R;
   constexpr int RGN_T = R / 2;
   constexpr int H = Tile<P, MODE, R>::H;
@@ -199,7 +215,7 @@ __global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs
   __shared__ float xs[2][RGN][RGN / 2];
   __shared__ float rs[MODE == MODE_PRE ? RGN : 1][MODE == MODE_PRE ? RGN : 1];
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int X0 = blockIdx.x * T, Y0 = blockIdx.y * T;
+  const int X0 = bx * T, Y0 = by * T;
   const int GX = X0 - H, GY = Y0 - H;
   const int nx = a.nx, ny = a.ny;
 
@@ -216,8 +232,8 @@ __global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs
       if (gi >= 0 && gj >= 0 && gi < nx && gj < ny) {
         const long k = gi + (long)gj * nx;
         cd[r][o] = a.code[k];
-        bb[r][o] = a.b[k];
-        xx[r][o] = a.x_is_zero ? 0.0f : a.xin[k];
+        bb[r][o] = ld_coherent<COH>(a.b + k);
+        xx[r][o] = a.x_is_zero ? 0.0f : ld_coherent<COH>(a.xin + k);
         if (MODE == MODE_POST && (cd[r][o] & 3u) == FLUID) {
           // pressureMultigrid.ts:192-207 — x += 9/16, 3/16, 3/16, 1/16 of e
           const int I = gi >> 1, J = gj >> 1;
@@ -225,8 +241,9 @@ __global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs
           const int J2 = (gj & 1) ? min(J + 1, a.cny - 1) : max(J - 1, 0);
           const float* e = a.ec;
           const long cs = a.cnx;
-          xx[r][o] += 0.5625f * __ldg(e + I + J * cs) + 0.1875f * (__ldg(e + I2 + J * cs) + __ldg(e + I + J2 * cs)) +
-                      0.0625f * __ldg(e + I2 + J2 * cs);
+          xx[r][o] += 0.5625f * ld_ro<COH>(e + I + J * cs) +
+                      0.1875f * (ld_ro<COH>(e + I2 + J * cs) + ld_ro<COH>(e + I + J2 * cs)) +
+                      0.0625f * ld_ro<COH>(e + I2 + J2 * cs);
         }
       } else {
         cd[r][o] = CODE_OUTSIDE;
@@ -376,6 +393,11 @@ __global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs
       }
     }
   }
+}
+
+template <int P, int MODE, int R>
+__global__ void __launch_bounds__(R* R / 4, R == 64 ? 1 : 4) k_smooth(SmoothArgs a) {
+  smooth_tile<P, MODE, R, false>(a, blockIdx.x, blockIdx.y);
 }
 
 // ----------------------------------------------------- single-CTA coarse tail
