@@ -178,26 +178,50 @@ def test_warm_started_solve_reaches_the_tolerance(net):
 def test_trained_network_gains_over_the_previous_pressure():
     """The packaged, trained network against the reference's warm start (the
     previous step's pressure, pressureSolver.ts:28-30) on a plume the
-    training never saw (384^2, sources of sigma 6 cells): the solve starts
-    from a smaller relative residual (the gain the network exists for) and
-    still reaches the tolerance. The V-cycles saved are reported: at 1e-6
-    each V-cycle contracts the residual ~20x, so a cycle is saved only when
-    the start is ~10x better, which the network does not reach."""
+    training never saw (384^2, sources of sigma 6 cells): over 8 steps of a
+    running scene, its guess p_prev + s_p * net(b / s_b, mask, p_prev / s_p)
+    lies closer to the pressure the multigrid converges to than p_prev does
+    (the RMS error over fluid cells, the quantity the network is trained to
+    lower), and the warm-started solve still reaches the tolerance. The
+    V-cycles saved are reported, not required: at 1e-6 a V(3,3) cycle
+    contracts the residual ~20x, so a cycle is saved only by a guess ~10x
+    better than p_prev (tests/test_warmstart_bound.py)."""
     import os
     from flowlab_gb300 import autotune, warmstart
 
     if not os.path.exists(warmstart.DEFAULT_WEIGHTS):
         pytest.fail("the packaged network parameters are missing")
     params, meta = warmstart.load(warmstart.DEFAULT_WEIGHTS)
-    scene = configs.plume(384, sigma_cells=6.0)
+    n = 384
+    g, f, patch = configs.plume(n, sigma_cells=6.0)
     prm = configs.plume_params()
-    trained = native.Unet(384 * 384)
+    trained = native.Unet(n * n)
+    eng = native.Engine(g.nx, g.ny, g.h, params=prm)
     try:
         trained.set_params(params)
-        res = autotune.tune_warm_start(scene, prm, trained, steps=12, warmup=10)
+        eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+        eng.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
+                 ptr(f32(f.dye)))
+        eng.call("fl_step_auto", 10, None)
+        fl = f.label == 0
+        p = np.empty(n * n, np.float32)
+        b = np.empty(n * n, np.float32)
+        ratios = []
+        for _ in range(8):
+            eng.call("fl_read_pressure", native.FL_F32, ptr(p))
+            p_prev = p.copy()
+            eng.call("fl_step_auto", 1, None)
+            eng.call("fl_read_rhs", native.FL_F32, ptr(b))
+            eng.call("fl_read_pressure", native.FL_F32, ptr(p))
+            x, sb, sp = warmstart.features(b.reshape(n, n), f.label.reshape(n, n), p_prev.reshape(n, n))
+            out = trained.forward(x[None])[0].ravel()
+            guess = np.where(fl, p_prev + np.float32(sp) * out, p_prev)
+            ratios.append(np.linalg.norm((guess - p)[fl]) / np.linalg.norm((p_prev - p)[fl]))
+        res = autotune.tune_warm_start((g, f, patch), prm, trained, steps=8, warmup=10)
     finally:
+        eng.close()
         trained.close()
-    plain, warm = res["plain"], res["warm"]
-    print("plain", plain, "warm", warm, "gate", res["attach"], res["reason"])
-    assert 0 <= warm["rel_max"] <= prm.tol
-    assert 0 < warm["rel0_mean"] < 0.9 * plain["rel0_mean"], (warm, plain)
+    print("error ratio per step", ["%.3f" % r for r in ratios], "plain", res["plain"], "warm", res["warm"],
+          "gate", res["attach"], res["reason"])
+    assert 0 <= res["warm"]["rel_max"] <= prm.tol
+    assert float(np.mean(ratios)) < 0.95, ratios
