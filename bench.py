@@ -757,6 +757,7 @@ def run_batch(args, world, rank, local, pg):
         b.synchronize()
         alone_ms += a.elapsed_time(b) / 2
     bt = native.Batch(engines)
+    worklist = bt.worklist
     stream = torch.cuda.ExternalStream(bt.stream(), device=local)
     bt.step(args.warmup)
     torch.cuda.synchronize()
@@ -790,8 +791,13 @@ def run_batch(args, world, rank, local, pg):
         "data": "synthetic (seeded random closed-box scenes)",
         "config": {"workload": "%d closed-box scenes, sides 2^U{6..10} (%d cells), 0-12 discs, smoothed-noise "
                                "velocity, multigrid V(3,3) to 1e-6 (float32 fields and smoothing, float64 residual; "
-                               "cap 40 cycles), each scene's step graph on its own stream (%s hardware queues)"
-                               % (args.scenes, total_cells, os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8")),
+                               "cap 40 cycles), %s"
+                               % (args.scenes, total_cells,
+                                  "one graph per step: the scenes' solves as one launch per V-cycle phase over a "
+                                  "(scene, level, tile) work list, each scene's other passes as concurrent branches"
+                                  if worklist else "each scene's step graph on its own stream (%s hardware queues)"
+                                  % os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8")),
+                   "worklist": worklist,
                    "scenes": args.scenes, "cells": total_cells, "l2": "working set far above L2 (no flush)",
                    "parallelism": "scenes dealt to ranks by cost" if world > 1 else "single GPU"},
         "cell_updates_per_s": value * total_cells,

@@ -635,6 +635,7 @@ void destroy_step_graphs(Engine* e) {
     g = nullptr;
   }
   e->graphs_valid = false;
+  e->graph_gen++;
 }
 
 void destroy_graphs(Engine* e) {
@@ -1636,6 +1637,19 @@ struct fl_batch {
   cudaEvent_t start = nullptr;
   std::vector<cudaEvent_t> events;
   std::string err;
+  // The work-list path: every scene's pressure solve batched into one
+  // launch per V-cycle phase (BatchSolve), inside one graph per step with
+  // the scenes' own passes before and after it as concurrent branches.
+  // Null when some scene does not qualify (why_not): then every engine's
+  // own step graph is launched on its own stream instead.
+  BatchSolve* solve = nullptr;
+  std::string why_not;
+  cudaStream_t body = nullptr;  // capture stream of the solve's cycle body
+  cudaEvent_t mid = nullptr;    // the solve's end, where the post-solve branches fork
+  std::vector<cudaEvent_t> joins;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [0]: every engine at its built parity, [1]: flipped
+  std::vector<int> built_cur;
+  std::vector<unsigned long long> built_gen;
 };
 
 namespace {
@@ -1653,22 +1667,112 @@ int bfail(fl_batch* b, int code, const char* fmt, ...) {
   return code;
 }
 
+void batch_graphs_free(fl_batch* b) {
+  for (auto& g : b->graph) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  b->built_cur.clear();
+  b->built_gen.clear();
+}
+
 void batch_free(fl_batch* b) {
+  batch_graphs_free(b);
+  batch_solve_destroy(b->solve);
+  b->solve = nullptr;
   for (cudaEvent_t ev : b->events) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : b->joins) cudaEventDestroy(ev);
+  if (b->mid) cudaEventDestroy(b->mid);
   if (b->start) cudaEventDestroy(b->start);
+  if (b->body) cudaStreamDestroy(b->body);
   if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+std::vector<Engine*> batch_engines(fl_batch* b) {
+  std::vector<Engine*> es;
+  for (int k : b->order) es.push_back(&b->engines[k]->e);
+  return es;
+}
+
+// Captures one batch step for the engines at parity cur ^ flip: each
+// engine's passes up to the divergence on its own stream (forked from the
+// batch stream), the batched solve on the batch stream, then each engine's
+// projection, dye and CFL passes on its own stream again, joined back.
+int batch_capture(fl_batch* b, int flip, cudaGraphExec_t* out) {
+  cudaStream_t s = b->stream;
+  cudaError_t err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (err != cudaSuccess) return bfail(b, FL_EDEVICE, "batch capture: %s", cudaGetErrorString(err));
+  cudaEventRecord(b->start, s);
+  for (int k : b->order) {
+    Engine* e = &b->engines[k]->e;
+    cudaStreamWaitEvent(e->stream, b->start, 0);
+    enqueue_pre(e, e->stream, e->cur ^ flip, false);
+    cudaEventRecord(b->events[k], e->stream);
+    cudaStreamWaitEvent(s, b->events[k], 0);
+  }
+  err = batch_solve_enqueue(*b->solve, s, b->body);
+  cudaEventRecord(b->mid, s);
+  for (int k : b->order) {
+    Engine* e = &b->engines[k]->e;
+    cudaStreamWaitEvent(e->stream, b->mid, 0);
+    const cudaError_t pe = enqueue_post(e, e->stream, e->cur ^ flip, true);
+    if (err == cudaSuccess) err = pe;
+    cudaEventRecord(b->joins[k], e->stream);
+    cudaStreamWaitEvent(s, b->joins[k], 0);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t end = cudaStreamEndCapture(s, &g);
+  if (err == cudaSuccess) err = end;
+  if (err == cudaSuccess) err = cudaGetLastError();
+  if (err == cudaSuccess) err = cudaGraphInstantiate(out, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (err != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return bfail(b, FL_EDEVICE, "batch graph: %s", cudaGetErrorString(err));
+  }
+  return FL_OK;
+}
+
+// The graph for the engines' current parities: rebuilt (with the solve's
+// plan) when an engine's step graphs changed since, or when the engines'
+// parities no longer move together.
+int batch_graph_for_now(fl_batch* b, cudaGraphExec_t* out) {
+  const size_t n = b->engines.size();
+  const bool fresh = b->built_gen.empty();  // no graphs yet: the plan is current
+  bool stale = false;
+  for (size_t k = 0; !fresh && !stale && k < n; k++) stale = b->built_gen[k] != b->engines[k]->e.graph_gen;
+  int flip = -1;
+  if (!fresh && !stale) {
+    bool same = true, flipped = true;
+    for (size_t k = 0; k < n; k++) {
+      same = same && b->engines[k]->e.cur == b->built_cur[k];
+      flipped = flipped && b->engines[k]->e.cur != b->built_cur[k];
+    }
+    flip = same ? 0 : flipped ? 1 : -1;
+  }
+  if (fresh || stale || flip < 0) {
+    batch_graphs_free(b);
+    if (stale) {
+      batch_solve_destroy(b->solve);
+      b->solve = batch_solve_create(batch_engines(b), b->why_not);
+      if (!b->solve) return bfail(b, FL_EDEVICE, "batched solve: %s", b->why_not.c_str());
+    }
+    for (size_t k = 0; k < n; k++) {
+      b->built_cur.push_back(b->engines[k]->e.cur);
+      b->built_gen.push_back(b->engines[k]->e.graph_gen);
+    }
+    for (int f = 0; f < 2; f++) TRY(batch_capture(b, f, &b->graph[f]));
+    flip = 0;
+  }
+  *out = b->graph[flip];
+  return FL_OK;
 }
 
 }  // namespace
 
 extern "C" {
 
-// A batch launches every engine's own step graph on the engine's own stream,
-// largest scenes first, so that the scenes' steps run concurrently (up to the
-// number of hardware queues, CUDA_DEVICE_MAX_CONNECTIONS). One graph holding
-// every engine's step as a branch was measured to run the branches one after
-// another (each branch has its own device-side WHILE loop): 16 scenes of 64^2
-// took 10.3 ms that way against 1.4 ms launched on their own streams.
 int fl_batch_create(fl_engine* const* engines, int count, fl_batch** out) {
   if (!out) return bfail(nullptr, FL_EINVAL, "null output pointer");
   *out = nullptr;
@@ -1699,15 +1803,27 @@ int fl_batch_create(fl_engine* const* engines, int count, fl_batch** out) {
   });
   cudaSetDevice(b->device);
   cudaError_t err = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&b->body, cudaStreamNonBlocking);
   if (err == cudaSuccess) err = cudaEventCreateWithFlags(&b->start, cudaEventDisableTiming);
+  if (err == cudaSuccess) err = cudaEventCreateWithFlags(&b->mid, cudaEventDisableTiming);
   b->events.resize(count, nullptr);
-  for (int k = 0; k < count && err == cudaSuccess; k++)
+  b->joins.resize(count, nullptr);
+  for (int k = 0; k < count && err == cudaSuccess; k++) {
     err = cudaEventCreateWithFlags(&b->events[k], cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&b->joins[k], cudaEventDisableTiming);
+  }
   if (err != cudaSuccess) {
     batch_free(b);
     delete b;
     return bfail(nullptr, FL_EDEVICE, "batch: %s", cudaGetErrorString(err));
   }
+  // the work-list solve when every scene qualifies (multigrid, one V-cycle
+  // shape); otherwise b->why_not says why and the engines' own graphs run
+  bool worklist = true;
+  for (int k = 0; k < count; k++) worklist = worklist && engines[k]->e.prm.solver == FL_SOLVER_MG;
+  if (worklist) b->solve = batch_solve_create(batch_engines(b), b->why_not);
+  else b->why_not = "a scene solves with red-black SOR";
+  // (the step graphs are captured on the first fl_batch_step)
   *out = b;
   return FL_OK;
 }
@@ -1725,6 +1841,8 @@ const char* fl_batch_last_error(const fl_batch* b) { return b ? b->err.c_str() :
 
 void* fl_batch_stream(fl_batch* b) { return b ? (void*)b->stream : nullptr; }
 
+int fl_batch_worklist(const fl_batch* b) { return b && b->solve ? 1 : 0; }
+
 int fl_batch_step(fl_batch* b, int nsteps) {
   if (!b) return bfail(nullptr, FL_EINVAL, "null batch");
   if (nsteps < 0) return bfail(b, FL_EINVAL, "nsteps < 0");
@@ -1733,6 +1851,31 @@ int fl_batch_step(fl_batch* b, int nsteps) {
     Engine* e = &b->engines[k]->e;
     if (e->busy.load() != 0) return bfail(b, FL_EBUSY, "engine %zu is inside a call", k);
     if (!graph_eligible(e)) return bfail(b, FL_EINVAL, "engine %zu is no longer eligible for graph steps", k);
+  }
+  if (b->solve) {
+    // the batch stream follows every engine's earlier work, then runs the
+    // steps; each engine's later work follows the batch's
+    for (size_t k = 0; k < b->engines.size(); k++) {
+      cudaEventRecord(b->events[k], b->engines[k]->e.stream);
+      cudaStreamWaitEvent(b->stream, b->events[k], 0);
+    }
+    for (int n = 0; n < nsteps; n++) {
+      cudaGraphExec_t g = nullptr;
+      const int st = batch_graph_for_now(b, &g);
+      if (st != FL_OK) return st;
+      cudaError_t err = cudaGraphLaunch(g, b->stream);
+      if (err != cudaSuccess) return bfail(b, FL_EDEVICE, "batch step: %s", cudaGetErrorString(err));
+      for (auto* h : b->engines) {
+        Engine* e = &h->e;
+        e->cur = 1 - e->cur;
+        e->steps++;
+        e->stats_on_device = true;
+      }
+    }
+    cudaEventRecord(b->start, b->stream);
+    for (auto* h : b->engines) cudaStreamWaitEvent(h->e.stream, b->start, 0);
+    cudaError_t err = cudaGetLastError();
+    return err == cudaSuccess ? FL_OK : bfail(b, FL_EDEVICE, "batch step: %s", cudaGetErrorString(err));
   }
   // each engine's steps follow its earlier work (its own stream) and the
   // batch stream's earlier work

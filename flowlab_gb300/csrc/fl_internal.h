@@ -86,6 +86,9 @@ struct Engine {
   uint8_t* label_in = nullptr;
   int* label_flag = nullptr;
   bool graphs_valid = false;
+  // counts every destruction of the step graphs (parameters, patch, warm
+  // start or levels changed): a batch rebuilds its own graphs when it moves
+  unsigned long long graph_gen = 0;
   bool use_graphs = true;
   bool stats_on_device = false;  // the last solve's statistics live in ctl
 
@@ -190,6 +193,15 @@ void launch_forces(cudaStream_t s, int nx, int ny, float h, int dnx, int dny, fl
 void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, const float* v, float* out,
                        bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc,
                        float* out_lo = nullptr);
+// The batched pressure solve of fl_batch (fl_multigrid.cu): the plan over
+// the engines' buffers, or null with the reason when some engine does not
+// qualify; the solve enqueued on a capturing stream (cycle body captured
+// from `body`).
+struct BatchSolve;
+BatchSolve* batch_solve_create(const std::vector<Engine*>& engines, std::string& why);
+void batch_solve_destroy(BatchSolve* b);
+cudaError_t batch_solve_enqueue(const BatchSolve& b, cudaStream_t s, cudaStream_t body);
+
 // The end-of-step CFL scan with the residual diagnostic folded in (every
 // residual_every steps: the post-step divergence and its statistics); the
 // step's dt joins the clock and the next step's scalars are written.

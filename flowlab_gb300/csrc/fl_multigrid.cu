@@ -23,6 +23,7 @@
 #include <mutex>
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 
 #include "fl_internal.h"
 
@@ -599,8 +600,9 @@ __device__ void tail_smooth(unsigned char* smem, const CoarseLevel& L, int l, in
   if (pairs <= 0) tail_bar(l, L.nwarps);
 }
 
-__global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
+// The whole tail, run by one 1024-thread block over `smem` (the layout of
+// coarse_smem_bytes).
+__device__ __forceinline__ void mg_coarse_body(const CoarseArgs& a, unsigned char* smem) {
   const int tid = threadIdx.x + 32 * threadIdx.y;
   const int lane = tid & 31, w = tid >> 5;
   if (tid == 0) reinterpret_cast<float*>(smem)[0] = 0.0f;  // the zero word tail_smooth's unlinked neighbours read
@@ -716,6 +718,11 @@ __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
   }
 }
 
+__global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  mg_coarse_body(a, smem);
+}
+
 // The float64 defect-correction pass (iterative refinement, solveMixed):
 // p64' = p64 + e (when `update`), then r = b - (count*p64' - sum) in double
 // with the neighbour sum in the order +x, -x, +y, -y, r32 = float(r), and
@@ -739,23 +746,22 @@ __global__ void __launch_bounds__(1024, 1) k_mg_coarse(CoarseArgs a) {
 constexpr int UR_ROWS = 16;
 constexpr int UR_WARPS = 4;
 
+// One block's rows of the float64 pass: block (bx, by) of its grid.
 template <bool UPDATE>
-__global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny, double* __restrict__ p64a,
-                                                                double* __restrict__ p64b,
-                                                                const SolveCtl* __restrict__ ctl,
-                                                                const float* __restrict__ e,
-                                                                const float* __restrict__ b,
-                                                                const float* __restrict__ b_lo,
-                                                                const uint8_t* __restrict__ code,
-                                                                float* __restrict__ r32, StepAccum* acc) {
+__device__ __forceinline__ void update_resid64_tile(int nx, int ny, double* __restrict__ p64a,
+                                                    double* __restrict__ p64b, const SolveCtl* __restrict__ ctl,
+                                                    const float* __restrict__ e, const float* __restrict__ b,
+                                                    const float* __restrict__ b_lo,
+                                                    const uint8_t* __restrict__ code, float* __restrict__ r32,
+                                                    StepAccum* acc, int bx, int by) {
   __shared__ double red[32];
   __shared__ unsigned long long redn[32];
   const int par = ctl->par;
   const double* p_in = par ? p64b : p64a;
   double* p_out = par ? p64a : p64b;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int gx = blockIdx.x * 30 - 1 + lane;
-  const int y0 = (blockIdx.y * UR_WARPS + w) * UR_ROWS;
+  const int gx = bx * 30 - 1 + lane;
+  const int y0 = (by * UR_WARPS + w) * UR_ROWS;
   const bool col = gx >= 0 && gx < nx;
   const bool own = col && lane != 0 && lane != 31;
 
@@ -865,23 +871,22 @@ __global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny
 constexpr int DF_ROWS = 8;
 constexpr int DF_WARPS = 4;
 
+// One block's rows of the double-float pass: block (bx, by) of its grid.
 template <bool UPDATE>
-__global__ void __launch_bounds__(32 * DF_WARPS, 8) k_update_resid_df(int nx, int ny, float2* __restrict__ p2a,
-                                                                   float2* __restrict__ p2b,
-                                                                   const SolveCtl* __restrict__ ctl,
-                                                                   const float* __restrict__ e,
-                                                                   const float* __restrict__ b,
-                                                                   const float* __restrict__ b_lo,
-                                                                   const uint8_t* __restrict__ code,
-                                                                   float* __restrict__ r32, StepAccum* acc) {
+__device__ __forceinline__ void update_resid_df_tile(int nx, int ny, float2* __restrict__ p2a,
+                                                     float2* __restrict__ p2b, const SolveCtl* __restrict__ ctl,
+                                                     const float* __restrict__ e, const float* __restrict__ b,
+                                                     const float* __restrict__ b_lo,
+                                                     const uint8_t* __restrict__ code, float* __restrict__ r32,
+                                                     StepAccum* acc, int bx, int by) {
   __shared__ double red[32];
   __shared__ unsigned long long redn[32];
   const int par = ctl->par;
   const float2* p_in = par ? p2b : p2a;
   float2* p_out = par ? p2a : p2b;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int gx = blockIdx.x * 30 - 1 + lane;
-  const int y0 = (blockIdx.y * DF_WARPS + w) * DF_ROWS;
+  const int gx = bx * 30 - 1 + lane;
+  const int y0 = (by * DF_WARPS + w) * DF_ROWS;
   const bool col = gx >= 0 && gx < nx;
   const bool own = col && lane != 0 && lane != 31;
 
@@ -976,7 +981,7 @@ __device__ __forceinline__ double acc_rms(double sq, unsigned long long n) { ret
 // Before the cycle loop (pressureMultigrid.ts:294-300, solveMixed): the rhs
 // RMS; a vanishing rhs means p = 0 and no cycle; the float64 path also tests
 // its initial residual, so a converged warm start costs no cycle.
-__global__ void k_solve_begin(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaGraphConditionalHandle h) {
+__device__ int solve_begin(StepAccum* acc, SolveCtl* ctl) {
   const double b_rms = acc_rms(acc->b_sq, acc->n_fluid);
   ctl->b_rms = b_rms;
   ctl->cycles = 0;
@@ -999,13 +1004,18 @@ __global__ void k_solve_begin(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaG
   acc->res_sq = 0.0;
   acc->n_res = 0ull;
   ctl->cont = cont;
+  return cont;
+}
+
+__global__ void k_solve_begin(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaGraphConditionalHandle h) {
+  const int cont = solve_begin(acc, ctl);
   if (use_cond) cudaGraphSetConditional(h, cont);
 }
 
 // After each cycle: count it, evaluate the relative residual the cycle's
 // last kernel accumulated, and decide on another (pressureMultigrid.ts:
 // 314-317 for float32, solveMixed for float64 defect correction).
-__global__ void k_solve_check(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaGraphConditionalHandle h) {
+__device__ int solve_check(StepAccum* acc, SolveCtl* ctl) {
   ctl->cycles += 1;
   if (ctl->mode == SOLVE_MIXED) ctl->par = 1 - ctl->par;
   const double rel = acc_rms(acc->res_sq, acc->n_res) / ctl->b_rms;
@@ -1022,6 +1032,11 @@ __global__ void k_solve_check(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaG
   acc->res_sq = 0.0;
   acc->n_res = 0ull;
   ctl->cont = cont;
+  return cont;
+}
+
+__global__ void k_solve_check(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaGraphConditionalHandle h) {
+  const int cont = solve_check(acc, ctl);
   if (use_cond) cudaGraphSetConditional(h, cont);
 }
 
@@ -1159,6 +1174,30 @@ void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* 
   a.scale = scale;
   a.omega = omega;
   launch_smooth(s, a, pairs, MODE_PLAIN);
+}
+
+template <bool UPDATE>
+__global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny, double* __restrict__ p64a,
+                                                                double* __restrict__ p64b,
+                                                                const SolveCtl* __restrict__ ctl,
+                                                                const float* __restrict__ e,
+                                                                const float* __restrict__ b,
+                                                                const float* __restrict__ b_lo,
+                                                                const uint8_t* __restrict__ code,
+                                                                float* __restrict__ r32, StepAccum* acc) {
+  update_resid64_tile<UPDATE>(nx, ny, p64a, p64b, ctl, e, b, b_lo, code, r32, acc, blockIdx.x, blockIdx.y);
+}
+
+template <bool UPDATE>
+__global__ void __launch_bounds__(32 * DF_WARPS, 8) k_update_resid_df(int nx, int ny, float2* __restrict__ p2a,
+                                                                   float2* __restrict__ p2b,
+                                                                   const SolveCtl* __restrict__ ctl,
+                                                                   const float* __restrict__ e,
+                                                                   const float* __restrict__ b,
+                                                                   const float* __restrict__ b_lo,
+                                                                   const uint8_t* __restrict__ code,
+                                                                   float* __restrict__ r32, StepAccum* acc) {
+  update_resid_df_tile<UPDATE>(nx, ny, p2a, p2b, ctl, e, b, b_lo, code, r32, acc, blockIdx.x, blockIdx.y);
 }
 
 void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, const SolveCtl* ctl,
@@ -1316,6 +1355,33 @@ void mg_vcycle(Engine& e, StepAccum* acc) { mg_vcycle_on(e, e.levels[0].b, false
 // One V-cycle with level 0's rhs `b0`; with `zero_start` the level-0 unknown
 // starts from 0 (the correction equation of the defect-correction loop)
 // instead of the warm start in levels[0].x[0].
+// The single-CTA tail's arguments for a V-cycle on b0 (the finest level's
+// rhs when the tail starts there), from zero when zero_start, accumulating
+// the finest residual into acc when the tail holds the finest level.
+static CoarseArgs coarse_args(const Engine& e, const float* b0, bool zero_start, StepAccum* acc) {
+  const int lc = e.coarse_level;
+  CoarseArgs a{};
+  int ox[MAX_LEVELS], ob[MAX_LEVELS], oc[MAX_LEVELS];
+  coarse_smem_bytes(e, lc, ox, ob, oc);
+  a.nlev = (int)e.levels.size() - lc;
+  for (int l = 0; l < a.nlev; l++) {
+    const Level& L = e.levels[lc + l];
+    const int lsh = tail_lsh(L.nx);
+    const int rows_per_warp = 32 >> lsh;
+    const int groups = (L.ny + rows_per_warp - 1) / rows_per_warp;
+    a.lv[l] = CoarseLevel{L.nx, L.ny, L.code, ox[l], ob[l], oc[l], lsh, std::min(32, groups), groups > 32 ? 2 : 1};
+  }
+  a.b_top = lc == 0 ? b0 : e.levels[lc].b;
+  a.x_top = e.levels[lc].x[0];
+  a.x_is_zero = lc > 0 || zero_start;
+  a.pre = e.prm.mg_pre;
+  a.post = e.prm.mg_post;
+  a.coarse_sweeps = e.prm.mg_coarse_sweeps;
+  a.omega = (float)e.prm.mg_omega;
+  a.acc = lc == 0 ? acc : nullptr;
+  return a;
+}
+
 void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc) {
   cudaStream_t s = e.stream;
   const int lc = e.coarse_level;
@@ -1346,25 +1412,7 @@ void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc) {
     const int tok = prof_begin(e, FL_PH_MG_COARSE);
     double bytes = (lc == 0 ? 4.0 : 0.0) * cells(lc) + 8.0 * cells(lc);
     for (int l = lc; l < (int)e.levels.size(); l++) bytes += cells(l);
-    CoarseArgs a{};
-    int ox[MAX_LEVELS], ob[MAX_LEVELS], oc[MAX_LEVELS];
-    coarse_smem_bytes(e, lc, ox, ob, oc);
-    a.nlev = (int)e.levels.size() - lc;
-    for (int l = 0; l < a.nlev; l++) {
-      const Level& L = e.levels[lc + l];
-      const int lsh = tail_lsh(L.nx);
-      const int rows_per_warp = 32 >> lsh;
-      const int groups = (L.ny + rows_per_warp - 1) / rows_per_warp;
-      a.lv[l] = CoarseLevel{L.nx, L.ny, L.code, ox[l], ob[l], oc[l], lsh, std::min(32, groups), groups > 32 ? 2 : 1};
-    }
-    a.b_top = lc == 0 ? b0 : e.levels[lc].b;
-    a.x_top = e.levels[lc].x[0];
-    a.x_is_zero = lc > 0 || zero_start;
-    a.pre = e.prm.mg_pre;
-    a.post = e.prm.mg_post;
-    a.coarse_sweeps = e.prm.mg_coarse_sweeps;
-    a.omega = omega;
-    a.acc = lc == 0 ? acc : nullptr;
+    const CoarseArgs a = coarse_args(e, b0, zero_start, acc);
     k_mg_coarse<<<1, dim3(32, 32), e.coarse_smem, s>>>(a);
     prof_end(e, tok, bytes, 1);
   }
@@ -1389,6 +1437,327 @@ void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc) {
     launch_smooth(s, a, e.prm.mg_post, MODE_POST);
     prof_end(e, tok, 13.0 * cells(l) + 4.0 * cells(l + 1), 1);
   }
+}
+
+
+// ------------------------------------------------------------ batched solve
+//
+// The pressure solves of many engines advanced together (fl_batch): each
+// V-cycle phase is ONE launch over a list of (scene, level, tile) items
+// drawn from every scene of the batch, the scenes' tails aligned (a scene
+// with fewer levels above its tail joins the descent later and leaves the
+// ascent earlier), and the cycle loop is one device-side WHILE over "some
+// scene still iterates". A scene that has converged (its control block's
+// `cont` cleared by its own test) leaves its items at once, so every scene
+// runs exactly the cycles it would run alone, through the same per-tile code
+// (smooth_tile, mg_coarse_body, the defect-pass tiles, solve_begin /
+// solve_check): its results are bit-identical to stepping it alone.
+
+struct BatchLevel {
+  int nx, ny;
+  float* x0;
+  float* x1;
+  float* b;
+  const uint8_t* code;
+};
+
+struct BatchScene {
+  BatchLevel lv[MAX_LEVELS];
+  CoarseArgs tail;
+  double* p64a;
+  double* p64b;
+  float* r32;
+  float* b_lo;
+  SolveCtl* ctl;
+  StepAccum* acc;
+  long cells;
+  int nlev, lc, mixed;
+  float omega;
+};
+
+struct BatchItem {
+  int scene, level, bx, by;
+};
+
+struct BatchSolve {
+  int device = 0;
+  int n = 0;
+  int pre = 0, post = 0;
+  bool any_mixed = false;
+  size_t tail_smem = 0;
+  BatchScene* scenes = nullptr;  // device
+  BatchItem* items = nullptr;    // device
+  // (offset, count) into items, per phase
+  std::vector<std::pair<int, int>> pre_ph, post_ph;
+  std::pair<int, int> tail_ph{0, 0}, defect_ph{0, 0}, zero_ph{0, 0};
+};
+
+template <int P, int MODE>
+__global__ void __launch_bounds__(1024, 1) k_batch_smooth(const BatchScene* __restrict__ sc,
+                                                         const BatchItem* __restrict__ items) {
+  const BatchItem it = items[blockIdx.x];
+  const BatchScene& S = sc[it.scene];
+  if (!S.ctl->cont) return;  // the scene has converged: the same for the whole block
+  const int l = it.level;
+  const BatchLevel& L = S.lv[l];
+  const BatchLevel& C = S.lv[l + 1];
+  // the arguments mg_vcycle_on gives this level (mixed: a V-cycle on the
+  // defect pass's residual from zero; otherwise on b from the warm start)
+  SmoothArgs a{};
+  a.nx = L.nx;
+  a.ny = L.ny;
+  a.code = L.code;
+  a.scale = -1.0f;
+  a.omega = S.omega;
+  a.cnx = C.nx;
+  a.cny = C.ny;
+  a.b = l == 0 && S.mixed ? S.r32 : L.b;
+  if (MODE == MODE_PRE) {
+    a.xin = L.x0;
+    a.xout = L.x1;
+    a.bc = C.b;
+    a.x_is_zero = l > 0 || S.mixed;
+  } else {
+    a.xin = L.x1;
+    a.xout = L.x0;
+    a.ec = C.x0;
+    a.acc = l == 0 && !S.mixed ? S.acc : nullptr;
+  }
+  smooth_tile<P, MODE, 64, false>(a, it.bx, it.by);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_batch_tail(const BatchScene* __restrict__ sc,
+                                                       const BatchItem* __restrict__ items) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const BatchScene& S = sc[items[blockIdx.x].scene];
+  if (!S.ctl->cont) return;
+  mg_coarse_body(S.tail, smem);
+}
+
+// The defect pass of the scenes with a refined pressure: the initial
+// residual (UPDATE false, every scene, before the loop) or p += e and the new
+// residual (UPDATE true, the scenes still iterating).
+template <bool UPDATE>
+__global__ void __launch_bounds__(32 * UR_WARPS) k_batch_defect(const BatchScene* __restrict__ sc,
+                                                               const BatchItem* __restrict__ items) {
+  const BatchItem it = items[blockIdx.x];
+  const BatchScene& S = sc[it.scene];
+  if (UPDATE && !S.ctl->cont) return;
+  const BatchLevel& L0 = S.lv[0];
+  const float* e = UPDATE ? L0.x0 : nullptr;
+  if (S.mixed == MIXED_DF)
+    update_resid_df_tile<UPDATE>(L0.nx, L0.ny, reinterpret_cast<float2*>(S.p64a), reinterpret_cast<float2*>(S.p64b),
+                                 S.ctl, e, L0.b, S.b_lo, L0.code, S.r32, S.acc, it.bx, it.by);
+  else
+    update_resid64_tile<UPDATE>(L0.nx, L0.ny, S.p64a, S.p64b, S.ctl, e, L0.b, S.b_lo, L0.code, S.r32, S.acc, it.bx,
+                                it.by);
+}
+
+// Every scene's begin test; the WHILE node runs while any scene iterates.
+__global__ void __launch_bounds__(1024) k_batch_begin(const BatchScene* __restrict__ sc, int n,
+                                                      cudaGraphConditionalHandle h) {
+  int any = 0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) any |= solve_begin(sc[k].acc, sc[k].ctl);
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) cudaGraphSetConditional(h, any ? 1u : 0u);
+}
+
+// Every iterating scene's cycle test (the others keep their state).
+__global__ void __launch_bounds__(1024) k_batch_check(const BatchScene* __restrict__ sc, int n,
+                                                      cudaGraphConditionalHandle h) {
+  int any = 0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x)
+    if (sc[k].ctl->cont) any |= solve_check(sc[k].acc, sc[k].ctl);
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) cudaGraphSetConditional(h, any ? 1u : 0u);
+}
+
+// k_zero_if per scene: item (scene, -, block, blocks of the scene).
+__global__ void __launch_bounds__(256) k_batch_zero(const BatchScene* __restrict__ sc,
+                                                    const BatchItem* __restrict__ items) {
+  const BatchItem it = items[blockIdx.x];
+  const BatchScene& S = sc[it.scene];
+  if (!S.ctl->zero_p) return;
+  float* p32 = S.mixed ? nullptr : S.lv[0].x0;
+  double* p64 = S.mixed ? (S.ctl->par ? S.p64b : S.p64a) : nullptr;
+  for (long k = it.bx * 256L + threadIdx.x; k < S.cells; k += (long)it.by * 256) {
+    if (p32) p32[k] = 0.0f;
+    if (p64) p64[k] = 0.0;
+  }
+}
+
+BatchSolve* batch_solve_create(const std::vector<Engine*>& es, std::string& why) {
+  if (es.empty()) {
+    why = "no scenes";
+    return nullptr;
+  }
+  const fl_params& p0 = es[0]->prm;
+  for (const Engine* e : es) {
+    if (e->prm.solver != FL_SOLVER_MG) why = "a scene solves with red-black SOR";
+    else if (e->prm.mg_pre != p0.mg_pre || e->prm.mg_post != p0.mg_post)
+      why = "the scenes' V-cycle shapes differ";
+    else if (e->prm.mg_pre < 0 || e->prm.mg_pre > 4 || e->prm.mg_post < 0 || e->prm.mg_post > 4)
+      why = "sweep pairs beyond 4";
+    else if ((int)e->levels.size() > MAX_LEVELS || e->levels.empty())
+      why = "too many levels";
+    if (!why.empty()) return nullptr;
+  }
+  BatchSolve* b = new BatchSolve();
+  b->device = es[0]->device;
+  b->n = (int)es.size();
+  b->pre = p0.mg_pre;
+  b->post = p0.mg_post;
+  std::vector<BatchScene> hs(es.size());
+  int depth = 0;
+  for (size_t k = 0; k < es.size(); k++) {
+    const Engine& e = *es[k];
+    BatchScene& S = hs[k];
+    std::memset(&S, 0, sizeof S);
+    S.nlev = (int)e.levels.size();
+    S.lc = e.coarse_level;
+    S.mixed = e.prm.mixed;
+    S.omega = (float)e.prm.mg_omega;
+    S.cells = e.cells();
+    for (int l = 0; l < S.nlev; l++) {
+      const Level& L = e.levels[l];
+      S.lv[l] = BatchLevel{L.nx, L.ny, L.x[0], L.x[1], L.b, L.code};
+    }
+    const bool mixed = e.prm.mixed != 0;
+    S.tail = coarse_args(e, mixed ? e.r32 : e.levels[0].b, mixed, mixed ? nullptr : e.acc);
+    S.p64a = e.p64[0];
+    S.p64b = e.p64[1];
+    S.r32 = e.r32;
+    S.b_lo = e.b_lo;
+    S.ctl = e.ctl;
+    S.acc = e.acc;
+    b->any_mixed = b->any_mixed || mixed;
+    b->tail_smem = std::max(b->tail_smem, e.coarse_smem);
+    depth = std::max(depth, S.lc);
+  }
+  // items, largest scenes first within each phase (blocks start in order)
+  std::vector<int> order(es.size());
+  for (size_t k = 0; k < es.size(); k++) order[k] = (int)k;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return hs[x].cells > hs[y].cells; });
+  std::vector<BatchItem> items;
+  auto smooth_items = [&](int k, int l, int halo) {
+    const int T = 64 - 2 * halo;
+    const BatchLevel& L = hs[k].lv[l];
+    for (int by = 0; by < (L.ny + T - 1) / T; by++)
+      for (int bx = 0; bx < (L.nx + T - 1) / T; bx++) items.push_back(BatchItem{k, l, bx, by});
+  };
+  // PRE: scene k smooths level lc_k - depth + d at phase d (tails aligned)
+  for (int d = 0; d < depth; d++) {
+    const int off = (int)items.size();
+    for (int k : order) {
+      const int l = hs[k].lc - depth + d;
+      if (l >= 0) smooth_items(k, l, 2 * b->pre + 1);
+    }
+    b->pre_ph.push_back({off, (int)items.size() - off});
+  }
+  b->tail_ph.first = (int)items.size();
+  for (int k : order) items.push_back(BatchItem{k, hs[k].lc, 0, 0});
+  b->tail_ph.second = (int)items.size() - b->tail_ph.first;
+  // POST: level lc_k - 1 - d at phase d
+  for (int d = 0; d < depth; d++) {
+    const int off = (int)items.size();
+    for (int k : order) {
+      const int l = hs[k].lc - 1 - d;
+      if (l >= 0) smooth_items(k, l, 2 * b->post + 1);
+    }
+    b->post_ph.push_back({off, (int)items.size() - off});
+  }
+  b->defect_ph.first = (int)items.size();
+  for (int k : order) {
+    if (!hs[k].mixed) continue;
+    const BatchLevel& L = hs[k].lv[0];
+    const int rows = hs[k].mixed == MIXED_DF ? DF_WARPS * DF_ROWS : UR_WARPS * UR_ROWS;
+    for (int by = 0; by < (L.ny + rows - 1) / rows; by++)
+      for (int bx = 0; bx < (L.nx + 29) / 30; bx++) items.push_back(BatchItem{k, 0, bx, by});
+  }
+  b->defect_ph.second = (int)items.size() - b->defect_ph.first;
+  b->zero_ph.first = (int)items.size();
+  for (int k : order) {
+    const int blocks = (int)std::min<long>(64, std::max<long>(1, (hs[k].cells + 255) / 256));
+    for (int q = 0; q < blocks; q++) items.push_back(BatchItem{k, 0, q, blocks});
+  }
+  b->zero_ph.second = (int)items.size() - b->zero_ph.first;
+  cudaError_t err = cudaMalloc(&b->scenes, hs.size() * sizeof(BatchScene));
+  if (err == cudaSuccess) err = cudaMalloc(&b->items, items.size() * sizeof(BatchItem));
+  if (err == cudaSuccess)
+    err = cudaMemcpy(b->scenes, hs.data(), hs.size() * sizeof(BatchScene), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess)
+    err = cudaMemcpy(b->items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess && b->tail_smem > 48 * 1024)
+    err = cudaFuncSetAttribute(k_batch_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->tail_smem);
+  if (err != cudaSuccess) {
+    why = cudaGetErrorString(err);
+    batch_solve_destroy(b);
+    return nullptr;
+  }
+  return b;
+}
+
+void batch_solve_destroy(BatchSolve* b) {
+  if (!b) return;
+  cudaFree(b->scenes);
+  cudaFree(b->items);
+  delete b;
+}
+
+template <int MODE>
+static void launch_batch_smooth(cudaStream_t s, const BatchSolve& b, int pairs, std::pair<int, int> ph) {
+  if (ph.second == 0) return;
+  const BatchItem* it = b.items + ph.first;
+  const dim3 blk(32, 32);
+  switch (pairs) {
+    case 0: k_batch_smooth<0, MODE><<<ph.second, blk, 0, s>>>(b.scenes, it); break;
+    case 1: k_batch_smooth<1, MODE><<<ph.second, blk, 0, s>>>(b.scenes, it); break;
+    case 2: k_batch_smooth<2, MODE><<<ph.second, blk, 0, s>>>(b.scenes, it); break;
+    case 3: k_batch_smooth<3, MODE><<<ph.second, blk, 0, s>>>(b.scenes, it); break;
+    default: k_batch_smooth<4, MODE><<<ph.second, blk, 0, s>>>(b.scenes, it); break;
+  }
+}
+
+// The whole batched solve, enqueued on `s` while it is being captured: the
+// initial defect pass and begin test, a WHILE node whose body (captured from
+// `body`) is one V-cycle of every iterating scene plus the defect pass and
+// the cycle tests, then the p = 0 fill of scenes whose rhs vanished.
+cudaError_t batch_solve_enqueue(const BatchSolve& b, cudaStream_t s, cudaStream_t body) {
+  if (b.any_mixed && b.defect_ph.second > 0)
+    k_batch_defect<false><<<b.defect_ph.second, 32 * UR_WARPS, 0, s>>>(b.scenes, b.items + b.defect_ph.first);
+  cudaStreamCaptureStatus cst;
+  cudaGraph_t cap = nullptr;
+  cudaError_t err = cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap, nullptr, nullptr, nullptr);
+  cudaGraphConditionalHandle h = 0;
+  if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&h, cap, 0, cudaGraphCondAssignDefault);
+  if (err != cudaSuccess) return err;
+  k_batch_begin<<<1, 1024, 0, s>>>(b.scenes, b.n, h);
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  err = cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap, &deps, nullptr, &ndeps);
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  if (err == cudaSuccess) err = cudaGraphAddNode(&node, cap, deps, nullptr, ndeps, &cp);
+  if (err == cudaSuccess) err = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  if (err == cudaSuccess)
+    err = cudaStreamBeginCaptureToGraph(body, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal);
+  if (err != cudaSuccess) return err;
+  for (const auto& ph : b.pre_ph) launch_batch_smooth<MODE_PRE>(body, b, b.pre, ph);
+  k_batch_tail<<<b.tail_ph.second, dim3(32, 32), b.tail_smem, body>>>(b.scenes, b.items + b.tail_ph.first);
+  for (const auto& ph : b.post_ph) launch_batch_smooth<MODE_POST>(body, b, b.post, ph);
+  if (b.any_mixed && b.defect_ph.second > 0)
+    k_batch_defect<true><<<b.defect_ph.second, 32 * UR_WARPS, 0, body>>>(b.scenes, b.items + b.defect_ph.first);
+  k_batch_check<<<1, 1024, 0, body>>>(b.scenes, b.n, h);
+  cudaGraph_t done = nullptr;
+  err = cudaStreamEndCapture(body, &done);
+  if (err != cudaSuccess) return err;
+  k_batch_zero<<<b.zero_ph.second, 256, 0, s>>>(b.scenes, b.items + b.zero_ph.first);
+  return cudaGetLastError();
 }
 
 }  // namespace fl

@@ -157,6 +157,7 @@ SIGNATURES = [
     ("fl_batch_destroy", _I, [_P]),
     ("fl_batch_last_error", ctypes.c_char_p, [_P]),
     ("fl_batch_stream", _P, [_P]),
+    ("fl_batch_worklist", _I, [_P]),
     ("fl_batch_step", _I, [_P, _I]),
 ]
 
@@ -362,6 +363,11 @@ class Batch:
 
     def stream(self):
         return self.lib.fl_batch_stream(self.h)
+
+    @property
+    def worklist(self):
+        """True when the scenes' solves run as one launch per V-cycle phase."""
+        return bool(self.lib.fl_batch_worklist(self.h))
 
     def close(self):
         if self.h:

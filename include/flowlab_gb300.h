@@ -374,16 +374,25 @@ int fl_read_rhs(fl_engine* e, int dtype, void* b);
 
 /* ------------------------------------------------------- batched scenes
  * No counterpart in the reference (one scene per Simulation). A batch
- * steps several engines (scenes of any sizes and parameters on one device)
- * together: each step launches every engine's own step graph (its whole
- * step with its device-side V-cycle loop) on the engine's own stream,
- * largest scenes first, so independent scenes run concurrently; how many at
- * once is bounded by the process's hardware queues (the environment
- * variable CUDA_DEVICE_MAX_CONNECTIONS, read when CUDA initialises; 8 by
- * default, up to 32). The engines must have uploaded fields and be eligible
- * for graph steps (no profiling, pending stir or label edit; multigrid, or
- * red-black SOR with a fixed sweep count). Statistics and fields are read
- * per engine. */
+ * steps several engines (scenes of any sizes on one device) together, one
+ * graph launch per step. When every scene solves with the multigrid and
+ * the same V-cycle shape (mg_pre, mg_post), the scenes' pressure solves run
+ * as ONE launch per V-cycle phase over a work list of (scene, level, tile)
+ * items of every scene, the scenes' single-CTA tails aligned, inside one
+ * device-side cycle loop that runs while any scene iterates; a scene that
+ * has converged leaves its items at once, so each scene runs the cycles it
+ * would run alone, with bit-identical results. Each scene's passes before
+ * and after the solve (advection, forces, divergence; projection, dye,
+ * CFL) are concurrent branches of the same graph. Otherwise (a red-black
+ * scene, differing shapes) each step launches every engine's own step
+ * graph on the engine's own stream, largest scenes first, as many at once
+ * as the process's hardware queues allow (CUDA_DEVICE_MAX_CONNECTIONS, read
+ * when CUDA initialises; 8 by default, up to 32). The engines must have
+ * uploaded fields and be eligible for graph steps (no profiling, pending
+ * stir or label edit; multigrid, or red-black SOR with a fixed sweep
+ * count). Statistics and fields are read per engine; an engine may be
+ * stepped alone between batch steps, or change its parameters (the batch
+ * then rebuilds its graphs). */
 typedef struct fl_batch fl_batch;
 int fl_batch_create(fl_engine* const* engines, int count, fl_batch** out);
 int fl_batch_destroy(fl_batch* b);
@@ -391,6 +400,10 @@ const char* fl_batch_last_error(const fl_batch* b);
 /* A stream (cudaStream_t) that completes after every engine's last step of
  * the latest fl_batch_step. */
 void* fl_batch_stream(fl_batch* b);
+/* 1 when the batch steps through the work-list solve (every scene solves
+ * with the multigrid, one V-cycle shape), 0 when it launches each engine's
+ * own step graph on its own stream. */
+int fl_batch_worklist(const fl_batch* b);
 /* nsteps steps of every engine, asynchronous; each engine's steps are
  * ordered after its earlier work and before its later work (its stream),
  * and after the batch stream's earlier work. */

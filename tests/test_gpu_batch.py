@@ -102,3 +102,95 @@ def test_engine_listed_twice_is_refused():
             native.Batch([es[0], es[0]])
     finally:
         batch.close_all(es)
+
+
+def plume_engine(n=64):
+    g, f, patch = configs.plume(n)
+    e = native.Engine(g.nx, g.ny, g.h, params=configs.plume_params(max_cycles=20))
+    e.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+    e.call("fl_upload_fields", native.FL_F32, ptr(f32(f.u)), ptr(f32(f.v)), ptr(f32(f.p)), ptr(f.label),
+           ptr(f32(f.dye)))
+    return e
+
+
+def assert_same(alone, together, what):
+    for k, (x, y) in enumerate(zip(alone, together)):
+        for name, fx, fy in zip(("u", "v", "p", "dye"), fields(x), fields(y)):
+            assert np.array_equal(fx, fy), "%s, scene %d: %s differs" % (what, k, name)
+        sx, sy = x.stats(), y.stats()
+        assert sx["cycles"] == sy["cycles"] and sx["steps"] == sy["steps"], (what, k, sx, sy)
+        assert sx["rel_residual"] == sy["rel_residual"] or abs(sx["rel_residual"] - sy["rel_residual"]) <= \
+            1e-9 * abs(sx["rel_residual"]), (what, k)
+
+
+@pytest.mark.parametrize("mixed", [0, 1, 2])
+def test_worklist_batch_equals_engines_stepped_alone(mixed):
+    """All-multigrid batches run the work-list solve (one launch per V-cycle
+    phase over every scene's tiles): uneven sides, 32^2 (tail only) to 256^2,
+    in float32, with the float64 and with the double-float defect
+    correction; a plume with its dye patch, buoyancy and confinement joins
+    the double-float batch. Every scene equals the same scene stepped
+    alone, bit for bit, cycle counts included."""
+    sides = [64, 256, 32, 128, 64]
+    steps = 4
+    tol = 1e-4 if mixed == 0 else 1e-6  # float32 alone stalls above 1e-6 on these scenes
+    alone = batch.make_engines(sides, seed=21, mixed=mixed, tol=tol)
+    together = batch.make_engines(sides, seed=21, mixed=mixed, tol=tol)
+    if mixed == 2:
+        alone.append(plume_engine())
+        together.append(plume_engine())
+    try:
+        for e in alone:
+            e.call("fl_step_auto", steps, None)
+        b = native.Batch(together)
+        try:
+            assert b.worklist
+            b.step(steps)
+        finally:
+            b.close()
+        assert_same(alone, together, "mixed %d" % mixed)
+    finally:
+        batch.close_all(alone + together)
+
+
+def test_worklist_batch_follows_engine_changes():
+    """Between work-list batch steps: one engine steps alone (its parity
+    moves away from the others') and another changes its tolerance (its
+    graphs are rebuilt); the batch rebuilds its own graphs and the results
+    equal the same sequence without the batch."""
+    sides = [64, 128, 64]
+    alone = batch.make_engines(sides, seed=8)
+    together = batch.make_engines(sides, seed=8)
+    try:
+        b = native.Batch(together)
+        try:
+            assert b.worklist
+            b.step(2)
+            together[0].call("fl_step_auto", 1, None)
+            tighter = configs.random_scene_params(tol=1e-7, max_cycles=40, mixed=1)
+            together[1].set_params(tighter)
+            b.step(3)
+        finally:
+            b.close()
+        for e in alone:
+            e.call("fl_step_auto", 2, None)
+        alone[0].call("fl_step_auto", 1, None)
+        alone[1].set_params(configs.random_scene_params(tol=1e-7, max_cycles=40, mixed=1))
+        for e in alone:
+            e.call("fl_step_auto", 3, None)
+        assert_same(alone, together, "after changes")
+    finally:
+        batch.close_all(alone + together)
+
+
+def test_batch_with_a_red_black_scene_launches_engine_graphs():
+    es = batch.make_engines([64], seed=2) + [karman_engine()]
+    try:
+        b = native.Batch(es)
+        try:
+            assert not b.worklist
+            b.step(1)
+        finally:
+            b.close()
+    finally:
+        batch.close_all(es)
