@@ -394,6 +394,29 @@ __device__ __forceinline__ float df_diff(float2 a, float2 b) {
   return __fadd_rn(s.x, e);
 }
 __device__ __forceinline__ double df_to_double(float2 x) { return (double)x.x + (double)x.y; }
+
+// Block-wide sum of double-float pairs on the float32 pipe (one df_add per
+// shuffle step), widened to double once, in the block's first thread: the
+// float64 pipe issues ~1.6 lanes per clock per SM, so a double-precision
+// tree over every block costs more than the sums it reduces.
+__device__ inline double block_sum_df(float2 v, float2* shm32) {
+  for (int o = 16; o > 0; o >>= 1)
+    v = df_add(v, make_float2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o)));
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int lane = tid & 31, w = tid >> 5;
+  __syncthreads();
+  if (lane == 0) shm32[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (w == 0) {
+    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    float2 u = lane < nw ? shm32[lane] : make_float2(0.0f, 0.0f);
+    for (int o = 16; o > 0; o >>= 1)
+      u = df_add(u, make_float2(__shfl_down_sync(0xffffffffu, u.x, o), __shfl_down_sync(0xffffffffu, u.y, o)));
+    t = df_to_double(u);
+  }
+  return t;  // valid in thread 0
+}
 __device__ __forceinline__ float2 df_from_double(double d) {
   const float hi = (float)d;
   return make_float2(hi, (float)(d - (double)hi));

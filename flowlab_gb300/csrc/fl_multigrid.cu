@@ -968,7 +968,7 @@ __device__ __forceinline__ void update_resid_df_tile(int nx, int ny, float2* __r
       r32[k] = r;
     }
   }
-  const double bs = block_sum(df_to_double(acc2), red);
+  const double bs = block_sum_df(acc2, reinterpret_cast<float2*>(red));
   const unsigned long long bn = block_sum_u64(n, redn);
   if (threadIdx.x == 0) {
     atomicAdd(&acc->res_sq, bs);

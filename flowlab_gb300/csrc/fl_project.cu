@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
     }
   }
   if (acc == nullptr) return;
-  double bs = block_sum(df_to_double(sq), red);
+  double bs = block_sum_df(sq, reinterpret_cast<float2*>(red));
   unsigned long long bn = block_sum_u64(n, redn);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     atomicAdd(&acc->b_sq, bs);
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(256) k_scale_rhs(long n, const float* __restri
       cnt += 1;
     }
   }
-  const double bs = block_sum(df_to_double(sq), red);
+  const double bs = block_sum_df(sq, reinterpret_cast<float2*>(red));
   const unsigned long long bn = block_sum_u64(cnt, redn);
   if (threadIdx.x == 0) {
     atomicAdd(&acc->b_sq, bs);
@@ -487,7 +487,9 @@ void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, 
                        bool as_rhs, const uint8_t* label, const StepScalars* sc, StepAccum* acc, float* out_lo) {
   dim3 b(32, 8);
   dim3 g = grid2(nx, ny, b);
-  g.y = std::min(g.y, std::max(1u, 1024u / g.x));
+  // about four blocks per SM, rows strided: every block ends in same-word
+  // atomics, which serialise
+  g.y = std::min(g.y, std::max(1u, 608u / g.x));
   k_divergence<<<g, b, 0, s>>>(nx, ny, h, u, v, out, as_rhs, label, sc, acc, out_lo);
 }
 
@@ -555,7 +557,7 @@ __global__ void __launch_bounds__(256) k_cfl_residual(int nx, int ny, float h, c
   unsigned long long bn = 0;
   float bx = 0.0f;
   if (on) {  // the same for the whole block
-    bs = block_sum(df_to_double(sq), red);
+    bs = block_sum_df(sq, reinterpret_cast<float2*>(red));
     bn = block_sum_u64(n, redn);
     __syncthreads();
     bx = block_max(mx, redm);
@@ -601,7 +603,9 @@ void launch_cfl_residual(cudaStream_t s, int nx, int ny, float h, const float* u
                          double* time_dev, const fl_params* prm, bool write_scalars, bool add_time) {
   dim3 b(32, 8);
   dim3 g = grid2(nx, ny, b);
-  g.y = std::min(g.y, std::max(1u, 1024u / g.x));
+  // about four blocks per SM, rows strided: every block ends in same-word
+  // atomics, which serialise
+  g.y = std::min(g.y, std::max(1u, 608u / g.x));
   k_cfl_residual<<<g, b, 0, s>>>(nx, ny, h, u, v, div_out, label, every, d, acc, sc_next, time_dev,
                                  (float)prm->cfl_target, (float)prm->dt_max, (float)prm->rho, prm->dye_decay[0],
                                  prm->dye_decay[1], prm->dye_decay[2], (float)prm->beta, (float)prm->alpha,
