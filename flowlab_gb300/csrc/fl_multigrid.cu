@@ -1479,70 +1479,135 @@ struct BatchItem {
   int scene, level, bx, by;
 };
 
+// The plan's device-side lists. Cycle phases ph: PRE at depth d (0..D-1),
+// the tail (D), POST at depth d (D+1..2D), the defect pass (2D+1); items of
+// scene k in phase ph are items[base[ph][k] .. + count[ph][k]). The begin and
+// check kernels compact, per phase, the scenes still iterating: act_scene
+// (in the plan's order, largest scenes first), act_pre (exclusive prefix of
+// their item counts), act_n and act_total; a phase kernel's blocks walk
+// 0 .. act_total by the grid's stride.
+struct BatchPlan {
+  const BatchScene* sc;
+  const BatchItem* items;
+  const int* base;
+  const int* count;
+  int* act_scene;
+  int* act_pre;
+  int* act_n;
+  int* act_total;
+  int n, nph;
+};
+
 struct BatchSolve {
   int device = 0;
-  int n = 0;
+  int n = 0, depth = 0, sms = 0;
   int pre = 0, post = 0;
   bool any_mixed = false;
   size_t tail_smem = 0;
-  BatchScene* scenes = nullptr;  // device
+  BatchScene* scenes = nullptr;  // device, largest scene first
   BatchItem* items = nullptr;    // device
-  // (offset, count) into items, per phase
-  std::vector<std::pair<int, int>> pre_ph, post_ph;
-  std::pair<int, int> tail_ph{0, 0}, defect_ph{0, 0}, zero_ph{0, 0};
+  int* lists = nullptr;          // device: base, count, act_scene, act_pre, act_n, act_total
+  BatchPlan plan{};
+  std::vector<int> max_items;    // per cycle phase: all scenes' items (the grid's bound)
+  std::pair<int, int> init_ph{0, 0}, zero_ph{0, 0};  // prologue defect pass, p = 0 fill: every scene
 };
 
-template <int P, int MODE>
-__global__ void __launch_bounds__(1024, 1) k_batch_smooth(const BatchScene* __restrict__ sc,
-                                                         const BatchItem* __restrict__ items) {
-  const BatchItem it = items[blockIdx.x];
-  const BatchScene& S = sc[it.scene];
-  if (!S.ctl->cont) return;  // the scene has converged: the same for the whole block
-  const int l = it.level;
-  const BatchLevel& L = S.lv[l];
-  const BatchLevel& C = S.lv[l + 1];
-  // the arguments mg_vcycle_on gives this level (mixed: a V-cycle on the
-  // defect pass's residual from zero; otherwise on b from the warm start)
-  SmoothArgs a{};
-  a.nx = L.nx;
-  a.ny = L.ny;
-  a.code = L.code;
-  a.scale = -1.0f;
-  a.omega = S.omega;
-  a.cnx = C.nx;
-  a.cny = C.ny;
-  a.b = l == 0 && S.mixed ? S.r32 : L.b;
-  if (MODE == MODE_PRE) {
-    a.xin = L.x0;
-    a.xout = L.x1;
-    a.bc = C.b;
-    a.x_is_zero = l > 0 || S.mixed;
-  } else {
-    a.xin = L.x1;
-    a.xout = L.x0;
-    a.ec = C.x0;
-    a.acc = l == 0 && !S.mixed ? S.acc : nullptr;
+__device__ __forceinline__ bool batch_item(const BatchPlan& P, int ph, int i, BatchItem& it) {
+  if (i >= P.act_total[ph]) return false;
+  const int* pre = P.act_pre + (long)ph * (P.n + 1);
+  int lo = 0, hi = P.act_n[ph] - 1;  // the last active scene whose prefix is <= i
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= i)
+      lo = mid;
+    else
+      hi = mid - 1;
   }
-  smooth_tile<P, MODE, 64, false>(a, it.bx, it.by);
+  const int k = P.act_scene[(long)ph * P.n + lo];
+  it = P.items[P.base[(long)ph * P.n + k] + (i - pre[lo])];
+  return true;
 }
 
-__global__ void __launch_bounds__(1024, 1) k_batch_tail(const BatchScene* __restrict__ sc,
-                                                       const BatchItem* __restrict__ items) {
+// Per phase, the items of the scenes whose control block says they iterate
+// (one warp per phase, a warp-wide scan per 32 scenes). Called by a whole
+// block after the scenes' tests, behind a barrier.
+__device__ void batch_compact(const BatchPlan& P) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int ph = w; ph < P.nph; ph += nw) {
+    int run = 0, nact = 0;
+    for (int c = 0; c < P.n; c += 32) {
+      const int k = c + lane;
+      const int cnt = k < P.n && P.sc[k].ctl->cont ? P.count[(long)ph * P.n + k] : 0;
+      int x = cnt;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      const unsigned on = __ballot_sync(0xffffffffu, cnt > 0);
+      if (cnt > 0) {
+        const int pos = nact + __popc(on & ((1u << lane) - 1u));
+        P.act_scene[(long)ph * P.n + pos] = k;
+        P.act_pre[(long)ph * (P.n + 1) + pos] = run + x - cnt;
+      }
+      run += __shfl_sync(0xffffffffu, x, 31);
+      nact += __popc(on);
+    }
+    if (lane == 0) {
+      P.act_total[ph] = run;
+      P.act_n[ph] = nact;
+      P.act_pre[(long)ph * (P.n + 1) + nact] = run;
+    }
+  }
+}
+
+template <int P, int MODE>
+__global__ void __launch_bounds__(1024, 1) k_batch_smooth(BatchPlan plan, int ph) {
+  for (int i = blockIdx.x;; i += gridDim.x) {
+    BatchItem it;
+    if (!batch_item(plan, ph, i, it)) return;  // the same for the whole block
+    const BatchScene& S = plan.sc[it.scene];
+    const int l = it.level;
+    const BatchLevel& L = S.lv[l];
+    const BatchLevel& C = S.lv[l + 1];
+    // the arguments mg_vcycle_on gives this level (mixed: a V-cycle on the
+    // defect pass's residual from zero; otherwise on b from the warm start)
+    SmoothArgs a{};
+    a.nx = L.nx;
+    a.ny = L.ny;
+    a.code = L.code;
+    a.scale = -1.0f;
+    a.omega = S.omega;
+    a.cnx = C.nx;
+    a.cny = C.ny;
+    a.b = l == 0 && S.mixed ? S.r32 : L.b;
+    if (MODE == MODE_PRE) {
+      a.xin = L.x0;
+      a.xout = L.x1;
+      a.bc = C.b;
+      a.x_is_zero = l > 0 || S.mixed;
+    } else {
+      a.xin = L.x1;
+      a.xout = L.x0;
+      a.ec = C.x0;
+      a.acc = l == 0 && !S.mixed ? S.acc : nullptr;
+    }
+    smooth_tile<P, MODE, 64, false>(a, it.bx, it.by);
+    __syncthreads();  // the next region reuses the shared tiles
+  }
+}
+
+__global__ void __launch_bounds__(1024, 1) k_batch_tail(BatchPlan plan, int ph) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const BatchScene& S = sc[items[blockIdx.x].scene];
-  if (!S.ctl->cont) return;
-  mg_coarse_body(S.tail, smem);
+  for (int i = blockIdx.x;; i += gridDim.x) {
+    BatchItem it;
+    if (!batch_item(plan, ph, i, it)) return;
+    mg_coarse_body(plan.sc[it.scene].tail, smem);
+    __syncthreads();
+  }
 }
 
-// The defect pass of the scenes with a refined pressure: the initial
-// residual (UPDATE false, every scene, before the loop) or p += e and the new
-// residual (UPDATE true, the scenes still iterating).
 template <bool UPDATE>
-__global__ void __launch_bounds__(32 * UR_WARPS) k_batch_defect(const BatchScene* __restrict__ sc,
-                                                               const BatchItem* __restrict__ items) {
-  const BatchItem it = items[blockIdx.x];
-  const BatchScene& S = sc[it.scene];
-  if (UPDATE && !S.ctl->cont) return;
+__device__ __forceinline__ void batch_defect_item(const BatchScene& S, const BatchItem& it) {
   const BatchLevel& L0 = S.lv[0];
   const float* e = UPDATE ? L0.x0 : nullptr;
   if (S.mixed == MIXED_DF)
@@ -1553,22 +1618,43 @@ __global__ void __launch_bounds__(32 * UR_WARPS) k_batch_defect(const BatchScene
                                 it.by);
 }
 
-// Every scene's begin test; the WHILE node runs while any scene iterates.
-__global__ void __launch_bounds__(1024) k_batch_begin(const BatchScene* __restrict__ sc, int n,
-                                                      cudaGraphConditionalHandle h) {
+// The defect pass of the iterating scenes with a refined pressure: p += e
+// and the new residual.
+__global__ void __launch_bounds__(32 * UR_WARPS) k_batch_defect(BatchPlan plan, int ph) {
+  for (int i = blockIdx.x;; i += gridDim.x) {
+    BatchItem it;
+    if (!batch_item(plan, ph, i, it)) return;
+    batch_defect_item<true>(plan.sc[it.scene], it);
+    __syncthreads();
+  }
+}
+
+// The initial defect pass of every scene with a refined pressure (before
+// the loop), one item per block.
+__global__ void __launch_bounds__(32 * UR_WARPS) k_batch_defect_init(const BatchScene* __restrict__ sc,
+                                                                    const BatchItem* __restrict__ items) {
+  const BatchItem it = items[blockIdx.x];
+  batch_defect_item<false>(sc[it.scene], it);
+}
+
+// Every scene's begin test, the compacted lists of the first cycle; the
+// WHILE node runs while any scene iterates.
+__global__ void __launch_bounds__(1024) k_batch_begin(BatchPlan plan, cudaGraphConditionalHandle h) {
   int any = 0;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) any |= solve_begin(sc[k].acc, sc[k].ctl);
+  for (int k = threadIdx.x; k < plan.n; k += blockDim.x) any |= solve_begin(plan.sc[k].acc, plan.sc[k].ctl);
   any = __syncthreads_or(any);
+  batch_compact(plan);
   if (threadIdx.x == 0) cudaGraphSetConditional(h, any ? 1u : 0u);
 }
 
-// Every iterating scene's cycle test (the others keep their state).
-__global__ void __launch_bounds__(1024) k_batch_check(const BatchScene* __restrict__ sc, int n,
-                                                      cudaGraphConditionalHandle h) {
+// Every iterating scene's cycle test (the others keep their state), the
+// compacted lists of the next cycle.
+__global__ void __launch_bounds__(1024) k_batch_check(BatchPlan plan, cudaGraphConditionalHandle h) {
   int any = 0;
-  for (int k = threadIdx.x; k < n; k += blockDim.x)
-    if (sc[k].ctl->cont) any |= solve_check(sc[k].acc, sc[k].ctl);
+  for (int k = threadIdx.x; k < plan.n; k += blockDim.x)
+    if (plan.sc[k].ctl->cont) any |= solve_check(plan.sc[k].acc, plan.sc[k].ctl);
   any = __syncthreads_or(any);
+  batch_compact(plan);
   if (threadIdx.x == 0) cudaGraphSetConditional(h, any ? 1u : 0u);
 }
 
@@ -1586,13 +1672,13 @@ __global__ void __launch_bounds__(256) k_batch_zero(const BatchScene* __restrict
   }
 }
 
-BatchSolve* batch_solve_create(const std::vector<Engine*>& es, std::string& why) {
-  if (es.empty()) {
+BatchSolve* batch_solve_create(const std::vector<Engine*>& es_in, std::string& why) {
+  if (es_in.empty()) {
     why = "no scenes";
     return nullptr;
   }
-  const fl_params& p0 = es[0]->prm;
-  for (const Engine* e : es) {
+  const fl_params& p0 = es_in[0]->prm;
+  for (const Engine* e : es_in) {
     if (e->prm.solver != FL_SOLVER_MG) why = "a scene solves with red-black SOR";
     else if (e->prm.mg_pre != p0.mg_pre || e->prm.mg_post != p0.mg_post)
       why = "the scenes' V-cycle shapes differ";
@@ -1602,13 +1688,17 @@ BatchSolve* batch_solve_create(const std::vector<Engine*>& es, std::string& why)
       why = "too many levels";
     if (!why.empty()) return nullptr;
   }
+  // the plan's scenes, largest first (blocks walk the items in this order)
+  std::vector<const Engine*> es(es_in.begin(), es_in.end());
+  std::stable_sort(es.begin(), es.end(), [](const Engine* x, const Engine* y) { return x->cells() > y->cells(); });
   BatchSolve* b = new BatchSolve();
   b->device = es[0]->device;
   b->n = (int)es.size();
   b->pre = p0.mg_pre;
   b->post = p0.mg_post;
+  cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+  if (b->sms < 1) b->sms = 1;
   std::vector<BatchScene> hs(es.size());
-  int depth = 0;
   for (size_t k = 0; k < es.size(); k++) {
     const Engine& e = *es[k];
     BatchScene& S = hs[k];
@@ -1632,61 +1722,69 @@ BatchSolve* batch_solve_create(const std::vector<Engine*>& es, std::string& why)
     S.acc = e.acc;
     b->any_mixed = b->any_mixed || mixed;
     b->tail_smem = std::max(b->tail_smem, e.coarse_smem);
-    depth = std::max(depth, S.lc);
+    b->depth = std::max(b->depth, S.lc);
   }
-  // items, largest scenes first within each phase (blocks start in order)
-  std::vector<int> order(es.size());
-  for (size_t k = 0; k < es.size(); k++) order[k] = (int)k;
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return hs[x].cells > hs[y].cells; });
+  const int n = b->n, depth = b->depth, nph = 2 * depth + 2;
   std::vector<BatchItem> items;
+  std::vector<int> base((size_t)nph * n, 0), count((size_t)nph * n, 0);
+  b->max_items.assign(nph, 0);
+  // scene k's items of phase ph, appended
+  auto add = [&](int ph, int k, auto&& emit) {
+    base[(size_t)ph * n + k] = (int)items.size();
+    emit();
+    count[(size_t)ph * n + k] = (int)items.size() - base[(size_t)ph * n + k];
+    b->max_items[ph] += count[(size_t)ph * n + k];
+  };
   auto smooth_items = [&](int k, int l, int halo) {
     const int T = 64 - 2 * halo;
     const BatchLevel& L = hs[k].lv[l];
     for (int by = 0; by < (L.ny + T - 1) / T; by++)
       for (int bx = 0; bx < (L.nx + T - 1) / T; bx++) items.push_back(BatchItem{k, l, bx, by});
   };
-  // PRE: scene k smooths level lc_k - depth + d at phase d (tails aligned)
-  for (int d = 0; d < depth; d++) {
-    const int off = (int)items.size();
-    for (int k : order) {
-      const int l = hs[k].lc - depth + d;
-      if (l >= 0) smooth_items(k, l, 2 * b->pre + 1);
-    }
-    b->pre_ph.push_back({off, (int)items.size() - off});
-  }
-  b->tail_ph.first = (int)items.size();
-  for (int k : order) items.push_back(BatchItem{k, hs[k].lc, 0, 0});
-  b->tail_ph.second = (int)items.size() - b->tail_ph.first;
-  // POST: level lc_k - 1 - d at phase d
-  for (int d = 0; d < depth; d++) {
-    const int off = (int)items.size();
-    for (int k : order) {
-      const int l = hs[k].lc - 1 - d;
-      if (l >= 0) smooth_items(k, l, 2 * b->post + 1);
-    }
-    b->post_ph.push_back({off, (int)items.size() - off});
-  }
-  b->defect_ph.first = (int)items.size();
-  for (int k : order) {
-    if (!hs[k].mixed) continue;
+  auto defect_items = [&](int k) {
     const BatchLevel& L = hs[k].lv[0];
     const int rows = hs[k].mixed == MIXED_DF ? DF_WARPS * DF_ROWS : UR_WARPS * UR_ROWS;
     for (int by = 0; by < (L.ny + rows - 1) / rows; by++)
       for (int bx = 0; bx < (L.nx + 29) / 30; bx++) items.push_back(BatchItem{k, 0, bx, by});
+  };
+  for (int k = 0; k < n; k++) {
+    // PRE: level lc_k - depth + d at phase d (the tails aligned); POST: level
+    // lc_k - 1 - d at phase depth + 1 + d
+    for (int d = 0; d < depth; d++) {
+      const int l = hs[k].lc - depth + d;
+      if (l >= 0) add(d, k, [&] { smooth_items(k, l, 2 * b->pre + 1); });
+    }
+    add(depth, k, [&] { items.push_back(BatchItem{k, hs[k].lc, 0, 0}); });
+    for (int d = 0; d < depth; d++) {
+      const int l = hs[k].lc - 1 - d;
+      if (l >= 0) add(depth + 1 + d, k, [&] { smooth_items(k, l, 2 * b->post + 1); });
+    }
+    if (hs[k].mixed) add(2 * depth + 1, k, [&] { defect_items(k); });
   }
-  b->defect_ph.second = (int)items.size() - b->defect_ph.first;
+  b->init_ph.first = (int)items.size();
+  for (int k = 0; k < n; k++)
+    if (hs[k].mixed) defect_items(k);
+  b->init_ph.second = (int)items.size() - b->init_ph.first;
   b->zero_ph.first = (int)items.size();
-  for (int k : order) {
+  for (int k = 0; k < n; k++) {
     const int blocks = (int)std::min<long>(64, std::max<long>(1, (hs[k].cells + 255) / 256));
     for (int q = 0; q < blocks; q++) items.push_back(BatchItem{k, 0, q, blocks});
   }
   b->zero_ph.second = (int)items.size() - b->zero_ph.first;
+  // lists: base, count [nph*n]; act_scene [nph*n]; act_pre [nph*(n+1)]; act_n, act_total [nph]
+  const size_t nl = 3 * (size_t)nph * n + (size_t)nph * (n + 1) + 2 * (size_t)nph;
   cudaError_t err = cudaMalloc(&b->scenes, hs.size() * sizeof(BatchScene));
   if (err == cudaSuccess) err = cudaMalloc(&b->items, items.size() * sizeof(BatchItem));
+  if (err == cudaSuccess) err = cudaMalloc(&b->lists, nl * sizeof(int));
+  if (err == cudaSuccess) err = cudaMemset(b->lists, 0, nl * sizeof(int));
   if (err == cudaSuccess)
     err = cudaMemcpy(b->scenes, hs.data(), hs.size() * sizeof(BatchScene), cudaMemcpyHostToDevice);
   if (err == cudaSuccess)
     err = cudaMemcpy(b->items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess)
+    err = cudaMemcpy(b->lists, base.data(), base.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess)
+    err = cudaMemcpy(b->lists + base.size(), count.data(), count.size() * sizeof(int), cudaMemcpyHostToDevice);
   if (err == cudaSuccess && b->tail_smem > 48 * 1024)
     err = cudaFuncSetAttribute(k_batch_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->tail_smem);
   if (err != cudaSuccess) {
@@ -1694,6 +1792,17 @@ BatchSolve* batch_solve_create(const std::vector<Engine*>& es, std::string& why)
     batch_solve_destroy(b);
     return nullptr;
   }
+  BatchPlan& P = b->plan;
+  P.sc = b->scenes;
+  P.items = b->items;
+  P.base = b->lists;
+  P.count = b->lists + (size_t)nph * n;
+  P.act_scene = b->lists + 2 * (size_t)nph * n;
+  P.act_pre = b->lists + 3 * (size_t)nph * n;
+  P.act_n = P.act_pre + (size_t)nph * (n + 1);
+  P.act_total = P.act_n + nph;
+  P.n = n;
+  P.nph = nph;
   return b;
 }
 
@@ -1701,20 +1810,26 @@ void batch_solve_destroy(BatchSolve* b) {
   if (!b) return;
   cudaFree(b->scenes);
   cudaFree(b->items);
+  cudaFree(b->lists);
   delete b;
 }
 
+// A cycle phase: a grid of at most `per_sm` blocks per SM (bounded by the
+// phase's items over all scenes) walking the iterating scenes' items.
+static unsigned phase_grid(const BatchSolve& b, int ph, int per_sm) {
+  return (unsigned)std::max(1, std::min(b.max_items[ph], b.sms * per_sm));
+}
+
 template <int MODE>
-static void launch_batch_smooth(cudaStream_t s, const BatchSolve& b, int pairs, std::pair<int, int> ph) {
-  if (ph.second == 0) return;
-  const BatchItem* it = b.items + ph.first;
-  const dim3 blk(32, 32);
+static void launch_batch_smooth(cudaStream_t s, const BatchSolve& b, int pairs, int ph) {
+  if (b.max_items[ph] == 0) return;
+  const dim3 blk(32, 32), g(phase_grid(b, ph, 1));
   switch (pairs) {
-    case 0: k_batch_smooth<0, MODE><<<ph.second, blk, 0, s>>>(b.scenes, it); break;
-    case 1: k_batch_smooth<1, MODE><<<ph.second, blk, 0, s>>>(b.scenes, it); break;
-    case 2: k_batch_smooth<2, MODE><<<ph.second, blk, 0, s>>>(b.scenes, it); break;
-    case 3: k_batch_smooth<3, MODE><<<ph.second, blk, 0, s>>>(b.scenes, it); break;
-    default: k_batch_smooth<4, MODE><<<ph.second, blk, 0, s>>>(b.scenes, it); break;
+    case 0: k_batch_smooth<0, MODE><<<g, blk, 0, s>>>(b.plan, ph); break;
+    case 1: k_batch_smooth<1, MODE><<<g, blk, 0, s>>>(b.plan, ph); break;
+    case 2: k_batch_smooth<2, MODE><<<g, blk, 0, s>>>(b.plan, ph); break;
+    case 3: k_batch_smooth<3, MODE><<<g, blk, 0, s>>>(b.plan, ph); break;
+    default: k_batch_smooth<4, MODE><<<g, blk, 0, s>>>(b.plan, ph); break;
   }
 }
 
@@ -1723,15 +1838,15 @@ static void launch_batch_smooth(cudaStream_t s, const BatchSolve& b, int pairs, 
 // `body`) is one V-cycle of every iterating scene plus the defect pass and
 // the cycle tests, then the p = 0 fill of scenes whose rhs vanished.
 cudaError_t batch_solve_enqueue(const BatchSolve& b, cudaStream_t s, cudaStream_t body) {
-  if (b.any_mixed && b.defect_ph.second > 0)
-    k_batch_defect<false><<<b.defect_ph.second, 32 * UR_WARPS, 0, s>>>(b.scenes, b.items + b.defect_ph.first);
+  if (b.init_ph.second > 0)
+    k_batch_defect_init<<<b.init_ph.second, 32 * UR_WARPS, 0, s>>>(b.scenes, b.items + b.init_ph.first);
   cudaStreamCaptureStatus cst;
   cudaGraph_t cap = nullptr;
   cudaError_t err = cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap, nullptr, nullptr, nullptr);
   cudaGraphConditionalHandle h = 0;
   if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&h, cap, 0, cudaGraphCondAssignDefault);
   if (err != cudaSuccess) return err;
-  k_batch_begin<<<1, 1024, 0, s>>>(b.scenes, b.n, h);
+  k_batch_begin<<<1, 1024, 0, s>>>(b.plan, h);
   const cudaGraphNode_t* deps = nullptr;
   size_t ndeps = 0;
   err = cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap, &deps, nullptr, &ndeps);
@@ -1747,12 +1862,13 @@ cudaError_t batch_solve_enqueue(const BatchSolve& b, cudaStream_t s, cudaStream_
     err = cudaStreamBeginCaptureToGraph(body, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                         cudaStreamCaptureModeThreadLocal);
   if (err != cudaSuccess) return err;
-  for (const auto& ph : b.pre_ph) launch_batch_smooth<MODE_PRE>(body, b, b.pre, ph);
-  k_batch_tail<<<b.tail_ph.second, dim3(32, 32), b.tail_smem, body>>>(b.scenes, b.items + b.tail_ph.first);
-  for (const auto& ph : b.post_ph) launch_batch_smooth<MODE_POST>(body, b, b.post, ph);
-  if (b.any_mixed && b.defect_ph.second > 0)
-    k_batch_defect<true><<<b.defect_ph.second, 32 * UR_WARPS, 0, body>>>(b.scenes, b.items + b.defect_ph.first);
-  k_batch_check<<<1, 1024, 0, body>>>(b.scenes, b.n, h);
+  const int D = b.depth;
+  for (int d = 0; d < D; d++) launch_batch_smooth<MODE_PRE>(body, b, b.pre, d);
+  k_batch_tail<<<phase_grid(b, D, 1), dim3(32, 32), b.tail_smem, body>>>(b.plan, D);
+  for (int d = 0; d < D; d++) launch_batch_smooth<MODE_POST>(body, b, b.post, D + 1 + d);
+  if (b.max_items[2 * D + 1] > 0)
+    k_batch_defect<<<phase_grid(b, 2 * D + 1, 8), 32 * UR_WARPS, 0, body>>>(b.plan, 2 * D + 1);
+  k_batch_check<<<1, 1024, 0, body>>>(b.plan, h);
   cudaGraph_t done = nullptr;
   err = cudaStreamEndCapture(body, &done);
   if (err != cudaSuccess) return err;
