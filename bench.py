@@ -17,7 +17,8 @@ advection with decay and inlet, CFL reduction.
           holding the whole state between steps: every step is one
           fl_step_host call (the GpuStep.step seam after invalidate()) that
           uploads u, v, p, label and dye from pinned host memory, steps, and
-          reads u, v, p and dye back.
+          reads back what the seam returns: u, v and the dye (p stays on the
+          device, as in the reference's GPU step).
   roofline  the phase with the most device time, algorithmic bytes / its
           event-timed duration, against MEASURED_PEAKS.json's HBM copy rate.
           Timed steps run as one CUDA graph each (the V-cycle loop is a
@@ -638,13 +639,15 @@ def run_ours(args, world, rank, local, pg):
     barrier(pg)
     te = time.perf_counter()
     for _ in range(args.e2e_steps):
-        # GpuStep.step with invalidate(): upload, step, readback in one call
-        eng.call("fl_step_host", native.FL_F32, ptr(hu), ptr(hv), ptr(hp), ptr(hl), ptr(hd), ptr(hu), ptr(hv), ptr(hp),
+        # GpuStep.step with invalidate() (stepGpu.ts:419-433: u, v, label, p
+        # and dye up), the step, and what the seam brings back: u and v
+        # (stepGpu.ts:578-604) and the dye (readDye); p stays on the device
+        eng.call("fl_step_host", native.FL_F32, ptr(hu), ptr(hv), ptr(hp), ptr(hl), ptr(hd), ptr(hu), ptr(hv), None,
                  ptr(hd), ctypes.byref(iters))
     e2e_s = max_over_ranks(pg, time.perf_counter() - te)
     e2e_value = world * args.e2e_steps / e2e_s
     h2d = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len) + eng.cells
-    d2h = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len)
+    d2h = 4 * (eng.ufaces + eng.vfaces + eng.dye_len)
 
     cnn = cnn_arm(args, local, stream, flush, state0=(f, patch)) if args.cnn_steps > 0 else None
     parity = parity_check(args, state, local) if state is not None and args.parity_steps > 0 else None
@@ -757,6 +760,11 @@ def run_batch(args, world, rank, local, pg):
         b.synchronize()
         alone_ms += a.elapsed_time(b) / 2
     bt = native.Batch(engines)
+    # the path (work-list solve or every engine's own graph) the autotuner
+    # measures faster on these scenes; results are identical either way
+    from flowlab_gb300 import autotune
+
+    path = autotune.tune_batch(bt, steps=2, warmup=1, device=local)
     worklist = bt.worklist
     stream = torch.cuda.ExternalStream(bt.stream(), device=local)
     bt.step(args.warmup)
@@ -797,7 +805,7 @@ def run_batch(args, world, rank, local, pg):
                                   "(scene, level, tile) work list, each scene's other passes as concurrent branches"
                                   if worklist else "each scene's step graph on its own stream (%s hardware queues)"
                                   % os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8")),
-                   "worklist": worklist,
+                   "worklist": worklist, "path_times_ms": path,
                    "scenes": args.scenes, "cells": total_cells, "l2": "working set far above L2 (no flush)",
                    "parallelism": "scenes dealt to ranks by cost" if world > 1 else "single GPU"},
         "cell_updates_per_s": value * total_cells,

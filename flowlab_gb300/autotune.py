@@ -116,6 +116,34 @@ def tune_warm_start(scene, prm, net, steps=8, warmup=3, device=0):
     return {"attach": attach, "reason": reason, "plain": plain, "warm": warm}
 
 
+def tune_batch(bt, steps=2, warmup=1, device=0):
+    """The batched scenes' path (native.Batch): the work-list solve (one
+    launch per V-cycle phase over every scene's tiles, the scenes in lock
+    step) against every engine's own step graph on its own stream (the
+    scenes overlapping freely), each timed on the batch itself; the faster
+    is kept. Both paths give identical results, so the batch advances
+    2 * (warmup + steps) steps here. Returns the times and the choice."""
+    import torch
+
+    out = {}
+    modes = [False] + ([True] if bt.worklist else [])
+    for on in modes:
+        bt.set_worklist(on)
+        stream = torch.cuda.ExternalStream(bt.stream(), device=device)
+        bt.step(warmup)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        bt.step(steps)
+        b.record(stream)
+        b.synchronize()
+        out["worklist_ms" if on else "engine_graphs_ms"] = a.elapsed_time(b) / steps
+    use = "worklist_ms" in out and out["worklist_ms"] < out["engine_graphs_ms"]
+    bt.set_worklist(use)
+    out["worklist"] = use
+    return out
+
+
 def pick_omega(results):
     """The omega with the smallest residual after the budget (ties: the
     smaller omega); results: [(omega, relative residual)]."""

@@ -1843,6 +1843,19 @@ void* fl_batch_stream(fl_batch* b) { return b ? (void*)b->stream : nullptr; }
 
 int fl_batch_worklist(const fl_batch* b) { return b && b->solve ? 1 : 0; }
 
+int fl_batch_set_worklist(fl_batch* b, int on) {
+  if (!b) return bfail(nullptr, FL_EINVAL, "null batch");
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  batch_graphs_free(b);
+  batch_solve_destroy(b->solve);
+  b->solve = nullptr;
+  if (!on) return FL_OK;
+  b->why_not.clear();
+  b->solve = batch_solve_create(batch_engines(b), b->why_not);
+  return b->solve ? FL_OK : bfail(b, FL_EINVAL, "work-list solve: %s", b->why_not.c_str());
+}
+
 int fl_batch_step(fl_batch* b, int nsteps) {
   if (!b) return bfail(nullptr, FL_EINVAL, "null batch");
   if (nsteps < 0) return bfail(b, FL_EINVAL, "nsteps < 0");

@@ -158,6 +158,7 @@ SIGNATURES = [
     ("fl_batch_last_error", ctypes.c_char_p, [_P]),
     ("fl_batch_stream", _P, [_P]),
     ("fl_batch_worklist", _I, [_P]),
+    ("fl_batch_set_worklist", _I, [_P, _I]),
     ("fl_batch_step", _I, [_P, _I]),
 ]
 
@@ -368,6 +369,11 @@ class Batch:
     def worklist(self):
         """True when the scenes' solves run as one launch per V-cycle phase."""
         return bool(self.lib.fl_batch_worklist(self.h))
+
+    def set_worklist(self, on):
+        st = self.lib.fl_batch_set_worklist(self.h, int(bool(on)))
+        if st != FL_OK:
+            raise FlowlabError(st, self.lib.fl_batch_last_error(self.h).decode())
 
     def close(self):
         if self.h:

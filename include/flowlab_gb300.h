@@ -404,6 +404,12 @@ void* fl_batch_stream(fl_batch* b);
  * with the multigrid, one V-cycle shape), 0 when it launches each engine's
  * own step graph on its own stream. */
 int fl_batch_worklist(const fl_batch* b);
+/* Chooses the path: 1 the work-list solve (FL_EINVAL, and the message in
+ * fl_batch_last_error, when some scene does not qualify), 0 every engine's
+ * own step graph on its own stream. Results are identical either way;
+ * which is faster depends on the scenes (flowlab_gb300/autotune.py times
+ * both). A batch starts on the work list when every scene qualifies. */
+int fl_batch_set_worklist(fl_batch* b, int on);
 /* nsteps steps of every engine, asynchronous; each engine's steps are
  * ordered after its earlier work and before its later work (its stream),
  * and after the batch stream's earlier work. */

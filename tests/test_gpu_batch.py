@@ -194,3 +194,29 @@ def test_batch_with_a_red_black_scene_launches_engine_graphs():
             b.close()
     finally:
         batch.close_all(es)
+
+
+def test_switching_paths_keeps_results():
+    """The same batch stepped through both paths in turn (work list, engine
+    graphs, work list) equals the scenes stepped alone."""
+    sides = [128, 64, 32]
+    alone = batch.make_engines(sides, seed=13)
+    together = batch.make_engines(sides, seed=13)
+    try:
+        for e in alone:
+            e.call("fl_step_auto", 6, None)
+        b = native.Batch(together)
+        try:
+            assert b.worklist
+            b.step(2)
+            b.set_worklist(False)
+            assert not b.worklist
+            b.step(2)
+            b.set_worklist(True)
+            assert b.worklist
+            b.step(2)
+        finally:
+            b.close()
+        assert_same(alone, together, "switching")
+    finally:
+        batch.close_all(alone + together)
