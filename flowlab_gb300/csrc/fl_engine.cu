@@ -202,6 +202,7 @@ void free_all(Engine* e) {
   if (e->diag_host) cudaFreeHost(e->diag_host);
   if (e->ev_dye) cudaEventDestroy(e->ev_dye);
   if (e->ev_proj) cudaEventDestroy(e->ev_proj);
+  if (e->ev_dye_done) cudaEventDestroy(e->ev_dye_done);
   if (e->ev_prior) cudaEventDestroy(e->ev_prior);
   if (e->stream2) cudaStreamDestroy(e->stream2);
   if (e->stream) cudaStreamDestroy(e->stream);
@@ -515,6 +516,8 @@ cudaError_t enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
   // forward: u,v + 3 planes + label in, 3 planes out (MacCormack: + backtrace
   // positions out); correction adds the hat planes and the positions
   prof_end(*e, tok, mac ? (4 * F + 32 * D + N) + (4 * F + 44 * D + N) : 4 * F + 24 * D + N, mac ? 2 : 1);
+  // the dye is final: fl_step_host reads it back from here on
+  cudaEventRecordWithFlags(e->ev_dye_done, s, capturing(s) ? cudaEventRecordExternal : 0);
   tok = prof_begin(*e, FL_PH_CFL);
   if (e->prm.residual_every > 0) {
     // with the residual diagnostic (simulation.ts:539-540) on its cadence
@@ -878,6 +881,7 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   if (cudaStreamCreateWithFlags(&e->stream2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_dye, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_proj, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->ev_dye_done, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_prior, cudaEventDisableTiming) != cudaSuccess) {
     fail(e, FL_EDEVICE, "stream creation failed");
     return bail(FL_EDEVICE);
@@ -1143,7 +1147,7 @@ int fl_step_host(fl_engine* h, int dtype, const void* u, const void* v, const vo
   TRY(graph_eligible(e) ? step_graph(e) : step_eager(e, true));
   TRY(check_launch(e, "step"));
   // velocity and pressure on the second stream once the projection is done
-  // (the step records ev_proj there), the dye after the whole step
+  // (the step records ev_proj there), the dye once the dye advection is done
   TRY(cuda_status(e, cudaStreamWaitEvent(e->stream2, e->ev_proj, 0), "read back"));
   if (u_out)
     TRY(cuda_status(e, cudaMemcpyAsync(u_out, e->u[e->cur], e->ufaces() * sizeof(float), cudaMemcpyDeviceToHost,
@@ -1163,9 +1167,13 @@ int fl_step_host(fl_engine* h, int dtype, const void* u, const void* v, const vo
                                          e->stream2), "read p"));
     }
   }
-  if (dye_out)
+  if (dye_out) {
+    // on the second stream once the dye advection is done (the step records
+    // ev_dye_done there), overlapping the CFL scan
+    TRY(cuda_status(e, cudaStreamWaitEvent(e->stream2, e->ev_dye_done, 0), "read back"));
     TRY(cuda_status(e, cudaMemcpyAsync(dye_out, e->dye[e->cur], 3 * e->dye_cells() * sizeof(float),
-                                       cudaMemcpyDeviceToHost, e->stream), "read dye"));
+                                       cudaMemcpyDeviceToHost, e->stream2), "read dye"));
+  }
   TRY(sync2(e, "read back"));
   TRY(sync(e, "step"));
   TRY(solve_stats(e));

@@ -77,6 +77,9 @@ struct Engine {
   // dye reader), the projection's end (velocity and pressure final), and
   // the stream's earlier work (before stream2 overwrites an input)
   cudaEvent_t ev_dye = nullptr, ev_proj = nullptr, ev_prior = nullptr;
+  // the dye advection's end: fl_step_host reads the dye back from here on,
+  // while the step's CFL scan runs
+  cudaEvent_t ev_dye_done = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   // the device-side work of fl_upload_fields after its copies (float32 p)
   cudaGraphExec_t upload_graph = nullptr;

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 
 #include "fl_internal.h"
 
@@ -287,30 +288,40 @@ __device__ __forceinline__ void smooth_tile(const SmoothArgs& a, int bx, int by)
         rc[r][c] = cnt == 4 ? 0.25f : (cnt == 2 ? 0.5f : (cnt == 1 ? 1.0f : 0.0f));
         xc[r][c] = o ? xx[r][1] : xx[r][0];
       }
+    // With omega = 1 (the multigrid's relaxation) the blend (1 - omega) x +
+    // omega pGS is pGS for every finite x, up to the sign of an exact zero
+    // (0 x + (-0) is +0), which compares equal: the sweeps then skip it.
+    auto sweeps = [&](auto unit) {
+      constexpr bool UNIT = decltype(unit)::value;
 #pragma unroll
-    for (int hs = 0; hs < 2 * P; hs++) {
-      const int c = hs & 1;
-      const int q = c ^ g;  // local parity plane of colour c
-      const float(*xo)[RGN / 2] = xs[1 - q];
+      for (int hs = 0; hs < 2 * P; hs++) {
+        const int c = hs & 1;
+        const int q = c ^ g;  // local parity plane of colour c
+        const float(*xo)[RGN / 2] = xs[1 - q];
 #pragma unroll
-      for (int r = 0; r < 2; r++) {
-        if (!act[r][c]) continue;
-        const int lj = ty + RGN_T * r;
-        const int o = oc[c];
-        float sum = 0.0f;
-        sum += xo[lj][tx + o];
-        sum += xo[lj][tx + o - 1];
-        sum += xo[lj + 1][tx];
-        sum += xo[lj - 1][tx];
-        const float d = sum - sb[r][c];
-        const float third = div3(d);
-        const float pgs = rc[r][c] != 0.0f ? d * rc[r][c] : third;
-        const float nv = keep * xc[r][c] + omega * pgs;
-        xc[r][c] = nv;
-        xs[q][lj][tx] = nv;
+        for (int r = 0; r < 2; r++) {
+          if (!act[r][c]) continue;
+          const int lj = ty + RGN_T * r;
+          const int o = oc[c];
+          float sum = 0.0f;
+          sum += xo[lj][tx + o];
+          sum += xo[lj][tx + o - 1];
+          sum += xo[lj + 1][tx];
+          sum += xo[lj - 1][tx];
+          const float d = sum - sb[r][c];
+          const float third = div3(d);
+          const float pgs = rc[r][c] != 0.0f ? d * rc[r][c] : third;
+          const float nv = UNIT ? pgs : keep * xc[r][c] + omega * pgs;
+          xc[r][c] = nv;
+          xs[q][lj][tx] = nv;
+        }
+        __syncthreads();
       }
-      __syncthreads();
-    }
+    };
+    if (omega == 1.0f)
+      sweeps(std::true_type{});
+    else
+      sweeps(std::false_type{});
 #pragma unroll
     for (int r = 0; r < 2; r++) {
       xx[r][0] = oc[0] == 0 ? xc[r][0] : xc[r][1];
@@ -571,32 +582,40 @@ __device__ void tail_smooth(unsigned char* smem, const CoarseLevel& L, int l, in
     }
   const bool two = L.slots == 2;
   const float keep = 1.0f - omega;
+  // omega = 1: pGS itself (see smooth_tile)
+  auto sweeps = [&](auto unit) {
+    constexpr bool UNIT = decltype(unit)::value;
 #pragma unroll 1
-  for (int hs = 0; hs < 2 * pairs; hs += 2) {
+    for (int hs = 0; hs < 2 * pairs; hs += 2) {
 #pragma unroll
-    for (int c = 0; c < 2; c++) {
+      for (int c = 0; c < 2; c++) {
 #pragma unroll
-      for (int s = 0; s < 2; s++) {
-        if (s == 1 && !two) continue;  // warp-uniform: the level has one row group per warp
-        const float v0 = lds_f32((uint32_t)nb[s][c][0]), v1 = lds_f32((uint32_t)nb[s][c][1]);
-        const float v2 = lds_f32((uint32_t)nb[s][c][2]), v3 = lds_f32((uint32_t)nb[s][c][3]);
-        float sum = 0.0f;
-        sum += v0;
-        sum += v1;
-        sum += v2;
-        sum += v3;
-        const float dv = sum - (-1.0f) * bq[s][c];
-        const float third = div3(dv);
-        const float pgs = rc[s][c] != 0.0f ? dv * rc[s][c] : third;
-        const float nv = keep * xq[s][c] + omega * pgs;
-        if (upd[s][c]) {
-          xq[s][c] = nv;
-          sts_f32((uint32_t)own[s][c], nv);
+        for (int s = 0; s < 2; s++) {
+          if (s == 1 && !two) continue;  // warp-uniform: the level has one row group per warp
+          const float v0 = lds_f32((uint32_t)nb[s][c][0]), v1 = lds_f32((uint32_t)nb[s][c][1]);
+          const float v2 = lds_f32((uint32_t)nb[s][c][2]), v3 = lds_f32((uint32_t)nb[s][c][3]);
+          float sum = 0.0f;
+          sum += v0;
+          sum += v1;
+          sum += v2;
+          sum += v3;
+          const float dv = sum - (-1.0f) * bq[s][c];
+          const float third = div3(dv);
+          const float pgs = rc[s][c] != 0.0f ? dv * rc[s][c] : third;
+          const float nv = UNIT ? pgs : keep * xq[s][c] + omega * pgs;
+          if (upd[s][c]) {
+            xq[s][c] = nv;
+            sts_f32((uint32_t)own[s][c], nv);
+          }
         }
+        tail_bar(l, L.nwarps);
       }
-      tail_bar(l, L.nwarps);
     }
-  }
+  };
+  if (omega == 1.0f)
+    sweeps(std::true_type{});
+  else
+    sweeps(std::false_type{});
   if (pairs <= 0) tail_bar(l, L.nwarps);
 }
 

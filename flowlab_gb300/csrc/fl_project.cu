@@ -152,6 +152,8 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
   const float coef = 1.0f / h;
   const float ns = as_rhs ? sc->neg_scale : 0.0f;
   // rows strided over a bounded grid, so that few blocks feed the atomics
+  // unrolled so that several rows' loads are in flight per thread
+#pragma unroll 4
   for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
     if (i >= nx) break;
     const long k = i + (long)j * nx;
@@ -536,6 +538,8 @@ __global__ void __launch_bounds__(256) k_cfl_residual(int nx, int ny, float h, c
   float2 sq = make_float2(0.0f, 0.0f);
   unsigned long long n = 0;
   const float coef = 1.0f / h;
+  // unrolled so that several rows' loads are in flight per thread
+#pragma unroll 4
   for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
     if (i >= nx) break;
     const long ku = i + (long)j * (nx + 1), kv = i + (long)j * nx;

@@ -213,8 +213,9 @@ int fl_step_auto(fl_engine* e, int nsteps, int* iters_last);
  * as after invalidate() (fl_upload_fields semantics); then one step with dt
  * from the device (fl_step_auto); then the results are copied into the
  * non-null outputs. With FL_F32 the dye upload overlaps the step's first
- * kernels and the velocity and pressure readback overlaps the dye
- * advection; FL_F64 converts on the device around synchronous copies.
+ * kernels, the velocity and pressure readback overlaps the dye advection
+ * and the dye readback the final CFL scan; FL_F64 converts on the device
+ * around synchronous copies.
  * Returns when every copy completed; results equal fl_upload_fields +
  * fl_step_auto + fl_read_* bit for bit. */
 int fl_step_host(fl_engine* e, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
