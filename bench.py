@@ -144,7 +144,7 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU-baseline sample")
     ap.add_argument("--parity-steps", type=int, default=2,
                     help="steps from the warmed-up state diffed against the float32 and float64 oracles (0: skip)")
-    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--profile-steps", type=int, default=8, help="eager steps with phase events, after the timed ones")
     ap.add_argument("--cnn-steps", type=int, default=30,
                     help="timed steps of the same workload with the trained U-Net warm start attached (0: skip)")
@@ -799,8 +799,8 @@ def run_batch(args, world, rank, local, pg):
         "data": "synthetic (seeded random closed-box scenes)",
         "config": {"workload": "%d closed-box scenes, sides 2^U{6..10} (%d cells), 0-12 discs, smoothed-noise "
                                "velocity, multigrid V(3,3) to 1e-6 (float32 fields and smoothing, float64 residual; "
-                               "cap 40 cycles), %s"
-                               % (args.scenes, total_cells,
+                               "cap %d cycles), %s"
+                               % (args.scenes, total_cells, batch.BATCH_MAX_CYCLES,
                                   "one graph per step: the scenes' solves as one launch per V-cycle phase over a "
                                   "(scene, level, tile) work list, each scene's other passes as concurrent branches"
                                   if worklist else "each scene's step graph on its own stream (%s hardware queues)"
@@ -813,6 +813,7 @@ def run_batch(args, world, rank, local, pg):
         "rank0_sum_of_single_scene_step_ms": alone_ms,
         "rank0_concurrency_gain": alone_ms / (ms / args.steps),
         "vcycles_per_step_mean": statistics.mean(s["cycles"] for s in stats),
+        "vcycles_last_step_max": max(s["cycles"] for s in stats),
         "rel_residual_max": max(s["rel_residual"] for s in stats),
         # scenes whose last step reached the tolerance within the cycle cap
         # (obstacle-rich scenes contract ~0.9 per V-cycle in this multigrid,

@@ -41,7 +41,14 @@ def shard(costs, world, rank):
     return [k for k in range(len(costs)) if owner[k] == rank]
 
 
-def make_engines(sides, seed=2024, device=0, params=None, tol=1e-6, max_cycles=40, mixed=1):
+# Obstacle-rich scenes contract ~0.9 per V-cycle in this multigrid (the
+# float64 oracle alike), so a step from a relative residual of 1e-2 to 1e-6
+# can take ~90 cycles; they are small, latency-bound scenes that run beside
+# the large ones, so a cap of 100 costs little and lets every scene converge.
+BATCH_MAX_CYCLES = 100
+
+
+def make_engines(sides, seed=2024, device=0, params=None, tol=1e-6, max_cycles=BATCH_MAX_CYCLES, mixed=1):
     """One engine per side, fields uploaded; scene k uses seed + k."""
     engines = []
     for k, n in enumerate(sides):
