@@ -733,9 +733,9 @@ int step_graph(Engine* e) {
 
 // Fills last_iters / last_relres / last_div_rms from the control block when
 // the last solve ran under the device's control (synchronises).
-int solve_stats(Engine* e) {
+int solve_stats(Engine* e, bool ctl_read = false) {
   if (!e->stats_on_device) return FL_OK;
-  TRY(read_ctl(e));
+  if (!ctl_read) TRY(read_ctl(e));
   const SolveCtl& c = *e->ctl_host;
   e->last_div_rms = c.b_rms;
   if (c.mode == SOLVE_RB) {
@@ -1174,9 +1174,14 @@ int fl_step_host(fl_engine* h, int dtype, const void* u, const void* v, const vo
     TRY(cuda_status(e, cudaMemcpyAsync(dye_out, e->dye[e->cur], 3 * e->dye_cells() * sizeof(float),
                                        cudaMemcpyDeviceToHost, e->stream2), "read dye"));
   }
+  // the solve's control block comes back with the step (one synchronisation)
+  const bool ctl_read = e->stats_on_device;
+  if (ctl_read)
+    TRY(cuda_status(e, cudaMemcpyAsync(e->ctl_host, e->ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, e->stream),
+                    "read solve state"));
   TRY(sync2(e, "read back"));
   TRY(sync(e, "step"));
-  TRY(solve_stats(e));
+  TRY(solve_stats(e, ctl_read));
   if (iters) *iters = e->last_iters;
   return FL_OK;
 }
