@@ -203,6 +203,7 @@ void free_all(Engine* e) {
   if (e->ev_dye) cudaEventDestroy(e->ev_dye);
   if (e->ev_proj) cudaEventDestroy(e->ev_proj);
   if (e->ev_dye_done) cudaEventDestroy(e->ev_dye_done);
+  if (e->ev_p) cudaEventDestroy(e->ev_p);
   if (e->ev_prior) cudaEventDestroy(e->ev_prior);
   if (e->stream2) cudaStreamDestroy(e->stream2);
   if (e->stream) cudaStreamDestroy(e->stream);
@@ -376,6 +377,12 @@ void wait_dye(Engine* e, cudaStream_t s) {
   cudaStreamWaitEvent(s, e->ev_dye, capturing(s) ? cudaEventWaitExternal : 0);
 }
 
+// Likewise for the pressure fl_step_host uploads on the second stream: the
+// first reader of p (the warm starts, the solve) waits here.
+void wait_p(Engine* e, cudaStream_t s) {
+  cudaStreamWaitEvent(s, e->ev_p, capturing(s) ? cudaEventWaitExternal : 0);
+}
+
 // advect u,v -> [stir] -> [confinement] -> body forces -> divergence
 void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
   Level& L0 = e->levels[0];
@@ -413,6 +420,7 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
   launch_divergence(s, e->nx, e->ny, e->h, u, v, L0.b, e->prm.solver == FL_SOLVER_MG, L0.label, e->sc, e->acc,
                     step_mixed(e) ? e->b_lo : nullptr);
   prof_end(*e, tok, 4 * F + N + 4 * N, 1);
+  wait_p(e, s);
   if (e->prm.warm_extrapolate && e->prm.solver == FL_SOLVER_MG) {
     const bool mixed = e->prm.mixed != 0;
     launch_extrapolate(s, e->cells(), L0.label, L0.x[0], e->pprev32, mixed ? e->p64[0] : nullptr,
@@ -645,6 +653,8 @@ void destroy_graphs(Engine* e) {
   destroy_step_graphs(e);
   if (e->upload_graph) cudaGraphExecDestroy(e->upload_graph);
   e->upload_graph = nullptr;
+  if (e->upload_graph_nop) cudaGraphExecDestroy(e->upload_graph_nop);
+  e->upload_graph_nop = nullptr;
 }
 
 // Enqueues one whole step for buffer parity `par` on e->stream while that
@@ -882,6 +892,7 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
       cudaEventCreateWithFlags(&e->ev_dye, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_proj, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_dye_done, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->ev_p, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_prior, cudaEventDisableTiming) != cudaSuccess) {
     fail(e, FL_EDEVICE, "stream creation failed");
     return bail(FL_EDEVICE);
@@ -957,12 +968,19 @@ int fl_synchronize(fl_engine* h) {
 // every time; captured (`capture`), the rebuild is the body of an IF node
 // that runs only when some label changed (the caller forces it by filling
 // levels[0].label with a value no label has, when the codes are stale).
-cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture) {
-  cudaStream_t s = e->stream;
-  cudaError_t err = cudaSuccess;
+// The pressure's part of it: the refined pressure from the float32 one (when
+// it came as float32) and the warm-start history, on stream `s`.
+void enqueue_p_after_upload(Engine* e, cudaStream_t s, bool p64_from_p32) {
   if (p64_from_p32) launch_convert(s, e->levels[0].x[0], FL_F32, e->p64[0], refined_df(e) ? DT_DF : FL_F64, e->cells());
   cudaMemcpyAsync(e->pprev32, e->levels[0].x[0], e->cells() * 4, cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(e->pprev64, e->p64[0], e->cells() * 8, cudaMemcpyDeviceToDevice, s);
+}
+
+// with_p false: without the pressure's part (the caller enqueues it elsewhere)
+cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture, bool with_p = true) {
+  cudaStream_t s = e->stream;
+  cudaError_t err = cudaSuccess;
+  if (with_p) enqueue_p_after_upload(e, s, p64_from_p32);
   launch_label_sync(s, e->label_in, e->levels[0].label, e->cells(), e->label_flag);
   if (!capture) {
     cudaMemsetAsync(e->label_flag, 0, sizeof(int), s);
@@ -1020,13 +1038,19 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
   e->cur = 0;
   e->stats_on_device = false;
   if (dye_async && !dye) return fail(e, FL_EINVAL, "upload dye: null pointer");
+  // fl_step_host's float32 upload: the pressure (and what is formed from it)
+  // and the dye go on the second stream behind the copies the step starts
+  // with; the step waits for them where it first reads them
+  const bool async_p = dye_async && dtype == FL_F32 && e->use_graphs;
   TRY(put_step_ctl(e, true));
   TRY(upload(e, e->u[0], u, e->ufaces(), dtype, "upload u"));
   TRY(upload(e, e->v[0], v, e->vfaces(), dtype, "upload v"));
-  if (p)
-    TRY(upload(e, e->levels[0].x[0], p, e->cells(), dtype, "upload p"));
-  else
-    TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].x[0], 0, e->cells() * 4, e->stream), "zero p"));
+  if (!async_p) {
+    if (p)
+      TRY(upload(e, e->levels[0].x[0], p, e->cells(), dtype, "upload p"));
+    else
+      TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].x[0], 0, e->cells() * 4, e->stream), "zero p"));
+  }
   const bool p64_direct = p && dtype == FL_F64;
   if (p64_direct && refined_df(e)) {
     // the double-float pairs from the float64 pressure
@@ -1041,15 +1065,26 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
   if (dye_async) {
     // after the copies the step starts with (which it would otherwise share
     // the host link with) and the stream's earlier work (which may still read
-    // the dye buffer)
+    // the dye and pressure buffers)
     TRY(cuda_status(e, cudaEventRecord(e->ev_prior, e->stream), "upload dye"));
     TRY(cuda_status(e, cudaStreamWaitEvent(e->stream2, e->ev_prior, 0), "upload dye"));
+    if (async_p) {
+      if (p)
+        TRY(cuda_status(e, cudaMemcpyAsync(e->levels[0].x[0], p, e->cells() * sizeof(float), cudaMemcpyHostToDevice,
+                                           e->stream2), "upload p"));
+      else
+        TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].x[0], 0, e->cells() * 4, e->stream2), "zero p"));
+      enqueue_p_after_upload(e, e->stream2, true);
+      TRY(check_launch(e, "upload p"));
+    }
+    TRY(cuda_status(e, cudaEventRecord(e->ev_p, e->stream2), "upload p"));
     TRY(cuda_status(e, cudaMemcpyAsync(e->dye[0], dye, 3 * e->dye_cells() * sizeof(float), cudaMemcpyHostToDevice,
                                        e->stream2), "upload dye"));
   } else {
     TRY(upload(e, e->dye[0], dye, 3 * e->dye_cells(), dtype, "upload dye"));
   }
   TRY(cuda_status(e, cudaEventRecord(e->ev_dye, e->stream2), "upload dye"));
+  if (!dye_async) TRY(cuda_status(e, cudaEventRecord(e->ev_p, e->stream2), "upload p"));
   // stale codes (new levels, labels written by another entry point): make
   // every cell differ so that the rebuild runs
   if (!e->codes_valid || e->labels_dirty)
@@ -1059,23 +1094,24 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
   } else {
     // one graph launch instead of ~20 launches (captured once per parameter
     // set); the label rebuild runs only when the labels changed
-    if (!e->upload_graph) {
+    cudaGraphExec_t& ug = async_p ? e->upload_graph_nop : e->upload_graph;
+    if (!ug) {
       cudaGraph_t g = nullptr;
       cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
       if (err == cudaSuccess) {
-        err = enqueue_after_upload(e, true, true);
+        err = enqueue_after_upload(e, true, true, !async_p);
         cudaError_t end = cudaStreamEndCapture(e->stream, &g);
         if (err == cudaSuccess) err = end;
       }
-      if (err == cudaSuccess) err = cudaGraphInstantiate(&e->upload_graph, g, 0);
+      if (err == cudaSuccess) err = cudaGraphInstantiate(&ug, g, 0);
       if (g) cudaGraphDestroy(g);
       if (err != cudaSuccess) {
         cudaGetLastError();
-        e->upload_graph = nullptr;
+        ug = nullptr;
         return cuda_status(e, err, "upload graph");
       }
     }
-    TRY(cuda_status(e, cudaGraphLaunch(e->upload_graph, e->stream), "upload graph"));
+    TRY(cuda_status(e, cudaGraphLaunch(ug, e->stream), "upload graph"));
   }
   TRY(check_launch(e, "upload"));
   e->codes_valid = true;
