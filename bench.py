@@ -17,8 +17,7 @@ advection with decay and inlet, CFL reduction.
           holding the whole state between steps: every step is one
           fl_step_host call (the GpuStep.step seam after invalidate()) that
           uploads u, v, p, label and dye from pinned host memory, steps, and
-          reads back what the seam returns: u, v and the dye (p stays on the
-          device, as in the reference's GPU step).
+          reads u, v, p and dye back.
   roofline  the phase with the most device time, algorithmic bytes / its
           event-timed duration, against MEASURED_PEAKS.json's HBM copy rate.
           Timed steps run as one CUDA graph each (the V-cycle loop is a
@@ -640,14 +639,15 @@ def run_ours(args, world, rank, local, pg):
     te = time.perf_counter()
     for _ in range(args.e2e_steps):
         # GpuStep.step with invalidate() (stepGpu.ts:419-433: u, v, label, p
-        # and dye up), the step, and what the seam brings back: u and v
-        # (stepGpu.ts:578-604) and the dye (readDye); p stays on the device
-        eng.call("fl_step_host", native.FL_F32, ptr(hu), ptr(hv), ptr(hp), ptr(hl), ptr(hd), ptr(hu), ptr(hv), None,
+        # and dye up), the step, and the whole state back: the host holds it
+        # between steps, so p comes back too (re-uploading a stale p would
+        # hand the solve an old warm start)
+        eng.call("fl_step_host", native.FL_F32, ptr(hu), ptr(hv), ptr(hp), ptr(hl), ptr(hd), ptr(hu), ptr(hv), ptr(hp),
                  ptr(hd), ctypes.byref(iters))
     e2e_s = max_over_ranks(pg, time.perf_counter() - te)
     e2e_value = world * args.e2e_steps / e2e_s
     h2d = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len) + eng.cells
-    d2h = 4 * (eng.ufaces + eng.vfaces + eng.dye_len)
+    d2h = 4 * (eng.ufaces + eng.vfaces + eng.cells + eng.dye_len)
 
     cnn = cnn_arm(args, local, stream, flush, state0=(f, patch)) if args.cnn_steps > 0 else None
     parity = parity_check(args, state, local) if state is not None and args.parity_steps > 0 else None
