@@ -1068,6 +1068,10 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
     // the dye and pressure buffers)
     TRY(cuda_status(e, cudaEventRecord(e->ev_prior, e->stream), "upload dye"));
     TRY(cuda_status(e, cudaStreamWaitEvent(e->stream2, e->ev_prior, 0), "upload dye"));
+    // the dye first: the step's body forces read it before the solve reads p
+    TRY(cuda_status(e, cudaMemcpyAsync(e->dye[0], dye, 3 * e->dye_cells() * sizeof(float), cudaMemcpyHostToDevice,
+                                       e->stream2), "upload dye"));
+    TRY(cuda_status(e, cudaEventRecord(e->ev_dye, e->stream2), "upload dye"));
     if (async_p) {
       if (p)
         TRY(cuda_status(e, cudaMemcpyAsync(e->levels[0].x[0], p, e->cells() * sizeof(float), cudaMemcpyHostToDevice,
@@ -1078,13 +1082,11 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
       TRY(check_launch(e, "upload p"));
     }
     TRY(cuda_status(e, cudaEventRecord(e->ev_p, e->stream2), "upload p"));
-    TRY(cuda_status(e, cudaMemcpyAsync(e->dye[0], dye, 3 * e->dye_cells() * sizeof(float), cudaMemcpyHostToDevice,
-                                       e->stream2), "upload dye"));
   } else {
     TRY(upload(e, e->dye[0], dye, 3 * e->dye_cells(), dtype, "upload dye"));
+    TRY(cuda_status(e, cudaEventRecord(e->ev_dye, e->stream2), "upload dye"));
+    TRY(cuda_status(e, cudaEventRecord(e->ev_p, e->stream2), "upload p"));
   }
-  TRY(cuda_status(e, cudaEventRecord(e->ev_dye, e->stream2), "upload dye"));
-  if (!dye_async) TRY(cuda_status(e, cudaEventRecord(e->ev_p, e->stream2), "upload p"));
   // stale codes (new levels, labels written by another entry point): make
   // every cell differ so that the rebuild runs
   if (!e->codes_valid || e->labels_dirty)
