@@ -415,7 +415,7 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
     flaunch += 1;
   }
   prof_end(*e, tok, fbytes, flaunch);
-  cudaMemsetAsync(e->acc, 0, 4 * sizeof(double), s);
+  launch_fill32(s, e->acc, 4 * sizeof(double) / 4, 0u);  // b_sq, res_sq, n_fluid, n_res
   tok = prof_begin(*e, FL_PH_DIVERGENCE);
   launch_divergence(s, e->nx, e->ny, e->h, u, v, L0.b, e->prm.solver == FL_SOLVER_MG, L0.label, e->sc, e->acc,
                     step_mixed(e) ? e->b_lo : nullptr);
@@ -498,7 +498,7 @@ void enqueue_rb_fixed(Engine* e, cudaStream_t s) {
     src = 1 - src;
     k += chunk;
   }
-  if (src == 1) cudaMemcpyAsync(L.x[0], L.x[1], e->cells() * sizeof(float), cudaMemcpyDeviceToDevice, s);
+  if (src == 1) launch_copy32(s, L.x[1], L.x[0], e->cells());
   launch_zero_if(s, e->ctl, L.x[0], nullptr, nullptr, e->cells());
 }
 
@@ -972,8 +972,8 @@ int fl_synchronize(fl_engine* h) {
 // it came as float32) and the warm-start history, on stream `s`.
 void enqueue_p_after_upload(Engine* e, cudaStream_t s, bool p64_from_p32) {
   if (p64_from_p32) launch_convert(s, e->levels[0].x[0], FL_F32, e->p64[0], refined_df(e) ? DT_DF : FL_F64, e->cells());
-  cudaMemcpyAsync(e->pprev32, e->levels[0].x[0], e->cells() * 4, cudaMemcpyDeviceToDevice, s);
-  cudaMemcpyAsync(e->pprev64, e->p64[0], e->cells() * 8, cudaMemcpyDeviceToDevice, s);
+  launch_copy32(s, e->levels[0].x[0], e->pprev32, e->cells());
+  launch_copy32(s, e->p64[0], e->pprev64, 2 * e->cells());
 }
 
 // with_p false: without the pressure's part (the caller enqueues it elsewhere)
@@ -1019,7 +1019,7 @@ cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture, boo
       }
     }
   }
-  cudaMemsetAsync(e->time_dev, 0, sizeof(double), s);
+  launch_fill32(s, e->time_dev, 2, 0u);
   launch_max_speed(s, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);
   return err;
 }

@@ -209,6 +209,9 @@ BatchSolve* batch_solve_create(const std::vector<Engine*>& engines, std::string&
 void batch_solve_destroy(BatchSolve* b);
 cudaError_t batch_solve_enqueue(const BatchSolve& b, cudaStream_t s, cudaStream_t body);
 
+// Word fills and copies as kernels (not copy-engine nodes) in the graphs.
+void launch_fill32(cudaStream_t s, void* p, long words, uint32_t v);
+void launch_copy32(cudaStream_t s, const void* src, void* dst, long words);
 // The end-of-step CFL scan with the residual diagnostic folded in (every
 // residual_every steps: the post-step divergence and its statistics); the
 // step's dt joins the clock and the next step's scalars are written.

@@ -616,6 +616,28 @@ void launch_cfl_residual(cudaStream_t s, int nx, int ny, float h, const float* u
                                  write_scalars, add_time);
 }
 
+// Fills and device-to-device copies inside the step and upload graphs run as
+// kernels: as memset or memcpy nodes they would queue on the copy engine
+// behind the host transfers of fl_step_host (measured: the upload graph took
+// 64 us behind the dye upload, 43 us without it).
+__global__ void __launch_bounds__(256) k_fill32(uint32_t* __restrict__ p, long n, uint32_t v) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) p[k] = v;
+}
+
+__global__ void __launch_bounds__(256) k_copy32(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, long n) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) dst[k] = src[k];
+}
+
+void launch_fill32(cudaStream_t s, void* p, long words, uint32_t v) {
+  const long blocks = std::max(1L, std::min((words + 255) / 256, 152L * 8));
+  k_fill32<<<(unsigned)blocks, 256, 0, s>>>(static_cast<uint32_t*>(p), words, v);
+}
+
+void launch_copy32(cudaStream_t s, const void* src, void* dst, long words) {
+  const long blocks = std::max(1L, std::min((words + 255) / 256, 152L * 8));
+  k_copy32<<<(unsigned)blocks, 256, 0, s>>>(static_cast<const uint32_t*>(src), static_cast<uint32_t*>(dst), words);
+}
+
 void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const float* v, StepAccum* acc,
                       StepScalars* sc_next, double* time_dev, const fl_params* prm, float h, bool write_scalars,
                       bool add_time) {
