@@ -204,6 +204,9 @@ void free_all(Engine* e) {
   if (e->ev_proj) cudaEventDestroy(e->ev_proj);
   if (e->ev_dye_done) cudaEventDestroy(e->ev_dye_done);
   if (e->ev_p) cudaEventDestroy(e->ev_p);
+  if (e->ev_lab) cudaEventDestroy(e->ev_lab);
+  if (e->ev_lab_done) cudaEventDestroy(e->ev_lab_done);
+  if (e->stream3) cudaStreamDestroy(e->stream3);
   if (e->ev_prior) cudaEventDestroy(e->ev_prior);
   if (e->stream2) cudaStreamDestroy(e->stream2);
   if (e->stream) cudaStreamDestroy(e->stream);
@@ -653,8 +656,8 @@ void destroy_graphs(Engine* e) {
   destroy_step_graphs(e);
   if (e->upload_graph) cudaGraphExecDestroy(e->upload_graph);
   e->upload_graph = nullptr;
-  if (e->upload_graph_nop) cudaGraphExecDestroy(e->upload_graph_nop);
-  e->upload_graph_nop = nullptr;
+  if (e->upload_graph_labels) cudaGraphExecDestroy(e->upload_graph_labels);
+  e->upload_graph_labels = nullptr;
 }
 
 // Enqueues one whole step for buffer parity `par` on e->stream while that
@@ -893,6 +896,9 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
       cudaEventCreateWithFlags(&e->ev_proj, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_dye_done, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_p, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->ev_lab, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->ev_lab_done, cudaEventDisableTiming) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&e->stream3, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_prior, cudaEventDisableTiming) != cudaSuccess) {
     fail(e, FL_EDEVICE, "stream creation failed");
     return bail(FL_EDEVICE);
@@ -976,8 +982,10 @@ void enqueue_p_after_upload(Engine* e, cudaStream_t s, bool p64_from_p32) {
   launch_copy32(s, e->p64[0], e->pprev64, 2 * e->cells());
 }
 
-// with_p false: without the pressure's part (the caller enqueues it elsewhere)
-cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture, bool with_p = true) {
+// with_p false: without the pressure's part; with_cfl false: without the
+// clock reset and the CFL scalars (the caller enqueues them elsewhere)
+cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture, bool with_p = true,
+                                 bool with_cfl = true) {
   cudaStream_t s = e->stream;
   cudaError_t err = cudaSuccess;
   if (with_p) enqueue_p_after_upload(e, s, p64_from_p32);
@@ -1019,8 +1027,10 @@ cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture, boo
       }
     }
   }
-  launch_fill32(s, e->time_dev, 2, 0u);
-  launch_max_speed(s, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);
+  if (with_cfl) {
+    launch_fill32(s, e->time_dev, 2, 0u);
+    launch_max_speed(s, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);
+  }
   return err;
 }
 
@@ -1033,16 +1043,54 @@ namespace {
 // fields' copies, and ev_dye marks its end; the step's first dye reader
 // waits for it (wait_dye). Otherwise
 // ev_dye is recorded on the second stream with nothing in flight.
+// The label part of fl_step_host's upload as a graph (captured on the third
+// stream: label compare, then the rebuild only when some label changed).
+int label_graph(Engine* e) {
+  if (e->upload_graph_labels) return FL_OK;
+  cudaStream_t s = e->stream;
+  e->stream = e->stream3;
+  cudaGraph_t g = nullptr;
+  cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+  if (err == cudaSuccess) {
+    err = enqueue_after_upload(e, false, true, false, false);
+    cudaError_t end = cudaStreamEndCapture(e->stream, &g);
+    if (err == cudaSuccess) err = end;
+  }
+  e->stream = s;
+  if (err == cudaSuccess) err = cudaGraphInstantiate(&e->upload_graph_labels, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (err != cudaSuccess) {
+    cudaGetLastError();
+    e->upload_graph_labels = nullptr;
+    return cuda_status(e, err, "label graph");
+  }
+  return FL_OK;
+}
+
 int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
                   const void* dye, bool dye_async) {
   e->cur = 0;
   e->stats_on_device = false;
   if (dye_async && !dye) return fail(e, FL_EINVAL, "upload dye: null pointer");
-  // fl_step_host's float32 upload: the pressure (and what is formed from it)
-  // and the dye go on the second stream behind the copies the step starts
-  // with; the step waits for them where it first reads them
+  // fl_step_host's float32 upload, on three streams: the labels first, their
+  // compare and rebuild on the third stream while u and v arrive on the
+  // engine's stream (followed by the CFL scalars); the dye, then the
+  // pressure (and what is formed from it) on the second stream behind u and
+  // v. The step waits for each where it first reads it.
   const bool async_p = dye_async && dtype == FL_F32 && e->use_graphs;
+  if (async_p) TRY(label_graph(e));
   TRY(put_step_ctl(e, true));
+  if (async_p) {
+    // stale codes (new levels, labels written by another entry point): make
+    // every cell differ so that the rebuild runs
+    if (!e->codes_valid || e->labels_dirty)
+      TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].label, 0xff, (size_t)e->cells(), e->stream), "upload label"));
+    TRY(up32(e, e->label_in, label, (size_t)e->cells(), "upload label"));
+    TRY(cuda_status(e, cudaEventRecord(e->ev_lab, e->stream), "upload label"));
+    TRY(cuda_status(e, cudaStreamWaitEvent(e->stream3, e->ev_lab, 0), "upload label"));
+    TRY(cuda_status(e, cudaGraphLaunch(e->upload_graph_labels, e->stream3), "label graph"));
+    TRY(cuda_status(e, cudaEventRecord(e->ev_lab_done, e->stream3), "upload label"));
+  }
   TRY(upload(e, e->u[0], u, e->ufaces(), dtype, "upload u"));
   TRY(upload(e, e->v[0], v, e->vfaces(), dtype, "upload v"));
   if (!async_p) {
@@ -1061,7 +1109,7 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
     TRY(cuda_status(e, cudaMemcpyAsync(e->p64[0], p, e->cells() * sizeof(double), cudaMemcpyHostToDevice, e->stream),
                     "upload p64"));
   }
-  TRY(up32(e, e->label_in, label, (size_t)e->cells(), "upload label"));
+  if (!async_p) TRY(up32(e, e->label_in, label, (size_t)e->cells(), "upload label"));
   if (dye_async) {
     // after the copies the step starts with (which it would otherwise share
     // the host link with) and the stream's earlier work (which may still read
@@ -1087,33 +1135,41 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
     TRY(cuda_status(e, cudaEventRecord(e->ev_dye, e->stream2), "upload dye"));
     TRY(cuda_status(e, cudaEventRecord(e->ev_p, e->stream2), "upload p"));
   }
-  // stale codes (new levels, labels written by another entry point): make
-  // every cell differ so that the rebuild runs
-  if (!e->codes_valid || e->labels_dirty)
-    TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].label, 0xff, (size_t)e->cells(), e->stream), "upload label"));
-  if (p64_direct || !e->use_graphs) {
-    TRY(cuda_status(e, enqueue_after_upload(e, !p64_direct, false), "upload"));
+  if (async_p) {
+    // the clock and the first step's CFL scalars from the uploaded velocity,
+    // then the labels' part joins
+    launch_fill32(e->stream, e->time_dev, 2, 0u);
+    launch_max_speed(e->stream, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true,
+                     false);
+    TRY(cuda_status(e, cudaStreamWaitEvent(e->stream, e->ev_lab_done, 0), "upload label"));
   } else {
-    // one graph launch instead of ~20 launches (captured once per parameter
-    // set); the label rebuild runs only when the labels changed
-    cudaGraphExec_t& ug = async_p ? e->upload_graph_nop : e->upload_graph;
-    if (!ug) {
-      cudaGraph_t g = nullptr;
-      cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
-      if (err == cudaSuccess) {
-        err = enqueue_after_upload(e, true, true, !async_p);
-        cudaError_t end = cudaStreamEndCapture(e->stream, &g);
-        if (err == cudaSuccess) err = end;
+    // stale codes (new levels, labels written by another entry point): make
+    // every cell differ so that the rebuild runs
+    if (!e->codes_valid || e->labels_dirty)
+      TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].label, 0xff, (size_t)e->cells(), e->stream), "upload label"));
+    if (p64_direct || !e->use_graphs) {
+      TRY(cuda_status(e, enqueue_after_upload(e, !p64_direct, false), "upload"));
+    } else {
+      // one graph launch instead of ~20 launches (captured once per parameter
+      // set); the label rebuild runs only when the labels changed
+      if (!e->upload_graph) {
+        cudaGraph_t g = nullptr;
+        cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+        if (err == cudaSuccess) {
+          err = enqueue_after_upload(e, true, true);
+          cudaError_t end = cudaStreamEndCapture(e->stream, &g);
+          if (err == cudaSuccess) err = end;
+        }
+        if (err == cudaSuccess) err = cudaGraphInstantiate(&e->upload_graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (err != cudaSuccess) {
+          cudaGetLastError();
+          e->upload_graph = nullptr;
+          return cuda_status(e, err, "upload graph");
+        }
       }
-      if (err == cudaSuccess) err = cudaGraphInstantiate(&ug, g, 0);
-      if (g) cudaGraphDestroy(g);
-      if (err != cudaSuccess) {
-        cudaGetLastError();
-        ug = nullptr;
-        return cuda_status(e, err, "upload graph");
-      }
+      TRY(cuda_status(e, cudaGraphLaunch(e->upload_graph, e->stream), "upload graph"));
     }
-    TRY(cuda_status(e, cudaGraphLaunch(ug, e->stream), "upload graph"));
   }
   TRY(check_launch(e, "upload"));
   e->codes_valid = true;

@@ -83,10 +83,14 @@ struct Engine {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   // the device-side work of fl_upload_fields after its copies (float32 p)
   cudaGraphExec_t upload_graph = nullptr;
-  // the same without the pressure's part, for fl_step_host, whose pressure
-  // arrives on the second stream (ev_p marks it and its refined copies)
-  cudaGraphExec_t upload_graph_nop = nullptr;
+  // fl_step_host's pressure arrives on the second stream (ev_p marks it and
+  // its refined copies)
   cudaEvent_t ev_p = nullptr;
+  // fl_step_host's label part of the upload (compare, rebuild when changed)
+  // runs on a third stream while u and v are still arriving
+  cudaStream_t stream3 = nullptr;
+  cudaEvent_t ev_lab = nullptr, ev_lab_done = nullptr;
+  cudaGraphExec_t upload_graph_labels = nullptr;
   // fl_upload_fields copies the labels here; the upload compares them with
   // levels[0].label and rebuilds the multigrid labels and codes only where
   // they changed (label_flag: set when any cell differs)
