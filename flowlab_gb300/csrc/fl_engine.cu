@@ -1078,12 +1078,14 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
   // pressure (and what is formed from it) on the second stream behind u and
   // v. The step waits for each where it first reads it.
   const bool async_p = dye_async && dtype == FL_F32 && e->use_graphs;
+  // stale codes (new levels, labels written by another entry point): every
+  // cell is made to differ so that the rebuild runs. Read before a capture
+  // of the rebuild, which marks the codes valid.
+  const bool stale_codes = !e->codes_valid || e->labels_dirty;
   if (async_p) TRY(label_graph(e));
   TRY(put_step_ctl(e, true));
   if (async_p) {
-    // stale codes (new levels, labels written by another entry point): make
-    // every cell differ so that the rebuild runs
-    if (!e->codes_valid || e->labels_dirty)
+    if (stale_codes)
       TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].label, 0xff, (size_t)e->cells(), e->stream), "upload label"));
     TRY(up32(e, e->label_in, label, (size_t)e->cells(), "upload label"));
     TRY(cuda_status(e, cudaEventRecord(e->ev_lab, e->stream), "upload label"));
@@ -1143,9 +1145,7 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
                      false);
     TRY(cuda_status(e, cudaStreamWaitEvent(e->stream, e->ev_lab_done, 0), "upload label"));
   } else {
-    // stale codes (new levels, labels written by another entry point): make
-    // every cell differ so that the rebuild runs
-    if (!e->codes_valid || e->labels_dirty)
+    if (stale_codes)
       TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].label, 0xff, (size_t)e->cells(), e->stream), "upload label"));
     if (p64_direct || !e->use_graphs) {
       TRY(cuda_status(e, enqueue_after_upload(e, !p64_direct, false), "upload"));

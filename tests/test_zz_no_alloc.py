@@ -76,6 +76,50 @@ def test_noalloc_matches_allocating_entry_point_twice(scheme):
         assert np.array_equal(ev, gv), "v differs in %d faces" % int((ev != gv).sum())
 
 
+def test_noalloc_records_into_a_cuda_graph():
+    """After its set-up call, the entry point can be recorded by stream
+    capture (it makes no allocating or synchronising call, either of which
+    would invalidate a global-mode capture); the recorded launch, replayed on
+    new inputs written into the same buffers, matches the allocating entry
+    point on those inputs."""
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    nx, ny = 256, 192
+    h, dt, u, v, _, _, _, _, _ = fx.advect_fixture(1, nx, ny)
+    label = fx.scaled_block_labels(nx, ny)
+    dev = torch.device("cuda", 0)
+    du = torch.from_numpy(f32(u)).to(dev)
+    dv = torch.from_numpy(f32(v)).to(dev)
+    dl = torch.from_numpy(np.ascontiguousarray(label, np.uint8)).to(dev)
+    uo = torch.full_like(du, float("nan"))
+    vo = torch.full_like(dv, float("nan"))
+
+    def call():
+        s = torch.cuda.current_stream().cuda_stream
+        return lib.fl_advect_velocity_noalloc(native.FL_MACCORMACK, nx, ny, float(h), float(np.float32(dt)),
+                                              du.data_ptr(), dv.data_ptr(), uo.data_ptr(), vo.data_ptr(),
+                                              dl.data_ptr(), ctypes.c_void_p(s))
+
+    assert call() == native.FL_OK, lib.fl_last_error(None).decode()  # the set-up call
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        st = call()
+    assert st == native.FL_OK, lib.fl_last_error(None).decode()
+    u2, v2 = -0.7 * np.asarray(u, np.float32), 1.3 * np.asarray(v, np.float32)
+    du.copy_(torch.from_numpy(f32(u2)))
+    dv.copy_(torch.from_numpy(f32(v2)))
+    uo.fill_(float("nan"))
+    vo.fill_(float("nan"))
+    graph.replay()
+    torch.cuda.synchronize()
+    eu, ev = engine_advect(nx, ny, h, native.FL_MACCORMACK, u2, v2, label, dt)
+    gu, gv = uo.cpu().numpy(), vo.cpu().numpy()
+    assert np.array_equal(eu, gu), "u differs in %d faces" % int((eu != gu).sum())
+    assert np.array_equal(ev, gv), "v differs in %d faces" % int((ev != gv).sum())
+    del graph
+
+
 def test_noalloc_rejects_overlapping_outputs():
     torch = pytest.importorskip("torch")
     lib = native.load()
