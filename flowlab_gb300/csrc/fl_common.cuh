@@ -57,6 +57,8 @@ struct StepAccum {
   unsigned int blocks_done;     // last-block detection of the CFL reduction
   unsigned int last_max_bits;   // the finished max face speed, for the report
   unsigned int nonfinite;
+  unsigned int test_done;       // last-block detection of the defect pass that runs the cycle test
+  unsigned int pad0;
 };
 
 // The residual diagnostic (simulation.ts:539-540, SimulationParams.

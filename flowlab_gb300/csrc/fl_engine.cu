@@ -445,11 +445,13 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
 void enqueue_solve_prologue(Engine* e, cudaStream_t s, bool mixed, bool use_cond, cudaGraphConditionalHandle h) {
   Level& L0 = e->levels[0];
   if (mixed) {
+    // the begin test runs in the pass's last block
     const int tok = prof_begin(*e, FL_PH_DEFECT64);
     launch_update_resid64(s, e->nx, e->ny, e->p64[0], e->p64[1], e->ctl, nullptr, L0.b, e->b_lo, L0.code, false,
-                          e->r32, e->acc, refined_df(e));
+                          e->r32, e->acc, refined_df(e), 1, use_cond, h);
     // p64, b, code in; r32 out
     prof_end(*e, tok, 17.0 * e->cells(), 1);
+    return;
   }
   const int tok = prof_begin(*e, FL_PH_CONTROL);
   launch_solve_begin(s, e->acc, e->ctl, use_cond, h);
@@ -462,15 +464,16 @@ void enqueue_solve_prologue(Engine* e, cudaStream_t s, bool mixed, bool use_cond
 void enqueue_solve_body(Engine* e, cudaStream_t s, bool mixed, bool use_cond, cudaGraphConditionalHandle h) {
   Level& L0 = e->levels[0];
   if (mixed) {
+    // the cycle test runs in the pass's last block
     mg_vcycle_on(*e, e->r32, true, nullptr);
     const int tok = prof_begin(*e, FL_PH_DEFECT64);
     launch_update_resid64(s, e->nx, e->ny, e->p64[0], e->p64[1], e->ctl, L0.x[0], L0.b, e->b_lo, L0.code, true,
-                          e->r32, e->acc, refined_df(e));
+                          e->r32, e->acc, refined_df(e), 2, use_cond, h);
     // p64, e, b, code in; p64 (other buffer), r32 out
     prof_end(*e, tok, 29.0 * e->cells(), 1);
-  } else {
-    mg_vcycle_on(*e, L0.b, false, e->acc);
+    return;
   }
+  mg_vcycle_on(*e, L0.b, false, e->acc);
   const int tok = prof_begin(*e, FL_PH_CONTROL);
   launch_solve_check(s, e->acc, e->ctl, use_cond, h);
   prof_end(*e, tok, 0, 1);

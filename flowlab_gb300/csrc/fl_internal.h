@@ -255,9 +255,13 @@ void mg_build_codes(Engine& e);  // label chain + stencil codes from levels[0].l
 void mg_vcycle(Engine& e, StepAccum* acc_for_residual);
 void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc_for_residual);
 // the refined-pressure pass: float64, or double-float pairs in the same buffers when df
-void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, const SolveCtl* ctl,
+// test 1 / 2: the pass's last block also runs the begin / cycle test
+// (k_solve_begin / k_solve_check) on the residual it accumulated and, with
+// use_cond, sets the graph's conditional handle h.
+void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, SolveCtl* ctl,
                            const float* e, const float* b, const float* b_lo, const uint8_t* code, bool update,
-                           float* r32, StepAccum* acc, bool df);
+                           float* r32, StepAccum* acc, bool df, int test = 0, bool use_cond = false,
+                           cudaGraphConditionalHandle h = 0);
 void launch_solve_begin(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h);
 void launch_solve_check(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h);
 void launch_zero_if(cudaStream_t s, const SolveCtl* ctl, float* p32, double* p64a, double* p64b, long n);

@@ -768,7 +768,7 @@ constexpr int UR_WARPS = 4;
 // One block's rows of the float64 pass: block (bx, by) of its grid.
 template <bool UPDATE>
 __device__ __forceinline__ void update_resid64_tile(int nx, int ny, double* __restrict__ p64a,
-                                                    double* __restrict__ p64b, const SolveCtl* __restrict__ ctl,
+                                                    double* __restrict__ p64b, const SolveCtl* ctl,
                                                     const float* __restrict__ e, const float* __restrict__ b,
                                                     const float* __restrict__ b_lo,
                                                     const uint8_t* __restrict__ code, float* __restrict__ r32,
@@ -893,7 +893,7 @@ constexpr int DF_WARPS = 4;
 // One block's rows of the double-float pass: block (bx, by) of its grid.
 template <bool UPDATE>
 __device__ __forceinline__ void update_resid_df_tile(int nx, int ny, float2* __restrict__ p2a,
-                                                     float2* __restrict__ p2b, const SolveCtl* __restrict__ ctl,
+                                                     float2* __restrict__ p2b, const SolveCtl* ctl,
                                                      const float* __restrict__ e, const float* __restrict__ b,
                                                      const float* __restrict__ b_lo,
                                                      const uint8_t* __restrict__ code, float* __restrict__ r32,
@@ -1000,7 +1000,7 @@ __device__ __forceinline__ double acc_rms(double sq, unsigned long long n) { ret
 // Before the cycle loop (pressureMultigrid.ts:294-300, solveMixed): the rhs
 // RMS; a vanishing rhs means p = 0 and no cycle; the float64 path also tests
 // its initial residual, so a converged warm start costs no cycle.
-__device__ int solve_begin(StepAccum* acc, SolveCtl* ctl) {
+__device__ int solve_begin_sums(StepAccum* acc, SolveCtl* ctl, double res_sq, unsigned long long n_res) {
   const double b_rms = acc_rms(acc->b_sq, acc->n_fluid);
   ctl->b_rms = b_rms;
   ctl->cycles = 0;
@@ -1012,7 +1012,7 @@ __device__ int solve_begin(StepAccum* acc, SolveCtl* ctl) {
   } else if (ctl->nonfinite) {
     ctl->rel = -1.0;
   } else if (ctl->mode == SOLVE_MIXED) {
-    const double rel = acc_rms(acc->res_sq, acc->n_res) / b_rms;
+    const double rel = acc_rms(res_sq, n_res) / b_rms;
     ctl->rel = rel;
     cont = ctl->max_cycles > 0 && !(rel <= ctl->tol);
   } else {
@@ -1026,6 +1026,8 @@ __device__ int solve_begin(StepAccum* acc, SolveCtl* ctl) {
   return cont;
 }
 
+__device__ int solve_begin(StepAccum* acc, SolveCtl* ctl) { return solve_begin_sums(acc, ctl, acc->res_sq, acc->n_res); }
+
 __global__ void k_solve_begin(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaGraphConditionalHandle h) {
   const int cont = solve_begin(acc, ctl);
   if (use_cond) cudaGraphSetConditional(h, cont);
@@ -1034,10 +1036,10 @@ __global__ void k_solve_begin(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaG
 // After each cycle: count it, evaluate the relative residual the cycle's
 // last kernel accumulated, and decide on another (pressureMultigrid.ts:
 // 314-317 for float32, solveMixed for float64 defect correction).
-__device__ int solve_check(StepAccum* acc, SolveCtl* ctl) {
+__device__ int solve_check_sums(StepAccum* acc, SolveCtl* ctl, double res_sq, unsigned long long n_res) {
   ctl->cycles += 1;
   if (ctl->mode == SOLVE_MIXED) ctl->par = 1 - ctl->par;
-  const double rel = acc_rms(acc->res_sq, acc->n_res) / ctl->b_rms;
+  const double rel = acc_rms(res_sq, n_res) / ctl->b_rms;
   ctl->rel = rel;
   int cont = ctl->cycles < ctl->max_cycles;
   if (!isfinite(rel)) {
@@ -1052,6 +1054,39 @@ __device__ int solve_check(StepAccum* acc, SolveCtl* ctl) {
   acc->n_res = 0ull;
   ctl->cont = cont;
   return cont;
+}
+
+__device__ int solve_check(StepAccum* acc, SolveCtl* ctl) { return solve_check_sums(acc, ctl, acc->res_sq, acc->n_res); }
+
+// The begin test (test 1) or the cycle test (test 2) run by the last block
+// of the defect pass that accumulated the residual, instead of a one-thread
+// launch after it. Each block's thread 0 has added its sums (the tile's
+// last statement) before it counts itself done; the last block reads the
+// totals from L2 once every block has counted, and resets the counter.
+__device__ __noinline__ void defect_pass_test_last(StepAccum* acc, SolveCtl* ctl, int test, int use_cond,
+                                                   cudaGraphConditionalHandle h) {
+  __threadfence();
+  acc->test_done = 0u;
+  const double sq = __ldcg(&acc->res_sq);
+  const unsigned long long n = __ldcg(&acc->n_res);
+  const int cont = test == 1 ? solve_begin_sums(acc, ctl, sq, n) : solve_check_sums(acc, ctl, sq, n);
+  if (use_cond) cudaGraphSetConditional(h, cont);
+}
+
+__device__ __forceinline__ void defect_pass_test(StepAccum* acc, SolveCtl* ctl, int test, int use_cond,
+                                                 cudaGraphConditionalHandle h) {
+  if (test == 0) return;
+  __shared__ int last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int done = atomicAdd(&acc->test_done, 1u);
+    last = done == gridDim.x * gridDim.y - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  // out of line: the tests' float64 arithmetic stays out of the pass's
+  // register budget (64 registers for 8 blocks per SM)
+  defect_pass_test_last(acc, ctl, test, use_cond, h);
 }
 
 __global__ void k_solve_check(StepAccum* acc, SolveCtl* ctl, int use_cond, cudaGraphConditionalHandle h) {
@@ -1198,45 +1233,53 @@ void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* 
 template <bool UPDATE>
 __global__ void __launch_bounds__(32 * UR_WARPS) k_update_resid64(int nx, int ny, double* __restrict__ p64a,
                                                                 double* __restrict__ p64b,
-                                                                const SolveCtl* __restrict__ ctl,
-                                                                const float* __restrict__ e,
+                                                                SolveCtl* ctl, const float* __restrict__ e,
                                                                 const float* __restrict__ b,
                                                                 const float* __restrict__ b_lo,
                                                                 const uint8_t* __restrict__ code,
-                                                                float* __restrict__ r32, StepAccum* acc) {
+                                                                float* __restrict__ r32, StepAccum* acc, int test,
+                                                                int use_cond, cudaGraphConditionalHandle h) {
   update_resid64_tile<UPDATE>(nx, ny, p64a, p64b, ctl, e, b, b_lo, code, r32, acc, blockIdx.x, blockIdx.y);
+  defect_pass_test(acc, ctl, test, use_cond, h);
 }
 
 template <bool UPDATE>
 __global__ void __launch_bounds__(32 * DF_WARPS, 8) k_update_resid_df(int nx, int ny, float2* __restrict__ p2a,
                                                                    float2* __restrict__ p2b,
-                                                                   const SolveCtl* __restrict__ ctl,
-                                                                   const float* __restrict__ e,
+                                                                   SolveCtl* ctl, const float* __restrict__ e,
                                                                    const float* __restrict__ b,
                                                                    const float* __restrict__ b_lo,
                                                                    const uint8_t* __restrict__ code,
-                                                                   float* __restrict__ r32, StepAccum* acc) {
+                                                                   float* __restrict__ r32, StepAccum* acc,
+                                                                   int test, int use_cond,
+                                                                   cudaGraphConditionalHandle h) {
   update_resid_df_tile<UPDATE>(nx, ny, p2a, p2b, ctl, e, b, b_lo, code, r32, acc, blockIdx.x, blockIdx.y);
+  defect_pass_test(acc, ctl, test, use_cond, h);
 }
 
-void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, const SolveCtl* ctl,
+void launch_update_resid64(cudaStream_t s, int nx, int ny, double* p64a, double* p64b, SolveCtl* ctl,
                            const float* e, const float* b, const float* b_lo, const uint8_t* code, bool update,
-                           float* r32, StepAccum* acc, bool df) {
+                           float* r32, StepAccum* acc, bool df, int test, bool use_cond,
+                           cudaGraphConditionalHandle h) {
+  const int uc = use_cond ? 1 : 0;
   if (df) {
     float2* a = reinterpret_cast<float2*>(p64a);
     float2* bb = reinterpret_cast<float2*>(p64b);
     dim3 g((nx + 29) / 30, (ny + DF_WARPS * DF_ROWS - 1) / (DF_WARPS * DF_ROWS));
     if (update)
-      k_update_resid_df<true><<<g, 32 * DF_WARPS, 0, s>>>(nx, ny, a, bb, ctl, e, b, b_lo, code, r32, acc);
+      k_update_resid_df<true><<<g, 32 * DF_WARPS, 0, s>>>(nx, ny, a, bb, ctl, e, b, b_lo, code, r32, acc, test, uc, h);
     else
-      k_update_resid_df<false><<<g, 32 * DF_WARPS, 0, s>>>(nx, ny, a, bb, ctl, e, b, b_lo, code, r32, acc);
+      k_update_resid_df<false><<<g, 32 * DF_WARPS, 0, s>>>(nx, ny, a, bb, ctl, e, b, b_lo, code, r32, acc, test, uc,
+                                                           h);
     return;
   }
   dim3 g((nx + 29) / 30, (ny + UR_WARPS * UR_ROWS - 1) / (UR_WARPS * UR_ROWS));
   if (update)
-    k_update_resid64<true><<<g, 32 * UR_WARPS, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, b_lo, code, r32, acc);
+    k_update_resid64<true><<<g, 32 * UR_WARPS, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, b_lo, code, r32, acc, test, uc,
+                                                       h);
   else
-    k_update_resid64<false><<<g, 32 * UR_WARPS, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, b_lo, code, r32, acc);
+    k_update_resid64<false><<<g, 32 * UR_WARPS, 0, s>>>(nx, ny, p64a, p64b, ctl, e, b, b_lo, code, r32, acc, test,
+                                                        uc, h);
 }
 
 void launch_solve_begin(cudaStream_t s, StepAccum* acc, SolveCtl* ctl, bool use_cond, cudaGraphConditionalHandle h) {
