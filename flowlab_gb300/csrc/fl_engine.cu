@@ -206,6 +206,7 @@ void free_all(Engine* e) {
   if (e->ev_p) cudaEventDestroy(e->ev_p);
   if (e->ev_lab) cudaEventDestroy(e->ev_lab);
   if (e->ev_lab_done) cudaEventDestroy(e->ev_lab_done);
+  if (e->ev_lab_sync) cudaEventDestroy(e->ev_lab_sync);
   if (e->stream3) cudaStreamDestroy(e->stream3);
   if (e->ev_prior) cudaEventDestroy(e->ev_prior);
   if (e->stream2) cudaStreamDestroy(e->stream2);
@@ -386,6 +387,12 @@ void wait_p(Engine* e, cudaStream_t s) {
   cudaStreamWaitEvent(s, e->ev_p, capturing(s) ? cudaEventWaitExternal : 0);
 }
 
+// And for the multigrid labels and stencil codes fl_step_host rebuilds on
+// the third stream: the first reader of the codes (the solve) waits here.
+void wait_codes(Engine* e, cudaStream_t s) {
+  cudaStreamWaitEvent(s, e->ev_lab_done, capturing(s) ? cudaEventWaitExternal : 0);
+}
+
 // advect u,v -> [stir] -> [confinement] -> body forces -> divergence
 void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
   Level& L0 = e->levels[0];
@@ -424,6 +431,7 @@ void enqueue_pre(Engine* e, cudaStream_t s, int par, bool stir) {
                     step_mixed(e) ? e->b_lo : nullptr);
   prof_end(*e, tok, 4 * F + N + 4 * N, 1);
   wait_p(e, s);
+  wait_codes(e, s);
   if (e->prm.warm_extrapolate && e->prm.solver == FL_SOLVER_MG) {
     const bool mixed = e->prm.mixed != 0;
     launch_extrapolate(s, e->cells(), L0.label, L0.x[0], e->pprev32, mixed ? e->p64[0] : nullptr,
@@ -901,6 +909,7 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
       cudaEventCreateWithFlags(&e->ev_p, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_lab, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_lab_done, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->ev_lab_sync, cudaEventDisableTiming) != cudaSuccess ||
       cudaStreamCreateWithFlags(&e->stream3, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&e->ev_prior, cudaEventDisableTiming) != cudaSuccess) {
     fail(e, FL_EDEVICE, "stream creation failed");
@@ -985,13 +994,10 @@ void enqueue_p_after_upload(Engine* e, cudaStream_t s, bool p64_from_p32) {
   launch_copy32(s, e->p64[0], e->pprev64, 2 * e->cells());
 }
 
-// with_p false: without the pressure's part; with_cfl false: without the
-// clock reset and the CFL scalars (the caller enqueues them elsewhere)
-cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture, bool with_p = true,
-                                 bool with_cfl = true) {
+cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture) {
   cudaStream_t s = e->stream;
   cudaError_t err = cudaSuccess;
-  if (with_p) enqueue_p_after_upload(e, s, p64_from_p32);
+  enqueue_p_after_upload(e, s, p64_from_p32);
   launch_label_sync(s, e->label_in, e->levels[0].label, e->cells(), e->label_flag);
   if (!capture) {
     cudaMemsetAsync(e->label_flag, 0, sizeof(int), s);
@@ -1030,10 +1036,8 @@ cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture, boo
       }
     }
   }
-  if (with_cfl) {
-    launch_fill32(s, e->time_dev, 2, 0u);
-    launch_max_speed(s, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);
-  }
+  launch_fill32(s, e->time_dev, 2, 0u);
+  launch_max_speed(s, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);
   return err;
 }
 
@@ -1046,20 +1050,20 @@ namespace {
 // fields' copies, and ev_dye marks its end; the step's first dye reader
 // waits for it (wait_dye). Otherwise
 // ev_dye is recorded on the second stream with nothing in flight.
-// The label part of fl_step_host's upload as a graph (captured on the third
-// stream: label compare, then the rebuild only when some label changed).
+// The rebuild part of fl_step_host's upload as a graph on the third stream:
+// the multigrid labels and codes rebuilt by kernels that run only when the
+// label compare before them found a changed cell (a plain graph: an IF node
+// here held up the engine stream's kernels meanwhile).
 int label_graph(Engine* e) {
   if (e->upload_graph_labels) return FL_OK;
-  cudaStream_t s = e->stream;
-  e->stream = e->stream3;
   cudaGraph_t g = nullptr;
-  cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+  cudaError_t err = cudaStreamBeginCapture(e->stream3, cudaStreamCaptureModeThreadLocal);
   if (err == cudaSuccess) {
-    err = enqueue_after_upload(e, false, true, false, false);
-    cudaError_t end = cudaStreamEndCapture(e->stream, &g);
+    mg_build_codes_if(*e, e->stream3, e->label_flag);
+    err = cudaGetLastError();
+    cudaError_t end = cudaStreamEndCapture(e->stream3, &g);
     if (err == cudaSuccess) err = end;
   }
-  e->stream = s;
   if (err == cudaSuccess) err = cudaGraphInstantiate(&e->upload_graph_labels, g, 0);
   if (g) cudaGraphDestroy(g);
   if (err != cudaSuccess) {
@@ -1093,6 +1097,9 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
     TRY(up32(e, e->label_in, label, (size_t)e->cells(), "upload label"));
     TRY(cuda_status(e, cudaEventRecord(e->ev_lab, e->stream), "upload label"));
     TRY(cuda_status(e, cudaStreamWaitEvent(e->stream3, e->ev_lab, 0), "upload label"));
+    launch_label_sync(e->stream3, e->label_in, e->levels[0].label, e->cells(), e->label_flag);
+    TRY(check_launch(e, "upload label"));
+    TRY(cuda_status(e, cudaEventRecord(e->ev_lab_sync, e->stream3), "upload label"));
     TRY(cuda_status(e, cudaGraphLaunch(e->upload_graph_labels, e->stream3), "label graph"));
     TRY(cuda_status(e, cudaEventRecord(e->ev_lab_done, e->stream3), "upload label"));
   }
@@ -1141,12 +1148,13 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
     TRY(cuda_status(e, cudaEventRecord(e->ev_p, e->stream2), "upload p"));
   }
   if (async_p) {
-    // the clock and the first step's CFL scalars from the uploaded velocity,
-    // then the labels' part joins
+    // the clock and the first step's CFL scalars from the uploaded velocity;
+    // the step starts once the finest labels are in place too (it waits for
+    // the rebuilt codes where the solve first reads them)
     launch_fill32(e->stream, e->time_dev, 2, 0u);
     launch_max_speed(e->stream, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true,
                      false);
-    TRY(cuda_status(e, cudaStreamWaitEvent(e->stream, e->ev_lab_done, 0), "upload label"));
+    TRY(cuda_status(e, cudaStreamWaitEvent(e->stream, e->ev_lab_sync, 0), "upload label"));
   } else {
     if (stale_codes)
       TRY(cuda_status(e, cudaMemsetAsync(e->levels[0].label, 0xff, (size_t)e->cells(), e->stream), "upload label"));

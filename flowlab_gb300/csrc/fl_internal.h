@@ -87,9 +87,12 @@ struct Engine {
   // its refined copies)
   cudaEvent_t ev_p = nullptr;
   // fl_step_host's label part of the upload (compare, rebuild when changed)
-  // runs on a third stream while u and v are still arriving
+  // runs on a third stream while u and v are still arriving: ev_lab_sync
+  // marks the finest labels (the step waits for them before it starts),
+  // ev_lab_done the multigrid labels and codes (the step's first reader of
+  // the codes waits for them, wait_codes)
   cudaStream_t stream3 = nullptr;
-  cudaEvent_t ev_lab = nullptr, ev_lab_done = nullptr;
+  cudaEvent_t ev_lab = nullptr, ev_lab_sync = nullptr, ev_lab_done = nullptr;
   cudaGraphExec_t upload_graph_labels = nullptr;
   // fl_upload_fields copies the labels here; the upload compares them with
   // levels[0].label and rebuilds the multigrid labels and codes only where
@@ -252,6 +255,7 @@ void launch_convert(cudaStream_t s, const void* src, int src_dtype, void* dst, i
 void mg_setup(Engine& e);  // allocates levels for e.nx, e.ny and the coarsest size
 void mg_free(Engine& e);
 void mg_build_codes(Engine& e);  // label chain + stencil codes from levels[0].label
+void mg_build_codes_if(Engine& e, cudaStream_t s, int* flag);  // the same when *flag is set; clears it
 void mg_vcycle(Engine& e, StepAccum* acc_for_residual);
 void mg_vcycle_on(Engine& e, const float* b0, bool zero_start, StepAccum* acc_for_residual);
 // the refined-pressure pass: float64, or double-float pairs in the same buffers when df
@@ -269,7 +273,8 @@ void launch_rb_sweeps(cudaStream_t s, int nx, int ny, const float* x_in, float* 
                       const uint8_t* code, float scale, float omega, int pairs, const float* scale_dev = nullptr);
 void launch_rms_remaining(cudaStream_t s, int nx, int ny, const float* p, const float* div, const uint8_t* code,
                           float scale, StepAccum* acc);
-void launch_build_codes(cudaStream_t s, int nx, int ny, const uint8_t* label, uint8_t* code);
+void launch_build_codes(cudaStream_t s, int nx, int ny, const uint8_t* label, uint8_t* code,
+                        const int* only_if = nullptr);
 // cur = in, raising *flag when any of the n labels changed
 void launch_label_sync(cudaStream_t s, const uint8_t* in, uint8_t* cur, long n, int* flag);
 // the conditional `h` = (*flag != 0), then *flag = 0

@@ -35,7 +35,10 @@ constexpr int MAX_LEVELS = 24;
 
 // ------------------------------------------------------------ label codes
 
-__global__ void k_build_codes(int nx, int ny, const uint8_t* __restrict__ label, uint8_t* __restrict__ code) {
+// only_if (when set): the kernel does nothing unless *only_if is nonzero
+__global__ void k_build_codes(int nx, int ny, const uint8_t* __restrict__ label, uint8_t* __restrict__ code,
+                              const int* only_if) {
+  if (only_if != nullptr && *only_if == 0) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
@@ -87,7 +90,8 @@ void launch_label_cond(cudaStream_t s, int* flag, cudaGraphConditionalHandle h) 
 
 // pressureMultigrid.ts:92-110 (multigrid.wgsl:259-286): Air > Fluid > Solid.
 __global__ void k_coarsen_labels(int fnx, int fny, const uint8_t* __restrict__ fine, int cnx, int cny,
-                                 uint8_t* __restrict__ coarse) {
+                                 uint8_t* __restrict__ coarse, const int* only_if) {
+  if (only_if != nullptr && *only_if == 0) return;
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
   if (I >= cnx || J >= cny) return;
@@ -1204,9 +1208,9 @@ static bool launch_smooth(cudaStream_t s, const SmoothArgs& a, int pairs, int mo
   return launch_smooth_p<MODE_POST>(s, a, pairs);
 }
 
-void launch_build_codes(cudaStream_t s, int nx, int ny, const uint8_t* label, uint8_t* code) {
+void launch_build_codes(cudaStream_t s, int nx, int ny, const uint8_t* label, uint8_t* code, const int* only_if) {
   dim3 b(32, 8), g((nx + 31) / 32, (ny + 7) / 8);
-  k_build_codes<<<g, b, 0, s>>>(nx, ny, label, code);
+  k_build_codes<<<g, b, 0, s>>>(nx, ny, label, code, only_if);
 }
 
 void launch_rb_halfsweep(cudaStream_t s, int nx, int ny, float* p, const float* b, const uint8_t* code,
@@ -1402,10 +1406,26 @@ void mg_build_codes(Engine& e) {
     const Level& F = e.levels[l - 1];
     const Level& C = e.levels[l];
     dim3 b(32, 8), g((C.nx + 31) / 32, (C.ny + 7) / 8);
-    k_coarsen_labels<<<g, b, 0, s>>>(F.nx, F.ny, F.label, C.nx, C.ny, C.label);
+    k_coarsen_labels<<<g, b, 0, s>>>(F.nx, F.ny, F.label, C.nx, C.ny, C.label, nullptr);
   }
   for (const Level& L : e.levels) launch_build_codes(s, L.nx, L.ny, L.label, L.code);
   e.codes_valid = true;
+}
+
+__global__ void k_clear_flag(int* flag) { *flag = 0; }
+
+// The same rebuild on stream s as kernels that each return at once unless
+// *flag is set (the label compare's result), then the flag cleared: a
+// plain graph's worth of launches where an IF node would otherwise decide.
+void mg_build_codes_if(Engine& e, cudaStream_t s, int* flag) {
+  for (size_t l = 1; l < e.levels.size(); l++) {
+    const Level& F = e.levels[l - 1];
+    const Level& C = e.levels[l];
+    dim3 b(32, 8), g((C.nx + 31) / 32, (C.ny + 7) / 8);
+    k_coarsen_labels<<<g, b, 0, s>>>(F.nx, F.ny, F.label, C.nx, C.ny, C.label, flag);
+  }
+  for (const Level& L : e.levels) launch_build_codes(s, L.nx, L.ny, L.label, L.code, flag);
+  k_clear_flag<<<1, 1, 0, s>>>(flag);
 }
 
 // One V-cycle (pressureMultigrid.ts:253-275) on levels[0].b with the warm
