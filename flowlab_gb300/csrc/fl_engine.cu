@@ -659,6 +659,10 @@ void destroy_step_graphs(Engine* e) {
     if (g) cudaGraphExecDestroy(g);
     g = nullptr;
   }
+  for (auto& g : e->graph_up) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
   e->graphs_valid = false;
   e->graph_gen++;
 }
@@ -674,9 +678,15 @@ void destroy_graphs(Engine* e) {
 // Enqueues one whole step for buffer parity `par` on e->stream while that
 // stream is being captured; the pressure solve becomes a WHILE node whose
 // body is captured from e->stream2.
-cudaError_t capture_step(Engine* e, int par) {
+// cfl_first: led by the clock reset and the CFL scalars of the current
+// velocity (the work an upload otherwise enqueues after its copies).
+cudaError_t capture_step(Engine* e, int par, bool cfl_first) {
   cudaStream_t s = e->stream;
   cudaError_t err = cudaSuccess;
+  if (cfl_first) {
+    launch_fill32(s, e->time_dev, 2, 0u);
+    launch_max_speed(s, e->nx, e->ny, e->u[par], e->v[par], e->acc, e->sc, e->time_dev, &e->prm, e->h, true, false);
+  }
   enqueue_pre(e, s, par, false);
   if (e->prm.solver == FL_SOLVER_MG) {
     cudaStreamCaptureStatus cst;
@@ -720,11 +730,11 @@ cudaError_t capture_step(Engine* e, int par) {
 }
 
 // Captures the whole step for buffer parity `par` into an executable graph.
-int build_graph(Engine* e, int par, cudaGraphExec_t* out) {
+int build_graph(Engine* e, int par, cudaGraphExec_t* out, bool cfl_first = false) {
   cudaStream_t s = e->stream;
   cudaError_t err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (err != cudaSuccess) return cuda_status(e, err, "begin capture");
-  err = capture_step(e, par);
+  err = capture_step(e, par, cfl_first);
   cudaGraph_t graph = nullptr;
   cudaError_t end = cudaStreamEndCapture(s, &graph);
   if (err == cudaSuccess) err = end;
@@ -742,13 +752,17 @@ bool graph_eligible(const Engine* e) {
   return e->use_graphs && !e->profiling && !e->stir_pending && !e->labels_dirty && solve_on_device(e);
 }
 
-int step_graph(Engine* e) {
+// cfl_first: the step right after fl_step_host's upload, which left the
+// clock reset and the CFL scalars to the step's graph.
+int step_graph(Engine* e, bool cfl_first = false) {
   if (!e->graphs_valid) {
     destroy_step_graphs(e);
     for (int par = 0; par < 2; par++) TRY(build_graph(e, par, &e->graph[par]));
     e->graphs_valid = true;
   }
-  TRY(cuda_status(e, cudaGraphLaunch(e->graph[e->cur], e->stream), "graph launch"));
+  cudaGraphExec_t& g = cfl_first ? e->graph_up[e->cur] : e->graph[e->cur];
+  if (!g) TRY(build_graph(e, e->cur, &g, true));
+  TRY(cuda_status(e, cudaGraphLaunch(g, e->stream), "graph launch"));
   e->cur = 1 - e->cur;
   e->steps++;
   e->stats_on_device = true;
@@ -1074,8 +1088,12 @@ int label_graph(Engine* e) {
   return FL_OK;
 }
 
+// With cfl_deferred (fl_step_host's float32 upload), the clock reset and
+// the CFL scalars are left to the caller (*cfl_deferred says so), which runs
+// them at the head of the step's graph.
 int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
-                  const void* dye, bool dye_async) {
+                  const void* dye, bool dye_async, bool* cfl_deferred = nullptr) {
+  if (cfl_deferred) *cfl_deferred = false;
   e->cur = 0;
   e->stats_on_device = false;
   if (dye_async && !dye) return fail(e, FL_EINVAL, "upload dye: null pointer");
@@ -1148,12 +1166,17 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
     TRY(cuda_status(e, cudaEventRecord(e->ev_p, e->stream2), "upload p"));
   }
   if (async_p) {
-    // the clock and the first step's CFL scalars from the uploaded velocity;
-    // the step starts once the finest labels are in place too (it waits for
-    // the rebuilt codes where the solve first reads them)
-    launch_fill32(e->stream, e->time_dev, 2, 0u);
-    launch_max_speed(e->stream, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true,
-                     false);
+    // the clock and the first step's CFL scalars from the uploaded velocity
+    // (here, or at the head of the caller's step graph); the step starts
+    // once the finest labels are in place too (it waits for the rebuilt
+    // codes where the solve first reads them)
+    if (cfl_deferred) {
+      *cfl_deferred = true;
+    } else {
+      launch_fill32(e->stream, e->time_dev, 2, 0u);
+      launch_max_speed(e->stream, e->nx, e->ny, e->u[0], e->v[0], e->acc, e->sc, e->time_dev, &e->prm, e->h, true,
+                       false);
+    }
     TRY(cuda_status(e, cudaStreamWaitEvent(e->stream, e->ev_lab_sync, 0), "upload label"));
   } else {
     if (stale_codes)
@@ -1244,12 +1267,22 @@ int fl_step_host(fl_engine* h, int dtype, const void* u, const void* v, const vo
     if (iters) *iters = e->last_iters;
     return FL_OK;
   }
+  bool cfl_first = false;
   if (upload_in) {
-    TRY(upload_fields(e, FL_F32, u, v, p, label, dye, true));
+    TRY(upload_fields(e, FL_F32, u, v, p, label, dye, true, &cfl_first));
   } else {
     TRY(cuda_status(e, cudaEventRecord(e->ev_dye, e->stream2), "step"));
   }
-  TRY(graph_eligible(e) ? step_graph(e) : step_eager(e, true));
+  if (graph_eligible(e)) {
+    TRY(step_graph(e, cfl_first));
+  } else {
+    if (cfl_first) {
+      launch_fill32(e->stream, e->time_dev, 2, 0u);
+      launch_max_speed(e->stream, e->nx, e->ny, e->u[e->cur], e->v[e->cur], e->acc, e->sc, e->time_dev, &e->prm, e->h,
+                       true, false);
+    }
+    TRY(step_eager(e, true));
+  }
   TRY(check_launch(e, "step"));
   // velocity and pressure on the second stream once the projection is done
   // (the step records ev_proj there), the dye once the dye advection is done

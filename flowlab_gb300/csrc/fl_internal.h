@@ -81,6 +81,11 @@ struct Engine {
   // while the step's CFL scan runs
   cudaEvent_t ev_dye_done = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  // the same steps led by the clock reset and the CFL scalars of freshly
+  // uploaded velocities (fl_step_host): one graph launch instead of two
+  // kernel launches and a graph launch while the dye is still arriving,
+  // which delays separately launched kernels (built on first use)
+  cudaGraphExec_t graph_up[2] = {nullptr, nullptr};
   // the device-side work of fl_upload_fields after its copies (float32 p)
   cudaGraphExec_t upload_graph = nullptr;
   // fl_step_host's pressure arrives on the second stream (ev_p marks it and
