@@ -174,6 +174,7 @@ void free_all(Engine* e) {
   cudaFree(e->acc);
   cudaFree(e->time_dev);
   cudaFree(e->staging);
+  cudaFree(e->p32_final);
   cudaFree(e->p64[0]);
   cudaFree(e->p64[1]);
   cudaFree(e->r32);
@@ -526,8 +527,8 @@ cudaError_t enqueue_post(Engine* e, cudaStream_t s, int par, bool device_dt) {
   float* v = e->v[1 - par];
   int tok = prof_begin(*e, FL_PH_PROJECT);
   launch_subtract_outflow(s, e->nx, e->ny, L0.x[0], u, v, L0.label, e->sc, true, true, mixed ? e->p64[0] : nullptr,
-                          mixed ? e->p64[1] : nullptr, e->ctl, refined_df(e));
-  prof_end(*e, tok, (mixed ? 8 : 4) * N + 4 * F + N + 4 * F, 1);
+                          mixed ? e->p64[1] : nullptr, e->ctl, refined_df(e), mixed ? e->p32_final : nullptr);
+  prof_end(*e, tok, (mixed ? 8 + 4 : 4) * N + 4 * F + N + 4 * F, 1);
   // velocity and pressure are final: fl_step_host reads them back from here
   // on while the dye advection runs
   cudaEventRecordWithFlags(e->ev_proj, s, capturing(s) ? cudaEventRecordExternal : 0);
@@ -885,6 +886,7 @@ int fl_create(int nx, int ny, double h, int dye_scale, const fl_params* params, 
   s = s ? s : dalloc(e, (void**)&e->acc, sizeof(StepAccum), "accumulators");
   s = s ? s : dalloc(e, (void**)&e->time_dev, sizeof(double), "clock");
   s = s ? s : dalloc(e, &e->staging, e->staging_bytes, "staging");
+  s = s ? s : dalloc(e, (void**)&e->p32_final, (size_t)e->cells() * sizeof(float), "rounded pressure");
   s = s ? s : dalloc(e, (void**)&e->p64[0], (size_t)e->cells() * 8, "p64");
   s = s ? s : dalloc(e, (void**)&e->p64[1], (size_t)e->cells() * 8, "p64");
   s = s ? s : dalloc(e, (void**)&e->r32, cf, "residual");
@@ -1296,10 +1298,9 @@ int fl_step_host(fl_engine* h, int dtype, const void* u, const void* v, const vo
   if (p_out) {
     const long n = e->cells();
     if (step_mixed(e)) {
-      launch_select_p64(e->stream2, e->ctl, e->p64[0], e->p64[1], e->staging, false, n, refined_df(e));
-      TRY(check_launch(e, "read p"));
-      TRY(cuda_status(e, cudaMemcpyAsync(p_out, e->staging, n * sizeof(float), cudaMemcpyDeviceToHost, e->stream2),
-                      "read p"));
+      // rounded to float by the projection
+      TRY(cuda_status(e, cudaMemcpyAsync(p_out, e->p32_final, n * sizeof(float), cudaMemcpyDeviceToHost,
+                                         e->stream2), "read p"));
     } else {
       TRY(cuda_status(e, cudaMemcpyAsync(p_out, e->levels[0].x[0], n * sizeof(float), cudaMemcpyDeviceToHost,
                                          e->stream2), "read p"));

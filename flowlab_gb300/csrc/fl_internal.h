@@ -137,6 +137,9 @@ struct Engine {
 
   // staging for dtype conversion and the per-pass entry points
   void* staging = nullptr;
+  // the step's refined pressure rounded to float by the projection (the
+  // defect-correction paths), which fl_step_host reads back
+  float* p32_final = nullptr;
   size_t staging_bytes = 0;
 
   bool uploaded = false;
@@ -234,7 +237,7 @@ void launch_cfl_residual(cudaStream_t s, int nx, int ny, float h, const float* u
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
                              const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow,
                              const double* p64a = nullptr, const double* p64b = nullptr,
-                             const SolveCtl* ctl = nullptr, bool df = false);
+                             const SolveCtl* ctl = nullptr, bool df = false, float* p32_out = nullptr);
 void launch_max_speed(cudaStream_t s, int nx, int ny, const float* u, const float* v, StepAccum* acc,
                       StepScalars* sc_next, double* time_dev, const fl_params* prm, float h, bool write_scalars,
                       bool add_time);

@@ -228,11 +228,17 @@ __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const 
                                                           const SolveCtl* __restrict__ ctl, float* __restrict__ u,
                                                           float* __restrict__ v, const uint8_t* __restrict__ label,
                                                           const StepScalars* __restrict__ sc, int subtract,
-                                                          int outflow, int df) {
+                                                          int outflow, int df, float* __restrict__ p32_out) {
   // the float64 pressure, when there is one, is the buffer ctl->par names
   const double* p64 = p64a ? (ctl->par ? p64b : p64a) : nullptr;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  // the refined pressure rounded to float (as k_select_p64 rounds it), for
+  // a readback that then needs no kernel of its own
+  if (p32_out != nullptr && p64 != nullptr && i < nx && j < ny) {
+    const long k = i + (long)j * nx;
+    p32_out[k] = df ? df_round(reinterpret_cast<const float2*>(p64)[k]) : (float)p64[k];
+  }
   const float gs = subtract ? sc->grad_scale : 0.0f;
   // u faces: threads 1..nx-1 write; faces 0 and nx are written only by outflow.
   if (j < ny && i >= 1 && i < nx) {
@@ -497,10 +503,11 @@ void launch_divergence(cudaStream_t s, int nx, int ny, float h, const float* u, 
 
 void launch_subtract_outflow(cudaStream_t s, int nx, int ny, const float* p, float* u, float* v,
                              const uint8_t* label, const StepScalars* sc, bool subtract, bool outflow,
-                             const double* p64a, const double* p64b, const SolveCtl* ctl, bool df) {
+                             const double* p64a, const double* p64b, const SolveCtl* ctl, bool df,
+                             float* p32_out) {
   dim3 b(32, 8);
   k_subtract_outflow<<<grid2(nx + 1, ny + 1, b), b, 0, s>>>(nx, ny, p, p64a, p64b, ctl, u, v, label, sc, subtract,
-                                                            outflow, df);
+                                                            outflow, df, p32_out);
 }
 
 void launch_scale_rhs(cudaStream_t s, long n, const float* div, float* b, float neg_scale, const uint8_t* label,
