@@ -1079,15 +1079,12 @@ __device__ __noinline__ void defect_pass_test_last(StepAccum* acc, SolveCtl* ctl
 
 __device__ __forceinline__ void defect_pass_test(StepAccum* acc, SolveCtl* ctl, int test, int use_cond,
                                                  cudaGraphConditionalHandle h) {
-  if (test == 0) return;
-  __shared__ int last;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned int done = atomicAdd(&acc->test_done, 1u);
-    last = done == gridDim.x * gridDim.y - 1;
-  }
-  __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  // only the first thread, which added the block's sums, takes part: the
+  // block's other threads are done
+  if (test == 0 || threadIdx.x != 0) return;
+  __threadfence();
+  const unsigned int done = atomicAdd(&acc->test_done, 1u);
+  if (done != gridDim.x * gridDim.y - 1) return;
   // out of line: the tests' float64 arithmetic stays out of the pass's
   // register budget (64 registers for 8 blocks per SM)
   defect_pass_test_last(acc, ctl, test, use_cond, h);

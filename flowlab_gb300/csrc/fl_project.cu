@@ -237,7 +237,9 @@ __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const 
   // a readback that then needs no kernel of its own
   if (p32_out != nullptr && p64 != nullptr && i < nx && j < ny) {
     const long k = i + (long)j * nx;
-    p32_out[k] = df ? df_round(reinterpret_cast<const float2*>(p64)[k]) : (float)p64[k];
+    // (d2f_rn: the float64 rounding on the integer pipe, so that the
+    // double-float case carries no predicated float64 conversion)
+    p32_out[k] = df ? df_round(reinterpret_cast<const float2*>(p64)[k]) : d2f_rn(p64[k]);
   }
   const float gs = subtract ? sc->grad_scale : 0.0f;
   // u faces: threads 1..nx-1 write; faces 0 and nx are written only by outflow.
