@@ -52,6 +52,7 @@ sys.path.insert(0, ROOT)
 METRIC = "steps/s at 1024\u00b2 to 1e-6 residual: plain MG vs CNN warm-start MG; HBM GB/s"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 REF_BUDGET_S = 60.0  # the CPU reference arm's timed seconds (about; its warm-up is the requested one)
+CPU_SAMPLE_S = 12.0  # the cpu_baseline sample's timed seconds (about), at most --cpu-steps steps
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -140,7 +141,8 @@ def parse():
     ap.add_argument("--size", type=int, default=None)
     ap.add_argument("--tol", type=float, default=None)
     ap.add_argument("--max-cycles", type=int, default=None)
-    ap.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU-baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=40,
+                    help="at most this many steps of the CPU-baseline sample (which stops after ~CPU_SAMPLE_S seconds)")
     ap.add_argument("--parity-steps", type=int, default=2,
                     help="steps from the warmed-up state diffed against the float32 and float64 oracles (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=100)
@@ -654,11 +656,11 @@ def run_ours(args, world, rank, local, pg):
 
     cpu = None
     if rank == 0 and args.cpu_steps > 0:
-        sps, secs, _ = cpu_port_steps(args, args.cpu_steps, 0, state)
+        sps, secs, done = cpu_port_steps(args, args.cpu_steps, 0, state, budget_s=CPU_SAMPLE_S)
         cpu = {"value": sps, "unit": "steps/s", "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
                "sample": "%d steps of the %d^2 %s continuing from the GPU's warmed-up state, float64 CPU "
                          "port of the reference's Simulation.step, one thread (%.1f s)"
-                         % (args.cpu_steps, args.size, workload_name(args), secs)}
+                         % (done, args.size, workload_name(args), secs)}
     eng.close()
     if rank != 0:
         return
