@@ -236,7 +236,9 @@ __device__ __forceinline__ void smooth_tile(const SmoothArgs& a, int bx, int by)
       const int li = 2 * tx + o;
       const int gi = GX + li;
       if (gi >= 0 && gj >= 0 && gi < nx && gj < ny) {
-        const long k = gi + (long)gj * nx;
+        // 32-bit offsets: a level holds fewer than 2^31 cells (the engine's
+        // grid limits)
+        const int k = gi + gj * nx;
         cd[r][o] = a.code[k];
         bb[r][o] = ld_coherent<COH>(a.b + k);
         xx[r][o] = a.x_is_zero ? 0.0f : ld_coherent<COH>(a.xin + k);
@@ -246,7 +248,7 @@ __device__ __forceinline__ void smooth_tile(const SmoothArgs& a, int bx, int by)
           const int I2 = (gi & 1) ? min(I + 1, a.cnx - 1) : max(I - 1, 0);
           const int J2 = (gj & 1) ? min(J + 1, a.cny - 1) : max(J - 1, 0);
           const float* e = a.ec;
-          const long cs = a.cnx;
+          const int cs = a.cnx;
           xx[r][o] += 0.5625f * ld_ro<COH>(e + I + J * cs) +
                       0.1875f * (ld_ro<COH>(e + I2 + J * cs) + ld_ro<COH>(e + I + J2 * cs)) +
                       0.0625f * ld_ro<COH>(e + I2 + J2 * cs);
@@ -348,13 +350,14 @@ __device__ __forceinline__ void smooth_tile(const SmoothArgs& a, int bx, int by)
         if ((c & 3u) == FLUID) {
           const int cnt = code_count(c);
           if (cnt > 0) {
-            // r = b - (count*x - sum), sum order +x, -x, +y, -y (pressureMultigrid.ts:117-151)
+            // r = b - (count*x - sum), sum order +x, -x, +y, -y (pressureMultigrid.ts:117-151);
+            // every neighbour read, an unlinked one being +0.0 (as in the sweeps)
             const float(*xq)[RGN / 2] = xs[1 - ((li + lj) & 1)];
             float sum = 0.0f;
-            if (c & LINK_XP) sum += xq[lj][tx + o];
-            if (c & LINK_XM) sum += xq[lj][tx + o - 1];
-            if (c & LINK_YP) sum += xq[lj + 1][tx];
-            if (c & LINK_YM) sum += xq[lj - 1][tx];
+            sum += xq[lj][tx + o];
+            sum += xq[lj][tx + o - 1];
+            sum += xq[lj + 1][tx];
+            sum += xq[lj - 1][tx];
             res = bb[r][o] - ((float)cnt * xx[r][o] - sum);
             rsq = fma(f2d_exact(res), f2d_exact(res), rsq);
             rn += 1;
@@ -379,7 +382,7 @@ __device__ __forceinline__ void smooth_tile(const SmoothArgs& a, int bx, int by)
               const int i = 2 * I + di, j = 2 * J + dj;
               if (i < nx && j < ny) sum += rs[j - GY][i - GX];
             }
-          a.bc[I + (long)J * a.cnx] = sum;
+          a.bc[I + J * a.cnx] = sum;
         }
       }
     } else {
@@ -405,7 +408,7 @@ __device__ __forceinline__ void smooth_tile(const SmoothArgs& a, int bx, int by)
         const int li = 2 * tx + o;
         const int gi = GX + li;
         if (li < H || li >= H + T || gi >= nx) continue;
-        a.xout[gi + (long)gj * nx] = xx[r][o];
+        a.xout[gi + gj * nx] = xx[r][o];
       }
     }
   }
