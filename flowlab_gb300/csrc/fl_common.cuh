@@ -26,8 +26,13 @@ constexpr uint8_t LINK_YM = 1u << 5;  // (i, j-1)
 constexpr uint8_t CODE_OUTSIDE = SOLID;
 
 __host__ __device__ inline uint8_t code_label(uint8_t c) { return c & 3u; }
+// the number of links (bits 2..5)
 __host__ __device__ inline int code_count(uint8_t c) {
+#ifdef __CUDA_ARCH__
+  return __popc((unsigned int)c & 0x3cu);
+#else
   return ((c >> 2) & 1) + ((c >> 3) & 1) + ((c >> 4) & 1) + ((c >> 5) & 1);
+#endif
 }
 
 // Scalars of one step, written on the device (from the CFL reduction) or by

@@ -235,7 +235,7 @@ __device__ __forceinline__ void smooth_tile(const SmoothArgs& a, int bx, int by)
     for (int o = 0; o < 2; o++) {
       const int li = 2 * tx + o;
       const int gi = GX + li;
-      if (gi >= 0 && gj >= 0 && gi < nx && gj < ny) {
+      if ((unsigned)gi < (unsigned)nx && (unsigned)gj < (unsigned)ny) {
         // 32-bit offsets: a level holds fewer than 2^31 cells (the engine's
         // grid limits)
         const int k = gi + gj * nx;
@@ -344,7 +344,7 @@ __device__ __forceinline__ void smooth_tile(const SmoothArgs& a, int bx, int by)
 #pragma unroll
       for (int o = 0; o < 2; o++) {
         const int li = 2 * tx + o;
-        if (li < H || li >= H + T || lj < H || lj >= H + T) continue;
+        if ((unsigned)(li - H) >= (unsigned)T || (unsigned)(lj - H) >= (unsigned)T) continue;
         const uint8_t c = cd[r][o];
         float res = 0.0f;
         if ((c & 3u) == FLUID) {
