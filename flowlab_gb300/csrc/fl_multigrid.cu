@@ -242,28 +242,43 @@ __device__ __forceinline__ void smooth_tile(const SmoothArgs& a, int bx, int by)
         cd[r][o] = a.code[k];
         bb[r][o] = ld_coherent<COH>(a.b + k);
         xx[r][o] = a.x_is_zero ? 0.0f : ld_coherent<COH>(a.xin + k);
-        if (MODE == MODE_POST && (cd[r][o] & 3u) == FLUID) {
-          // pressureMultigrid.ts:192-207 — x += 9/16, 3/16, 3/16, 1/16 of e
-          const int I = gi >> 1, J = gj >> 1;
-          const int I2 = (gi & 1) ? min(I + 1, a.cnx - 1) : max(I - 1, 0);
-          const int J2 = (gj & 1) ? min(J + 1, a.cny - 1) : max(J - 1, 0);
-          const float* e = a.ec;
-          const int cs = a.cnx;
-          xx[r][o] += 0.5625f * ld_ro<COH>(e + I + J * cs) +
-                      0.1875f * (ld_ro<COH>(e + I2 + J * cs) + ld_ro<COH>(e + I + J2 * cs)) +
-                      0.0625f * ld_ro<COH>(e + I2 + J2 * cs);
-        }
       } else {
         cd[r][o] = CODE_OUTSIDE;
         bb[r][o] = 0.0f;
         xx[r][o] = 0.0f;
       }
+    }
+    if constexpr (MODE == MODE_POST) {
+      // pressureMultigrid.ts:192-207 — a fluid cell's x += 9/16, 3/16, 3/16,
+      // 1/16 of e at coarse columns (I, I2) and rows (J, J2), I = i >> 1, I2
+      // = I + 1 (odd i, clamped) or I - 1 (even i, clamped). The row's two
+      // cells are the odd column GX + 2tx (H is odd, T even) and the even one
+      // after it, so both read coarse columns A = max(I, 0) and B = min(I +
+      // 1, cnx - 1) of I = (GX + 2tx - 1) / 2: the odd cell as (I, I2) =
+      // (A, B), the even one as (B, A). Four loads serve the two cells.
+      static_assert(H % 2 == 1, "the prolongation pairs an odd column with the even one after it");
+      const bool f0 = (cd[r][0] & 3u) == FLUID, f1 = (cd[r][1] & 3u) == FLUID;
+      if (f0 || f1) {
+        const int I = (GX + 2 * tx - 1) / 2;
+        const int A = max(I, 0), B = min(I + 1, a.cnx - 1);
+        const int J = gj >> 1;
+        const int J2 = (gj & 1) ? min(J + 1, a.cny - 1) : max(J - 1, 0);
+        const float* e = a.ec;
+        const int cs = a.cnx;
+        const float eAJ = ld_ro<COH>(e + A + J * cs), eBJ = ld_ro<COH>(e + B + J * cs);
+        const float eAJ2 = ld_ro<COH>(e + A + J2 * cs), eBJ2 = ld_ro<COH>(e + B + J2 * cs);
+        if (f0) xx[r][0] += 0.5625f * eAJ + 0.1875f * (eBJ + eAJ2) + 0.0625f * eBJ2;
+        if (f1) xx[r][1] += 0.5625f * eBJ + 0.1875f * (eAJ + eBJ2) + 0.0625f * eAJ2;
+      }
+    }
+#pragma unroll
+    for (int o = 0; o < 2; o++) {
       // Solid cells (and cells outside the grid) are exactly the neighbours
       // no link points to; they hold +0.0 in shared memory (their own value
       // stays in xx), so that a sweep can add all four neighbours without a
       // test: an unlinked one adds +0.0, which leaves the sum's bits
       // unchanged (a sum that starts at +0.0 never becomes -0.0).
-      xs[(li + lj) & 1][lj][tx] = (cd[r][o] & 3u) == SOLID ? 0.0f : xx[r][o];
+      xs[(2 * tx + o + lj) & 1][lj][tx] = (cd[r][o] & 3u) == SOLID ? 0.0f : xx[r][o];
     }
   }
   __syncthreads();
