@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256) k_advect_velocity(int nx, int ny, Spacing
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const float dt = sc->dt;
   if (i <= nx && j < ny) {
-    const long k = i + (long)j * (nx + 1);
+    const int k = i + j * (nx + 1);
     if (solid_or_outside(label, nx, ny, i - 1, j) || solid_or_outside(label, nx, ny, i, j)) {
       u_out[k] = u_in[k];
     } else {
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(256) k_advect_velocity(int nx, int ny, Spacing
     }
   }
   if (i < nx && j <= ny) {
-    const long k = i + (long)j * nx;
+    const int k = i + j * nx;
     if (solid_or_outside(label, nx, ny, i, j - 1) || solid_or_outside(label, nx, ny, i, j)) {
       v_out[k] = v_in[k];
     } else {
@@ -118,8 +118,9 @@ __global__ void __launch_bounds__(256) k_advect_dye(int nx, int ny, Spacing h, i
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= dnx || j >= dny) return;
+  // 64-bit: the three planes together may hold more than 2^31 values
   const long cells = (long)dnx * dny;
-  const long k = i + (long)j * dnx;
+  const int k = i + j * dnx;
   const float dt = sc->dt;
   const float ratio = dh.h / h.h;
   const int lj = (int)floorf(((float)j + 0.5f) * ratio);
@@ -166,8 +167,8 @@ __global__ void __launch_bounds__(256) k_advect_dye(int nx, int ny, Spacing h, i
     if (patch != nullptr) {
       const int pi = i - pi0, pj = j - pj0;
       if (pi >= 0 && pj >= 0 && pi < pnx && pj < pny) {
-        const long pc = (long)pnx * pny;
-        const long s = pi + (long)pj * pnx;
+        const long pc = (long)pnx * pny;  // 64-bit: five planes
+        const int s = pi + pj * pnx;
         const float cov = patch[DYE_CHANNELS * pc + s];
         if (cov != 0.0f) {
 #pragma unroll

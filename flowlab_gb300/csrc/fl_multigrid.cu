@@ -811,7 +811,7 @@ __device__ __forceinline__ void update_resid64_tile(int nx, int ny, double* __re
     rp = 0.0;
     re = 0.0f;
     if (col && y >= 0 && y < ny) {
-      const long k = gx + (long)y * nx;
+      const int k = gx + y * nx;
       rp = p_in[k];
       if (UPDATE) re = e[k];
     }
@@ -826,7 +826,7 @@ __device__ __forceinline__ void update_resid64_tile(int nx, int ny, double* __re
   float bnext = 0.0f, blnext = 0.0f;
   uint8_t cnext = (uint8_t)CODE_OUTSIDE;
   if (own && y0 < ny) {
-    const long k = gx + (long)y0 * nx;
+    const int k = gx + y0 * nx;
     bnext = b[k];
     blnext = b_lo[k];
     cnext = code[k];
@@ -843,7 +843,7 @@ __device__ __forceinline__ void update_resid64_tile(int nx, int ny, double* __re
     const float bv = bnext, blv = blnext;
     const uint8_t c = cnext;
     if (own && gy + 1 < ny && t + 1 < UR_ROWS) {
-      const long k = gx + (long)(gy + 1) * nx;
+      const int k = gx + (gy + 1) * nx;
       bnext = b[k];
       blnext = b_lo[k];
       cnext = code[k];
@@ -851,7 +851,7 @@ __device__ __forceinline__ void update_resid64_tile(int nx, int ny, double* __re
     const double left = __shfl_up_sync(0xffffffffu, pc, 1);
     const double right = __shfl_down_sync(0xffffffffu, pc, 1);
     if (own) {
-      const long k = gx + (long)gy * nx;
+      const int k = gx + gy * nx;
       if (UPDATE) p_out[k] = pc;
       float r = 0.0f;
       const int cnt = code_count(c);
@@ -943,7 +943,7 @@ __device__ __forceinline__ void update_resid_df_tile(int nx, int ny, float2* __r
     P[r] = make_float2(0.0f, 0.0f);
     E[r] = 0.0f;
     if (col && y >= 0 && y < ny) {
-      const long k = gx + (long)y * nx;
+      const int k = gx + y * nx;  // 32-bit offsets: a grid holds fewer than 2^31 cells
       P[r] = p_in[k];
       if (UPDATE) E[r] = e[k];
     }
@@ -955,7 +955,7 @@ __device__ __forceinline__ void update_resid_df_tile(int nx, int ny, float2* __r
     BL[r] = 0.0f;
     C[r] = (uint8_t)CODE_OUTSIDE;
     if (own && y < ny) {
-      const long k = gx + (long)y * nx;
+      const int k = gx + y * nx;
       B[r] = b[k];
       BL[r] = b_lo[k];
       C[r] = code[k];
@@ -976,7 +976,7 @@ __device__ __forceinline__ void update_resid_df_tile(int nx, int ny, float2* __r
     const float2 right =
         make_float2(__shfl_down_sync(0xffffffffu, pc.x, 1), __shfl_down_sync(0xffffffffu, pc.y, 1));
     if (own && gy < ny) {
-      const long k = gx + (long)gy * nx;
+      const int k = gx + gy * nx;
       if (UPDATE) p_out[k] = pc;
       const uint8_t c = C[t];
       float r = 0.0f;

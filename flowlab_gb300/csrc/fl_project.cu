@@ -12,8 +12,8 @@ namespace fl {
 // vorticity.ts:9-14
 __device__ __forceinline__ float curl_at_corner(const float* __restrict__ u, const float* __restrict__ v, int nx,
                                                 const Spacing& h, int i, int j) {
-  return over(v[i + (long)j * nx] - v[(i - 1) + (long)j * nx], h) -
-         over(u[i + (long)j * (nx + 1)] - u[i + (long)(j - 1) * (nx + 1)], h);
+  return over(v[i + j * nx] - v[(i - 1) + j * nx], h) -
+         over(u[i + j * (nx + 1)] - u[i + (j - 1) * (nx + 1)], h);
 }
 
 // vorticity.ts:24-42 — corner curls averaged to the centre, clamped at walls.
@@ -25,7 +25,7 @@ __global__ void k_vorticity(int nx, int ny, Spacing h, const float* __restrict__
   const int hiI = nx - 1, hiJ = ny - 1;
   const int j0 = min(max(j, 1), hiJ), j1 = min(max(j + 1, 1), hiJ);
   const int i0 = min(max(i, 1), hiI), i1 = min(max(i + 1, 1), hiI);
-  w[i + (long)j * nx] = 0.25f * (curl_at_corner(u, v, nx, h, i0, j0) + curl_at_corner(u, v, nx, h, i1, j0) +
+  w[i + j * nx] = 0.25f * (curl_at_corner(u, v, nx, h, i0, j0) + curl_at_corner(u, v, nx, h, i1, j0) +
                                  curl_at_corner(u, v, nx, h, i0, j1) + curl_at_corner(u, v, nx, h, i1, j1));
 }
 
@@ -38,7 +38,7 @@ __global__ void k_confinement_force(int nx, int ny, Spacing h1, Spacing h2, cons
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
-  const long k = i + (long)j * nx;
+  const int k = i + j * nx;
   if (label[k] == SOLID) {
     fx[k] = 0.0f;
     fy[k] = 0.0f;
@@ -47,8 +47,8 @@ __global__ void k_confinement_force(int nx, int ny, Spacing h1, Spacing h2, cons
   const int ie = min(i + 1, nx - 1), iw = max(i - 1, 0);
   const int jn = min(j + 1, ny - 1), js = max(j - 1, 0);
   // (ie-iw)*h is h or 2h: both powers of two when h is one
-  const float gx = over(fabsf(w[ie + (long)j * nx]) - fabsf(w[iw + (long)j * nx]), ie - iw == 2 ? h2 : h1);
-  const float gy = over(fabsf(w[i + (long)jn * nx]) - fabsf(w[i + (long)js * nx]), jn - js == 2 ? h2 : h1);
+  const float gx = over(fabsf(w[ie + j * nx]) - fabsf(w[iw + j * nx]), ie - iw == 2 ? h2 : h1);
+  const float gy = over(fabsf(w[i + jn * nx]) - fabsf(w[i + js * nx]), jn - js == 2 ? h2 : h1);
   const float mag = sqrtf(gx * gx + gy * gy) + 1e-20f;
   const float Nx = gx / mag, Ny = gy / mag;
   const float wk = w[k];
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256) k_vort_confine(int nx, int ny, Spacing h,
   __syncthreads();
   const int i = X0 + threadIdx.x, j = Y0 + threadIdx.y;
   if (i >= nx || j >= ny) return;
-  const long k = i + (long)j * nx;
+  const int k = i + j * nx;
   if (label[k] == SOLID) {
     fx[k] = 0.0f;
     fy[k] = 0.0f;
@@ -117,20 +117,20 @@ __global__ void __launch_bounds__(256) k_forces(int nx, int ny, float h, int dnx
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (conf_on && i >= 1 && i < nx && j < ny) {
     if (!(solid_cell(label, nx, ny, i - 1, j) || solid_cell(label, nx, ny, i, j))) {
-      const long k = i + (long)j * (nx + 1);
-      u[k] += sc->half_dt * (fx[(i - 1) + (long)j * nx] + fx[i + (long)j * nx]);
+      const int k = i + j * (nx + 1);
+      u[k] += sc->half_dt * (fx[(i - 1) + j * nx] + fx[i + j * nx]);
     }
   }
   if (i < nx && j >= 1 && j < ny) {
     if (!(solid_cell(label, nx, ny, i, j - 1) || solid_cell(label, nx, ny, i, j))) {
-      const long k = i + (long)j * nx;
+      const int k = i + j * nx;
       const float x = ((float)i + 0.5f) * h;
       const float y = (float)j * h;
-      const long dcells = (long)dnx * dny;
+      const int dcells = dnx * dny;
       float vk = v[k];
       if (beta_on) vk += sc->gain_beta * sample_p(dye, dnx, dny, dh, x, y);
       if (alpha_on) vk += sc->gain_alpha * sample_p(dye + dcells, dnx, dny, dh, x, y);
-      if (conf_on) vk += sc->half_dt * (fy[i + (long)(j - 1) * nx] + fy[i + (long)j * nx]);
+      if (conf_on) vk += sc->half_dt * (fy[i + (j - 1) * nx] + fy[i + j * nx]);
       v[k] = vk;
     }
   }
@@ -156,9 +156,9 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
 #pragma unroll 4
   for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
     if (i >= nx) break;
-    const long k = i + (long)j * nx;
-    const float d = coef * (u[(i + 1) + (long)j * (nx + 1)] - u[i + (long)j * (nx + 1)] + v[i + (long)(j + 1) * nx] -
-                            v[i + (long)j * nx]);
+    const int k = i + j * nx;
+    const float d = coef * (u[(i + 1) + j * (nx + 1)] - u[i + j * (nx + 1)] + v[i + (j + 1) * nx] -
+                            v[i + j * nx]);
     const float o = as_rhs ? ns * d : d;
     out[k] = o;
     // the rounding error of b = (-scale) * div, exactly (an FMA of the
@@ -192,8 +192,8 @@ __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, float h, con
 // pressure the difference formed in double and rounded once (the rounding
 // on the integer pipe: d2f_rn equals the conversion instruction), or with
 // the double-float pressure (`df`) the pairs' difference rounded once.
-__device__ __forceinline__ float pdiff(const float* __restrict__ p, const double* __restrict__ p64, bool df, long a,
-                                       long b) {
+__device__ __forceinline__ float pdiff(const float* __restrict__ p, const double* __restrict__ p64, bool df, int a,
+                                       int b) {
   if (p64 && df) {
     const float2* q = reinterpret_cast<const float2*>(p64);
     return df_diff(q[a], q[b]);
@@ -204,20 +204,20 @@ __device__ __forceinline__ float pdiff(const float* __restrict__ p, const double
 __device__ __forceinline__ float projected_u(const float* __restrict__ p, const double* __restrict__ p64, bool df,
                                              const float* __restrict__ u, const uint8_t* __restrict__ label, int nx,
                                              int ny, int i, int j, float gs, bool subtract) {
-  float val = u[i + (long)j * (nx + 1)];
+  float val = u[i + j * (nx + 1)];
   if (subtract && i >= 1 && i < nx) {
     if (!(solid_or_outside(label, nx, ny, i - 1, j) || solid_or_outside(label, nx, ny, i, j)))
-      val -= gs * pdiff(p, p64, df, i + (long)j * nx, (i - 1) + (long)j * nx);
+      val -= gs * pdiff(p, p64, df, i + j * nx, (i - 1) + j * nx);
   }
   return val;
 }
 __device__ __forceinline__ float projected_v(const float* __restrict__ p, const double* __restrict__ p64, bool df,
                                              const float* __restrict__ v, const uint8_t* __restrict__ label, int nx,
                                              int ny, int i, int j, float gs, bool subtract) {
-  float val = v[i + (long)j * nx];
+  float val = v[i + j * nx];
   if (subtract && j >= 1 && j < ny) {
     if (!(solid_or_outside(label, nx, ny, i, j - 1) || solid_or_outside(label, nx, ny, i, j)))
-      val -= gs * pdiff(p, p64, df, i + (long)j * nx, i + (long)(j - 1) * nx);
+      val -= gs * pdiff(p, p64, df, i + j * nx, i + (j - 1) * nx);
   }
   return val;
 }
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const 
   // the refined pressure rounded to float (as k_select_p64 rounds it), for
   // a readback that then needs no kernel of its own
   if (p32_out != nullptr && p64 != nullptr && i < nx && j < ny) {
-    const long k = i + (long)j * nx;
+    const int k = i + j * nx;
     // (d2f_rn: the float64 rounding on the integer pipe, so that the
     // double-float case carries no predicated float64 conversion)
     p32_out[k] = df ? df_round(reinterpret_cast<const float2*>(p64)[k]) : d2f_rn(p64[k]);
@@ -246,16 +246,16 @@ __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const 
   if (j < ny && i >= 1 && i < nx) {
     float val = projected_u(p, p64, df, u, label, nx, ny, i, j, gs, subtract);
     if (outflow) {
-      if (i == 1 && label[0 + (long)j * nx] == AIR) {
+      if (i == 1 && label[0 + j * nx] == AIR) {
         val = smin(val, 0.0f);
-        u[0 + (long)j * (nx + 1)] = val;
+        u[0 + j * (nx + 1)] = val;
       }
-      if (i == nx - 1 && label[(nx - 1) + (long)j * nx] == AIR) {
+      if (i == nx - 1 && label[(nx - 1) + j * nx] == AIR) {
         val = smax(val, 0.0f);
-        u[nx + (long)j * (nx + 1)] = val;
+        u[nx + j * (nx + 1)] = val;
       }
     }
-    u[i + (long)j * (nx + 1)] = val;
+    u[i + j * (nx + 1)] = val;
   }
   if (i < nx && j >= 1 && j < ny) {
     float val = projected_v(p, p64, df, v, label, nx, ny, i, j, gs, subtract);
@@ -264,12 +264,12 @@ __global__ void __launch_bounds__(256) k_subtract_outflow(int nx, int ny, const 
         val = smin(val, 0.0f);
         v[i] = val;
       }
-      if (j == ny - 1 && label[i + (long)(ny - 1) * nx] == AIR) {
+      if (j == ny - 1 && label[i + (ny - 1) * nx] == AIR) {
         val = smax(val, 0.0f);
-        v[i + (long)ny * nx] = val;
+        v[i + ny * nx] = val;
       }
     }
-    v[i + (long)j * nx] = val;
+    v[i + j * nx] = val;
   }
 }
 
@@ -378,7 +378,7 @@ __global__ void k_commit_labels(int nx, int ny, const uint8_t* __restrict__ labe
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i < nx && j < ny) {
-    const long k = i + (long)j * nx;
+    const int k = i + j * nx;
     const uint8_t l = label[k];
     if (l != FLUID) {
       if (p) p[k] = 0.0f;
@@ -389,10 +389,10 @@ __global__ void k_commit_labels(int nx, int ny, const uint8_t* __restrict__ labe
     }
   }
   if (i <= nx && j < ny) {
-    if (solid_cell(label, nx, ny, i - 1, j) || solid_cell(label, nx, ny, i, j)) u[i + (long)j * (nx + 1)] = 0.0f;
+    if (solid_cell(label, nx, ny, i - 1, j) || solid_cell(label, nx, ny, i, j)) u[i + j * (nx + 1)] = 0.0f;
   }
   if (i < nx && j <= ny) {
-    if (solid_cell(label, nx, ny, i, j - 1) || solid_cell(label, nx, ny, i, j)) v[i + (long)j * nx] = 0.0f;
+    if (solid_cell(label, nx, ny, i, j - 1) || solid_cell(label, nx, ny, i, j)) v[i + j * nx] = 0.0f;
   }
 }
 
@@ -413,7 +413,7 @@ __global__ void k_stir(int nx, int ny, float h, float* __restrict__ u, float* __
     if (!(solid_cell(label, nx, ny, i - 1, j) || solid_cell(label, nx, ny, i, j))) {
       const float dy = ((float)j + 0.5f) * h - sy;
       const float dx = (float)i * h - sx;
-      u[i + (long)j * (nx + 1)] += sdx * expf(-(dx * dx + dy * dy) * invR2);
+      u[i + j * (nx + 1)] += sdx * expf(-(dx * dx + dy * dy) * invR2);
     }
   }
   if (j >= min(max(r0, 1), ny - 1) && j <= min(max(r1, 1), ny - 1) && i >= min(max(c0, 0), nx - 1) &&
@@ -421,7 +421,7 @@ __global__ void k_stir(int nx, int ny, float h, float* __restrict__ u, float* __
     if (!(solid_cell(label, nx, ny, i, j - 1) || solid_cell(label, nx, ny, i, j))) {
       const float dy = (float)j * h - sy;
       const float dx = ((float)i + 0.5f) * h - sx;
-      v[i + (long)j * nx] += sdy * expf(-(dx * dx + dy * dy) * invR2);
+      v[i + j * nx] += sdy * expf(-(dx * dx + dy * dy) * invR2);
     }
   }
 }
@@ -434,12 +434,12 @@ __global__ void k_dye_patch(int dnx, int dny, float* __restrict__ dye, const flo
   if (pi >= pnx || pj >= pny) return;
   const int di = pi0 + pi, dj = pj0 + pj;
   if (di < 0 || dj < 0 || di >= dnx || dj >= dny) return;
-  const long pc = (long)pnx * pny;
-  const long s = pi + (long)pj * pnx;
+  const long pc = (long)pnx * pny;  // 64-bit: the planes together may exceed 2^31 values
+  const int s = pi + pj * pnx;
   const float cov = patch[DYE_CHANNELS * pc + s];
   if (cov == 0.0f) return;
   const long cells = (long)dnx * dny;
-  const long k = di + (long)dj * dnx;
+  const int k = di + dj * dnx;
   for (int c = 0; c < DYE_CHANNELS; c++) dye[k + c * cells] += cov * (patch[c * pc + s] - dye[k + c * cells]);
 }
 
@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(256) k_cfl_residual(int nx, int ny, float h, c
 #pragma unroll 4
   for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < ny; j += gridDim.y * blockDim.y) {
     if (i >= nx) break;
-    const long ku = i + (long)j * (nx + 1), kv = i + (long)j * nx;
+    const int ku = i + j * (nx + 1), kv = i + j * nx;
     const float u0 = u[ku], u1 = u[ku + 1], v0 = v[kv], v1 = v[kv + nx];
     m = smax(m, smax(smax(fabsf(u0), fabsf(u1)), smax(fabsf(v0), fabsf(v1))));
     if (on) {
