@@ -256,19 +256,21 @@ __device__ __forceinline__ void smooth_tile(const SmoothArgs& a, int bx, int by)
       // after it, so both read coarse columns A = max(I, 0) and B = min(I +
       // 1, cnx - 1) of I = (GX + 2tx - 1) / 2: the odd cell as (I, I2) =
       // (A, B), the even one as (B, A). Four loads serve the two cells.
+      // The loads do not wait for the codes: on rows inside the grid they
+      // run for every pair, at columns clamped into the coarse level (the
+      // clamps change nothing for a pair with a cell in the grid).
       static_assert(H % 2 == 1, "the prolongation pairs an odd column with the even one after it");
-      const bool f0 = (cd[r][0] & 3u) == FLUID, f1 = (cd[r][1] & 3u) == FLUID;
-      if (f0 || f1) {
+      if ((unsigned)gj < (unsigned)ny) {
         const int I = (GX + 2 * tx - 1) / 2;
-        const int A = max(I, 0), B = min(I + 1, a.cnx - 1);
+        const int A = min(max(I, 0), a.cnx - 1), B = max(min(I + 1, a.cnx - 1), 0);
         const int J = gj >> 1;
         const int J2 = (gj & 1) ? min(J + 1, a.cny - 1) : max(J - 1, 0);
         const float* e = a.ec;
         const int cs = a.cnx;
         const float eAJ = ld_ro<COH>(e + A + J * cs), eBJ = ld_ro<COH>(e + B + J * cs);
         const float eAJ2 = ld_ro<COH>(e + A + J2 * cs), eBJ2 = ld_ro<COH>(e + B + J2 * cs);
-        if (f0) xx[r][0] += 0.5625f * eAJ + 0.1875f * (eBJ + eAJ2) + 0.0625f * eBJ2;
-        if (f1) xx[r][1] += 0.5625f * eBJ + 0.1875f * (eAJ + eBJ2) + 0.0625f * eAJ2;
+        if ((cd[r][0] & 3u) == FLUID) xx[r][0] += 0.5625f * eAJ + 0.1875f * (eBJ + eAJ2) + 0.0625f * eBJ2;
+        if ((cd[r][1] & 3u) == FLUID) xx[r][1] += 0.5625f * eBJ + 0.1875f * (eAJ + eBJ2) + 0.0625f * eAJ2;
       }
     }
 #pragma unroll
