@@ -373,6 +373,57 @@ def test_stir_step_matches_oracle(o32):
         assert np.abs(np.asarray(a, np.float64) - b).max() <= 1e-5 * np.abs(a).max()
 
 
+def test_step_host_follows_label_and_parameter_changes():
+    """fl_step_host when the obstacles move between calls (a changed label
+    upload: the compare on the third stream raises the flag and the gated
+    multigrid rebuild runs before the solve reads the codes) and after
+    fl_set_params changes the V-cycle depth (every graph, the host step's
+    own included, rebuilt) gives the same fields and cycle counts as
+    fl_upload_fields + fl_step_auto + fl_read_* on a second engine."""
+    g, f, patch = configs.plume(96)
+    prm = configs.plume_params(tol=1e-6, max_cycles=20, mixed=1)
+    prm2 = configs.plume_params(tol=1e-6, max_cycles=20, mixed=1)
+    prm2.mg_coarsest = 4
+    labels = [np.ascontiguousarray(f.label)]
+    moved = labels[0].copy().reshape(g.ny, g.nx)
+    moved[40:52, 30:44] = 2  # a solid block appears
+    labels.append(np.ascontiguousarray(moved.ravel()))
+    moved2 = labels[0].copy().reshape(g.ny, g.nx)
+    moved2[44:56, 50:62] = 2  # and moves
+    labels.append(np.ascontiguousarray(moved2.ravel()))
+    engs = [native.Engine(g.nx, g.ny, g.h, params=prm) for _ in range(2)]
+    try:
+        for eng in engs:
+            eng.call("fl_set_dye_patch", patch.i0, patch.j0, patch.nx, patch.ny, ptr(f32(patch.data)))
+        a, b = engs
+        state = [f32(f.u).copy(), f32(f.v).copy(), f32(f.p).copy(), f32(f.dye).copy()]
+        out_b = [np.empty_like(x) for x in state]
+        schedule = [0, 0, 1, 1, 2, 2, 2, 0]
+        for step, which in enumerate(schedule):
+            if step == 5:
+                for eng in engs:
+                    eng.set_params(prm2)
+            label = labels[which]
+            a.call("fl_upload_fields", native.FL_F32, ptr(state[0]), ptr(state[1]), ptr(state[2]), ptr(label),
+                   ptr(state[3]))
+            ia = ctypes.c_int()
+            a.call("fl_step_auto", 1, ctypes.byref(ia))
+            out_a = [np.empty_like(x) for x in state]
+            a.call("fl_read_velocity", native.FL_F32, ptr(out_a[0]), ptr(out_a[1]))
+            a.call("fl_read_pressure", native.FL_F32, ptr(out_a[2]))
+            a.call("fl_read_dye", native.FL_F32, ptr(out_a[3]))
+            ib = ctypes.c_int()
+            b.call("fl_step_host", native.FL_F32, ptr(state[0]), ptr(state[1]), ptr(state[2]), ptr(label),
+                   ptr(state[3]), ptr(out_b[0]), ptr(out_b[1]), ptr(out_b[2]), ptr(out_b[3]), ctypes.byref(ib))
+            for name, x, y in zip(("u", "v", "p", "dye"), out_a, out_b):
+                assert mismatch(x, y) == 0, "step %d %s: %d values differ" % (step, name, mismatch(x, y))
+            assert ia.value == ib.value
+            state = [x.copy() for x in out_a]
+    finally:
+        for eng in engs:
+            eng.close()
+
+
 @pytest.mark.parametrize("mixed", [0, 1])
 def test_extrapolated_warm_start_matches_float32_oracle(o32, mixed):
     """The second-order warm start 2 p(n) - p(n-1) (no reference
