@@ -225,11 +225,11 @@ __device__ __forceinline__ float clamp_stencil_p(const float* __restrict__ q, in
 
 // grid.ts:159-161 isSolidOrOutside on the velocity grid's labels.
 __device__ __forceinline__ bool solid_or_outside(const uint8_t* __restrict__ label, int nx, int ny, int i, int j) {
-  return i < 0 || j < 0 || i >= nx || j >= ny || __ldg(label + i + (long)j * nx) == SOLID;
+  return (unsigned)i >= (unsigned)nx || (unsigned)j >= (unsigned)ny || __ldg(label + i + j * nx) == SOLID;
 }
 // boundaries.ts:23-25 isSolidCell
 __device__ __forceinline__ bool solid_cell(const uint8_t* __restrict__ label, int nx, int ny, int i, int j) {
-  return i >= 0 && j >= 0 && i < nx && j < ny && __ldg(label + i + (long)j * nx) == SOLID;
+  return (unsigned)i < (unsigned)nx && (unsigned)j < (unsigned)ny && __ldg(label + i + j * nx) == SOLID;
 }
 
 // Block-wide reductions (thread count a multiple of 32, <= 1024); the result
