@@ -1061,11 +1061,6 @@ cudaError_t enqueue_after_upload(Engine* e, bool p64_from_p32, bool capture) {
 
 namespace {
 
-// The body of fl_upload_fields. With `dye_async` the dye (float32) is copied
-// on the second stream, after the stream's earlier work and the other
-// fields' copies, and ev_dye marks its end; the step's first dye reader
-// waits for it (wait_dye). Otherwise
-// ev_dye is recorded on the second stream with nothing in flight.
 // The rebuild part of fl_step_host's upload as a graph on the third stream:
 // the multigrid labels and codes rebuilt by kernels that run only when the
 // label compare before them found a changed cell (a plain graph: an IF node
@@ -1090,9 +1085,13 @@ int label_graph(Engine* e) {
   return FL_OK;
 }
 
-// With cfl_deferred (fl_step_host's float32 upload), the clock reset and
-// the CFL scalars are left to the caller (*cfl_deferred says so), which runs
-// them at the head of the step's graph.
+// The body of fl_upload_fields. With `dye_async` the dye (float32) is copied
+// on the second stream, after the stream's earlier work and the other
+// fields' copies, and ev_dye marks its end; the step's first dye reader
+// waits for it (wait_dye). Otherwise ev_dye is recorded on the second stream
+// with nothing in flight. With cfl_deferred (fl_step_host's float32 upload),
+// the clock reset and the CFL scalars are left to the caller (*cfl_deferred
+// says so), which runs them at the head of the step's graph.
 int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void* p, const uint8_t* label,
                   const void* dye, bool dye_async, bool* cfl_deferred = nullptr) {
   if (cfl_deferred) *cfl_deferred = false;
@@ -1100,10 +1099,11 @@ int upload_fields(Engine* e, int dtype, const void* u, const void* v, const void
   e->stats_on_device = false;
   if (dye_async && !dye) return fail(e, FL_EINVAL, "upload dye: null pointer");
   // fl_step_host's float32 upload, on three streams: the labels first, their
-  // compare and rebuild on the third stream while u and v arrive on the
-  // engine's stream (followed by the CFL scalars); the dye, then the
-  // pressure (and what is formed from it) on the second stream behind u and
-  // v. The step waits for each where it first reads it.
+  // compare and the gated rebuild on the third stream while u and v arrive
+  // on the engine's stream; the dye, then the pressure (and what is formed
+  // from it) on the second stream behind u and v. The step (led by the CFL
+  // scalars of the new velocity, cfl_deferred) starts once the finest labels
+  // are compared and waits for the rest where it first reads each.
   const bool async_p = dye_async && dtype == FL_F32 && e->use_graphs;
   // stale codes (new levels, labels written by another entry point): every
   // cell is made to differ so that the rebuild runs. Read before a capture
